@@ -1,0 +1,606 @@
+/*
+ * tc_tessellation.h — C ABI of the GB300 (sm_103a) tessellated-cluster build pipeline.
+ *
+ * This library re-implements, as CUDA kernels, the per-frame compute chain of
+ * nvpro-samples/vk_tessellated_clusters that turns clustered meshes into
+ * cluster-acceleration-structure build inputs:
+ *
+ *   instances_classify -> clusters_cull -> build_setup -> cluster_classify
+ *   -> triangle_split (multi-pass) -> triangle_tess_template_instantiate
+ *   -> blas_setup_insertion -> blas_clusters_insert
+ *
+ * The boundary is the reference's buffer protocol (shaders/shaderio_*.h): every
+ * array is a 64-bit device address inside tc_SceneBuilding / tc_RenderInstance,
+ * counters live in tc_SceneBuilding, statistics in tc_Readback, and the layouts
+ * below are byte-identical to the reference's C++ view of those structs, so the
+ * buffers this library fills are what the cluster AS build consumes
+ * (src/renderer_raytrace_clusters_tess.cpp:592-733).
+ *
+ * Ownership follows the reference (src/renderer_raytrace_clusters_tess.cpp:200-310):
+ * the caller allocates every buffer referenced by tc_SceneBuilding and
+ * tc_RenderInstance. The context owns only the uploaded tessellation table and a
+ * scratch block sized at creation. No call below allocates device memory except
+ * tc_context_create and tc_table_init.
+ *
+ * All entry points are asynchronous on the given stream and return a tc_status
+ * describing argument validation and launch errors. Faults detected by kernels
+ * (a look-back wait that ran out, inconsistent input) are recorded in a device
+ * error word read by tc_read_device_errors.
+ *
+ * Arithmetic: IEEE single precision without contraction (no FMA), IEEE division
+ * and square root, round-half-to-even for the GLSL round() of tess factors.
+ */
+#ifndef TC_TESSELLATION_H_
+#define TC_TESSELLATION_H_
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TC_API_VERSION 1
+
+/* ------------------------------------------------------------------------- */
+/* constants mirroring shaders/shaderio*.h                                    */
+/* ------------------------------------------------------------------------- */
+
+#define TC_TESSTABLE_COORD_MAX (1u << 15) /* shaderio_scene.h:24 */
+#define TC_TESSTABLE_SIZE 11u             /* shaderio_scene.h:25 */
+#define TC_TESSTABLE_LOOKUP_SIZE 16u      /* shaderio_scene.h:40 (next pow2 of 11) */
+#define TC_TESSTABLE_LOOKUP_ENTRIES (TC_TESSTABLE_LOOKUP_SIZE * TC_TESSTABLE_LOOKUP_SIZE * TC_TESSTABLE_LOOKUP_SIZE)
+#define TC_MAX_CLUSTER_TRIANGLES 64u
+#define TC_MAX_CLUSTER_VERTICES 64u
+
+#define TC_INSTANCE_FRUSTUM_BIT 1u /* shaderio_building.h:54 */
+#define TC_INSTANCE_VISIBLE_BIT 2u /* shaderio_building.h:55 */
+
+/* build_setup modes, shaderio.h:67-72 */
+#define TC_BUILD_SETUP_CLASSIFY 0u
+#define TC_BUILD_SETUP_INSTANTIATE_TESS 1u
+#define TC_BUILD_SETUP_DRAW_TESS 2u
+#define TC_BUILD_SETUP_SPLIT 3u
+#define TC_BUILD_SETUP_SPLIT_PASS 4u
+#define TC_BUILD_SETUP_BUILD_BLAS 5u
+
+/* clusterID mode bits in TemplateInstantiateInfo.clusterIdOffset, shaderio.h:101-108 */
+#define TC_RT_CLUSTER_MODE_FULL_CLUSTER 0u
+#define TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED 1u
+
+/* ------------------------------------------------------------------------- */
+/* layouts (byte-identical to the reference's C++ structs)                    */
+/* ------------------------------------------------------------------------- */
+
+typedef struct tc_vec2 { float x, y; } tc_vec2;
+typedef struct tc_vec3 { float x, y, z; } tc_vec3;
+typedef struct tc_vec4 { float x, y, z, w; } tc_vec4;
+/* column-major like glm::mat4: m[col*4 + row] */
+typedef struct tc_mat4 { float m[16]; } tc_mat4;
+
+/* shaderio_scene.h:65-72 */
+typedef struct tc_TessTableEntry {
+  uint16_t firstTriangle;
+  uint16_t firstVertex;
+  uint16_t numTriangles;
+  uint16_t numVertices;
+} tc_TessTableEntry;
+
+/* shaderio_scene.h:75-87 */
+typedef struct tc_TessellationTable {
+  uint64_t vertices;                   /* u32[]: (v << 16) | u, 1<<15 == 1.0 */
+  uint64_t triangles;                  /* u32[]: 3 x u8 indices */
+  uint64_t entries;                    /* tc_TessTableEntry[4096] lookup */
+  uint64_t templateAddresses;          /* u64[4096] per config CLAS template */
+  uint64_t templateInstantiationSizes; /* u32[4096] worst-case CLAS size */
+} tc_TessellationTable;
+
+/* shaderio_scene.h:89-95 */
+typedef struct tc_BBox {
+  tc_vec3 lo;
+  tc_vec3 hi;
+  float   shortestEdge;
+  float   longestEdge;
+} tc_BBox;
+
+/* shaderio_scene.h:101-111 */
+typedef struct tc_Cluster {
+  uint16_t numVertices;
+  uint16_t numTriangles;
+  uint32_t firstTriangle;
+  uint32_t firstLocalVertex;
+  uint32_t firstLocalTriangle;
+} tc_Cluster;
+
+/* shaderio_scene.h:116-156 */
+typedef struct tc_RenderInstance {
+  tc_mat4  worldMatrix;
+  uint32_t geometryID;
+  uint32_t numTriangles;
+  uint32_t numVertices;
+  uint32_t numClusters;
+  int32_t  displacementIndex;
+  float    displacementScale;
+  float    displacementOffset;
+  float    _pad;
+  tc_vec4  geoLo;
+  tc_vec4  geoHi;
+  uint64_t positions;                        /* tc_vec3[] */
+  uint64_t normals;                          /* tc_vec3[] */
+  uint64_t texcoords;                        /* tc_vec2[] */
+  uint64_t clusters;                         /* tc_Cluster[] */
+  uint64_t clusterLocalTriangles;            /* u8[] */
+  uint64_t clusterBboxes;                    /* tc_BBox[] */
+  uint64_t clusterTemplateAdresses;          /* u64[] (spelling as in the reference) */
+  uint64_t clusterTemplateInstantiatonSizes; /* u32[] (spelling as in the reference) */
+} tc_RenderInstance;
+
+/* shaderio_building.h:62-68 */
+typedef struct tc_ClusterInfo {
+  uint32_t instanceID;
+  uint32_t clusterID;
+} tc_ClusterInfo;
+
+/* shaderio_building.h:71-92 */
+typedef struct tc_SubTriangleInfo {
+  uint32_t vtxEncoded[3];
+  uint32_t triangleID_config; /* triangleID | (config << 16), config bit 15 = flipped */
+} tc_SubTriangleInfo;
+
+typedef struct tc_TessTriangleInfo {
+  tc_ClusterInfo     cluster;
+  tc_SubTriangleInfo subTriangle;
+} tc_TessTriangleInfo;
+
+/* shaderio_building.h:95-127 */
+typedef struct tc_ClasBuildInfo {
+  uint32_t clusterID;
+  uint32_t clusterFlags;
+  uint32_t packed;
+  uint32_t baseGeometryIndexAndFlags;
+  uint16_t indexBufferStride;
+  uint16_t vertexBufferStride;
+  uint16_t geometryIndexAndFlagsBufferStride;
+  uint16_t opacityMicromapIndexBufferStride;
+  uint64_t indexBuffer;
+  uint64_t vertexBuffer;
+  uint64_t geometryIndexAndFlagsBuffer;
+  uint64_t opacityMicromapArray;
+  uint64_t opacityMicromapIndexBuffer;
+} tc_ClasBuildInfo;
+
+/* shaderio_building.h:130-138 */
+typedef struct tc_TemplateInstantiateInfo {
+  uint32_t clusterIdOffset;
+  uint32_t geometryIndexOffset;
+  uint64_t clusterTemplateAddress;
+  uint64_t vertexBufferAddress;
+  uint64_t vertexBufferStride;
+} tc_TemplateInstantiateInfo;
+
+/* shaderio_building.h:141-150 */
+typedef struct tc_BlasBuildInfo {
+  uint32_t clusterReferencesCount;
+  uint32_t clusterReferencesStride;
+  uint64_t clusterReferences;
+} tc_BlasBuildInfo;
+
+/* shaderio_core.h:99-111 */
+typedef struct tc_DispatchIndirectCommand {
+  uint32_t gridX, gridY, gridZ;
+} tc_DispatchIndirectCommand;
+
+typedef struct tc_DrawMeshTasksIndirectCommandNV {
+  uint32_t count, first;
+} tc_DrawMeshTasksIndirectCommandNV;
+
+/* shaderio_building.h:156-263 */
+typedef struct tc_SceneBuilding {
+  tc_vec3  viewPos;
+  uint32_t _pad;
+
+  uint32_t numRenderInstances;
+  uint32_t visibleClusterCounter;
+
+  uint32_t fullClusterCounter;
+  uint32_t partTriangleCounter;
+
+  uint64_t dualPartTriangleCounter;
+
+  int32_t  splitTriangleCounter;
+  uint32_t splitReadCounter;
+  uint32_t splitWriteCounter;
+  uint32_t splitPass;
+  uint32_t splitPassStart;
+  uint32_t splitPassEnd;
+
+  uint32_t genVertexCounter;
+  uint32_t genClusterCounter;
+  uint64_t genClusterDataCounter;
+
+  tc_DispatchIndirectCommand dispatchClassify;
+  tc_DispatchIndirectCommand dispatchTriangleSplit;
+
+  uint64_t instanceStates;  /* u32[numRenderInstances] */
+  uint64_t visibleClusters; /* tc_ClusterInfo[maxVisibleClusters] */
+  uint64_t fullClusters;    /* tc_ClusterInfo[] (optional here, see tc_frame_args) */
+  uint64_t splitTriangles;  /* tc_TessTriangleInfo[maxSplitTriangles] */
+  uint64_t partTriangles;   /* tc_TessTriangleInfo[maxPartTriangles] */
+
+  tc_DrawMeshTasksIndirectCommandNV drawFullClusters;
+  tc_DrawMeshTasksIndirectCommandNV drawPartTriangles;
+
+  tc_DispatchIndirectCommand dispatchClusterInstantiate;
+  tc_DispatchIndirectCommand dispatchTriangleInstantiate;
+  tc_DispatchIndirectCommand dispatchBlasTempInsert;
+  tc_DispatchIndirectCommand dispatchBlasTransInsert;
+
+  uint32_t positionTruncateBitCount;
+
+  uint32_t blasClusterCounter;
+  uint32_t tempInstantiateCounter;
+  uint32_t transBuildCounter;
+
+  uint64_t basicClusterSizes;
+
+  uint64_t genClusterData; /* base address of CLAS destination memory */
+  uint64_t genVertices;    /* tc_vec3[maxGeneratedVertices] */
+
+  uint64_t tempInstanceIDs;      /* u32[maxGeneratedClusters] */
+  uint64_t tempInstantiations;   /* tc_TemplateInstantiateInfo[maxGeneratedClusters] */
+  uint64_t tempClusterAddresses; /* u64[maxGeneratedClusters] */
+  uint64_t tempClusterSizes;     /* u32[maxGeneratedClusters] (written by the CLAS build) */
+
+  uint64_t transInstanceIDs;
+  uint64_t transBuilds;
+  uint64_t transClusterAddresses;
+  uint64_t transClusterSizes;
+
+  uint64_t transTriMappings;
+  uint64_t transTriIndices;
+
+  uint64_t blasBuildInfos;       /* tc_BlasBuildInfo[numRenderInstances] */
+  uint64_t blasBuildSizes;       /* u32[numRenderInstances] */
+  uint64_t blasClusterAddresses; /* u64[maxGeneratedClusters] */
+  uint64_t blasBuildData;
+
+  uint32_t numBlasReservedSizes;
+} tc_SceneBuilding;
+
+/*
+ * shaderio.h:180-261 up to and including visFilterClusterID. The reference's
+ * trailing `SkySimpleParameters skyParams` (declared in a header of a
+ * dependency that is not part of the reference) is only used by shading and is
+ * not part of this boundary, which is why the two frame constant blocks are
+ * passed as separate pointers (tc_frame_args.view / viewLast) instead of an
+ * array of two.
+ */
+typedef struct tc_FrameConstants {
+  tc_mat4  projMatrix;
+  tc_mat4  projMatrixI;
+  tc_mat4  viewProjMatrix;
+  tc_mat4  viewProjMatrixI;
+  tc_mat4  viewMatrix;
+  tc_mat4  viewMatrixI;
+  tc_vec4  viewPos;
+  tc_vec4  viewDir;
+  tc_vec4  viewPlane;
+  tc_mat4  skyProjMatrixI;
+  int32_t  viewport[2];
+  tc_vec2  viewportf;
+  tc_vec2  viewPixelSize;
+  tc_vec2  viewClipSize;
+  tc_vec3  wLightPos;
+  float    tessRate;
+  float    displacementScale;
+  float    displacementOffset;
+  float    lightMixer;
+  uint32_t doShadow;
+  tc_vec3  wUpDir;
+  float    sceneSize;
+  tc_vec4  bgColor;
+  float    lodScale;
+  float    animationState;
+  float    ambientOcclusionRadius;
+  int32_t  ambientOcclusionSamples;
+  int32_t  animationRippleEnabled;
+  float    animationRippleFrequency;
+  float    animationRippleAmplitude;
+  float    animationRippleSpeed;
+  uint32_t _pad[3];
+  uint32_t visualize;
+  uint32_t doAnimation;
+  uint32_t flipWinding;
+  float    nearPlane;
+  float    farPlane;
+  tc_vec4  hizSizeFactors;
+  tc_vec4  nearSizeFactors;
+  float    hizSizeMax;
+  int32_t  facetShading;
+  int32_t  supersample;
+  uint32_t colorXor;
+  uint32_t dbgUint;
+  float    dbgFloat;
+  float    time;
+  uint32_t frame;
+  uint32_t mousePosition[2];
+  float    wireThickness;
+  float    wireSmoothing;
+  tc_vec3  wireColor;
+  uint32_t wireStipple;
+  tc_vec3  wireBackfaceColor;
+  float    wireStippleRepeats;
+  float    wireStippleLength;
+  uint32_t doWireframe;
+  uint32_t visFilterInstanceID;
+  uint32_t visFilterClusterID;
+} tc_FrameConstants;
+
+/* shaderio.h:263-309 (C++ view) */
+typedef struct tc_Readback {
+  uint32_t numVisibleClusters;
+  uint32_t numFullClusters;
+  uint32_t numSplitTriangles;
+  uint32_t numPartTriangles;
+  uint32_t numTotalTriangles;
+  uint32_t numTempInstantiations;
+  uint32_t numGenVertices;
+  uint32_t numBlasClusters;
+  uint32_t numTransBuilds;
+  uint32_t numTransPartTriangles;
+  uint32_t numActualTransBuilds;
+  uint32_t numActualTempInstantiations;
+  uint64_t numGenDatas;
+  uint64_t numGenActualDatas;
+  uint32_t numBlasReservedSizes;
+  uint32_t numBlasActualSizes;
+  uint64_t debugU64;
+  uint32_t clusterTriangleId;
+  uint32_t _packedDepth0;
+  uint32_t instanceId;
+  uint32_t _packedDepth1;
+  int32_t  debugI;
+  uint32_t debugUI;
+  uint32_t debugF;
+  uint32_t debugA[64];
+  uint32_t debugB[64];
+  uint32_t debugC[64];
+} tc_Readback;
+
+/* Displacement texture: replaces the reference's `sampler2D displacementTextures[]`
+ * (cluster_classify.comp.glsl:105-107). Sampled bilinearly at mip 0 with REPEAT
+ * addressing and texel centres at (i + 0.5) / width. */
+#define TC_TEXEL_F32 0u
+#define TC_TEXEL_F16 1u
+#define TC_TEXEL_UNORM16 2u
+typedef struct tc_DisplacementTexture {
+  uint64_t texels; /* row-major, width * height texels */
+  uint32_t width;
+  uint32_t height;
+  uint32_t format; /* TC_TEXEL_* */
+  uint32_t _pad;
+} tc_DisplacementTexture;
+
+/* ------------------------------------------------------------------------- */
+/* runtime configuration                                                      */
+/* ------------------------------------------------------------------------- */
+
+/* Buffer capacities. The reference bakes these into the shaders as macros
+ * (src/renderer_raytrace_clusters_tess.cpp:126-131); here they are runtime values. */
+typedef struct tc_caps {
+  uint32_t maxVisibleClusters;      /* MAX_VISIBLE_CLUSTERS */
+  uint32_t maxPartTriangles;        /* MAX_PART_TRIANGLES */
+  uint32_t maxSplitTriangles;       /* MAX_SPLIT_TRIANGLES */
+  uint32_t maxGeneratedClusters;    /* MAX_GENERATED_CLUSTERS */
+  uint32_t maxGeneratedClusterMegs; /* MAX_GENERATED_CLUSTER_MEGS */
+  uint32_t maxGeneratedVertices;    /* MAX_GENERATED_VERTICES */
+  uint32_t splitFactor;             /* TESS_MAX_SPLIT_FACTOR, clamped to [2, 11] */
+  uint32_t _pad;
+} tc_caps;
+
+/* tc_frame_args.flags */
+#define TC_FLAG_CULLING 1u          /* DO_CULLING: invisible instances are not tessellated */
+#define TC_FLAG_FREEZE_VIEWPOS 2u   /* take SceneBuilding.viewPos from viewLast */
+#define TC_FLAG_RASTER_CULL 4u      /* clusters_cull drops clusters (raster semantics) */
+#define TC_FLAG_WRITE_FULLCLUSTERS 8u /* also record accepted full clusters in SceneBuilding.fullClusters */
+
+typedef struct tc_frame_args {
+  uint64_t view;      /* const tc_FrameConstants* (device): this frame */
+  uint64_t viewLast;  /* const tc_FrameConstants* (device): last frame, used for culling */
+  uint64_t instances; /* const tc_RenderInstance* (device) */
+  uint64_t build;     /* tc_SceneBuilding* (device), pointers filled by the caller */
+  uint64_t readback;  /* tc_Readback* (device) */
+  uint64_t textures;  /* const tc_DisplacementTexture* (device), may be 0 */
+  uint32_t numInstances;
+  uint32_t numTextures;
+  uint32_t totalClusters; /* sum of numClusters over all instances (host known) */
+  uint32_t flags;         /* TC_FLAG_* */
+  tc_caps  caps;
+} tc_frame_args;
+
+typedef enum tc_status {
+  TC_OK = 0,
+  TC_ERR_INVALID_ARG = 1,
+  TC_ERR_CAPACITY = 2,      /* a request exceeds what the context was created for */
+  TC_ERR_QUEUE_TIMEOUT = 3, /* a device-side wait gave up (see tc_read_device_errors) */
+  TC_ERR_CUDA = 4,
+  TC_ERR_NOT_INITIALIZED = 5
+} tc_status;
+
+/* device error word bits (tc_read_device_errors) */
+#define TC_DEVERR_LOOKBACK_TIMEOUT 1u   /* a tile waited too long for its predecessor */
+#define TC_DEVERR_BAD_CLUSTER 2u        /* cluster with more than 64 triangles/vertices */
+#define TC_DEVERR_BAD_CONFIG 4u         /* a tess config outside the table */
+#define TC_DEVERR_CAPACITY 8u           /* work beyond the context's scratch sizing was dropped */
+
+/* Launch schedule: block size and tile shape per stage, picked by the autotuner
+ * (vk_tessellated_clusters_gb300/autotune.py) or left at the defaults. */
+typedef struct tc_schedule {
+  uint32_t classifyWarpsPerBlock;   /* clusters per block (one warp each): 2,4,8,16 */
+  uint32_t splitBlockSize;          /* children per tile: 128,256,512 */
+  uint32_t instantiatePartsPerTile; /* part triangles per tile: 16,32,64 */
+  uint32_t instantiateBlockSize;    /* 128,256,512 */
+  uint32_t blocksPerSM;             /* persistent grid = SMs * blocksPerSM */
+  uint32_t _pad[3];
+} tc_schedule;
+
+typedef struct tc_context_desc {
+  uint32_t maxInstances;     /* largest numInstances a frame may use */
+  uint32_t maxTotalClusters; /* largest totalClusters a frame may use */
+  tc_caps  caps;             /* largest capacities a frame may use */
+  int32_t  device;           /* CUDA device ordinal */
+  uint32_t _pad;
+} tc_context_desc;
+
+typedef struct tc_context tc_context;
+
+typedef struct tc_table_info {
+  uint32_t maxSize;        /* 11 */
+  uint32_t maxSizeConfigs; /* 16 */
+  uint32_t numConfigs;     /* 4096 */
+  uint32_t maxVertices;    /* largest config vertex count (78) */
+  uint32_t maxTriangles;   /* largest config triangle count (121) */
+  uint32_t numRawConfigs;  /* 286 */
+  uint64_t deviceTable;    /* address of a device tc_TessellationTable */
+  tc_TessellationTable table; /* host copy of the same struct */
+} tc_table_info;
+
+const char* tc_version(void);
+const char* tc_status_string(tc_status status);
+
+/* Create/destroy a context: uploads nothing yet, allocates the scratch block
+ * sized by desc. Replaces the renderer init step
+ * (src/renderer_raytrace_clusters_tess.cpp:166-310, scratch part only). */
+tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx);
+tc_status tc_context_destroy(tc_context* ctx);
+
+/* Expand the raw tessellation table into the 16^3 lookup (including the
+ * permuted, flipped configs) and upload it.
+ * Replaces TessellationTable::init (src/tessellation_table.cpp:36-100). */
+tc_status tc_table_init(tc_context* ctx, const uint32_t* vertices, uint32_t numVertices, const uint32_t* triangles,
+                        uint32_t numTriangles, const uint16_t* configs, uint32_t numConfigs, uint32_t maxEdgeSegments,
+                        tc_table_info* outInfo);
+/* Per lookup-entry CLAS template addresses/sizes (4096 entries each), as produced
+ * by TessellationTable::initTemplates (src/tessellation_table.cpp:102-404). */
+tc_status tc_table_set_templates(tc_context* ctx, const uint64_t* templateAddresses, const uint32_t* instantiationSizes,
+                                 void* stream);
+
+/* Launch schedule used by the calls below. */
+tc_status tc_set_schedule(tc_context* ctx, const tc_schedule* schedule);
+tc_status tc_get_schedule(const tc_context* ctx, tc_schedule* schedule);
+
+/* ---- whole frame ---------------------------------------------------------- */
+
+/* One frame of the build chain, batched over all instances: one persistent
+ * launch per stage, build_setup fused into the producing kernels.
+ * Replaces RendererRayTraceClustersTess::render's compute part
+ * (src/renderer_raytrace_clusters_tess.cpp:410-692 minus the CLAS/BLAS builds). */
+tc_status tc_frame_build(tc_context* ctx, const tc_frame_args* args, void* stream);
+
+/* Same frame, recorded once into a CUDA graph and replayed. The graph is keyed by
+ * the args; a change of args re-records. */
+tc_status tc_frame_build_graph(tc_context* ctx, const tc_frame_args* args, void* stream);
+
+/* Same frame, with every stage launched once per instance (and per split pass)
+ * from the host: the reference's per-instance dispatch pattern of clusters_cull
+ * (src/renderer_raytrace_clusters_tess.cpp:454-460) applied to all stages.
+ * Output is byte-identical to tc_frame_build. */
+tc_status tc_frame_build_plain(tc_context* ctx, const tc_frame_args* args, void* stream);
+
+/* ---- per stage (same semantics as the reference shader of the same name) --- */
+
+/* Per-frame reset: counters of SceneBuilding zeroed, viewPos set, Readback zeroed,
+ * splitTriangles filled with ~0 (src/renderer_raytrace_clusters_tess.cpp:412-419). */
+tc_status tc_frame_begin(tc_context* ctx, const tc_frame_args* args, void* stream);
+/* shaders/instances_classify.comp.glsl:102-128 */
+tc_status tc_instances_classify(tc_context* ctx, const tc_frame_args* args, void* stream);
+/* shaders/clusters_cull.comp.glsl:112-161 over instances [instanceBegin, instanceEnd) */
+tc_status tc_clusters_cull(tc_context* ctx, const tc_frame_args* args, uint32_t instanceBegin, uint32_t instanceEnd,
+                           void* stream);
+/* shaders/build_setup.comp.glsl:102-265 */
+tc_status tc_build_setup(tc_context* ctx, const tc_frame_args* args, uint32_t mode, void* stream);
+/* shaders/cluster_classify.comp.glsl:150-666 for the visible clusters of
+ * instances [instanceBegin, instanceEnd) */
+tc_status tc_cluster_classify(tc_context* ctx, const tc_frame_args* args, uint32_t instanceBegin, uint32_t instanceEnd,
+                              void* stream);
+/* shaders/triangle_split.comp.glsl:598-632: one pass over the current split level
+ * (SceneBuilding.splitPassStart/End) restricted to instances [instanceBegin, instanceEnd) */
+tc_status tc_triangle_split(tc_context* ctx, const tc_frame_args* args, uint32_t instanceBegin, uint32_t instanceEnd,
+                            void* stream);
+/* shaders/triangle_tess_template_instantiate.comp.glsl:126-373 over all part
+ * triangles (the reference's single indirect dispatch). partBegin must be 0 and
+ * partEnd ~0u; the per-run form below covers sub-ranges. */
+tc_status tc_triangle_instantiate(tc_context* ctx, const tc_frame_args* args, uint32_t partBegin, uint32_t partEnd,
+                                  void* stream);
+/* Same, restricted to one part run (run 0: parts from cluster_classify, run r:
+ * parts from split pass r) and to instances [instanceBegin, instanceEnd).
+ * run = ~0u with the full instance range is the whole list. Launching the runs
+ * in order, and within a run the instances in order, reproduces the batched
+ * output exactly. */
+tc_status tc_triangle_instantiate_run(tc_context* ctx, const tc_frame_args* args, uint32_t run, uint32_t instanceBegin,
+                                      uint32_t instanceEnd, void* stream);
+/* shaders/blas_setup_insertion.comp.glsl:100-116 */
+tc_status tc_blas_setup_insertion(tc_context* ctx, const tc_frame_args* args, void* stream);
+/* shaders/blas_clusters_insert.comp.glsl:97-136 (template instantiations) */
+tc_status tc_blas_clusters_insert(tc_context* ctx, const tc_frame_args* args, void* stream);
+
+/* Number of split passes the host issues for a split factor
+ * (src/renderer_raytrace_clusters_tess.cpp:516-543). */
+uint32_t tc_split_pass_count(uint32_t splitFactor);
+
+/* ---- backward --------------------------------------------------------------- */
+
+/* Gradient targets for one instance: float3 arrays parallel to the instance's
+ * positions / normals (0 = not wanted). */
+typedef struct tc_GradTargets {
+  uint64_t dPositions;
+  uint64_t dNormals;
+} tc_GradTargets;
+
+/* Adjoint of the vertex generation of the last frame built in `args` (full
+ * clusters and part triangles, tessellation decisions held fixed): scatters
+ * dL/d(genVertices) into base positions, base normals and displacement texels.
+ * gradTargets: device tc_GradTargets[numInstances]; gradTexels: device
+ * uint64_t[numTextures] of float arrays (width*height) or 0 entries.
+ * Requires the frame to have been built with TC_FLAG_WRITE_FULLCLUSTERS. */
+tc_status tc_instantiate_backward(tc_context* ctx, const tc_frame_args* args, uint64_t gradVertices,
+                                  uint64_t gradTargets, uint64_t gradTexels, void* stream);
+
+/* ---- diagnostics ------------------------------------------------------------- */
+
+/* Synchronously read (and clear) the device error word. */
+tc_status tc_read_device_errors(tc_context* ctx, uint32_t* outBits, void* stream);
+/* Number of kernel launches issued by this context since creation. */
+uint64_t tc_launch_count(const tc_context* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#ifdef __cplusplus
+static_assert(sizeof(tc_TessTableEntry) == 8, "TessTableEntry");
+static_assert(sizeof(tc_TessellationTable) == 40, "TessellationTable");
+static_assert(sizeof(tc_BBox) == 32, "BBox");
+static_assert(sizeof(tc_Cluster) == 16, "Cluster");
+static_assert(sizeof(tc_RenderInstance) == 192, "RenderInstance");
+static_assert(sizeof(tc_ClusterInfo) == 8, "ClusterInfo_size (shaderio_building.h:68)");
+static_assert(sizeof(tc_TessTriangleInfo) == 24, "TessTriangleInfo_size (shaderio_building.h:92)");
+static_assert(sizeof(tc_ClasBuildInfo) == 64, "ClasBuildInfo");
+static_assert(sizeof(tc_TemplateInstantiateInfo) == 32, "TemplateInstantiateInfo");
+static_assert(sizeof(tc_BlasBuildInfo) == 16, "BlasBuildInfo");
+static_assert(sizeof(tc_SceneBuilding) == 368, "SceneBuilding");
+static_assert(offsetof(tc_SceneBuilding, genClusterDataCounter) == 72, "SceneBuilding layout");
+static_assert(offsetof(tc_SceneBuilding, instanceStates) == 104, "SceneBuilding layout");
+static_assert(offsetof(tc_SceneBuilding, positionTruncateBitCount) == 208, "SceneBuilding layout");
+static_assert(offsetof(tc_SceneBuilding, blasBuildInfos) == 328, "SceneBuilding layout");
+static_assert(offsetof(tc_FrameConstants, viewport) == 496, "FrameConstants layout");
+static_assert(offsetof(tc_FrameConstants, tessRate) == 540, "FrameConstants layout");
+static_assert(offsetof(tc_FrameConstants, nearPlane) == 648, "FrameConstants layout");
+static_assert(offsetof(tc_FrameConstants, hizSizeFactors) == 656, "FrameConstants layout");
+static_assert(sizeof(tc_FrameConstants) == 784, "FrameConstants prefix");
+static_assert(sizeof(tc_Readback) == 880, "Readback");
+static_assert(sizeof(tc_DisplacementTexture) == 24, "DisplacementTexture");
+static_assert(sizeof(tc_frame_args) == 96, "frame args");
+#endif
+
+#endif /* TC_TESSELLATION_H_ */

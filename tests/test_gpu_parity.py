@@ -1,0 +1,154 @@
+"""GPU path (through the C ABI) against the CPU oracle on the same seeded inputs."""
+import numpy as np
+import pytest
+
+from tests.conftest import cuda_available
+from tests.parity import assert_same, max_position_error, scene_diagonal
+from vk_tessellated_clusters_gb300 import layouts as L
+from vk_tessellated_clusters_gb300 import scene as S
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not cuda_available(), reason="needs a CUDA GPU")]
+
+FLAGS = L.FLAG_CULLING | L.FLAG_WRITE_FULLCLUSTERS
+
+
+def small_caps(**kw):
+    caps = L.default_caps(visible_bits=16, part_bits=18, split_bits=14, vertex_bits=21, megs=256)
+    caps.update(kw)
+    return caps
+
+
+def run_both(oracle, scene, cam, caps, flags=FLAGS, mode="batched", cam_last=None):
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    ref_state, runs = oracle.frame(scene, cam, caps, flags, camera_last=cam_last)
+    ref = ref_state.outputs(oracle.entries)
+    pipe = TessellationPipeline(scene, caps, flags)
+    pipe.set_cameras(cam, cam_last)
+    pipe.build(mode)
+    out = pipe.outputs()
+    return pipe, out, ref, ref_state
+
+
+@pytest.fixture(scope="module")
+def icosphere():
+    return S.scene_icosphere()
+
+
+def test_icosphere_batched_bit_exact(oracle, icosphere):
+    pipe, out, ref, ref_state = run_both(oracle, icosphere, S.camera_icosphere(), small_caps())
+    assert pipe.device_errors() == 0
+    assert int(ref["readback"]["numPartTriangles"]) > 10000
+    assert_same(out, ref, "icosphere batched")
+    # spec bar and the error against the FP64 twin
+    ref64 = oracle.vertices_f64(ref_state, len(ref["genVertices"]))
+    err = max_position_error(out["genVertices"], ref64)
+    assert err <= 1e-5 * scene_diagonal(icosphere), err
+    pipe.close()
+
+
+@pytest.mark.parametrize("mode", ["graph", "plain"])
+def test_icosphere_modes_identical(oracle, icosphere, mode):
+    pipe, out, ref, _ = run_both(oracle, icosphere, S.camera_icosphere(), small_caps(), mode=mode)
+    assert pipe.device_errors() == 0
+    assert_same(out, ref, f"icosphere {mode}")
+    pipe.close()
+
+
+def test_close_camera_splits_bit_exact(oracle):
+    """Camera just above the surface at 1 px per segment: factors in the
+    hundreds, several split passes."""
+    sc = S.scene_icosphere(subdivisions=3, map_size=256)
+    cam = S.Camera(eye=(0.0, 0.0, 1.08), center=(0.0, 0.0, 0.0), tess_rate_pixels=1.0, near=0.01, far=10.0)
+    pipe, out, ref, _ = run_both(oracle, sc, cam, small_caps(maxSplitTriangles=1 << 17, maxPartTriangles=1 << 19,
+                                                             maxGeneratedVertices=1 << 23))
+    b = ref["build"]
+    assert int(b["splitWriteCounter"]) > 0 and int(b["splitPass"]) >= 1
+    assert pipe.device_errors() == 0
+    assert_same(out, ref, "close camera")
+    pipe.close()
+
+
+@pytest.mark.parametrize("mode", ["batched", "plain", "graph"])
+def test_batched_scene_culling_bit_exact(oracle, mode):
+    sc = S.scene_batched(num_instances=24, map_size=128)
+    cam = S.camera_orbit(5)
+    last = S.camera_orbit(4)
+    pipe, out, ref, _ = run_both(oracle, sc, cam, small_caps(), mode=mode, cam_last=last)
+    states = ref["instanceStates"]
+    assert (states & L.INSTANCE_VISIBLE_BIT).any() and not (states & L.INSTANCE_VISIBLE_BIT).all()
+    assert pipe.device_errors() == 0
+    assert_same(out, ref, f"batched scene {mode}")
+    pipe.close()
+
+
+@pytest.mark.parametrize("which", ["parts", "splits", "vertices", "clusters", "megs", "visible"])
+def test_capacity_overflow_matches_reference_semantics(oracle, which):
+    """Tiny caps: the reference drops work past each cap and lets the raw
+    counters run on (cluster_classify.comp.glsl:351-360, build_setup.comp.glsl:108-117)."""
+    sc = S.scene_icosphere(subdivisions=3, map_size=128)
+    cam = S.Camera(eye=(0.0, 0.0, 1.3), center=(0.0, 0.0, 0.0), tess_rate_pixels=2.0)
+    kw = {"parts": dict(maxPartTriangles=300), "splits": dict(maxSplitTriangles=40),
+          "vertices": dict(maxGeneratedVertices=5000), "clusters": dict(maxGeneratedClusters=200),
+          "megs": dict(maxGeneratedClusterMegs=0), "visible": dict(maxVisibleClusters=7)}[which]
+    caps = small_caps(**kw)
+    pipe, out, ref, _ = run_both(oracle, sc, cam, caps)
+    assert pipe.device_errors() == 0
+    assert_same(out, ref, f"overflow {which}")
+    pipe.close()
+
+
+def test_split_factor_variants(oracle):
+    sc = S.scene_icosphere(subdivisions=2, map_size=64)
+    cam = S.Camera(eye=(0.0, 0.0, 1.02), center=(0.0, 0.0, 0.0), tess_rate_pixels=1.0)
+    for sf in (2, 5, 11):
+        pipe, out, ref, _ = run_both(oracle, sc, cam, small_caps(splitFactor=sf))
+        assert pipe.device_errors() == 0
+        assert_same(out, ref, f"split factor {sf}")
+        pipe.close()
+
+
+def test_per_stage_entry_points_match_frame(oracle, icosphere):
+    """Driving the stages one by one through the C ABI equals the fused frame."""
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    caps = small_caps()
+    cam = S.camera_icosphere()
+    pipe = TessellationPipeline(icosphere, caps, FLAGS)
+    pipe.set_cameras(cam)
+    pipe.build("batched")
+    want = pipe.outputs()
+    pipe.stage("frame_begin")
+    pipe.stage("instances_classify")
+    pipe.stage("clusters_cull", 0, 1)
+    pipe.stage("build_setup", L.BUILD_SETUP_CLASSIFY)
+    pipe.stage("cluster_classify", 0, 1)
+    pipe.stage("build_setup", L.BUILD_SETUP_SPLIT)
+    passes = pipe.split_passes()
+    for p in range(passes):
+        pipe.stage("triangle_split", 0, 1)
+        if p + 1 < passes:
+            pipe.stage("build_setup", L.BUILD_SETUP_SPLIT_PASS)
+    pipe.stage("build_setup", L.BUILD_SETUP_INSTANTIATE_TESS)
+    pipe.stage("triangle_instantiate", 0, 0xFFFFFFFF)
+    pipe.stage("build_setup", L.BUILD_SETUP_BUILD_BLAS)
+    pipe.stage("blas_setup_insertion")
+    pipe.stage("blas_clusters_insert")
+    got = pipe.outputs()
+    assert pipe.device_errors() == 0
+    assert_same(got, want, "per-stage vs frame")
+    pipe.close()
+
+
+def test_repeated_frames_are_stable(oracle, icosphere):
+    """Scratch reuse across frames (memset or self-clean) leaves no residue."""
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    caps = small_caps()
+    pipe = TessellationPipeline(icosphere, caps, FLAGS)
+    pipe.set_cameras(S.camera_icosphere())
+    outs = []
+    for mode in ("batched", "plain", "batched", "graph", "graph", "plain"):
+        pipe.build(mode)
+        outs.append(pipe.outputs())
+    for o in outs[1:]:
+        assert_same(o, outs[0], "repeat")
+    assert pipe.device_errors() == 0
+    pipe.close()

@@ -1,0 +1,797 @@
+// tc_api.cu — the C ABI (include/tc_tessellation.h): context and scratch
+// management, tessellation table upload, and the frame orchestrations
+// (batched, CUDA-graph replay, per-instance launches).
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "tc_kernels.h"
+#include "tc_stage.cuh"
+
+using namespace tc;
+
+namespace {
+
+constexpr u32 kMaxCounters = 5;
+
+// One look-back slot: state rows for up to kMaxCounters counters, plus the
+// ticket / done / totals words.
+struct SlotPlan
+{
+  size_t stateOffset;  // bytes into the scratch block
+  u32    stride;       // tiles
+  u32    counters;
+  size_t ctrlOffset;  // ticket, done (u32 x2) + totals (u64 x kMaxCounters)
+};
+
+constexpr size_t kCtrlBytes = 8 + 8 * kMaxCounters;
+
+struct Plan
+{
+  // slot indices
+  u32 slotInstances, slotCull, slotClassify, slotSplit0, slotInstantiate, slotBlas;
+  u32 numSlots;
+  std::vector<SlotPlan> slots;
+  size_t frameBytes;  // zeroed once per batched frame (all slots + segment tables)
+  size_t segOffset;   // segment tables (segStart then segEnd)
+  u32    segStride;   // instances
+  u32    segRows;     // runs
+  size_t runOffset;   // run starts (u32 x kMaxRuns+2)
+  size_t instOffset;  // instance cluster prefix (u32 x maxInstances+1)
+  size_t errOffset;   // device error word
+  size_t totalBytes;
+};
+
+u32 ceil_div(u64 a, u64 b) { return (u32)((a + b - 1) / b); }
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+struct tc_context
+{
+  int             device   = 0;
+  u32             numSMs   = 0;
+  tc_context_desc desc     = {};
+  tc_schedule     schedule = {};
+  uint64_t        launches = 0;
+
+  // tessellation table
+  bool                  tableReady = false;
+  u32*                  dVertices  = nullptr;
+  u32*                  dTriangles = nullptr;
+  tc_TessTableEntry*    dEntries   = nullptr;
+  u64*                  dTemplateAddresses = nullptr;
+  u32*                  dTemplateSizes     = nullptr;
+  tc_TessellationTable* dTable             = nullptr;
+  tc_TessellationTable  hTable             = {};
+
+  // scratch
+  Plan     plan;
+  uint8_t* dScratch = nullptr;
+
+  // graph cache
+  cudaGraphExec_t graphExec = nullptr;
+  cudaGraph_t     graph     = nullptr;
+  tc_frame_args   graphArgs = {};
+  tc_schedule     graphSchedule = {};
+  bool            graphValid = false;
+
+  std::mutex mutex;
+};
+
+namespace {
+
+#define TC_CHECK_CUDA(expr)                                                                                            \
+  do                                                                                                                   \
+  {                                                                                                                    \
+    cudaError_t _e = (expr);                                                                                           \
+    if(_e != cudaSuccess)                                                                                              \
+      return TC_ERR_CUDA;                                                                                              \
+  } while(0)
+
+u32 clamp_sf(u32 sf) { return std::max(2u, std::min(sf, TC_TESSTABLE_SIZE)); }
+
+u32 split_passes(u32 splitFactor)
+{
+  u32 sf = clamp_sf(splitFactor), n = 0, coord = TC_TESSTABLE_COORD_MAX;
+  while(coord > sf)
+  {
+    coord /= sf;
+    n++;
+  }
+  return n;
+}
+
+Plan make_plan(const tc_context_desc& d)
+{
+  Plan p;
+  const tc_caps& k     = d.caps;
+  const u32      passes = split_passes(2);  // worst case number of split passes
+  auto add = [&](u32 stride, u32 counters) {
+    SlotPlan s;
+    s.stride   = std::max(1u, stride);
+    s.counters = counters;
+    p.slots.push_back(s);
+    return (u32)p.slots.size() - 1;
+  };
+  p.slotInstances   = add(ceil_div(d.maxInstances, kInstanceTile), 1);
+  p.slotCull        = add(ceil_div(d.maxTotalClusters, kCullTile), 1);
+  p.slotClassify    = add(ceil_div(std::min<u64>(k.maxVisibleClusters, d.maxTotalClusters), kClassifyMinWarps), kMaxCounters);
+  p.slotSplit0      = add(ceil_div(k.maxSplitTriangles, kSplitMinItems), 2);
+  for(u32 i = 1; i < passes; i++)
+    add(ceil_div(k.maxSplitTriangles, kSplitMinItems), 2);
+  p.slotInstantiate = add(ceil_div(k.maxPartTriangles, kInstantiateTile), 3);
+  p.slotBlas        = add(ceil_div(d.maxInstances, kInstanceTile), 1);
+  p.numSlots        = (u32)p.slots.size();
+  size_t off        = 0;
+  for(SlotPlan& s : p.slots)
+  {
+    s.stateOffset = off;
+    off           = align_up(off + (size_t)s.stride * s.counters * 8, 256);
+    s.ctrlOffset  = off;
+    off           = align_up(off + kCtrlBytes, 256);
+  }
+  p.segStride = std::max(1u, d.maxInstances);
+  p.segRows   = kMaxRuns + 1;
+  p.segOffset = off;
+  off         = align_up(off + (size_t)p.segStride * p.segRows * 4 * 2, 256);
+  p.frameBytes = off;
+  p.runOffset  = off;
+  off          = align_up(off + 4 * (kMaxRuns + 2), 256);
+  p.instOffset = off;
+  off          = align_up(off + 4 * ((size_t)d.maxInstances + 1), 256);
+  p.errOffset  = off;
+  off          = align_up(off + 4, 256);
+  p.totalBytes = off;
+  return p;
+}
+
+bool caps_fit(const tc_caps& want, const tc_caps& have)
+{
+  return want.maxVisibleClusters <= have.maxVisibleClusters && want.maxPartTriangles <= have.maxPartTriangles
+         && want.maxSplitTriangles <= have.maxSplitTriangles;
+}
+
+tc_status validate(const tc_context* ctx, const tc_frame_args* a)
+{
+  if(!ctx || !a)
+    return TC_ERR_INVALID_ARG;
+  if(!ctx->tableReady)
+    return TC_ERR_NOT_INITIALIZED;
+  if(!a->view || !a->viewLast || !a->instances || !a->build || !a->readback)
+    return TC_ERR_INVALID_ARG;
+  if(a->numTextures && !a->textures)
+    return TC_ERR_INVALID_ARG;
+  if(a->numInstances > ctx->desc.maxInstances || a->totalClusters > ctx->desc.maxTotalClusters)
+    return TC_ERR_CAPACITY;
+  if(!caps_fit(a->caps, ctx->desc.caps))
+    return TC_ERR_CAPACITY;
+  if(a->caps.splitFactor < 2 || a->caps.splitFactor > TC_TESSTABLE_SIZE)
+    return TC_ERR_INVALID_ARG;
+  return TC_OK;
+}
+
+StageCtx base_ctx(tc_context* ctx, const tc_frame_args* a)
+{
+  StageCtx c;
+  std::memset(&c, 0, sizeof(c));
+  c.view                    = reinterpret_cast<const tc_FrameConstants*>(a->view);
+  c.viewLast                = reinterpret_cast<const tc_FrameConstants*>(a->viewLast);
+  c.instances               = reinterpret_cast<const tc_RenderInstance*>(a->instances);
+  c.build                   = reinterpret_cast<tc_SceneBuilding*>(a->build);
+  c.readback                = reinterpret_cast<tc_Readback*>(a->readback);
+  c.textures                = reinterpret_cast<const tc_DisplacementTexture*>(a->textures);
+  c.numInstances            = a->numInstances;
+  c.numTextures             = a->numTextures;
+  c.flags                   = a->flags;
+  c.table.entries           = ctx->dEntries;
+  c.table.vertices          = ctx->dVertices;
+  c.table.triangles         = ctx->dTriangles;
+  c.table.templateAddresses = ctx->dTemplateAddresses;
+  c.table.templateSizes     = ctx->dTemplateSizes;
+  c.caps                    = a->caps;
+  c.errorWord               = reinterpret_cast<u32*>(ctx->dScratch + ctx->plan.errOffset);
+  c.runStarts               = reinterpret_cast<u32*>(ctx->dScratch + ctx->plan.runOffset);
+  c.instClusterStart        = reinterpret_cast<u32*>(ctx->dScratch + ctx->plan.instOffset);
+  c.instBegin               = 0;
+  c.instEnd                 = a->numInstances;
+  c.fuseSetup               = kNoSetup;
+  c.run                     = kAllRuns;
+  return c;
+}
+
+void bind_slot(tc_context* ctx, StageCtx& c, u32 slot, bool selfClean)
+{
+  const SlotPlan& s   = ctx->plan.slots[slot];
+  c.scratch.lbState   = reinterpret_cast<u64*>(ctx->dScratch + s.stateOffset);
+  c.scratch.lbStride  = s.stride;
+  c.scratch.selfClean = selfClean ? 1u : 0u;
+  c.scratch.ticket    = reinterpret_cast<u32*>(ctx->dScratch + s.ctrlOffset);
+  c.scratch.done      = reinterpret_cast<u32*>(ctx->dScratch + s.ctrlOffset + 4);
+  c.scratch.totals    = reinterpret_cast<u64*>(ctx->dScratch + s.ctrlOffset + 8);
+}
+
+u32 persistent_grid(const tc_context* ctx, u32 maxTiles, u32 blocksPerSM)
+{
+  u32 g = ctx->numSMs * std::max(1u, blocksPerSM);
+  return std::max(1u, std::min(g, std::max(1u, maxTiles)));
+}
+
+u32 frame_begin_grid(const tc_context* ctx, const tc_frame_args* a)
+{
+  return std::max(1u, std::min(ctx->numSMs * 2, ceil_div((u64)a->caps.maxSplitTriangles * 6, 256)));
+}
+
+u32 classify_warps(const tc_schedule& s)
+{
+  u32 w = s.classifyWarpsPerBlock;
+  return (w == 2 || w == 4 || w == 8 || w == 16) ? w : 8;
+}
+u32 split_block(const tc_schedule& s)
+{
+  u32 b = s.splitBlockSize;
+  return (b == 128 || b == 256 || b == 512) ? b : 256;
+}
+u32 inst_block(const tc_schedule& s)
+{
+  u32 b = s.instantiateBlockSize;
+  return (b == 128 || b == 256 || b == 512) ? b : 256;
+}
+u32 split_items_per_tile(u32 block) { return block == 128 ? 16 : 32; }
+
+// The batched frame: one persistent launch per stage, build_setup fused into the
+// producers' last block. Graph-capturable (no host synchronisation, no allocation).
+tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStream_t s)
+{
+  const Plan&        p     = ctx->plan;
+  const tc_schedule& sched = ctx->schedule;
+  const u32          bpsm  = std::max(1u, sched.blocksPerSM);
+  TC_CHECK_CUDA(cudaMemsetAsync(ctx->dScratch, 0, p.frameBytes, s));
+
+  StageCtx c = base_ctx(ctx, a);
+  TC_CHECK_CUDA(launch_frame_begin(c, frame_begin_grid(ctx, a), s));
+
+  bind_slot(ctx, c, p.slotInstances, false);
+  TC_CHECK_CUDA(launch_instances_classify(c, std::max(1u, ceil_div(a->numInstances, kInstanceTile)), kInstanceTile, s));
+
+  bind_slot(ctx, c, p.slotCull, false);
+  c.fuseSetup = TC_BUILD_SETUP_CLASSIFY;
+  TC_CHECK_CUDA(launch_clusters_cull(c, persistent_grid(ctx, ceil_div(a->totalClusters, kCullTile), 4), kCullTile, s));
+
+  const u32 W = classify_warps(sched);
+  bind_slot(ctx, c, p.slotClassify, false);
+  c.fuseSetup = TC_BUILD_SETUP_SPLIT;
+  TC_CHECK_CUDA(launch_cluster_classify(
+      c, W, persistent_grid(ctx, ceil_div(std::min(a->totalClusters, a->caps.maxVisibleClusters), W), bpsm * (16 / W)), s));
+
+  const u32 passes = split_passes(a->caps.splitFactor);
+  const u32 sb     = split_block(sched);
+  for(u32 q = 0; q < passes; q++)
+  {
+    bind_slot(ctx, c, p.slotSplit0 + q, false);
+    c.fuseSetup = (q + 1 < passes) ? TC_BUILD_SETUP_SPLIT_PASS : TC_BUILD_SETUP_INSTANTIATE_TESS;
+    TC_CHECK_CUDA(launch_triangle_split(
+        c, sb, persistent_grid(ctx, ceil_div(a->caps.maxSplitTriangles, split_items_per_tile(sb)), bpsm * (512 / sb)), s));
+  }
+
+  const u32 ib = inst_block(sched);
+  bind_slot(ctx, c, p.slotInstantiate, false);
+  c.fuseSetup = TC_BUILD_SETUP_BUILD_BLAS;
+  TC_CHECK_CUDA(launch_triangle_instantiate(
+      c, ib, persistent_grid(ctx, ceil_div(a->caps.maxPartTriangles, kInstantiateTile), bpsm * (512 / ib)), s));
+
+  bind_slot(ctx, c, p.slotBlas, false);
+  c.fuseSetup = kNoSetup;
+  TC_CHECK_CUDA(launch_blas_setup_insertion(c, std::max(1u, ceil_div(a->numInstances, kInstanceTile)), kInstanceTile, s));
+
+  u32* seg = reinterpret_cast<u32*>(ctx->dScratch + p.segOffset);
+  TC_CHECK_CUDA(launch_blas_clusters_insert(c, seg, seg + (size_t)p.segStride * p.segRows, p.segStride, ctx->numSMs * 4, s));
+
+  ctx->launches += 9 + passes;
+  return TC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tc_version(void) { return "vk_tessellated_clusters_gb300 1.0 (sm_103a)"; }
+
+const char* tc_status_string(tc_status s)
+{
+  switch(s)
+  {
+    case TC_OK:
+      return "ok";
+    case TC_ERR_INVALID_ARG:
+      return "invalid argument";
+    case TC_ERR_CAPACITY:
+      return "request exceeds the context's capacity";
+    case TC_ERR_QUEUE_TIMEOUT:
+      return "device-side wait timed out";
+    case TC_ERR_CUDA:
+      return "CUDA error";
+    case TC_ERR_NOT_INITIALIZED:
+      return "tessellation table not initialised";
+  }
+  return "unknown";
+}
+
+uint32_t tc_split_pass_count(uint32_t splitFactor) { return split_passes(splitFactor); }
+
+tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
+{
+  if(!desc || !outCtx)
+    return TC_ERR_INVALID_ARG;
+  *outCtx = nullptr;
+  if(desc->caps.maxPartTriangles == 0 || desc->caps.maxSplitTriangles == 0 || desc->caps.maxVisibleClusters == 0)
+    return TC_ERR_INVALID_ARG;
+  tc_context* ctx = new(std::nothrow) tc_context();
+  if(!ctx)
+    return TC_ERR_INVALID_ARG;
+  ctx->device = desc->device;
+  ctx->desc   = *desc;
+  if(cudaSetDevice(desc->device) != cudaSuccess)
+  {
+    delete ctx;
+    return TC_ERR_CUDA;
+  }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, desc->device);
+  ctx->numSMs   = (u32)std::max(1, sms);
+  ctx->schedule = {8, 256, 32, 256, 4, {0, 0, 0}};
+  ctx->plan     = make_plan(*desc);
+  if(cudaMalloc(&ctx->dScratch, ctx->plan.totalBytes) != cudaSuccess
+     || cudaMemset(ctx->dScratch, 0, ctx->plan.totalBytes) != cudaSuccess)
+  {
+    cudaFree(ctx->dScratch);
+    delete ctx;
+    return TC_ERR_CUDA;
+  }
+  *outCtx = ctx;
+  return TC_OK;
+}
+
+tc_status tc_context_destroy(tc_context* ctx)
+{
+  if(!ctx)
+    return TC_ERR_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  if(ctx->graphExec)
+    cudaGraphExecDestroy(ctx->graphExec);
+  if(ctx->graph)
+    cudaGraphDestroy(ctx->graph);
+  cudaFree(ctx->dVertices);
+  cudaFree(ctx->dTriangles);
+  cudaFree(ctx->dEntries);
+  cudaFree(ctx->dTemplateAddresses);
+  cudaFree(ctx->dTemplateSizes);
+  cudaFree(ctx->dTable);
+  cudaFree(ctx->dScratch);
+  delete ctx;
+  return TC_OK;
+}
+
+// src/tessellation_table.cpp:36-100
+tc_status tc_table_init(tc_context* ctx, const uint32_t* vertices, uint32_t numVertices, const uint32_t* triangles,
+                        uint32_t numTriangles, const uint16_t* configs, uint32_t numConfigs, uint32_t maxEdgeSegments,
+                        tc_table_info* outInfo)
+{
+  if(!ctx || !vertices || !triangles || !configs)
+    return TC_ERR_INVALID_ARG;
+  if(maxEdgeSegments != TC_TESSTABLE_SIZE)
+    return TC_ERR_INVALID_ARG;
+  const u32 L = TC_TESSTABLE_LOOKUP_SIZE;
+  std::vector<tc_TessTableEntry> lookup(TC_TESSTABLE_LOOKUP_ENTRIES);
+  std::memset(lookup.data(), 0, lookup.size() * sizeof(tc_TessTableEntry));
+  auto idx = [&](u32 x, u32 y, u32 z) { return x + y * L + z * L * L - (1 + L + L * L); };
+  u32 ci = 0, maxV = 0, maxT = 0;
+  for(u32 x = 1; x <= maxEdgeSegments; x++)
+    for(u32 y = 1; y <= x; y++)
+      for(u32 z = 1; z <= y; z++, ci++)
+      {
+        if(ci >= numConfigs)
+          return TC_ERR_INVALID_ARG;
+        tc_TessTableEntry e = {configs[ci * 4 + 0], configs[ci * 4 + 1], configs[ci * 4 + 2], configs[ci * 4 + 3]};
+        // every config must stay inside the raw arrays and the per-config limits
+        // (TESSTABLE_MAX_TRIANGLES / TESSTABLE_MAX_VERTICES, shaderio_scene.h:43-49)
+        if((u32)e.firstTriangle + e.numTriangles > numTriangles || (u32)e.firstVertex + e.numVertices > numVertices
+           || e.numTriangles > TC_TESSTABLE_SIZE * TC_TESSTABLE_SIZE
+           || e.numVertices > ((TC_TESSTABLE_SIZE + 1) * (TC_TESSTABLE_SIZE + 2)) / 2)
+          return TC_ERR_INVALID_ARG;
+        lookup[idx(x, y, z)] = e;
+        if(z != y && x > 1)
+          lookup[idx(x, z, y)] = e;
+        maxT = std::max(maxT, (u32)e.numTriangles);
+        maxV = std::max(maxV, (u32)e.numVertices);
+      }
+  if(ci != numConfigs)
+    return TC_ERR_INVALID_ARG;
+  for(u32 t = 0; t < numTriangles; t++)
+  {
+    const u32 p = triangles[t];
+    // indices are relative to a config's first vertex; a config has at most 78 vertices
+    if((p & 0xFF) >= 78 || ((p >> 8) & 0xFF) >= 78 || ((p >> 16) & 0xFF) >= 78)
+      return TC_ERR_INVALID_ARG;
+  }
+
+  std::lock_guard<std::mutex> lock(ctx->mutex);
+  TC_CHECK_CUDA(cudaSetDevice(ctx->device));
+  cudaFree(ctx->dVertices);
+  cudaFree(ctx->dTriangles);
+  cudaFree(ctx->dEntries);
+  cudaFree(ctx->dTemplateAddresses);
+  cudaFree(ctx->dTemplateSizes);
+  cudaFree(ctx->dTable);
+  ctx->dVertices = nullptr;
+  ctx->dTriangles = nullptr;
+  ctx->dEntries = nullptr;
+  ctx->dTemplateAddresses = nullptr;
+  ctx->dTemplateSizes = nullptr;
+  ctx->dTable = nullptr;
+  TC_CHECK_CUDA(cudaMalloc(&ctx->dVertices, sizeof(u32) * numVertices));
+  TC_CHECK_CUDA(cudaMalloc(&ctx->dTriangles, sizeof(u32) * numTriangles));
+  TC_CHECK_CUDA(cudaMalloc(&ctx->dEntries, sizeof(tc_TessTableEntry) * TC_TESSTABLE_LOOKUP_ENTRIES));
+  TC_CHECK_CUDA(cudaMalloc(&ctx->dTemplateAddresses, sizeof(u64) * TC_TESSTABLE_LOOKUP_ENTRIES));
+  TC_CHECK_CUDA(cudaMalloc(&ctx->dTemplateSizes, sizeof(u32) * TC_TESSTABLE_LOOKUP_ENTRIES));
+  TC_CHECK_CUDA(cudaMalloc(&ctx->dTable, sizeof(tc_TessellationTable)));
+  TC_CHECK_CUDA(cudaMemcpy(ctx->dVertices, vertices, sizeof(u32) * numVertices, cudaMemcpyHostToDevice));
+  TC_CHECK_CUDA(cudaMemcpy(ctx->dTriangles, triangles, sizeof(u32) * numTriangles, cudaMemcpyHostToDevice));
+  TC_CHECK_CUDA(cudaMemcpy(ctx->dEntries, lookup.data(), sizeof(tc_TessTableEntry) * TC_TESSTABLE_LOOKUP_ENTRIES,
+                           cudaMemcpyHostToDevice));
+  TC_CHECK_CUDA(cudaMemset(ctx->dTemplateAddresses, 0, sizeof(u64) * TC_TESSTABLE_LOOKUP_ENTRIES));
+  TC_CHECK_CUDA(cudaMemset(ctx->dTemplateSizes, 0, sizeof(u32) * TC_TESSTABLE_LOOKUP_ENTRIES));
+  ctx->hTable.vertices                   = (uint64_t)(uintptr_t)ctx->dVertices;
+  ctx->hTable.triangles                  = (uint64_t)(uintptr_t)ctx->dTriangles;
+  ctx->hTable.entries                    = (uint64_t)(uintptr_t)ctx->dEntries;
+  ctx->hTable.templateAddresses          = (uint64_t)(uintptr_t)ctx->dTemplateAddresses;
+  ctx->hTable.templateInstantiationSizes = (uint64_t)(uintptr_t)ctx->dTemplateSizes;
+  TC_CHECK_CUDA(cudaMemcpy(ctx->dTable, &ctx->hTable, sizeof(tc_TessellationTable), cudaMemcpyHostToDevice));
+  ctx->tableReady = true;
+  ctx->graphValid = false;
+  if(outInfo)
+  {
+    outInfo->maxSize        = maxEdgeSegments;
+    outInfo->maxSizeConfigs = L;
+    outInfo->numConfigs     = TC_TESSTABLE_LOOKUP_ENTRIES;
+    outInfo->maxVertices    = maxV;
+    outInfo->maxTriangles   = maxT;
+    outInfo->numRawConfigs  = numConfigs;
+    outInfo->deviceTable    = (uint64_t)(uintptr_t)ctx->dTable;
+    outInfo->table          = ctx->hTable;
+  }
+  return TC_OK;
+}
+
+tc_status tc_table_set_templates(tc_context* ctx, const uint64_t* templateAddresses, const uint32_t* instantiationSizes,
+                                 void* stream)
+{
+  if(!ctx)
+    return TC_ERR_INVALID_ARG;
+  if(!ctx->tableReady)
+    return TC_ERR_NOT_INITIALIZED;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if(templateAddresses)
+    TC_CHECK_CUDA(cudaMemcpyAsync(ctx->dTemplateAddresses, templateAddresses, sizeof(u64) * TC_TESSTABLE_LOOKUP_ENTRIES,
+                                  cudaMemcpyHostToDevice, s));
+  if(instantiationSizes)
+    TC_CHECK_CUDA(cudaMemcpyAsync(ctx->dTemplateSizes, instantiationSizes, sizeof(u32) * TC_TESSTABLE_LOOKUP_ENTRIES,
+                                  cudaMemcpyHostToDevice, s));
+  TC_CHECK_CUDA(cudaStreamSynchronize(s));
+  return TC_OK;
+}
+
+tc_status tc_set_schedule(tc_context* ctx, const tc_schedule* schedule)
+{
+  if(!ctx || !schedule)
+    return TC_ERR_INVALID_ARG;
+  ctx->schedule   = *schedule;
+  ctx->graphValid = false;
+  return TC_OK;
+}
+
+tc_status tc_get_schedule(const tc_context* ctx, tc_schedule* schedule)
+{
+  if(!ctx || !schedule)
+    return TC_ERR_INVALID_ARG;
+  *schedule = ctx->schedule;
+  return TC_OK;
+}
+
+tc_status tc_frame_build(tc_context* ctx, const tc_frame_args* args, void* stream)
+{
+  tc_status st = validate(ctx, args);
+  if(st != TC_OK)
+    return st;
+  return record_batched_frame(ctx, args, reinterpret_cast<cudaStream_t>(stream));
+}
+
+tc_status tc_frame_build_graph(tc_context* ctx, const tc_frame_args* args, void* stream)
+{
+  tc_status st = validate(ctx, args);
+  if(st != TC_OK)
+    return st;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if(!ctx->graphValid || std::memcmp(&ctx->graphArgs, args, sizeof(tc_frame_args)) != 0
+     || std::memcmp(&ctx->graphSchedule, &ctx->schedule, sizeof(tc_schedule)) != 0)
+  {
+    if(ctx->graphExec)
+      cudaGraphExecDestroy(ctx->graphExec);
+    if(ctx->graph)
+      cudaGraphDestroy(ctx->graph);
+    ctx->graphExec  = nullptr;
+    ctx->graph      = nullptr;
+    ctx->graphValid = false;
+    // capture on a private stream so the caller's stream may be the legacy default stream
+    cudaStream_t cap;
+    TC_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    uint64_t launchesBefore = ctx->launches;
+    if(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    {
+      cudaStreamDestroy(cap);
+      return TC_ERR_CUDA;
+    }
+    tc_status rst = record_batched_frame(ctx, args, cap);
+    cudaGraph_t g  = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    ctx->launches = launchesBefore;
+    if(rst != TC_OK)
+    {
+      if(g)
+        cudaGraphDestroy(g);
+      return rst;
+    }
+    if(ce != cudaSuccess)
+      return TC_ERR_CUDA;
+    ctx->graph = g;
+    TC_CHECK_CUDA(cudaGraphInstantiate(&ctx->graphExec, g, 0));
+    ctx->graphArgs     = *args;
+    ctx->graphSchedule = ctx->schedule;
+    ctx->graphValid    = true;
+  }
+  TC_CHECK_CUDA(cudaGraphLaunch(ctx->graphExec, s));
+  ctx->launches += 9 + split_passes(args->caps.splitFactor);
+  return TC_OK;
+}
+
+tc_status tc_frame_begin(tc_context* ctx, const tc_frame_args* a, void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  TC_CHECK_CUDA(cudaMemsetAsync(ctx->dScratch, 0, ctx->plan.frameBytes, s));
+  StageCtx c = base_ctx(ctx, a);
+  TC_CHECK_CUDA(launch_frame_begin(c, frame_begin_grid(ctx, a), s));
+  ctx->launches += 1;
+  return TC_OK;
+}
+
+tc_status tc_instances_classify(tc_context* ctx, const tc_frame_args* a, void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  StageCtx c = base_ctx(ctx, a);
+  bind_slot(ctx, c, ctx->plan.slotInstances, true);
+  TC_CHECK_CUDA(launch_instances_classify(c, std::max(1u, ceil_div(a->numInstances, kInstanceTile)), kInstanceTile,
+                                          reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += 1;
+  return TC_OK;
+}
+
+tc_status tc_clusters_cull(tc_context* ctx, const tc_frame_args* a, uint32_t instanceBegin, uint32_t instanceEnd,
+                           void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  if(instanceBegin > instanceEnd || instanceEnd > a->numInstances)
+    return TC_ERR_INVALID_ARG;
+  StageCtx c  = base_ctx(ctx, a);
+  c.instBegin = instanceBegin;
+  c.instEnd   = instanceEnd;
+  bind_slot(ctx, c, ctx->plan.slotCull, true);
+  TC_CHECK_CUDA(launch_clusters_cull(c, persistent_grid(ctx, ceil_div(a->totalClusters, kCullTile), 2), kCullTile,
+                                     reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += 1;
+  return TC_OK;
+}
+
+tc_status tc_build_setup(tc_context* ctx, const tc_frame_args* a, uint32_t mode, void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  if(mode > TC_BUILD_SETUP_BUILD_BLAS)
+    return TC_ERR_INVALID_ARG;
+  StageCtx c = base_ctx(ctx, a);
+  TC_CHECK_CUDA(launch_build_setup(c, mode, reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += 1;
+  return TC_OK;
+}
+
+tc_status tc_cluster_classify(tc_context* ctx, const tc_frame_args* a, uint32_t instanceBegin, uint32_t instanceEnd,
+                              void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  if(instanceBegin > instanceEnd || instanceEnd > a->numInstances)
+    return TC_ERR_INVALID_ARG;
+  StageCtx c  = base_ctx(ctx, a);
+  c.instBegin = instanceBegin;
+  c.instEnd   = instanceEnd;
+  bind_slot(ctx, c, ctx->plan.slotClassify, true);
+  const u32 W = classify_warps(ctx->schedule);
+  TC_CHECK_CUDA(launch_cluster_classify(c, W,
+                                        persistent_grid(ctx, ceil_div(std::min(a->totalClusters, a->caps.maxVisibleClusters), W),
+                                                        std::max(1u, ctx->schedule.blocksPerSM) * (16 / W)),
+                                        reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += 1;
+  return TC_OK;
+}
+
+tc_status tc_triangle_split(tc_context* ctx, const tc_frame_args* a, uint32_t instanceBegin, uint32_t instanceEnd,
+                            void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  if(instanceBegin > instanceEnd || instanceEnd > a->numInstances)
+    return TC_ERR_INVALID_ARG;
+  StageCtx c  = base_ctx(ctx, a);
+  c.instBegin = instanceBegin;
+  c.instEnd   = instanceEnd;
+  bind_slot(ctx, c, ctx->plan.slotSplit0, true);
+  const u32 sb = split_block(ctx->schedule);
+  TC_CHECK_CUDA(launch_triangle_split(c, sb,
+                                      persistent_grid(ctx, ceil_div(a->caps.maxSplitTriangles, split_items_per_tile(sb)),
+                                                      std::max(1u, ctx->schedule.blocksPerSM) * (512 / sb)),
+                                      reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += 1;
+  return TC_OK;
+}
+
+tc_status tc_triangle_instantiate_run(tc_context* ctx, const tc_frame_args* a, uint32_t run, uint32_t instanceBegin,
+                                      uint32_t instanceEnd, void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  if(instanceBegin > instanceEnd || instanceEnd > a->numInstances || (run != kAllRuns && run >= kMaxRuns))
+    return TC_ERR_INVALID_ARG;
+  if(run == kAllRuns && !(instanceBegin == 0 && instanceEnd == a->numInstances))
+    return TC_ERR_INVALID_ARG;  // part triangles are only instance-sorted within a run
+  StageCtx c  = base_ctx(ctx, a);
+  c.instBegin = instanceBegin;
+  c.instEnd   = instanceEnd;
+  c.run       = run;
+  bind_slot(ctx, c, ctx->plan.slotInstantiate, true);
+  const u32 ib = inst_block(ctx->schedule);
+  TC_CHECK_CUDA(launch_triangle_instantiate(c, ib,
+                                            persistent_grid(ctx, ceil_div(a->caps.maxPartTriangles, kInstantiateTile),
+                                                            std::max(1u, ctx->schedule.blocksPerSM) * (512 / ib)),
+                                            reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += 1;
+  return TC_OK;
+}
+
+tc_status tc_triangle_instantiate(tc_context* ctx, const tc_frame_args* a, uint32_t partBegin, uint32_t partEnd,
+                                  void* stream)
+{
+  // whole part list only (the per-run form is tc_triangle_instantiate_run)
+  if(partBegin != 0 || partEnd != 0xFFFFFFFFu)
+    return TC_ERR_INVALID_ARG;
+  return tc_triangle_instantiate_run(ctx, a, kAllRuns, 0, a ? a->numInstances : 0, stream);
+}
+
+tc_status tc_blas_setup_insertion(tc_context* ctx, const tc_frame_args* a, void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  StageCtx c = base_ctx(ctx, a);
+  bind_slot(ctx, c, ctx->plan.slotBlas, true);
+  TC_CHECK_CUDA(launch_blas_setup_insertion(c, std::max(1u, ceil_div(a->numInstances, kInstanceTile)), kInstanceTile,
+                                            reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += 1;
+  return TC_OK;
+}
+
+tc_status tc_blas_clusters_insert(tc_context* ctx, const tc_frame_args* a, void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const Plan&  p = ctx->plan;
+  u32*         seg = reinterpret_cast<u32*>(ctx->dScratch + p.segOffset);
+  TC_CHECK_CUDA(cudaMemsetAsync(seg, 0, (size_t)p.segStride * p.segRows * 4 * 2, s));
+  StageCtx c = base_ctx(ctx, a);
+  TC_CHECK_CUDA(launch_blas_clusters_insert(c, seg, seg + (size_t)p.segStride * p.segRows, p.segStride, ctx->numSMs * 4, s));
+  ctx->launches += 2;
+  return TC_OK;
+}
+
+// Per-instance launches of every stage, level by level, separate build_setup
+// launches in between (the reference's per-instance clusters_cull dispatch,
+// src/renderer_raytrace_clusters_tess.cpp:454-460, applied to every stage).
+tc_status tc_frame_build_plain(tc_context* ctx, const tc_frame_args* a, void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+#define TC_TRY(x)                                                                                                      \
+  do                                                                                                                   \
+  {                                                                                                                    \
+    tc_status _s = (x);                                                                                                \
+    if(_s != TC_OK)                                                                                                    \
+      return _s;                                                                                                       \
+  } while(0)
+  const u32 n = a->numInstances;
+  TC_TRY(tc_frame_begin(ctx, a, stream));
+  TC_TRY(tc_instances_classify(ctx, a, stream));
+  for(u32 i = 0; i < n; i++)
+    TC_TRY(tc_clusters_cull(ctx, a, i, i + 1, stream));
+  TC_TRY(tc_build_setup(ctx, a, TC_BUILD_SETUP_CLASSIFY, stream));
+  for(u32 i = 0; i < n; i++)
+    TC_TRY(tc_cluster_classify(ctx, a, i, i + 1, stream));
+  TC_TRY(tc_build_setup(ctx, a, TC_BUILD_SETUP_SPLIT, stream));
+  const u32 passes = split_passes(a->caps.splitFactor);
+  for(u32 q = 0; q < passes; q++)
+  {
+    for(u32 i = 0; i < n; i++)
+      TC_TRY(tc_triangle_split(ctx, a, i, i + 1, stream));
+    if(q + 1 < passes)
+      TC_TRY(tc_build_setup(ctx, a, TC_BUILD_SETUP_SPLIT_PASS, stream));
+  }
+  TC_TRY(tc_build_setup(ctx, a, TC_BUILD_SETUP_INSTANTIATE_TESS, stream));
+  for(u32 r = 0; r <= passes && r < kMaxRuns; r++)
+    for(u32 i = 0; i < n; i++)
+      TC_TRY(tc_triangle_instantiate_run(ctx, a, r, i, i + 1, stream));
+  TC_TRY(tc_build_setup(ctx, a, TC_BUILD_SETUP_BUILD_BLAS, stream));
+  TC_TRY(tc_blas_setup_insertion(ctx, a, stream));
+  TC_TRY(tc_blas_clusters_insert(ctx, a, stream));
+#undef TC_TRY
+  return TC_OK;
+}
+
+tc_status tc_instantiate_backward(tc_context* ctx, const tc_frame_args* a, uint64_t gradVertices, uint64_t gradTargets,
+                                  uint64_t gradTexels, void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  if(!gradVertices || !gradTargets || (a->numTextures && !gradTexels))
+    return TC_ERR_INVALID_ARG;
+  if(!(a->flags & TC_FLAG_WRITE_FULLCLUSTERS))
+    return TC_ERR_INVALID_ARG;
+  StageCtx c = base_ctx(ctx, a);
+  TC_CHECK_CUDA(launch_instantiate_backward(c, reinterpret_cast<const float*>(gradVertices),
+                                            reinterpret_cast<const tc_GradTargets*>(gradTargets),
+                                            reinterpret_cast<float* const*>(gradTexels), ctx->numSMs * 8,
+                                            reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += 1;
+  return TC_OK;
+}
+
+tc_status tc_read_device_errors(tc_context* ctx, uint32_t* outBits, void* stream)
+{
+  if(!ctx || !outBits)
+    return TC_ERR_INVALID_ARG;
+  cudaStream_t s   = reinterpret_cast<cudaStream_t>(stream);
+  u32*         err = reinterpret_cast<u32*>(ctx->dScratch + ctx->plan.errOffset);
+  TC_CHECK_CUDA(cudaMemcpyAsync(outBits, err, 4, cudaMemcpyDeviceToHost, s));
+  TC_CHECK_CUDA(cudaMemsetAsync(err, 0, 4, s));
+  TC_CHECK_CUDA(cudaStreamSynchronize(s));
+  return TC_OK;
+}
+
+uint64_t tc_launch_count(const tc_context* ctx) { return ctx ? ctx->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,215 @@
+// tc_backward.cu — adjoint of the vertex generation with the tessellation
+// decisions (factors, configs, split tree, allocation) of the forward frame
+// held fixed: they are piecewise constant in the inputs.
+//
+// Forward being differentiated (per generated vertex):
+//   part triangle   (triangle_tess_template_instantiate.comp.glsl:343-371)
+//     w = interp(bb, tableVertex);  P = sum_k w_k p_k
+//     N = sum_k w_k normalize(n_k);  uv = sum_k w_k uv_k
+//     h = bilinear(tex, uv) * s + o;  v = P + normalize(N) * h
+//   full cluster    (cluster_classify.comp.glsl:457-482)
+//     v = p + normalize(n) * (bilinear(tex, uv) * s + o)
+// with s = instance.displacementScale * view.displacementScale.
+//
+// Gradients scattered: dL/dp, dL/dn (per base vertex) and dL/dtexel (the four
+// bilinear taps). One warp per instantiation: its lanes walk the vertices, the
+// per-base-vertex sums of a part triangle are reduced across the warp and
+// added with one atomic per component; texel taps use atomics (red.add).
+#include "tc_kernels.h"
+#include "tc_stage.cuh"
+
+namespace tc {
+
+namespace {
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+  for(int o = 16; o > 0; o >>= 1)
+    v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ void scatter_texels(float* grad, const tc_DisplacementTexture& tx, const Taps& t, float dB)
+{
+  const float gx = 1.0f - t.fx, gy = 1.0f - t.fy;
+  atomicAdd(grad + (u64)t.y0 * tx.width + t.x0, (gy * gx) * dB);
+  atomicAdd(grad + (u64)t.y0 * tx.width + t.x1, (gy * t.fx) * dB);
+  atomicAdd(grad + (u64)t.y1 * tx.width + t.x0, (t.fy * gx) * dB);
+  atomicAdd(grad + (u64)t.y1 * tx.width + t.x1, (t.fy * t.fx) * dB);
+}
+
+__device__ __forceinline__ void atomic_add3(float* base, u64 index, f3 v)
+{
+  atomicAdd(base + 3 * index + 0, v.x);
+  atomicAdd(base + 3 * index + 1, v.y);
+  atomicAdd(base + 3 * index + 2, v.z);
+}
+
+__global__ void __launch_bounds__(256) k_instantiate_backward(StageCtx c, const float* gradVertices,
+                                                             const tc_GradTargets* targets, float* const* gradTexels)
+{
+  const u32         lane  = threadIdx.x & 31;
+  const u32         gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const u32         nwarp = (gridDim.x * blockDim.x) >> 5;
+  tc_SceneBuilding* b     = c.build;
+  const u32         temps = b->tempInstantiateCounter;
+  const tc_TemplateInstantiateInfo* ti    = reinterpret_cast<const tc_TemplateInstantiateInfo*>(b->tempInstantiations);
+  const tc_TessTriangleInfo*        parts = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
+  const tc_ClusterInfo*             fulls = reinterpret_cast<const tc_ClusterInfo*>(b->fullClusters);
+  const bool  haveTextures = c.numTextures > 0 && c.textures != nullptr;
+  const float viewScale    = c.view->displacementScale;
+
+  for(u32 j = gwarp; j < temps; j += nwarp)
+  {
+    const tc_TemplateInstantiateInfo info = ti[j];
+    const u32 mode  = info.clusterIdOffset >> 30;
+    const u64 vbase = (info.vertexBufferAddress - b->genVertices) / 12;
+    if(mode == TC_RT_CLUSTER_MODE_FULL_CLUSTER)
+    {
+      if(!fulls)
+        continue;
+      const tc_ClusterInfo     ci = fulls[j];
+      const tc_RenderInstance& in = c.instances[ci.instanceID];
+      const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in.clusters)[ci.clusterID];
+      const tc_GradTargets     gt = targets[ci.instanceID];
+      const tc_DisplacementTexture* tx = (haveTextures && in.displacementIndex >= 0 && (u32)in.displacementIndex < c.numTextures)
+                                             ? c.textures + in.displacementIndex
+                                             : nullptr;
+      float* gtex = tx ? gradTexels[in.displacementIndex] : nullptr;
+      const float s = in.displacementScale * viewScale;
+      for(u32 v = lane; v < cl.numVertices; v += 32)
+      {
+        const u32 vi = cl.firstLocalVertex + v;
+        const f3  g  = ldg3(gradVertices, vbase + v);
+        if(gt.dPositions)
+          atomic_add3(reinterpret_cast<float*>(gt.dPositions), vi, g);
+        if(!tx)
+          continue;
+        const f3    n    = ldg3(reinterpret_cast<const float*>(in.normals), vi);
+        const f2    uv   = ldg2(reinterpret_cast<const float*>(in.texcoords), vi);
+        const float nl   = len3(n);
+        const f3    nh   = {__fdiv_rn(n.x, nl), __fdiv_rn(n.y, nl), __fdiv_rn(n.z, nl)};
+        const float hraw = sample_bilinear(*tx, uv);
+        const float h    = ((hraw * in.displacementScale) * viewScale + in.displacementOffset) + c.view->displacementOffset;
+        const float dh   = dot3(nh, g);
+        if(gt.dNormals)
+        {
+          // d normalize(n) / dn = (I - nh nh^T) / |n|
+          const float k  = h / nl;
+          const f3    dn = {k * (g.x - nh.x * dh), k * (g.y - nh.y * dh), k * (g.z - nh.z * dh)};
+          atomic_add3(reinterpret_cast<float*>(gt.dNormals), vi, dn);
+        }
+        if(gtex)
+          scatter_texels(gtex, *tx, bilinear_taps(*tx, uv), dh * s);
+      }
+    }
+    else
+    {
+      const tc_TessTriangleInfo pi   = parts[info.clusterIdOffset & 0x3FFFFFFFu];
+      const u32                 cfg  = pi.subTriangle.triangleID_config >> 16;
+      const u32                 tri  = pi.subTriangle.triangleID_config & 0xFFFFu;
+      const tc_RenderInstance&  in   = c.instances[pi.cluster.instanceID];
+      const tc_Cluster          cl   = reinterpret_cast<const tc_Cluster*>(in.clusters)[pi.cluster.clusterID];
+      const uint8_t*            lt   = reinterpret_cast<const uint8_t*>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
+      const tc_GradTargets      gt   = targets[pi.cluster.instanceID];
+      const tc_TessTableEntry   e    = table_entry(c.table, cfg);
+      const tc_DisplacementTexture* tx = (haveTextures && in.displacementIndex >= 0 && (u32)in.displacementIndex < c.numTextures)
+                                             ? c.textures + in.displacementIndex
+                                             : nullptr;
+      float*       gtex = tx ? gradTexels[in.displacementIndex] : nullptr;
+      const float  s    = in.displacementScale * viewScale;
+      u32          vi[3];
+      f3           bb[3], p[3], nr[3], nh[3];
+      f2           uvb[3];
+      float        nl[3];
+#pragma unroll
+      for(int k = 0; k < 3; k++)
+      {
+        vi[k]  = cl.firstLocalVertex + lt[tri * 3 + k];
+        bb[k]  = decode_bary(pi.subTriangle.vtxEncoded[k]);
+        p[k]   = ldg3(reinterpret_cast<const float*>(in.positions), vi[k]);
+        nr[k]  = ldg3(reinterpret_cast<const float*>(in.normals), vi[k]);
+        nl[k]  = len3(nr[k]);
+        nh[k]  = {__fdiv_rn(nr[k].x, nl[k]), __fdiv_rn(nr[k].y, nl[k]), __fdiv_rn(nr[k].z, nl[k])};
+        uvb[k] = ldg2(reinterpret_cast<const float*>(in.texcoords), vi[k]);
+      }
+      (void)p;
+      f3 dP[3]  = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+      f3 dNh[3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+      for(u32 v = lane; v < e.numVertices; v += 32)
+      {
+        f3 w = decode_bary(__ldg(c.table.vertices + e.firstVertex + v));
+        if(cfg_flipped(cfg))
+        {
+          float t = w.x;
+          w.x     = w.y;
+          w.y     = t;
+        }
+        w          = interp3(bb[0], bb[1], bb[2], w);
+        const f3 g = ldg3(gradVertices, vbase + v);
+        const float wk[3] = {w.x, w.y, w.z};
+#pragma unroll
+        for(int k = 0; k < 3; k++)
+        {
+          dP[k].x += wk[k] * g.x;
+          dP[k].y += wk[k] * g.y;
+          dP[k].z += wk[k] * g.z;
+        }
+        if(!tx)
+          continue;
+        const f3    N    = interp3(nh[0], nh[1], nh[2], w);
+        const f2    uv   = interp2(uvb[0], uvb[1], uvb[2], w);
+        const float Nl   = len3(N);
+        const f3    m    = {__fdiv_rn(N.x, Nl), __fdiv_rn(N.y, Nl), __fdiv_rn(N.z, Nl)};
+        const float hraw = sample_bilinear(*tx, uv);
+        const float h    = ((hraw * in.displacementScale) * viewScale + in.displacementOffset) + c.view->displacementOffset;
+        const float dh   = dot3(m, g);
+        // d normalize(N) / dN = (I - m m^T) / |N|
+        const float kN = h / Nl;
+        const f3    gN = {kN * (g.x - m.x * dh), kN * (g.y - m.y * dh), kN * (g.z - m.z * dh)};
+#pragma unroll
+        for(int k = 0; k < 3; k++)
+        {
+          dNh[k].x += wk[k] * gN.x;
+          dNh[k].y += wk[k] * gN.y;
+          dNh[k].z += wk[k] * gN.z;
+        }
+        if(gtex)
+          scatter_texels(gtex, *tx, bilinear_taps(*tx, uv), dh * s);
+      }
+      // warp reduction of the per-base-vertex sums, one lane scatters
+#pragma unroll
+      for(int k = 0; k < 3; k++)
+      {
+        dP[k]  = {warp_sum(dP[k].x), warp_sum(dP[k].y), warp_sum(dP[k].z)};
+        dNh[k] = {warp_sum(dNh[k].x), warp_sum(dNh[k].y), warp_sum(dNh[k].z)};
+      }
+      if(lane < 3)
+      {
+        const int k = lane;
+        if(gt.dPositions)
+          atomic_add3(reinterpret_cast<float*>(gt.dPositions), vi[k], dP[k]);
+        if(tx && gt.dNormals)
+        {
+          // d normalize(n_k) / dn_k = (I - nh nh^T) / |n_k|
+          const float d  = dot3(nh[k], dNh[k]);
+          const float r  = 1.0f / nl[k];
+          const f3    dn = {r * (dNh[k].x - nh[k].x * d), r * (dNh[k].y - nh[k].y * d), r * (dNh[k].z - nh[k].z * d)};
+          atomic_add3(reinterpret_cast<float*>(gt.dNormals), vi[k], dn);
+        }
+      }
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_instantiate_backward(const StageCtx& c, const float* gradVertices, const tc_GradTargets* targets,
+                                        float* const* gradTexels, u32 grid, cudaStream_t s)
+{
+  k_instantiate_backward<<<grid, 256, 0, s>>>(c, gradVertices, targets, gradTexels);
+  return cudaGetLastError();
+}
+
+}  // namespace tc

@@ -1,0 +1,379 @@
+// tc_device.cuh — device-side building blocks shared by all kernels.
+//
+// Arithmetic contract: the library is compiled with -fmad=false and IEEE
+// division/square root, and every expression below is written in the
+// evaluation order of the reference GLSL (left to right), so results are
+// bit-identical to the oracle's (g++ -ffp-contract=off).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+
+#include "tc_tessellation.h"
+
+namespace tc {
+
+typedef unsigned long long u64;
+typedef uint32_t           u32;
+
+// ---------------------------------------------------------------------------
+// vectors
+// ---------------------------------------------------------------------------
+
+struct f3
+{
+  float x, y, z;
+};
+struct f2
+{
+  float x, y;
+};
+
+__device__ __forceinline__ f3 ldg3(const float* base, u64 index)
+{
+  const float* p = base + 3 * index;
+  return {__ldg(p), __ldg(p + 1), __ldg(p + 2)};
+}
+__device__ __forceinline__ f2 ldg2(const float* base, u64 index)
+{
+  const float2 v = __ldg(reinterpret_cast<const float2*>(base) + index);
+  return {v.x, v.y};
+}
+
+__device__ __forceinline__ f3    sub3(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ float dot3(f3 a, f3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ __forceinline__ float len3(f3 a) { return __fsqrt_rn(dot3(a, a)); }
+__device__ __forceinline__ float dist3(f3 a, f3 b) { return len3(sub3(a, b)); }
+// GLSL normalize(): v / length(v)
+__device__ __forceinline__ f3 normalize3(f3 a)
+{
+  float l = len3(a);
+  return {__fdiv_rn(a.x, l), __fdiv_rn(a.y, l), __fdiv_rn(a.z, l)};
+}
+
+// (M * vec4(p, 1)).xyz, column-major M
+__device__ __forceinline__ f3 xform_point(const float* m, f3 p)
+{
+  f3 r;
+  r.x = ((m[0] * p.x + m[4] * p.y) + m[8] * p.z) + m[12];
+  r.y = ((m[1] * p.x + m[5] * p.y) + m[9] * p.z) + m[13];
+  r.z = ((m[2] * p.x + m[6] * p.y) + m[10] * p.z) + m[14];
+  return r;
+}
+
+// tessellation.glsl:191-201 tess_interpolate (precise)
+__device__ __forceinline__ f3 interp3(f3 b0, f3 b1, f3 b2, f3 w)
+{
+  f3 r;
+  r.x = (b0.x * w.x + b1.x * w.y) + b2.x * w.z;
+  r.y = (b0.y * w.x + b1.y * w.y) + b2.y * w.z;
+  r.z = (b0.z * w.x + b1.z * w.y) + b2.z * w.z;
+  return r;
+}
+__device__ __forceinline__ f2 interp2(f2 b0, f2 b1, f2 b2, f3 w)
+{
+  f2 r;
+  r.x = (b0.x * w.x + b1.x * w.y) + b2.x * w.z;
+  r.y = (b0.y * w.x + b1.y * w.y) + b2.y * w.z;
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// tessellation.glsl
+// ---------------------------------------------------------------------------
+
+// tessellation.glsl:48-59
+__device__ __forceinline__ u32 encode_bary(f3 w)
+{
+  u32 ix = __float2uint_rz(w.x * 32768.0f + 0.5f);
+  u32 iy = __float2uint_rz(w.y * 32768.0f + 0.5f);
+  u32 iz = __float2uint_rz(w.z * 32768.0f + 0.5f);
+  if(ix > max(iy, iz))
+    ix = 32768u - iy - iz;
+  else if(iy > iz)
+    iy = 32768u - ix - iz;
+  else
+    iz = 32768u - ix - iy;
+  return iy | (iz << 16);
+}
+
+// tessellation.glsl:66-76
+__device__ __forceinline__ f3 decode_bary(u32 vtx)
+{
+  f3 w;
+  w.y = __uint2float_rn(vtx & 0xFFFFu) * (1.0f / 32768.0f);
+  w.z = __uint2float_rn(vtx >> 16) * (1.0f / 32768.0f);
+  w.x = (1.0f - w.y) - w.z;
+  return w;
+}
+
+struct FactorParams
+{
+  f3    viewPos;
+  float nearPlane;
+  float viewportH;
+  float tessRate;
+};
+
+__device__ __forceinline__ u32 round_clamp_factor(float e, float spl, const FactorParams& fp)
+{
+  float f = rintf(((e * spl) * fp.viewportH) * fp.tessRate);
+  f       = fminf(fmaxf(f, 1.0f), 32768.0f);
+  return __float2uint_rz(f);
+}
+
+// tessellation.glsl:78-99
+__device__ __forceinline__ uint3 tess_factors(f3 a, f3 b, f3 c, const FactorParams& fp)
+{
+  float da = dist3(a, fp.viewPos);
+  float db = dist3(b, fp.viewPos);
+  float dc = dist3(c, fp.viewPos);
+  float sx = __fdiv_rn(1.0f, fmaxf(fp.nearPlane, fminf(da, db)));
+  float sy = __fdiv_rn(1.0f, fmaxf(fp.nearPlane, fminf(db, dc)));
+  float sz = __fdiv_rn(1.0f, fmaxf(fp.nearPlane, fminf(dc, da)));
+  uint3 f;
+  f.x = round_clamp_factor(dist3(a, b), sx, fp);
+  f.y = round_clamp_factor(dist3(b, c), sy, fp);
+  f.z = round_clamp_factor(dist3(c, a), sz, fp);
+  return f;
+}
+
+// tessellation.glsl:101-104
+__device__ __forceinline__ u32 split_factor1(u32 f, u32 sf) { return min((f + TC_TESSTABLE_SIZE - 1) / TC_TESSTABLE_SIZE, sf); }
+
+// tessellation.glsl:119-144: rotate the largest factor first (permuting the
+// three encoded sub-triangle vertices with it), flip bit when z > y
+__device__ __forceinline__ u32 get_config(uint3 f, u32& v0, u32& v1, u32& v2)
+{
+  u32 m = max(max(f.x, f.y), f.z);
+  if(m == f.y)
+  {
+    f       = make_uint3(f.y, f.z, f.x);
+    u32 t0 = v0;
+    v0 = v1, v1 = v2, v2 = t0;
+  }
+  else if(m == f.z)
+  {
+    f       = make_uint3(f.z, f.x, f.y);
+    u32 t2 = v2;
+    v2 = v1, v1 = v0, v0 = t2;
+  }
+  const u32 L   = TC_TESSTABLE_LOOKUP_SIZE;
+  u32       idx = f.x + f.y * L + f.z * L * L - (1 + L + L * L);
+  if(f.z > f.y)
+    idx |= 1u << 15;
+  return idx;
+}
+
+__device__ __forceinline__ u32  cfg_index(u32 cfg) { return cfg & 0x7FFFu; }
+__device__ __forceinline__ bool cfg_flipped(u32 cfg) { return (cfg & 0x8000u) != 0; }
+
+struct Table
+{
+  const tc_TessTableEntry* entries;
+  const u32*               vertices;
+  const u32*               triangles;
+  const u64*               templateAddresses;
+  const u32*               templateSizes;
+};
+
+__device__ __forceinline__ tc_TessTableEntry table_entry(const Table& t, u32 cfg)
+{
+  const uint2 raw = __ldg(reinterpret_cast<const uint2*>(t.entries) + cfg_index(cfg));
+  tc_TessTableEntry e;
+  e.firstTriangle = raw.x & 0xFFFF;
+  e.firstVertex   = raw.x >> 16;
+  e.numTriangles  = raw.y & 0xFFFF;
+  e.numVertices   = raw.y >> 16;
+  return e;
+}
+
+// tessellation.glsl:165-176 (flip -> .xzy)
+__device__ __forceinline__ uint3 cfg_triangle(const Table& t, const tc_TessTableEntry& e, u32 cfg, u32 tri)
+{
+  u32   p = __ldg(t.triangles + e.firstTriangle + tri);
+  uint3 r = make_uint3(p & 0xFF, (p >> 8) & 0xFF, (p >> 16) & 0xFF);
+  if(cfg_flipped(cfg))
+  {
+    u32 s = r.y;
+    r.y   = r.z;
+    r.z   = s;
+  }
+  return r;
+}
+
+// tessellation.glsl:178-189 (flip -> .yxz)
+__device__ __forceinline__ f3 cfg_vertex(const Table& t, const tc_TessTableEntry& e, u32 cfg, u32 vert)
+{
+  f3 w = decode_bary(__ldg(t.vertices + e.firstVertex + vert));
+  if(cfg_flipped(cfg))
+  {
+    float s = w.x;
+    w.x     = w.y;
+    w.y     = s;
+  }
+  return w;
+}
+
+// ---------------------------------------------------------------------------
+// displacement: bilinear, mip 0, REPEAT, texel centres at (i + 0.5) / size.
+// Texels are fetched with read-only (texture-path) loads; weights are fp32 and
+// computed here, so the result does not depend on the sampler's fixed-point
+// filter weights.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int wrapi(int i, int n)
+{
+  int r = i % n;
+  return r < 0 ? r + n : r;
+}
+
+__device__ __forceinline__ float fetch_texel(const tc_DisplacementTexture& tx, int x, int y)
+{
+  const u64 i = (u64)y * tx.width + (u64)x;
+  switch(tx.format)
+  {
+    case TC_TEXEL_F16:
+      return __half2float(__ushort_as_half(__ldg(reinterpret_cast<const unsigned short*>(tx.texels) + i)));
+    case TC_TEXEL_UNORM16:
+      return __fdiv_rn(__uint2float_rn(__ldg(reinterpret_cast<const unsigned short*>(tx.texels) + i)), 65535.0f);
+    default:
+      return __ldg(reinterpret_cast<const float*>(tx.texels) + i);
+  }
+}
+
+struct Taps
+{
+  int   x0, x1, y0, y1;
+  float fx, fy;
+};
+
+__device__ __forceinline__ Taps bilinear_taps(const tc_DisplacementTexture& tx, f2 uv)
+{
+  float x  = uv.x * __uint2float_rn(tx.width) - 0.5f;
+  float y  = uv.y * __uint2float_rn(tx.height) - 0.5f;
+  float xf = floorf(x);
+  float yf = floorf(y);
+  Taps  t;
+  t.fx   = x - xf;
+  t.fy   = y - yf;
+  int ix = __float2int_rz(xf), iy = __float2int_rz(yf);
+  t.x0   = wrapi(ix, (int)tx.width);
+  t.x1   = wrapi(ix + 1, (int)tx.width);
+  t.y0   = wrapi(iy, (int)tx.height);
+  t.y1   = wrapi(iy + 1, (int)tx.height);
+  return t;
+}
+
+__device__ __forceinline__ float sample_bilinear(const tc_DisplacementTexture& tx, f2 uv)
+{
+  Taps  b   = bilinear_taps(tx, uv);
+  float t00 = fetch_texel(tx, b.x0, b.y0);
+  float t10 = fetch_texel(tx, b.x1, b.y0);
+  float t01 = fetch_texel(tx, b.x0, b.y1);
+  float t11 = fetch_texel(tx, b.x1, b.y1);
+  float gx  = 1.0f - b.fx;
+  float top = gx * t00 + b.fx * t10;
+  float bot = gx * t01 + b.fx * t11;
+  return (1.0f - b.fy) * top + b.fy * bot;
+}
+
+// height = (h * instScale * viewScale) + instOffset + viewOffset; pos += normalize(n) * height
+// (cluster_classify.comp.glsl:471-478, triangle_tess_template_instantiate.comp.glsl:356-365)
+__device__ __forceinline__ f3 displace(f3 pos, f3 normal, float h, float instScale, float viewScale, float instOffset,
+                                       float viewOffset)
+{
+  h    = ((h * instScale) * viewScale + instOffset) + viewOffset;
+  f3 n = normalize3(normal);
+  return {pos.x + n.x * h, pos.y + n.y * h, pos.z + n.z * h};
+}
+
+// ---------------------------------------------------------------------------
+// memory-model helpers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void st_release_u64(u64* p, u64 v)
+{
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ u64 ld_acquire_u64(const u64* p)
+{
+  u64 v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ u32 ld_acquire_u32(const u32* p)
+{
+  u32 v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Decoupled look-back (single-pass chained scan) over tiles. Gives every tile
+// the exclusive prefix of per-tile aggregates in tile order, so appends are
+// ordered exactly like a serial loop. Each state word holds a 62-bit value and
+// a 2-bit flag (1 = tile aggregate, 2 = inclusive prefix). Tiles are handed out
+// through a ticket counter so a tile's predecessor is always owned by a running
+// block. Waits are bounded: after kSpinLimit empty polls the tile records
+// TC_DEVERR_LOOKBACK_TIMEOUT, uses what it accumulated and moves on.
+// ---------------------------------------------------------------------------
+
+constexpr u64 kLbValueMask = (1ull << 62) - 1;
+constexpr u64 kLbAggregate = 1ull << 62;
+constexpr u64 kLbPrefix    = 2ull << 62;
+constexpr u32 kSpinLimit   = 1u << 22;
+
+// Called by one lane per counter. `state` is this counter's tile-state array.
+// `base` is only used by tile 0 (counter value before this launch).
+__device__ __forceinline__ u64 lookback_exclusive(u64* state, u32 tile, u64 aggregate, u64 base, u32* errorWord)
+{
+  if(tile == 0)
+  {
+    st_release_u64(state, kLbPrefix | ((base + aggregate) & kLbValueMask));
+    return base;
+  }
+  st_release_u64(state + tile, kLbAggregate | (aggregate & kLbValueMask));
+  u64 acc   = 0;
+  int t     = (int)tile - 1;
+  u32 spins = 0;
+  while(t >= 0)
+  {
+    u64 s = ld_acquire_u64(state + t);
+    u64 f = s & ~kLbValueMask;
+    if(f == 0)
+    {
+      if(++spins > kSpinLimit)
+      {
+        atomicOr(errorWord, TC_DEVERR_LOOKBACK_TIMEOUT);
+        break;
+      }
+      __nanosleep(64);
+      continue;
+    }
+    acc += s & kLbValueMask;
+    if(f == kLbPrefix)
+      break;
+    t--;
+  }
+  st_release_u64(state + tile, kLbPrefix | ((acc + aggregate) & kLbValueMask));
+  return acc;
+}
+
+// binary search: first index in [lo, hi) whose instance id (read by `get`) is >= key
+template <class Get>
+__device__ __forceinline__ u32 lower_bound_instance(u32 lo, u32 hi, u32 key, Get get)
+{
+  while(lo < hi)
+  {
+    u32 mid = lo + ((hi - lo) >> 1);
+    if(get(mid) < key)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+}  // namespace tc

@@ -1,0 +1,251 @@
+// tc_stage.cuh — launch context shared by the stage kernels, the build_setup
+// logic (used both by the standalone build_setup kernel and fused into the last
+// block of the producing kernel), and the per-launch scratch layout.
+#pragma once
+
+#include "tc_device.cuh"
+
+namespace tc {
+
+// Per-launch scratch: look-back tile states, the tile ticket, the "blocks done"
+// counter and the totals the last tile publishes. Zeroed before every launch.
+struct LaunchScratch
+{
+  u64* lbState;   // [numCounters][lbStride]
+  u32  lbStride;  // max tiles per launch
+  u32  selfClean; // 1: the last block re-zeroes what the launch used (repeated launches on one slot)
+  u32* ticket;
+  u32* done;
+  u64* totals;  // [numCounters] inclusive totals (base included) of the last tile
+};
+
+struct StageCtx
+{
+  const tc_FrameConstants*      view;
+  const tc_FrameConstants*      viewLast;
+  const tc_RenderInstance*      instances;
+  tc_SceneBuilding*             build;
+  tc_Readback*                  readback;
+  const tc_DisplacementTexture* textures;
+  u32                           numInstances;
+  u32                           numTextures;
+  u32                           flags;
+  u32                           _pad0;
+  Table                         table;
+  tc_caps                       caps;
+  u32*                          errorWord;
+  u32*                          runStarts;         // [kMaxRuns + 2]: part counter at each run start, then full-cluster count
+  u32*                          instClusterStart;  // [numInstances + 1] exclusive prefix of numClusters
+  LaunchScratch                 scratch;
+  u32                           instBegin;  // instance window [instBegin, instEnd)
+  u32                           instEnd;
+  u32                           fuseSetup;  // build_setup mode run by the last block, or kNoSetup
+  u32                           run;        // instantiate: part run index or kAllRuns
+};
+
+constexpr u32 kNoSetup  = 0xFFFFFFFFu;
+constexpr u32 kAllRuns  = 0xFFFFFFFFu;
+constexpr u32 kMaxRuns  = 16;
+
+__device__ __forceinline__ u32 clamp_split_factor(u32 sf) { return max(2u, min(sf, TC_TESSTABLE_SIZE)); }
+
+__device__ __forceinline__ bool whole_window(const StageCtx& c) { return c.instBegin == 0 && c.instEnd >= c.numInstances; }
+
+// shaders/build_setup.comp.glsl:102-265 (RT target, no transient builds,
+// non-persistent split), plus bookkeeping of the part-run boundaries that the
+// per-instance launch path and the backward pass use.
+__device__ inline void build_setup_apply(const StageCtx& c, u32 mode)
+{
+  tc_SceneBuilding* b  = c.build;
+  tc_Readback*      rb = c.readback;
+  const tc_caps&    k  = c.caps;
+  switch(mode)
+  {
+    case TC_BUILD_SETUP_CLASSIFY:
+    {
+      u32 counter              = b->visibleClusterCounter;
+      rb->numVisibleClusters   = counter;
+      counter                  = min(counter, k.maxVisibleClusters);
+      b->visibleClusterCounter = counter;
+      b->dispatchClassify      = {counter, 1, 1};
+      break;
+    }
+    case TC_BUILD_SETUP_DRAW_TESS:
+    {
+      u32 full              = b->fullClusterCounter;
+      u32 part              = b->partTriangleCounter;
+      rb->numFullClusters   = full;
+      rb->numPartTriangles  = part;
+      rb->numSplitTriangles = b->splitWriteCounter;
+      full                  = min(full, k.maxVisibleClusters);
+      part                  = min(part, k.maxPartTriangles);
+      b->drawFullClusters   = {full, 0};
+      b->drawPartTriangles  = {(part + 31) / 32, 0};
+      rb->numBlasClusters   = full;
+      break;
+    }
+    case TC_BUILD_SETUP_SPLIT:
+    {
+      int32_t s                = b->splitTriangleCounter;
+      u32     count            = s < 0 ? 0u : min((u32)s, k.maxSplitTriangles);
+      b->splitWriteCounter     = count;
+      b->splitTriangleCounter  = (int32_t)count;
+      b->splitPassStart        = 0;
+      b->splitPassEnd          = count;
+      b->dispatchTriangleSplit = {(count + 63) / 64, 1, 1};
+      c.runStarts[0]           = 0;
+      c.runStarts[1]           = b->partTriangleCounter;
+      c.runStarts[kMaxRuns + 1] = b->genClusterCounter;  // full-cluster instantiation attempts
+      break;
+    }
+    case TC_BUILD_SETUP_SPLIT_PASS:
+    {
+      u32 pass                 = b->splitPass + 1;
+      b->splitPass             = pass;
+      u32 start                = min(b->splitPassEnd, k.maxSplitTriangles);
+      u32 end                  = min(b->splitWriteCounter, k.maxSplitTriangles);
+      b->splitPassStart        = start;
+      b->splitPassEnd          = end;
+      b->dispatchTriangleSplit = {(end - start + 63) / 64, 1, 1};
+      if(pass + 1 <= kMaxRuns)
+        c.runStarts[pass + 1] = b->partTriangleCounter;
+      break;
+    }
+    case TC_BUILD_SETUP_BUILD_BLAS:
+    {
+      u32 temp                        = b->tempInstantiateCounter;
+      rb->numBlasClusters             = temp;
+      rb->numTempInstantiations       = temp;
+      rb->numGenDatas                 = b->genClusterDataCounter;
+      rb->numGenVertices              = b->genVertexCounter;
+      rb->numBlasReservedSizes        = b->numBlasReservedSizes;
+      temp                            = min(k.maxGeneratedClusters, temp);
+      b->tempInstantiateCounter       = temp;
+      rb->numActualTempInstantiations = temp;
+      b->dispatchBlasTempInsert       = {(temp + 63) / 64, 1, 1};
+      break;
+    }
+    case TC_BUILD_SETUP_INSTANTIATE_TESS:
+    {
+      u32 part              = b->partTriangleCounter;
+      rb->numPartTriangles  = part;
+      rb->numSplitTriangles = b->splitWriteCounter;
+      if(b->splitPass + 2 <= kMaxRuns)
+        c.runStarts[b->splitPass + 2] = part;
+      part                           = min(part, k.maxPartTriangles);
+      b->partTriangleCounter         = part;
+      b->dispatchTriangleInstantiate = {(part + 31) / 32, 1, 1};
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// A launch never uses more look-back tiles than its scratch slot holds; a
+// request beyond that (inconsistent host-side sizes) is recorded and truncated.
+__device__ __forceinline__ u32 clamp_tiles(const StageCtx& c, u32 numTiles)
+{
+  if(numTiles > c.scratch.lbStride)
+  {
+    if(threadIdx.x == 0 && blockIdx.x == 0)
+      atomicOr(c.errorWord, TC_DEVERR_CAPACITY);
+    return c.scratch.lbStride;
+  }
+  return numTiles;
+}
+
+// Tile handout: one ticket per tile, broadcast through shared memory.
+__device__ __forceinline__ u32 next_tile(const StageCtx& c, u32* s_tile)
+{
+  if(threadIdx.x == 0)
+    *s_tile = atomicAdd(c.scratch.ticket, 1u);
+  __syncthreads();
+  u32 t = *s_tile;
+  __syncthreads();
+  return t;
+}
+
+// "Last block" detection: returns true in exactly one block, after every block
+// of the launch has finished its work (classic threadfence reduction pattern).
+__device__ __forceinline__ bool last_block_done(const StageCtx& c, u32* s_flag)
+{
+  __syncthreads();
+  if(threadIdx.x == 0)
+  {
+    __threadfence();
+    u32 prev = atomicAdd(c.scratch.done, 1u);
+    *s_flag  = (prev == gridDim.x - 1) ? 1u : 0u;
+  }
+  __syncthreads();
+  bool last = *s_flag != 0;
+  if(last)
+    __threadfence();
+  return last;
+}
+
+// Run by every thread of the last block after its finalisation: when the slot
+// is reused by the next launch without a memset, put it back to zero.
+__device__ inline void scratch_release(const StageCtx& c, u32 numTiles, u32 numCounters)
+{
+  if(!c.scratch.selfClean)
+    return;
+  __syncthreads();
+  const u32 n = min(numTiles, c.scratch.lbStride);
+  for(u32 q = 0; q < numCounters; q++)
+    for(u32 t = threadIdx.x; t < n; t += blockDim.x)
+      c.scratch.lbState[(u64)q * c.scratch.lbStride + t] = 0;
+  if(threadIdx.x == 0)
+  {
+    for(u32 q = 0; q < numCounters; q++)
+      c.scratch.totals[q] = 0;
+    *c.scratch.ticket = 0;
+    *c.scratch.done   = 0;
+  }
+}
+
+}  // namespace tc
+
+namespace tc {
+
+// Block-wide exclusive scan of one u32 per thread. `s_warp` needs 33
+// entries (one per warp plus the total). Returns the exclusive prefix; *total
+// receives the block sum.
+__device__ __forceinline__ u32 block_exclusive_scan(u32 v, u32* s_warp, u32* total)
+{
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  u32       x    = v;
+#pragma unroll
+  for(int d = 1; d < 32; d <<= 1)
+  {
+    u32 y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+    if(lane >= (u32)d)
+      x += y;
+  }
+  if(lane == 31)
+    s_warp[warp] = x;
+  __syncthreads();
+  if(warp == 0)
+  {
+    u32 w = lane < nwarps ? s_warp[lane] : 0;
+    u32 s = w;
+#pragma unroll
+    for(int d = 1; d < 32; d <<= 1)
+    {
+      u32 y = __shfl_up_sync(0xFFFFFFFFu, s, d);
+      if(lane >= (u32)d)
+        s += y;
+    }
+    if(lane < nwarps)
+      s_warp[lane] = s - w;  // exclusive warp offsets
+    if(lane == 31)
+      s_warp[32] = s;  // block total
+  }
+  __syncthreads();
+  u32 r  = s_warp[warp] + x - v;
+  *total = s_warp[32];
+  __syncthreads();
+  return r;
+}
+
+}  // namespace tc
