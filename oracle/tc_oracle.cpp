@@ -279,6 +279,8 @@ inline BilinearTaps bilinearTaps(const tc_DisplacementTexture& tx, f2 uv)
 
 float sampleBilinear(const tc_DisplacementTexture& tx, f2 uv)
 {
+  if(tx.width == 0 || tx.height == 0)
+    return 0.0f;
   BilinearTaps b   = bilinearTaps(tx, uv);
   float        t00 = texel(tx, b.x0, b.y0);
   float        t10 = texel(tx, b.x1, b.y0);

@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(W * 32) k_cluster_classify(StageCtx c)
   const tc_ClusterInfo* vis = reinterpret_cast<const tc_ClusterInfo*>(b->visibleClusters);
   if(threadIdx.x == 0)
   {
-    u32 lo = 0, hi = b->visibleClusterCounter;
+    u32 lo = 0, hi = min(b->visibleClusterCounter, c.caps.maxVisibleClusters);
     if(!whole_window(c))
     {
       auto get = [&](u32 i) { return vis[i].instanceID; };

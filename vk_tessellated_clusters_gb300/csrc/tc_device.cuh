@@ -268,6 +268,8 @@ __device__ __forceinline__ Taps bilinear_taps(const tc_DisplacementTexture& tx, 
 
 __device__ __forceinline__ float sample_bilinear(const tc_DisplacementTexture& tx, f2 uv)
 {
+  if(tx.width == 0 || tx.height == 0)
+    return 0.0f;
   Taps  b   = bilinear_taps(tx, uv);
   float t00 = fetch_texel(tx, b.x0, b.y0);
   float t10 = fetch_texel(tx, b.x1, b.y0);

@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(B) k_triangle_instantiate(StageCtx c)
 
   if(threadIdx.x == 0)
   {
-    u32 lo = 0, hi = b->partTriangleCounter;
+    u32 lo = 0, hi = min(b->partTriangleCounter, c.caps.maxPartTriangles);
     if(c.run != kAllRuns)
     {
       u32 rs = c.runStarts[c.run], re = c.runStarts[c.run + 1];

@@ -111,9 +111,8 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
 
   if(threadIdx.x == 0)
   {
-    u32 lo = b->splitPassStart, hi = b->splitPassEnd;
-    if(hi < lo)
-      hi = lo;
+    u32 hi = min(b->splitPassEnd, c.caps.maxSplitTriangles);
+    u32 lo = min(b->splitPassStart, hi);
     if(!whole_window(c))
     {
       auto get = [&](u32 i) { return queue[i].cluster.instanceID; };
