@@ -1,0 +1,499 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 tessellation chain (one JSON line on stdout).
+
+Workload (N=1): the batched scene — 256 instances of four procedural meshes of
+uneven size (icosphere 5,120 / torus 12,288 / planar grid 32,768 / subdivided
+cube 1,536 triangles; 3.31M base triangles, 51,840 clusters of <= 64
+triangles), seeded transforms in a 40^3 box, 512^2 fp32 value-noise maps at
+scale 0.03, camera orbiting at radius 30 over 60 frames, 1920x1080, 4 px per
+segment (the reference's default tessRatePixels), frustum culling on. One step
+= one frame of the chain (frame reset .. BLAS list insertion) recorded as a
+CUDA graph of one persistent launch per stage.
+
+  value : tessellated triangles per second (Readback.numTotalTriangles / frame
+          time), frame inputs resident in HBM, CUDA events on the launching
+          stream, L2 flushed (256 MiB write) between timed frames
+  e2e   : same metric through the C ABI with host buffers: per frame the
+          FrameConstants pair and the RenderInstance array are copied from
+          pinned host memory and the Readback copied back, inside the events
+  roofline : the frame's dominant kernel, algorithmic bytes (metrics.py) over
+          its CUDA-event duration, against the measured HBM copy bandwidth
+  cpu_baseline : the CPU oracle (C++ restatement of the reference shaders,
+          all host cores) on a time-bounded sample of the same frames
+
+--impl reference times that CPU restatement alone (the reference itself only
+exists as Vulkan GLSL, which cannot run here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NUM_ORBIT_FRAMES = 60
+WORKLOAD = ("batched scene: 256 instances of 4 procedural meshes (icosphere 5120, torus 12288, grid 32768, "
+            "cube 1536 tris; 3.31M base tris, 51840 clusters <=64 tris), 512^2 fp32 value-noise maps scale 0.03, "
+            "orbit camera r=30 over 60 frames, 1920x1080, 4 px/segment, frustum culling on, split factor 8")
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=30)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--no-extras", action="store_true", help="skip the plain-path and terrain measurements")
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--profile-case", choices=["batched", "terrain"], default=None,
+                   help="run only `warmup` + `steps` graph frames of one case (for ncu captures) and exit")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    parts = [x.strip() for x in line.split(",")]
+                    if len(parts) >= 9 and parts[1].isdigit():
+                        rows.append(parts)
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        mhz = [int(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": int(rows[0][2]), "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle leg (reference arm and cpu_baseline)
+# ---------------------------------------------------------------------------
+
+def cpu_oracle_rate(seconds: float, threads: int | None = None):
+    from oracle.binding import Oracle
+    from vk_tessellated_clusters_gb300 import layouts as L
+    from vk_tessellated_clusters_gb300 import scene as S
+    threads = threads or os.cpu_count()
+    ora = Oracle()
+    scene = S.scene_batched(256)
+    caps = L.default_caps()
+    st = ora.new_state(scene, caps, L.FLAG_CULLING)
+    fcs = [S.frame_constants(S.camera_orbit(f)) for f in range(NUM_ORBIT_FRAMES)]
+    tris, frames = 0, 0
+    t0 = time.perf_counter()
+    while True:
+        f = frames % NUM_ORBIT_FRAMES
+        st, _ = ora.frame(scene, fcs[f], caps, L.FLAG_CULLING, threads=threads,
+                          camera_last=fcs[(f - 1) % NUM_ORBIT_FRAMES], state=st)
+        tris += int(st.readback.read(L.Readback, 1)[0]["numTotalTriangles"])
+        frames += 1
+        el = time.perf_counter() - t0
+        if el >= seconds and frames >= 3:
+            break
+    return tris / el, el, frames, threads
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    steps = []
+    for _ in range(args.warmup):
+        cpu_oracle_rate(0.0)
+    tris_total, el_total, frames_total, threads = 0.0, 0.0, 0, os.cpu_count()
+    for _ in range(args.steps):
+        rate, el, frames, threads = cpu_oracle_rate(max(1.0, args.cpu_seconds / max(args.steps, 1)))
+        steps.append(el / frames * 1e3)
+        tris_total += rate * el
+        el_total += el
+        frames_total += frames
+    value = tris_total / el_total
+    line = {
+        "metric": "tessellated tris/s", "value": value, "unit": "tris/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": statistics.mean(steps), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural meshes and value-noise maps)",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "step": "one frame on the CPU"},
+        "cpu_baseline": {"value": value, "unit": "tris/s", "cores": threads, "kind": "port",
+                         "sample": f"{frames_total} frames of the batched scene in {el_total:.1f} s; the reference "
+                                   "has no CPU path and its GLSL needs Vulkan, so this is the C++ restatement"},
+        "e2e": {"value": value, "unit": "tris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU leg
+# ---------------------------------------------------------------------------
+
+def stage_sequence(pipe, n_inst):
+    from vk_tessellated_clusters_gb300 import layouts as L
+    seq = [("frame_begin", ()), ("instances_classify", ()), ("clusters_cull", (0, n_inst)),
+           ("build_setup", (L.BUILD_SETUP_CLASSIFY,)), ("cluster_classify", (0, n_inst)),
+           ("build_setup", (L.BUILD_SETUP_SPLIT,))]
+    passes = pipe.split_passes()
+    for p in range(passes):
+        seq.append(("triangle_split", (0, n_inst)))
+        if p + 1 < passes:
+            seq.append(("build_setup", (L.BUILD_SETUP_SPLIT_PASS,)))
+    seq += [("build_setup", (L.BUILD_SETUP_INSTANTIATE_TESS,)), ("triangle_instantiate", (0, 0xFFFFFFFF)),
+            ("build_setup", (L.BUILD_SETUP_BUILD_BLAS,)), ("blas_setup_insertion", ()), ("blas_clusters_insert", ())]
+    return seq
+
+
+def profile_stages(pipe, torch, frames, set_frame, flush, reps=1):
+    """Per-stage CUDA-event durations (ms) over the given frames."""
+    n_inst = pipe.args.numInstances
+    seq = stage_sequence(pipe, n_inst)
+    acc = {}
+    outs = []
+    for f in frames:
+        set_frame(f)
+        flush()
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(len(seq) + 1)]
+        evs[0].record()
+        for i, (name, extra) in enumerate(seq):
+            pipe.stage(name, *extra)
+            evs[i + 1].record()
+        torch.cuda.synchronize()
+        for i, (name, _) in enumerate(seq):
+            key = name if name not in ("build_setup", "triangle_split") else name
+            acc.setdefault(key, []).append(evs[i].elapsed_time(evs[i + 1]))
+        outs.append(pipe.outputs())
+    return acc, outs
+
+
+def run_ours(args):
+    import torch
+    from vk_tessellated_clusters_gb300 import build_lib, native
+    if not os.path.exists(native.LIB_PATH):
+        build_lib.build()
+    from vk_tessellated_clusters_gb300 import layouts as L
+    from vk_tessellated_clusters_gb300 import metrics as M
+    from vk_tessellated_clusters_gb300 import scene as S
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    scene = S.scene_batched(256)
+    caps = L.default_caps()
+    flags = L.FLAG_CULLING
+    pipe = TessellationPipeline(scene, caps, flags, device=local)
+    sched_path = os.path.join(ROOT, "profiles", "schedule_batched.json")
+    if os.path.exists(sched_path):
+        with open(sched_path) as f:
+            pipe.set_schedule(json.load(f)["schedule"])
+
+    # all orbit frames' constants resident on the device; a step copies its pair in
+    fcs = [S.frame_constants(S.camera_orbit(f)) for f in range(NUM_ORBIT_FRAMES)]
+    import numpy as np
+    fc_bytes = np.stack([np.frombuffer(fc.tobytes(), np.uint8) for fc in fcs])
+    fc_dev = torch.from_numpy(fc_bytes).to(dev)
+    view_t = pipe.state.view.handle
+    last_t = pipe.state.view_last.handle
+    FC = L.FrameConstants.itemsize
+
+    def set_frame(f):
+        view_t[:FC].copy_(fc_dev[f % NUM_ORBIT_FRAMES])
+        last_t[:FC].copy_(fc_dev[(f - 1) % NUM_ORBIT_FRAMES])
+
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def flush():
+        flush_buf.fill_(1)
+
+    rb_host = torch.empty(L.Readback.itemsize, dtype=torch.uint8, pin_memory=True)
+
+    def read_tris():
+        rb_host.copy_(pipe.state.readback.handle[:L.Readback.itemsize])
+        return int(rb_host.numpy().view(L.Readback)[0]["numTotalTriangles"])
+
+    # ---- warm-up --------------------------------------------------------------
+    for s in range(args.warmup):
+        set_frame(s)
+        pipe.build("graph")
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+
+    # ---- timed region: K frames, graph replay, L2 flushed between frames -------
+    launches0 = pipe.launch_count()
+    times, tris = [], []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        for s in range(args.steps):
+            set_frame(args.warmup + s)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            pipe.build("graph")
+            e1.record()
+            flush()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+            tris.append(read_tris())
+        torch.cuda.synchronize()
+    gpu_launches = pipe.launch_count() - launches0
+    if world > 1:
+        torch.distributed.barrier()
+    t_total = sum(times) / 1e3
+    tris_total = float(sum(tris))
+    if world > 1:
+        tt = torch.tensor([t_total], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        nt = torch.tensor([tris_total], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(nt)
+        t_total, tris_total = float(tt.item()), float(nt.item())
+    value = tris_total / t_total
+    errs = pipe.device_errors()
+
+    # ---- e2e through the C ABI with host buffers ------------------------------
+    fc_host = torch.from_numpy(fc_bytes).pin_memory()
+    inst_host = torch.from_numpy(pipe.state.res.instance_records.view(np.uint8).copy()).pin_memory()
+    inst_dev = pipe.state.res.instances.handle
+    h2d = 2 * FC + inst_host.numel()
+    e2e_times, e2e_tris = [], []
+    for s in range(args.warmup + args.steps):
+        f = s % NUM_ORBIT_FRAMES
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        view_t[:FC].copy_(fc_host[f], non_blocking=True)
+        last_t[:FC].copy_(fc_host[(f - 1) % NUM_ORBIT_FRAMES], non_blocking=True)
+        inst_dev[:inst_host.numel()].copy_(inst_host, non_blocking=True)
+        pipe.build("graph")
+        rb_host.copy_(pipe.state.readback.handle[:L.Readback.itemsize], non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        if s >= args.warmup:
+            e2e_times.append(e0.elapsed_time(e1))
+            e2e_tris.append(int(rb_host.numpy().view(L.Readback)[0]["numTotalTriangles"]))
+        flush()
+    e2e_value = sum(e2e_tris) / (sum(e2e_times) / 1e3)
+
+    # ---- per-stage profile and roofline of the dominant kernel ---------------------
+    prof_frames = list(range(0, NUM_ORBIT_FRAMES, max(1, NUM_ORBIT_FRAMES // 6)))[:6]
+    stage_ms, outs = profile_stages(pipe, torch, prof_frames, set_frame, flush)
+    means = {k: statistics.mean(v) for k, v in stage_ms.items()}
+    main_stages = {k: v for k, v in means.items() if k not in ("build_setup", "frame_begin")}
+    dominant = max(main_stages, key=main_stages.get)
+    byte_fn = {"cluster_classify": lambda o: M.classify_bytes(o, scene),
+               "triangle_instantiate": lambda o: M.instantiate_bytes(o, pipe.entries, scene)}
+    peak, peak_kind = measured_peak_hbm()
+    roof = None
+    if dominant in byte_fn:
+        alg = statistics.mean(byte_fn[dominant](o) for o in outs)
+        achieved = alg / (means[dominant] / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg,
+                "launch_ms": means[dominant], "traffic": None}
+        tpath = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tpath):
+            with open(tpath) as f:
+                roof["traffic"] = json.load(f).get(f"batched/{dominant}")
+    inst_alg = statistics.mean(M.instantiate_bytes(o, pipe.entries, scene) for o in outs)
+    stage_gbs = {"cluster_classify": statistics.mean(M.classify_bytes(o, scene) for o in outs)
+                 / (means["cluster_classify"] / 1e3) / 1e9,
+                 "triangle_instantiate": inst_alg / (means["triangle_instantiate"] / 1e3) / 1e9}
+
+    result = {
+        "metric": "tessellated tris/s", "value": value, "unit": "tris/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": statistics.mean(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural meshes and value-noise maps)",
+        "config": {"workload": WORKLOAD, "instances": 256, "base_triangles": scene.total_triangles,
+                   "clusters": scene.total_clusters, "tessellated_tris_per_frame": statistics.mean(tris),
+                   "l2": "flushed between timed frames (256 MiB write)", "mode": "CUDA graph, batched persistent stages",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e_value, "unit": "tris/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": L.Readback.itemsize, "ms_per_step": statistics.mean(e2e_times)},
+        "gpu_launches": gpu_launches,
+        "clocks": clk.summary(),
+        "roofline": roof,
+        "stages_ms": means,
+        "stage_gbs": stage_gbs,
+        "device_errors": errs,
+    }
+
+    if not args.no_extras:
+        result["batched_vs_plain"] = batched_vs_plain(pipe, torch, set_frame, flush)
+        pipe.close()
+        del pipe
+        torch.cuda.empty_cache()
+        result["terrain"] = terrain_bandwidth(torch, dev, local, peak)
+    if rank == 0:
+        result["cpu_baseline"] = cpu_baseline(args)
+        print(json.dumps(result))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def batched_vs_plain(pipe, torch, set_frame, flush, frames=(3, 17, 31)):
+    out = {}
+    for mode in ("graph", "batched", "plain"):
+        ts = []
+        for f in frames:
+            set_frame(f)
+            pipe.build(mode)  # warm
+            torch.cuda.synchronize()
+            flush()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            l0 = pipe.launch_count()
+            e0.record()
+            pipe.build(mode)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+            out[f"{mode}_launches"] = pipe.launch_count() - l0
+        out[f"{mode}_ms"] = statistics.mean(ts)
+    out["plain_over_graph"] = out["plain_ms"] / out["graph_ms"]
+    out["outputs_identical"] = "checked by tests/test_gpu_parity.py (batched, graph, plain byte-identical)"
+    return out
+
+
+def terrain_bandwidth(torch, dev, local, peak):
+    """Large bandwidth case: HBM GB/s of the instantiate kernel on the terrain."""
+    from vk_tessellated_clusters_gb300 import layouts as L
+    from vk_tessellated_clusters_gb300 import metrics as M
+    from vk_tessellated_clusters_gb300 import scene as S
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    scene = S.scene_terrain()
+    caps = terrain_caps()
+    pipe = TessellationPipeline(scene, caps, L.FLAG_CULLING, device=local)
+    pipe.set_cameras(S.camera_terrain())
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    pipe.build("graph")
+    torch.cuda.synchronize()
+    stage_ms, outs = profile_stages(pipe, torch, [0, 0, 0], lambda f: None, lambda: flush_buf.fill_(1))
+    means = {k: statistics.mean(v) for k, v in stage_ms.items()}
+    o = outs[-1]
+    alg = M.instantiate_bytes(o, pipe.entries, scene)
+    gbs = alg / (means["triangle_instantiate"] / 1e3) / 1e9
+    res = {"workload": "terrain 1024x1024 quads (2,097,152 tris), 4096^2 fp16 fBm 8 octaves, scale 0.1 extent, "
+                       "camera 10 deg grazing at height 2, 3840x2160, 4 px/segment",
+           "tessellated_tris": int(o["readback"]["numTotalTriangles"]),
+           "part_triangles": int(o["readback"]["numPartTriangles"]),
+           "split_triangles": int(o["readback"]["numSplitTriangles"]),
+           "generated_vertices": int(o["readback"]["numGenVertices"]),
+           "stages_ms": means, "instantiate_algorithmic_bytes": alg, "instantiate_gbs": gbs,
+           "instantiate_frac_of_peak": gbs / peak,
+           "frame_ms_graph": None}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush_buf.fill_(1)
+    e0.record()
+    pipe.build("graph")
+    e1.record()
+    torch.cuda.synchronize()
+    res["frame_ms_graph"] = e0.elapsed_time(e1)
+    res["tris_per_s"] = res["tessellated_tris"] / (res["frame_ms_graph"] / 1e3)
+    res["device_errors"] = pipe.device_errors()
+    pipe.close()
+    return res
+
+
+def cpu_baseline(args):
+    rate, el, frames, threads = cpu_oracle_rate(args.cpu_seconds)
+    return {"value": rate, "unit": "tris/s", "cores": threads, "kind": "port",
+            "sample": f"{frames} frames of the batched scene ({el:.1f} s, {threads} threads)"}
+
+
+def terrain_caps():
+    from vk_tessellated_clusters_gb300 import layouts as L
+    return L.default_caps(visible_bits=16, part_bits=21, split_bits=18, vertex_bits=25, megs=2048)
+
+
+def run_profile_case(args):
+    """A short, fixed sequence of frames of one case: the command ncu captures."""
+    import torch
+    from vk_tessellated_clusters_gb300 import layouts as L
+    from vk_tessellated_clusters_gb300 import scene as S
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    if args.profile_case == "batched":
+        scene, caps = S.scene_batched(256), L.default_caps()
+        cams = [S.camera_orbit(f) for f in range(args.warmup + args.steps)]
+    else:
+        scene, caps = S.scene_terrain(), terrain_caps()
+        cams = [S.camera_terrain()] * (args.warmup + args.steps)
+    pipe = TessellationPipeline(scene, caps, L.FLAG_CULLING)
+    for i, cam in enumerate(cams):
+        pipe.set_cameras(cam, cams[i - 1] if i else cam)
+        pipe.build("graph")
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": args.profile_case, "frames": len(cams), "device_errors": pipe.device_errors(),
+                      "readback_tris": int(pipe.state.readback.read(L.Readback, 1)[0]["numTotalTriangles"])}))
+    pipe.close()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.profile_case:
+        return run_profile_case(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

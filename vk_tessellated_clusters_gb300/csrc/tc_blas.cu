@@ -43,11 +43,16 @@ __global__ void k_blas_setup_insertion(StageCtx c)
     const u32  count = valid ? infos[i].clusterReferencesCount : 0u;
     u32        total;
     const u32  excl = block_exclusive_scan(count, s_warp, &total);
-    if(threadIdx.x == 0)
+    if(threadIdx.x < 32)
     {
-      s_excl = lookback_exclusive(c.scratch.lbState, tile, total, tile == 0 ? b->blasClusterCounter : 0, c.errorWord);
-      if(tile == numTiles - 1)
-        c.scratch.totals[0] = s_excl + total;
+      const u64 ex =
+          warp_lookback_exclusive(c.scratch.lbState, tile, total, tile == 0 ? b->blasClusterCounter : 0, c.errorWord);
+      if(threadIdx.x == 0)
+      {
+        s_excl = ex;
+        if(tile == numTiles - 1)
+          c.scratch.totals[0] = ex + total;
+      }
     }
     __syncthreads();
     if(valid)

@@ -177,17 +177,17 @@ __global__ void __launch_bounds__(W * 32) k_cluster_classify(StageCtx c)
     }
     __syncthreads();
 
-    // tile aggregates and look-back (one lane per counter)
-    if(warp == 0 && lane < kNumCounters)
+    // tile aggregates and look-back (one warp per counter)
+    for(u32 q = warp; q < kNumCounters; q += W)
     {
       u64 agg = 0;
 #pragma unroll
       for(int w = 0; w < W; w++)
-        agg += lane == kCntData ? s_data[w] : (u64)s_cnt[w][lane];
+        agg += q == kCntData ? s_data[w] : (u64)s_cnt[w][q];
       u64 base = 0;
       if(tile == 0)
       {
-        switch(lane)
+        switch(q)
         {
           case kCntParts:
             base = b->partTriangleCounter;
@@ -206,10 +206,13 @@ __global__ void __launch_bounds__(W * 32) k_cluster_classify(StageCtx c)
             break;
         }
       }
-      u64 ex       = lookback_exclusive(c.scratch.lbState + (u64)lane * c.scratch.lbStride, tile, agg, base, c.errorWord);
-      s_excl[lane] = ex;
-      if(tile == numTiles - 1)
-        c.scratch.totals[lane] = ex + agg;
+      const u64 ex = warp_lookback_exclusive(c.scratch.lbState + (u64)q * c.scratch.lbStride, tile, agg, base, c.errorWord);
+      if(lane == 0)
+      {
+        s_excl[q] = ex;
+        if(tile == numTiles - 1)
+          c.scratch.totals[q] = ex + agg;
+      }
     }
     __syncthreads();
 

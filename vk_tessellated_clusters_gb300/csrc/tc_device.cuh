@@ -317,8 +317,8 @@ __device__ __forceinline__ u32 ld_acquire_u32(const u32* p)
 // the exclusive prefix of per-tile aggregates in tile order, so appends are
 // ordered exactly like a serial loop. Each state word holds a 62-bit value and
 // a 2-bit flag (1 = tile aggregate, 2 = inclusive prefix). Tiles are handed out
-// through a ticket counter so a tile's predecessor is always owned by a running
-// block. Waits are bounded: after kSpinLimit empty polls the tile records
+// through a ticket counter so a tile's predecessors are always owned by running
+// blocks. Waits are bounded: after kSpinLimit polls the tile records
 // TC_DEVERR_LOOKBACK_TIMEOUT, uses what it accumulated and moves on.
 // ---------------------------------------------------------------------------
 
@@ -327,40 +327,69 @@ constexpr u64 kLbAggregate = 1ull << 62;
 constexpr u64 kLbPrefix    = 2ull << 62;
 constexpr u32 kSpinLimit   = 1u << 22;
 
-// Called by one lane per counter. `state` is this counter's tile-state array.
-// `base` is only used by tile 0 (counter value before this launch).
-__device__ __forceinline__ u64 lookback_exclusive(u64* state, u32 tile, u64 aggregate, u64 base, u32* errorWord)
+__device__ __forceinline__ u64 warp_sum_u64(u64 v)
 {
+#pragma unroll
+  for(int o = 16; o > 0; o >>= 1)
+    v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+  return v;
+}
+
+// Warp-cooperative look-back: all 32 lanes of one warp call it for one counter
+// and all receive the tile's exclusive prefix. Each step reads a window of the
+// 32 nearest predecessors at once (lane i reads tile - 1 - i), waits until all
+// of them have published, and either stops at the nearest inclusive prefix or
+// adds the 32 aggregates and moves the window back. `state` is this counter's
+// tile-state array; `base` (the counter value before this launch) is only used
+// by tile 0.
+__device__ __forceinline__ u64 warp_lookback_exclusive(u64* state, u32 tile, u64 aggregate, u64 base, u32* errorWord)
+{
+  const u32 lane = threadIdx.x & 31;
   if(tile == 0)
   {
-    st_release_u64(state, kLbPrefix | ((base + aggregate) & kLbValueMask));
+    if(lane == 0)
+      st_release_u64(state, kLbPrefix | ((base + aggregate) & kLbValueMask));
     return base;
   }
-  st_release_u64(state + tile, kLbAggregate | (aggregate & kLbValueMask));
-  u64 acc   = 0;
-  int t     = (int)tile - 1;
+  if(lane == 0)
+    st_release_u64(state + tile, kLbAggregate | (aggregate & kLbValueMask));
+  u64 excl  = 0;
+  int start = (int)tile - 1;
   u32 spins = 0;
-  while(t >= 0)
+  for(;;)
   {
-    u64 s = ld_acquire_u64(state + t);
-    u64 f = s & ~kLbValueMask;
-    if(f == 0)
+    const int t = start - (int)lane;
+    // window slots before tile 0 count as an empty inclusive prefix
+    u64 s = t >= 0 ? ld_acquire_u64(state + t) : kLbPrefix;
+    while(__any_sync(0xFFFFFFFFu, (s & ~kLbValueMask) == 0))
     {
       if(++spins > kSpinLimit)
       {
-        atomicOr(errorWord, TC_DEVERR_LOOKBACK_TIMEOUT);
+        if(lane == 0)
+          atomicOr(errorWord, TC_DEVERR_LOOKBACK_TIMEOUT);
+        s = kLbPrefix;  // give up on this window
         break;
       }
-      __nanosleep(64);
-      continue;
+      __nanosleep(32);
+      if((s & ~kLbValueMask) == 0)
+        s = ld_acquire_u64(state + t);
     }
-    acc += s & kLbValueMask;
-    if(f == kLbPrefix)
+    const u32 pmask = __ballot_sync(0xFFFFFFFFu, (s & ~kLbValueMask) == kLbPrefix);
+    u64       v     = s & kLbValueMask;
+    if(pmask)
+    {
+      const u32 first = __ffs(pmask) - 1;  // nearest predecessor holding an inclusive prefix
+      if(lane > first)
+        v = 0;
+      excl += warp_sum_u64(v);
       break;
-    t--;
+    }
+    excl += warp_sum_u64(v);
+    start -= 32;
   }
-  st_release_u64(state + tile, kLbPrefix | ((acc + aggregate) & kLbValueMask));
-  return acc;
+  if(lane == 0)
+    st_release_u64(state + tile, kLbPrefix | ((excl + aggregate) & kLbValueMask));
+  return excl;
 }
 
 // binary search: first index in [lo, hi) whose instance id (read by `get`) is >= key

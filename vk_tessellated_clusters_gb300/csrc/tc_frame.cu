@@ -177,11 +177,15 @@ __global__ void k_instances_classify(StageCtx c)
     }
     u32 total;
     u32 excl = block_exclusive_scan(nc, s_warp, &total);
-    if(threadIdx.x == 0)
+    if(threadIdx.x < 32)
     {
-      s_excl = lookback_exclusive(c.scratch.lbState, tile, total, 0, c.errorWord);
-      if(tile == numTiles - 1)
-        c.scratch.totals[0] = s_excl + total;
+      const u64 ex = warp_lookback_exclusive(c.scratch.lbState, tile, total, 0, c.errorWord);
+      if(threadIdx.x == 0)
+      {
+        s_excl = ex;
+        if(tile == numTiles - 1)
+          c.scratch.totals[0] = ex + total;
+      }
     }
     __syncthreads();
     if(valid)
@@ -257,11 +261,16 @@ __global__ void k_clusters_cull(StageCtx c)
     }
     u32 total;
     u32 rank = block_exclusive_scan(visible ? 1u : 0u, s_warp, &total);
-    if(threadIdx.x == 0)
+    if(threadIdx.x < 32)
     {
-      s_excl = lookback_exclusive(c.scratch.lbState, tile, total, tile == 0 ? b->visibleClusterCounter : 0, c.errorWord);
-      if(tile == numTiles - 1)
-        c.scratch.totals[0] = s_excl + total;
+      const u64 ex =
+          warp_lookback_exclusive(c.scratch.lbState, tile, total, tile == 0 ? b->visibleClusterCounter : 0, c.errorWord);
+      if(threadIdx.x == 0)
+      {
+        s_excl = ex;
+        if(tile == numTiles - 1)
+          c.scratch.totals[0] = ex + total;
+      }
     }
     __syncthreads();
     const u64 off = s_excl + rank;

@@ -51,6 +51,7 @@ __global__ void __launch_bounds__(B) k_triangle_instantiate(StageCtx c)
   __shared__ u32        s_vpre[kPartsPerTile + 1];  // vertex prefix within tile (accepted parts only)
   __shared__ __align__(16) float s_stage[kMaxTileVerts * 3 + 4];
   __shared__ u64 s_excl[kNumCounters];
+  __shared__ u64 s_agg[kNumCounters];
   __shared__ u64 s_vbase;
   __shared__ u32 s_tile, s_flag, s_range[2];
 
@@ -99,32 +100,34 @@ __global__ void __launch_bounds__(B) k_triangle_instantiate(StageCtx c)
     if(tile >= numTiles)
       break;
 
-    // ---- warp 0: allocation, arguments, per-part staging ------------------------
+    // ---- warp 0: read the tile's parts, per-part counts and their scans -----------
+    const u32           p     = begin + tile * kPartsPerTile + lane;
+    const bool          valid = warp == 0 && p < end;
+    tc_TessTriangleInfo info  = {};
+    u32                 cfg = 0, nv = 0, nt = 0;
+    u64                 ds = 0;
+    u32                 xv = 0;
+    u64                 xd = 0;
     if(warp == 0)
     {
-      const u32  p     = begin + tile * kPartsPerTile + lane;
-      const bool valid = p < end;
-      tc_TessTriangleInfo info;
-      u32                 cfg = 0, nv = 0, nt = 0;
-      u64                 ds  = 0;
       if(valid)
       {
-        const uint2* raw              = reinterpret_cast<const uint2*>(parts + p);
+        const uint2* raw                   = reinterpret_cast<const uint2*>(parts + p);
         uint2        r0 = raw[0], r1 = raw[1], r2 = raw[2];
-        info.cluster                  = {r0.x, r0.y};
-        info.subTriangle.vtxEncoded[0] = r1.x;
-        info.subTriangle.vtxEncoded[1] = r1.y;
-        info.subTriangle.vtxEncoded[2] = r2.x;
+        info.cluster                       = {r0.x, r0.y};
+        info.subTriangle.vtxEncoded[0]     = r1.x;
+        info.subTriangle.vtxEncoded[1]     = r1.y;
+        info.subTriangle.vtxEncoded[2]     = r2.x;
         info.subTriangle.triangleID_config = r2.y;
-        cfg                           = r2.y >> 16;
-        const tc_TessTableEntry e     = table_entry(c.table, cfg);
-        nv                            = e.numVertices;
-        nt                            = e.numTriangles;
-        ds                            = __ldg(c.table.templateSizes + cfg_index(cfg));
+        cfg                                = r2.y >> 16;
+        const tc_TessTableEntry e          = table_entry(c.table, cfg);
+        nv                                 = e.numVertices;
+        nt                                 = e.numTriangles;
+        ds                                 = __ldg(c.table.templateSizes + cfg_index(cfg));
       }
-      // warp scans (inclusive) of vertices (u32) and data (u64)
-      u32 xv = nv;
-      u64 xd = ds;
+      // warp scans (inclusive) of vertices (u32) and CLAS bytes (u64)
+      xv = nv;
+      xd = ds;
 #pragma unroll
       for(int d = 1; d < 32; d <<= 1)
       {
@@ -136,21 +139,35 @@ __global__ void __launch_bounds__(B) k_triangle_instantiate(StageCtx c)
           xd += yd;
         }
       }
-      const u32 tileParts = min((u32)kPartsPerTile, end - (begin + tile * kPartsPerTile));
-      const u32 aggV      = __shfl_sync(0xFFFFFFFFu, xv, 31);
-      const u64 aggD      = __shfl_sync(0xFFFFFFFFu, xd, 31);
-      if(lane < kNumCounters)
+      if(lane == 31)
       {
-        const u64 agg = lane == kCntGen ? tileParts : (lane == kCntData ? aggD : aggV);
-        u64       base = 0;
-        if(tile == 0)
-          base = lane == kCntGen ? b->genClusterCounter : (lane == kCntData ? b->genClusterDataCounter : b->genVertexCounter);
-        u64 ex       = lookback_exclusive(c.scratch.lbState + (u64)lane * c.scratch.lbStride, tile, agg, base, c.errorWord);
-        s_excl[lane] = ex;
-        if(tile == numTiles - 1)
-          c.scratch.totals[lane] = ex + agg;
+        s_agg[kCntGen]   = min((u32)kPartsPerTile, end - (begin + tile * kPartsPerTile));
+        s_agg[kCntData]  = xd;
+        s_agg[kCntVerts] = xv;
       }
-      __syncwarp();
+    }
+    __syncthreads();
+
+    // ---- look-back: warps 0..2, one counter each ------------------------------------
+    if(warp < kNumCounters)
+    {
+      u64 base = 0;
+      if(tile == 0)
+        base = warp == kCntGen ? b->genClusterCounter : (warp == kCntData ? b->genClusterDataCounter : b->genVertexCounter);
+      const u64 ex = warp_lookback_exclusive(c.scratch.lbState + (u64)warp * c.scratch.lbStride, tile, s_agg[warp], base,
+                                             c.errorWord);
+      if(lane == 0)
+      {
+        s_excl[warp] = ex;
+        if(tile == numTiles - 1)
+          c.scratch.totals[warp] = ex + s_agg[warp];
+      }
+    }
+    __syncthreads();
+
+    // ---- warp 0: acceptance, instantiation arguments, per-part staging ---------------
+    if(warp == 0)
+    {
       const u64 genOffset    = s_excl[kCntGen] + lane;
       const u64 dataOffset   = s_excl[kCntData] + (xd - ds);
       const u64 vertexOffset = s_excl[kCntVerts] + (xv - nv);

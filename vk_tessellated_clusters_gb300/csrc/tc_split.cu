@@ -233,22 +233,29 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
     }
 
     // ---- tile totals, look-back ------------------------------------------------
-    if(warp == 0 && lane < kNumCounters)
+    if(warp < kNumCounters)
     {
-      u32 agg = 0;
+      const u32 q   = warp;
+      u32       agg = 0;
       for(u32 ch = 0; ch < numChunks; ch++)
-      {
-        u32 v                  = s_chunkCnt[ch][lane];
-        s_chunkCnt[ch][lane]   = agg;  // exclusive within tile
-        agg += v;
-      }
+        agg += s_chunkCnt[ch][q];
       u64 base = 0;
       if(tile == 0)
-        base = lane == kCntSplit ? b->splitWriteCounter : b->partTriangleCounter;
-      u64 ex       = lookback_exclusive(c.scratch.lbState + (u64)lane * c.scratch.lbStride, tile, agg, base, c.errorWord);
-      s_excl[lane] = ex;
-      if(tile == numTiles - 1)
-        c.scratch.totals[lane] = ex + agg;
+        base = q == kCntSplit ? b->splitWriteCounter : b->partTriangleCounter;
+      const u64 ex = warp_lookback_exclusive(c.scratch.lbState + (u64)q * c.scratch.lbStride, tile, agg, base, c.errorWord);
+      if(lane == 0)
+      {
+        u32 run = 0;
+        for(u32 ch = 0; ch < numChunks; ch++)
+        {
+          u32 v              = s_chunkCnt[ch][q];
+          s_chunkCnt[ch][q]  = run;  // exclusive within tile
+          run += v;
+        }
+        s_excl[q] = ex;
+        if(tile == numTiles - 1)
+          c.scratch.totals[q] = ex + agg;
+      }
     }
     __syncthreads();
 
