@@ -433,14 +433,14 @@ typedef enum tc_status {
 #define TC_DEVERR_BAD_CONFIG 4u         /* a tess config outside the table */
 #define TC_DEVERR_CAPACITY 8u           /* work beyond the context's scratch sizing was dropped */
 
-/* Launch schedule: block size and tile shape per stage, picked by the autotuner
+/* Launch schedule: grid shapes per stage, picked by the autotuner
  * (vk_tessellated_clusters_gb300/autotune.py) or left at the defaults. */
 typedef struct tc_schedule {
-  uint32_t classifyWarpsPerBlock;   /* clusters per block (one warp each): 2,4,8,16 */
-  uint32_t splitBlockSize;          /* children per tile: 128,256,512 */
-  uint32_t instantiatePartsPerTile; /* part triangles per tile: 16,32,64 */
-  uint32_t instantiateBlockSize;    /* 128,256,512 */
-  uint32_t blocksPerSM;             /* persistent grid = SMs * blocksPerSM */
+  uint32_t classifyBlocksPerSM; /* grid of the per-cluster classify kernels = SMs x this (256 threads) */
+  uint32_t splitBlockSize;      /* split tile: 128 (16 items), 256 or 512 (32 items) threads */
+  uint32_t vertexBlocksPerSM;   /* grid of the vertex-generation kernel = SMs x this (256 threads) */
+  uint32_t scanBlocksPerSM;     /* grid of the scan / allocation kernels = SMs x this */
+  uint32_t blocksPerSM;         /* persistent grid of the split kernel = SMs x this x (512 / splitBlockSize) */
   uint32_t _pad[3];
 } tc_schedule;
 

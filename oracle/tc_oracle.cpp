@@ -38,11 +38,12 @@ inline f3    sub3(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 inline float dot3(f3 a, f3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
 inline float len3(f3 a) { return std::sqrt(dot3(a, a)); }
 inline float dist3(f3 a, f3 b) { return len3(sub3(a, b)); }
-// GLSL normalize(): v / length(v), per component IEEE division
+// GLSL normalize(): v * (1 / length(v)), one IEEE division then multiplies
+// (GLSL leaves the exact sequence to the implementation)
 inline f3 normalize3(f3 a)
 {
-  float l = len3(a);
-  return {a.x / l, a.y / l, a.z / l};
+  float r = 1.0f / len3(a);
+  return {a.x * r, a.y * r, a.z * r};
 }
 
 // (M * vec4(p, 1)).xyz with column-major M

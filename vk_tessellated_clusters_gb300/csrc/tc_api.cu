@@ -28,6 +28,11 @@ struct SlotPlan
 
 constexpr size_t kCtrlBytes = 8 + 8 * kMaxCounters;
 
+// kernels of a batched frame besides the split passes: frame_begin,
+// instances_classify, clusters_cull, classify (3), instantiate (2), blas setup,
+// blas insert (2)
+constexpr uint64_t kFrameFixedLaunches = 11;
+
 struct Plan
 {
   // slot indices
@@ -39,6 +44,9 @@ struct Plan
   u32    segStride;   // instances
   u32    segRows;     // runs
   size_t runOffset;   // run starts (u32 x kMaxRuns+2)
+  u32    classifyCap; // clusters the classify scratch holds
+  size_t clsCountsOffset, clsOffsetsOffset, clsTriWordsOffset;
+  size_t partVertexOffset;  // u32 per part triangle
   size_t instOffset;  // instance cluster prefix (u32 x maxInstances+1)
   size_t errOffset;   // device error word
   size_t totalBytes;
@@ -119,11 +127,12 @@ Plan make_plan(const tc_context_desc& d)
   };
   p.slotInstances   = add(ceil_div(d.maxInstances, kInstanceTile), 1);
   p.slotCull        = add(ceil_div(d.maxTotalClusters, kCullTile), 1);
-  p.slotClassify    = add(ceil_div(std::min<u64>(k.maxVisibleClusters, d.maxTotalClusters), kClassifyMinWarps), kMaxCounters);
+  p.classifyCap     = (u32)std::max<u64>(1, std::min<u64>(k.maxVisibleClusters, d.maxTotalClusters));
+  p.slotClassify    = add(classify_scan_tiles(p.classifyCap), kMaxCounters);
   p.slotSplit0      = add(ceil_div(k.maxSplitTriangles, kSplitMinItems), 2);
   for(u32 i = 1; i < passes; i++)
     add(ceil_div(k.maxSplitTriangles, kSplitMinItems), 2);
-  p.slotInstantiate = add(ceil_div(k.maxPartTriangles, kInstantiateTile), 3);
+  p.slotInstantiate = add(instantiate_alloc_tiles(k.maxPartTriangles), 3);
   p.slotBlas        = add(ceil_div(d.maxInstances, kInstanceTile), 1);
   p.numSlots        = (u32)p.slots.size();
   size_t off        = 0;
@@ -145,7 +154,16 @@ Plan make_plan(const tc_context_desc& d)
   off          = align_up(off + 4 * ((size_t)d.maxInstances + 1), 256);
   p.errOffset  = off;
   off          = align_up(off + 4, 256);
-  p.totalBytes = off;
+  // per-item scratch (written before it is read every launch; never zeroed)
+  p.clsCountsOffset   = off;
+  off                 = align_up(off + (size_t)p.classifyCap * 8, 256);
+  p.clsOffsetsOffset  = off;
+  off                 = align_up(off + (size_t)p.classifyCap * sizeof(ClusterOffsets), 256);
+  p.clsTriWordsOffset = off;
+  off                 = align_up(off + (size_t)p.classifyCap * TC_MAX_CLUSTER_TRIANGLES * 4, 256);
+  p.partVertexOffset  = off;
+  off                 = align_up(off + (size_t)std::max(1u, k.maxPartTriangles) * 4, 256);
+  p.totalBytes        = off;
   return p;
 }
 
@@ -209,9 +227,23 @@ void bind_slot(tc_context* ctx, StageCtx& c, u32 slot, bool selfClean)
   c.scratch.lbState   = reinterpret_cast<u64*>(ctx->dScratch + s.stateOffset);
   c.scratch.lbStride  = s.stride;
   c.scratch.selfClean = selfClean ? 1u : 0u;
+  c.scratch.itemCapacity = slot == ctx->plan.slotClassify ? ctx->plan.classifyCap : 0xFFFFFFFFu;
   c.scratch.ticket    = reinterpret_cast<u32*>(ctx->dScratch + s.ctrlOffset);
   c.scratch.done      = reinterpret_cast<u32*>(ctx->dScratch + s.ctrlOffset + 4);
   c.scratch.totals    = reinterpret_cast<u64*>(ctx->dScratch + s.ctrlOffset + 8);
+}
+
+ClassifyBuffers classify_buffers(tc_context* ctx)
+{
+  const Plan& p = ctx->plan;
+  return {reinterpret_cast<uint2*>(ctx->dScratch + p.clsCountsOffset),
+          reinterpret_cast<ClusterOffsets*>(ctx->dScratch + p.clsOffsetsOffset),
+          reinterpret_cast<u32*>(ctx->dScratch + p.clsTriWordsOffset)};
+}
+
+InstantiateBuffers instantiate_buffers(tc_context* ctx)
+{
+  return {reinterpret_cast<u32*>(ctx->dScratch + ctx->plan.partVertexOffset)};
 }
 
 u32 persistent_grid(const tc_context* ctx, u32 maxTiles, u32 blocksPerSM)
@@ -225,19 +257,9 @@ u32 frame_begin_grid(const tc_context* ctx, const tc_frame_args* a)
   return std::max(1u, std::min(ctx->numSMs * 2, ceil_div((u64)a->caps.maxSplitTriangles * 6, 256)));
 }
 
-u32 classify_warps(const tc_schedule& s)
-{
-  u32 w = s.classifyWarpsPerBlock;
-  return (w == 2 || w == 4 || w == 8 || w == 16) ? w : 8;
-}
 u32 split_block(const tc_schedule& s)
 {
   u32 b = s.splitBlockSize;
-  return (b == 128 || b == 256 || b == 512) ? b : 256;
-}
-u32 inst_block(const tc_schedule& s)
-{
-  u32 b = s.instantiateBlockSize;
   return (b == 128 || b == 256 || b == 512) ? b : 256;
 }
 u32 split_items_per_tile(u32 block) { return block == 128 ? 16 : 32; }
@@ -261,11 +283,10 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   c.fuseSetup = TC_BUILD_SETUP_CLASSIFY;
   TC_CHECK_CUDA(launch_clusters_cull(c, persistent_grid(ctx, ceil_div(a->totalClusters, kCullTile), 4), kCullTile, s));
 
-  const u32 W = classify_warps(sched);
   bind_slot(ctx, c, p.slotClassify, false);
   c.fuseSetup = TC_BUILD_SETUP_SPLIT;
-  TC_CHECK_CUDA(launch_cluster_classify(
-      c, W, persistent_grid(ctx, ceil_div(std::min(a->totalClusters, a->caps.maxVisibleClusters), W), bpsm * (16 / W)), s));
+  TC_CHECK_CUDA(launch_cluster_classify(c, classify_buffers(ctx), std::min(a->totalClusters, a->caps.maxVisibleClusters),
+                                        ctx->numSMs, s));
 
   const u32 passes = split_passes(a->caps.splitFactor);
   const u32 sb     = split_block(sched);
@@ -277,11 +298,10 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
         c, sb, persistent_grid(ctx, ceil_div(a->caps.maxSplitTriangles, split_items_per_tile(sb)), bpsm * (512 / sb)), s));
   }
 
-  const u32 ib = inst_block(sched);
   bind_slot(ctx, c, p.slotInstantiate, false);
   c.fuseSetup = TC_BUILD_SETUP_BUILD_BLAS;
-  TC_CHECK_CUDA(launch_triangle_instantiate(
-      c, ib, persistent_grid(ctx, ceil_div(a->caps.maxPartTriangles, kInstantiateTile), bpsm * (512 / ib)), s));
+  TC_CHECK_CUDA(launch_triangle_instantiate(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
+                                            std::max(1u, sched.vertexBlocksPerSM), s));
 
   bind_slot(ctx, c, p.slotBlas, false);
   c.fuseSetup = kNoSetup;
@@ -290,7 +310,7 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   u32* seg = reinterpret_cast<u32*>(ctx->dScratch + p.segOffset);
   TC_CHECK_CUDA(launch_blas_clusters_insert(c, seg, seg + (size_t)p.segStride * p.segRows, p.segStride, ctx->numSMs * 4, s));
 
-  ctx->launches += 9 + passes;
+  ctx->launches += kFrameFixedLaunches + passes;
   return TC_OK;
 }
 
@@ -342,7 +362,7 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, desc->device);
   ctx->numSMs   = (u32)std::max(1, sms);
-  ctx->schedule = {8, 256, 32, 256, 4, {0, 0, 0}};
+  ctx->schedule = {8, 256, 6, 8, 1, {0, 0, 0}};
   ctx->plan     = make_plan(*desc);
   if(cudaMalloc(&ctx->dScratch, ctx->plan.totalBytes) != cudaSuccess
      || cudaMemset(ctx->dScratch, 0, ctx->plan.totalBytes) != cudaSuccess)
@@ -554,7 +574,7 @@ tc_status tc_frame_build_graph(tc_context* ctx, const tc_frame_args* args, void*
     ctx->graphValid    = true;
   }
   TC_CHECK_CUDA(cudaGraphLaunch(ctx->graphExec, s));
-  ctx->launches += 9 + split_passes(args->caps.splitFactor);
+  ctx->launches += kFrameFixedLaunches + split_passes(args->caps.splitFactor);
   return TC_OK;
 }
 
@@ -627,12 +647,9 @@ tc_status tc_cluster_classify(tc_context* ctx, const tc_frame_args* a, uint32_t 
   c.instBegin = instanceBegin;
   c.instEnd   = instanceEnd;
   bind_slot(ctx, c, ctx->plan.slotClassify, true);
-  const u32 W = classify_warps(ctx->schedule);
-  TC_CHECK_CUDA(launch_cluster_classify(c, W,
-                                        persistent_grid(ctx, ceil_div(std::min(a->totalClusters, a->caps.maxVisibleClusters), W),
-                                                        std::max(1u, ctx->schedule.blocksPerSM) * (16 / W)),
-                                        reinterpret_cast<cudaStream_t>(stream)));
-  ctx->launches += 1;
+  TC_CHECK_CUDA(launch_cluster_classify(c, classify_buffers(ctx), std::min(a->totalClusters, a->caps.maxVisibleClusters),
+                                        ctx->numSMs, reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += 3;
   return TC_OK;
 }
 
@@ -672,12 +689,10 @@ tc_status tc_triangle_instantiate_run(tc_context* ctx, const tc_frame_args* a, u
   c.instEnd   = instanceEnd;
   c.run       = run;
   bind_slot(ctx, c, ctx->plan.slotInstantiate, true);
-  const u32 ib = inst_block(ctx->schedule);
-  TC_CHECK_CUDA(launch_triangle_instantiate(c, ib,
-                                            persistent_grid(ctx, ceil_div(a->caps.maxPartTriangles, kInstantiateTile),
-                                                            std::max(1u, ctx->schedule.blocksPerSM) * (512 / ib)),
+  TC_CHECK_CUDA(launch_triangle_instantiate(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
+                                            std::max(1u, ctx->schedule.vertexBlocksPerSM),
                                             reinterpret_cast<cudaStream_t>(stream)));
-  ctx->launches += 1;
+  ctx->launches += 2;
   return TC_OK;
 }
 

@@ -3,12 +3,19 @@
 //
 // shaders/cluster_classify.comp.glsl:150-666 (RT target, plain path).
 //
-// GB300 mapping: one warp per cluster (<= 64 triangles: two per lane), W
-// clusters per block, the cluster's vertices staged in shared memory. Appends
-// (part triangles, split triangles, full-cluster instantiations, generated
-// vertices, CLAS bytes) are ordered by a block scan plus a decoupled look-back
-// across tiles, so every offset equals the one a serial loop over the visible
-// clusters would produce. Persistent grid: blocks pull tiles from a ticket.
+// GB300 mapping, three launches per stage so that the heavy kernels have no
+// block-wide barriers and no cross-block waits:
+//   count : one warp per cluster (<= 64 triangles, two per lane), vertices
+//           staged in shared memory; segment counts, configs and the
+//           cluster's counts (part / split triangles, full-cluster vertices,
+//           CLAS bytes) go to scratch
+//   scan  : exclusive scan of those counts over the clusters in visible order
+//           (512 clusters per tile, decoupled look-back between tiles), so
+//           every offset equals what a serial loop over the clusters gives
+//   write : one warp per cluster again; part / split triangles, instantiation
+//           arguments and the displaced full-cluster vertices at their offsets
+#include <algorithm>
+
 #include "tc_kernels.h"
 #include "tc_stage.cuh"
 
@@ -16,375 +23,325 @@ namespace tc {
 
 namespace {
 
+constexpr u32 kScanItemsPerThread = 2;
+constexpr u32 kScanBlock          = 256;
+constexpr u32 kScanTile           = kScanItemsPerThread * kScanBlock;  // clusters per scan tile
+
 enum : int
 {
   kCntParts = 0,
   kCntSplits,
   kCntGen,
-  kCntData,
   kCntVerts,
+  kCntData,
   kNumCounters
 };
 
-__device__ __forceinline__ void store_tess_info(tc_TessTriangleInfo* dst, const tc_ClusterInfo& ci, u32 v0, u32 v1, u32 v2,
-                                                u32 tc)
+// per-cluster counts: x = parts | splits << 7 | full << 14 | fullVertices << 15, y = CLAS bytes
+__device__ __forceinline__ uint2 pack_counts(u32 parts, u32 splits, bool full, u32 nv, u32 data)
 {
-  uint2* p = reinterpret_cast<uint2*>(dst);
-  p[0]     = make_uint2(ci.instanceID, ci.clusterID);
-  p[1]     = make_uint2(v0, v1);
-  p[2]     = make_uint2(v2, tc);
+  return make_uint2(parts | (splits << 7) | ((full ? 1u : 0u) << 14) | ((full ? nv : 0u) << 15), full ? data : 0u);
+}
+__device__ __forceinline__ u32 cnt_parts(uint2 r) { return r.x & 0x7F; }
+__device__ __forceinline__ u32 cnt_splits(uint2 r) { return (r.x >> 7) & 0x7F; }
+__device__ __forceinline__ u32 cnt_full(uint2 r) { return (r.x >> 14) & 1; }
+__device__ __forceinline__ u32 cnt_verts(uint2 r) { return (r.x >> 15) & 0x7F; }
+
+// tessellation.glsl:119-144 tess_getConfig, also reporting how the three
+// sub-triangle corners were rotated (0: none, 1: .yzx, 2: .zxy)
+__device__ __forceinline__ u32 get_config_rot(uint3 f, u32& rot)
+{
+  u32 m = max(max(f.x, f.y), f.z);
+  rot   = 0;
+  if(m == f.y)
+  {
+    f   = make_uint3(f.y, f.z, f.x);
+    rot = 1;
+  }
+  else if(m == f.z)
+  {
+    f   = make_uint3(f.z, f.x, f.y);
+    rot = 2;
+  }
+  const u32 L   = TC_TESSTABLE_LOOKUP_SIZE;
+  u32       idx = f.x + f.y * L + f.z * L * L - (1 + L + L * L);
+  if(f.z > f.y)
+    idx |= 1u << 15;
+  return idx;
 }
 
-template <int W>
-__global__ void __launch_bounds__(W * 32) k_cluster_classify(StageCtx c)
+// per-triangle word: config | rotation << 16 | split << 18
+__device__ __forceinline__ u32 classify_triangle(uint3 f, u32 sf)
 {
-  __shared__ f3  s_vert[W][TC_MAX_CLUSTER_VERTICES];
-  __shared__ u32 s_cnt[W][kNumCounters];
-  __shared__ u64 s_data[W];
-  __shared__ u32 s_fullInst[W];  // instance of an accepted full cluster, ~0 otherwise
-  __shared__ u64 s_excl[kNumCounters];
-  __shared__ u32 s_tile, s_flag, s_range[2];
+  const u32  m     = max(max(f.x, f.y), f.z);
+  const bool split = m > TC_TESSTABLE_SIZE;
+  if(split)
+    f = make_uint3(split_factor1(f.x, sf), split_factor1(f.y, sf), split_factor1(f.z, sf));
+  u32       rot;
+  const u32 cfg = get_config_rot(f, rot);
+  return cfg | (rot << 16) | ((split ? 1u : 0u) << 18);
+}
 
-  const u32         lane = threadIdx.x & 31;
-  const u32         warp = threadIdx.x >> 5;
-  tc_SceneBuilding* b    = c.build;
-  const tc_caps&    k    = c.caps;
+struct ClassifyScratch
+{
+  uint2*          counts;    // per visible cluster of the window
+  ClusterOffsets* offsets;   // per visible cluster of the window
+  u32*            triWords;  // 64 per visible cluster
+};
 
-  // visible clusters of the instance window (visibleClusters is sorted by instance)
-  const tc_ClusterInfo* vis = reinterpret_cast<const tc_ClusterInfo*>(b->visibleClusters);
-  if(threadIdx.x == 0)
+// visible clusters of the instance window (visibleClusters is sorted by instance)
+__device__ inline void window_range(const StageCtx& c, u32& lo, u32& hi)
+{
+  const tc_ClusterInfo* vis = reinterpret_cast<const tc_ClusterInfo*>(c.build->visibleClusters);
+  lo                        = 0;
+  hi                        = min(c.build->visibleClusterCounter, c.caps.maxVisibleClusters);
+  if(!whole_window(c))
   {
-    u32 lo = 0, hi = min(b->visibleClusterCounter, c.caps.maxVisibleClusters);
-    if(!whole_window(c))
-    {
-      auto get = [&](u32 i) { return vis[i].instanceID; };
-      u32  e   = lower_bound_instance(lo, hi, c.instEnd, get);
-      lo       = lower_bound_instance(lo, e, c.instBegin, get);
-      hi       = e;
-    }
-    s_range[0] = lo;
-    s_range[1] = hi;
+    auto get = [&](u32 i) { return vis[i].instanceID; };
+    u32  e   = lower_bound_instance(lo, hi, c.instEnd, get);
+    lo       = lower_bound_instance(lo, e, c.instBegin, get);
+    hi       = e;
   }
-  __syncthreads();
-  const u32 begin = s_range[0], end = s_range[1];
-  u32 numTiles = (end - begin + W - 1) / W;
-  numTiles = clamp_tiles(c, numTiles);
+}
 
+__device__ __forceinline__ FactorParams factor_params(const StageCtx& c)
+{
   FactorParams fp;
-  fp.viewPos   = {b->viewPos.x, b->viewPos.y, b->viewPos.z};
+  fp.viewPos   = {c.build->viewPos.x, c.build->viewPos.y, c.build->viewPos.z};
   fp.nearPlane = c.view->nearPlane;
   fp.viewportH = c.view->viewportf.y;
   fp.tessRate  = c.view->tessRate;
+  return fp;
+}
 
-  const bool culling      = (c.flags & TC_FLAG_CULLING) != 0;
-  const bool haveTextures = c.numTextures > 0 && c.textures != nullptr;
-  const u64  maxData      = (u64)k.maxGeneratedClusterMegs * 1024ull * 1024ull;
-  const u32  sf           = clamp_split_factor(k.splitFactor);
+// ---------------------------------------------------------------------------
+// count
+// ---------------------------------------------------------------------------
 
-  u32 statFull = 0, statTotalTris = 0, statTemp = 0;
+__global__ void __launch_bounds__(256) k_classify_count(StageCtx c, ClassifyScratch cs)
+{
+  __shared__ f3  s_vert[8][TC_MAX_CLUSTER_VERTICES];
+  __shared__ u32 s_range[2];
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if(threadIdx.x == 0)
+    window_range(c, s_range[0], s_range[1]);
+  __syncthreads();
+  const u32 begin = s_range[0];
+  const u32 n     = min(s_range[1] - s_range[0], c.scratch.itemCapacity);
+
+  const tc_SceneBuilding* b       = c.build;
+  const tc_ClusterInfo*   vis     = reinterpret_cast<const tc_ClusterInfo*>(b->visibleClusters);
+  const FactorParams      fp      = factor_params(c);
+  const bool              culling = (c.flags & TC_FLAG_CULLING) != 0;
+  const u32               sf      = clamp_split_factor(c.caps.splitFactor);
+  const u32               nwarps  = (gridDim.x * blockDim.x) >> 5;
+
+  for(u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nwarps)
+  {
+    const tc_ClusterInfo     ci = vis[begin + v];
+    const tc_RenderInstance* in = c.instances + ci.instanceID;
+    const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
+    u32                      nt = cl.numTriangles, nv = cl.numVertices;
+    if(nt > TC_MAX_CLUSTER_TRIANGLES || nv > TC_MAX_CLUSTER_VERTICES)
+    {
+      if(lane == 0)
+        atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
+      nt = min(nt, TC_MAX_CLUSTER_TRIANGLES);
+      nv = min(nv, TC_MAX_CLUSTER_VERTICES);
+    }
+    const bool culled =
+        culling && (reinterpret_cast<const u32*>(b->instanceStates)[ci.instanceID] & TC_INSTANCE_VISIBLE_BIT) == 0;
+    u32 m0 = 0, m1 = 0, w0 = 0, w1 = 0;
+    u32 simple = nt;  // cluster_classify.comp.glsl:203-211: invisible instance, no tessellation
+    if(!culled)
+    {
+      // cluster_classify.comp.glsl:180-198 object-space vertices, then 217-246 factors
+      const float* pos = reinterpret_cast<const float*>(in->positions);
+      for(u32 i = lane; i < nv; i += 32)
+        s_vert[warp][i] = ldg3(pos, cl.firstLocalVertex + i);
+      float m[16];
+#pragma unroll
+      for(int j = 0; j < 16; j++)
+        m[j] = __ldg(in->worldMatrix.m + j);
+      __syncwarp();
+      // indices are masked to the staged range: a malformed index reads a wrong
+      // vertex of the same cluster, never outside shared memory
+      const uint8_t* lt = reinterpret_cast<const uint8_t*>(in->clusterLocalTriangles) + cl.firstLocalTriangle;
+      if(lane < nt)
+      {
+        const uint3 f = tess_factors(xform_point(m, s_vert[warp][lt[lane * 3 + 0] & 63u]),
+                                     xform_point(m, s_vert[warp][lt[lane * 3 + 1] & 63u]),
+                                     xform_point(m, s_vert[warp][lt[lane * 3 + 2] & 63u]), fp);
+        m0 = max(max(f.x, f.y), f.z);
+        w0 = classify_triangle(f, sf);
+      }
+      if(lane + 32 < nt)
+      {
+        const u32   t = lane + 32;
+        const uint3 f = tess_factors(xform_point(m, s_vert[warp][lt[t * 3 + 0] & 63u]),
+                                     xform_point(m, s_vert[warp][lt[t * 3 + 1] & 63u]),
+                                     xform_point(m, s_vert[warp][lt[t * 3 + 2] & 63u]), fp);
+        m1 = max(max(f.x, f.y), f.z);
+        w1 = classify_triangle(f, sf);
+      }
+      simple = __popc(__ballot_sync(0xFFFFFFFFu, lane < nt && m0 == 1))
+               + __popc(__ballot_sync(0xFFFFFFFFu, lane + 32 < nt && m1 == 1));
+      __syncwarp();  // s_vert is reused by the next cluster
+    }
+    const bool full  = simple == nt;
+    u32        parts = 0, splits = 0;
+    if(!full)
+    {
+      parts  = __popc(__ballot_sync(0xFFFFFFFFu, lane < nt && m0 <= TC_TESSTABLE_SIZE))
+               + __popc(__ballot_sync(0xFFFFFFFFu, lane + 32 < nt && m1 <= TC_TESSTABLE_SIZE));
+      splits = nt - parts;
+      u32* tw = cs.triWords + (u64)v * TC_MAX_CLUSTER_TRIANGLES;
+      if(lane < nt)
+        tw[lane] = w0;
+      if(lane + 32 < nt)
+        tw[lane + 32] = w1;
+    }
+    if(lane == 0)
+    {
+      const u32 data =
+          full ? __ldg(reinterpret_cast<const u32*>(in->clusterTemplateInstantiatonSizes) + ci.clusterID) : 0u;
+      cs.counts[v] = pack_counts(parts, splits, full, nv, data);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// scan
+// ---------------------------------------------------------------------------
+
+template <class T>
+__device__ __forceinline__ T warp_inclusive(T x, u32 lane)
+{
+#pragma unroll
+  for(int d = 1; d < 32; d <<= 1)
+  {
+    T y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+    if(lane >= (u32)d)
+      x += y;
+  }
+  return x;
+}
+
+// block-wide exclusive scan of kNumCounters values per thread
+__device__ inline void block_scan5(u64 (&v)[kNumCounters], u64 (&tot)[kNumCounters], u64 (*s_warp)[kNumCounters])
+{
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  u64       inc[kNumCounters];
+#pragma unroll
+  for(int q = 0; q < kNumCounters; q++)
+  {
+    inc[q] = warp_inclusive<u64>(v[q], lane);
+    if(lane == 31)
+      s_warp[warp][q] = inc[q];
+  }
+  __syncthreads();
+  if(warp == 0)
+  {
+#pragma unroll
+    for(int q = 0; q < kNumCounters; q++)
+    {
+      u64 w = lane < nw ? s_warp[lane][q] : 0;
+      u64 s = warp_inclusive<u64>(w, lane);
+      __syncwarp();
+      if(lane < nw)
+        s_warp[lane][q] = s - w;
+      if(lane == 31)
+        s_warp[32][q] = s;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for(int q = 0; q < kNumCounters; q++)
+  {
+    tot[q] = s_warp[32][q];
+    v[q]   = s_warp[warp][q] + inc[q] - v[q];
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_classify_scan(StageCtx c, ClassifyScratch cs)
+{
+  __shared__ u64 s_warp[33][kNumCounters];
+  __shared__ u64 s_excl[kNumCounters];
+  __shared__ u32 s_tile, s_flag, s_range[2];
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if(threadIdx.x == 0)
+    window_range(c, s_range[0], s_range[1]);
+  __syncthreads();
+  const u32 n        = min(s_range[1] - s_range[0], c.scratch.itemCapacity);
+  u32       numTiles = (n + kScanTile - 1) / kScanTile;
+  numTiles           = clamp_tiles(c, numTiles);
+  tc_SceneBuilding* b = c.build;
 
   for(;;)
   {
     const u32 tile = next_tile(c, &s_tile);
     if(tile >= numTiles)
       break;
-
-    const u32  v     = begin + tile * W + warp;
-    const bool valid = v < end;
-
-    tc_ClusterInfo           ci = {0, 0};
-    const tc_RenderInstance* in = nullptr;
-    tc_Cluster               cl = {};
-    uint3                    f0 = {1, 1, 1}, f1 = {1, 1, 1};
-    u32                      m0 = 0, m1 = 0;
-    u32                      nt = 0, nv = 0, simple = 0;
-    bool                     isFull = false;
-    if(valid)
-    {
-      ci = vis[v];
-      in = c.instances + ci.instanceID;
-      cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
-      nt = cl.numTriangles;
-      nv = cl.numVertices;
-      if(nt > TC_MAX_CLUSTER_TRIANGLES || nv > TC_MAX_CLUSTER_VERTICES)
-      {
-        if(lane == 0)
-          atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
-        nt = min(nt, TC_MAX_CLUSTER_TRIANGLES);
-        nv = min(nv, TC_MAX_CLUSTER_VERTICES);
-      }
-      const float* pos = reinterpret_cast<const float*>(in->positions);
-      // cluster_classify.comp.glsl:180-198: stage object-space vertices
-      for(u32 i = lane; i < nv; i += 32)
-        s_vert[warp][i] = ldg3(pos, cl.firstLocalVertex + i);
-      __syncwarp();
-
-      const bool culled = culling && (reinterpret_cast<const u32*>(b->instanceStates)[ci.instanceID] & TC_INSTANCE_VISIBLE_BIT) == 0;
-      if(culled)
-      {
-        // cluster_classify.comp.glsl:203-211: invisible instance, no tessellation
-        simple = nt;
-      }
-      else
-      {
-        // cluster_classify.comp.glsl:217-246
-        const uint8_t* lt = reinterpret_cast<const uint8_t*>(in->clusterLocalTriangles) + cl.firstLocalTriangle;
-        const float*   wm = in->worldMatrix.m;
-        float          m[16];
+    const u32 first = tile * kScanTile + threadIdx.x * kScanItemsPerThread;
+    uint2     rec[kScanItemsPerThread];
+    u64       sum[kNumCounters] = {0, 0, 0, 0, 0};
 #pragma unroll
-        for(int j = 0; j < 16; j++)
-          m[j] = __ldg(wm + j);
-        // vertex indices are masked to the staged range (a malformed index reads
-        // a wrong vertex of the same cluster, never outside shared memory)
-        if(lane < nt)
-        {
-          f0 = tess_factors(xform_point(m, s_vert[warp][lt[lane * 3 + 0] & 63u]),
-                            xform_point(m, s_vert[warp][lt[lane * 3 + 1] & 63u]),
-                            xform_point(m, s_vert[warp][lt[lane * 3 + 2] & 63u]), fp);
-          m0 = max(max(f0.x, f0.y), f0.z);
-        }
-        if(lane + 32 < nt)
-        {
-          const u32 t = lane + 32;
-          f1 = tess_factors(xform_point(m, s_vert[warp][lt[t * 3 + 0] & 63u]), xform_point(m, s_vert[warp][lt[t * 3 + 1] & 63u]),
-                            xform_point(m, s_vert[warp][lt[t * 3 + 2] & 63u]), fp);
-          m1 = max(max(f1.x, f1.y), f1.z);
-        }
-        simple = __popc(__ballot_sync(0xFFFFFFFFu, lane < nt && m0 == 1))
-                 + __popc(__ballot_sync(0xFFFFFFFFu, lane + 32 < nt && m1 == 1));
-      }
-      isFull = simple == nt;
-    }
-
-    // per-cluster counts
-    if(lane == 0)
+    for(u32 i = 0; i < kScanItemsPerThread; i++)
     {
-      s_data[warp] = (valid && isFull) ? __ldg(reinterpret_cast<const u32*>(in->clusterTemplateInstantiatonSizes) + ci.clusterID) : 0u;
-      s_cnt[warp][kCntGen]    = (valid && isFull) ? 1u : 0u;
-      s_cnt[warp][kCntVerts]  = (valid && isFull) ? nv : 0u;
-      s_cnt[warp][kCntParts]  = 0;
-      s_cnt[warp][kCntSplits] = 0;
+      rec[i] = first + i < n ? cs.counts[first + i] : make_uint2(0, 0);
+      sum[kCntParts] += cnt_parts(rec[i]);
+      sum[kCntSplits] += cnt_splits(rec[i]);
+      sum[kCntGen] += cnt_full(rec[i]);
+      sum[kCntVerts] += cnt_verts(rec[i]);
+      sum[kCntData] += rec[i].y;
     }
-    if(valid && !isFull)
+    u64 tot[kNumCounters];
+    block_scan5(sum, tot, s_warp);
+    if(warp < kNumCounters)
     {
-      u32 p = __popc(__ballot_sync(0xFFFFFFFFu, lane < nt && m0 <= TC_TESSTABLE_SIZE))
-              + __popc(__ballot_sync(0xFFFFFFFFu, lane + 32 < nt && m1 <= TC_TESSTABLE_SIZE));
-      if(lane == 0)
-      {
-        s_cnt[warp][kCntParts]  = p;
-        s_cnt[warp][kCntSplits] = nt - p;
-      }
-    }
-    __syncthreads();
-
-    // tile aggregates and look-back (one warp per counter)
-    for(u32 q = warp; q < kNumCounters; q += W)
-    {
-      u64 agg = 0;
-#pragma unroll
-      for(int w = 0; w < W; w++)
-        agg += q == kCntData ? s_data[w] : (u64)s_cnt[w][q];
-      u64 base = 0;
+      const u32 q    = warp;
+      u64       base = 0;
       if(tile == 0)
-      {
-        switch(q)
-        {
-          case kCntParts:
-            base = b->partTriangleCounter;
-            break;
-          case kCntSplits:
-            base = (u64)(u32)b->splitTriangleCounter;
-            break;
-          case kCntGen:
-            base = b->genClusterCounter;
-            break;
-          case kCntData:
-            base = b->genClusterDataCounter;
-            break;
-          default:
-            base = b->genVertexCounter;
-            break;
-        }
-      }
-      const u64 ex = warp_lookback_exclusive(c.scratch.lbState + (u64)q * c.scratch.lbStride, tile, agg, base, c.errorWord);
+        base = q == kCntParts    ? b->partTriangleCounter
+               : q == kCntSplits ? (u64)(u32)b->splitTriangleCounter
+               : q == kCntGen    ? b->genClusterCounter
+               : q == kCntVerts  ? b->genVertexCounter
+                                 : b->genClusterDataCounter;
+      const u64 ex =
+          warp_lookback_exclusive(c.scratch.lbState + (u64)q * c.scratch.lbStride, tile, tot[q], base, c.errorWord);
       if(lane == 0)
       {
         s_excl[q] = ex;
         if(tile == numTiles - 1)
-          c.scratch.totals[q] = ex + agg;
+          c.scratch.totals[q] = ex + tot[q];
       }
     }
     __syncthreads();
-
-    if(valid)
-    {
-      // this warp's exclusive offsets
-      u64 off[kNumCounters];
+    u64 run[kNumCounters];
 #pragma unroll
-      for(int q = 0; q < kNumCounters; q++)
-        off[q] = s_excl[q];
-      for(u32 w = 0; w < warp; w++)
-      {
-        off[kCntParts] += s_cnt[w][kCntParts];
-        off[kCntSplits] += s_cnt[w][kCntSplits];
-        off[kCntGen] += s_cnt[w][kCntGen];
-        off[kCntData] += s_data[w];
-        off[kCntVerts] += s_cnt[w][kCntVerts];
-      }
-
-      if(isFull)
-      {
-        // cluster_classify.comp.glsl:271-488: template instantiation of the full cluster
-        const u64 genOffset    = off[kCntGen];
-        const u64 dataOffset   = off[kCntData];
-        const u64 dataSize     = s_data[warp];
-        const u64 vertexOffset = off[kCntVerts];
-        const bool accept      = !(vertexOffset + nv > k.maxGeneratedVertices || genOffset + 1 > k.maxGeneratedClusters
-                                   || dataOffset + dataSize > maxData);
-        if(lane == 0)
-        {
-          statFull += 1;
-          s_fullInst[warp] = accept ? ci.instanceID : ~0u;
-        }
-        if(accept)
-        {
-          if(lane == 0)
-          {
-            // accepted instantiations form a prefix of the serial order, so
-            // the instantiation slot equals the generated-cluster slot
-            const u32                  tempOffset = (u32)genOffset;
-            tc_TemplateInstantiateInfo ti;
-            ti.clusterIdOffset        = 0;
-            ti.geometryIndexOffset    = 0;
-            ti.clusterTemplateAddress = __ldg(reinterpret_cast<const u64*>(in->clusterTemplateAdresses) + ci.clusterID);
-            ti.vertexBufferAddress    = b->genVertices + vertexOffset * 12ull;
-            ti.vertexBufferStride     = 12;
-            reinterpret_cast<tc_TemplateInstantiateInfo*>(b->tempInstantiations)[tempOffset] = ti;
-            reinterpret_cast<u32*>(b->tempInstanceIDs)[tempOffset]                          = ci.instanceID;
-            reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset]                     = b->genClusterData + dataOffset;
-            if((c.flags & TC_FLAG_WRITE_FULLCLUSTERS) && b->fullClusters)
-              reinterpret_cast<tc_ClusterInfo*>(b->fullClusters)[tempOffset] = ci;
-            statTemp += 1;
-            statTotalTris += simple;
-          }
-          // cluster_classify.comp.glsl:457-482: displaced cluster vertices
-          float*                        gv = reinterpret_cast<float*>(b->genVertices);
-          const tc_DisplacementTexture* tx = nullptr;
-          if(haveTextures && in->displacementIndex >= 0)
-          {
-            if((u32)in->displacementIndex < c.numTextures)
-              tx = c.textures + in->displacementIndex;
-            else if(lane == 0)
-              atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
-          }
-          const float* nrm = reinterpret_cast<const float*>(in->normals);
-          const float* uvs = reinterpret_cast<const float*>(in->texcoords);
-          for(u32 i = lane; i < nv; i += 32)
-          {
-            f3 p = s_vert[warp][i];
-            if(tx)
-            {
-              const u32 vi = cl.firstLocalVertex + i;
-              float     h  = sample_bilinear(*tx, ldg2(uvs, vi));
-              p = displace(p, ldg3(nrm, vi), h, in->displacementScale, c.view->displacementScale, in->displacementOffset,
-                           c.view->displacementOffset);
-            }
-            float* dst = gv + (vertexOffset + i) * 3;
-            dst[0]     = p.x;
-            dst[1]     = p.y;
-            dst[2]     = p.z;
-          }
-        }
-      }
-      else
-      {
-        // cluster_classify.comp.glsl:543-666: part and split triangles
-        const bool split0 = lane < nt && m0 > TC_TESSTABLE_SIZE;
-        const bool part0  = lane < nt && m0 <= TC_TESSTABLE_SIZE;
-        const bool split1 = lane + 32 < nt && m1 > TC_TESSTABLE_SIZE;
-        const bool part1  = lane + 32 < nt && m1 <= TC_TESSTABLE_SIZE;
-        const u32  bs0 = __ballot_sync(0xFFFFFFFFu, split0), bp0 = __ballot_sync(0xFFFFFFFFu, part0);
-        const u32  bs1 = __ballot_sync(0xFFFFFFFFu, split1), bp1 = __ballot_sync(0xFFFFFFFFu, part1);
-        const u32  lt_mask = (1u << lane) - 1u;
-        tc_TessTriangleInfo* splits = reinterpret_cast<tc_TessTriangleInfo*>(b->splitTriangles);
-        tc_TessTriangleInfo* parts  = reinterpret_cast<tc_TessTriangleInfo*>(b->partTriangles);
+    for(int q = 0; q < kNumCounters; q++)
+      run[q] = s_excl[q] + sum[q];
 #pragma unroll
-        for(int h = 0; h < 2; h++)
-        {
-          const bool isSplit = h == 0 ? split0 : split1;
-          const bool isPart  = h == 0 ? part0 : part1;
-          if(!isSplit && !isPart)
-            continue;
-          const u32 tri = lane + 32 * h;
-          uint3     f   = h == 0 ? f0 : f1;
-          u32       v0 = 0, v1 = TC_TESSTABLE_COORD_MAX, v2 = TC_TESSTABLE_COORD_MAX << 16;
-          if(isSplit)
-          {
-            const u64 o = off[kCntSplits] + (h == 0 ? __popc(bs0 & lt_mask) : __popc(bs0) + __popc(bs1 & lt_mask));
-            if(o < k.maxSplitTriangles)
-            {
-              f           = make_uint3(split_factor1(f.x, sf), split_factor1(f.y, sf), split_factor1(f.z, sf));
-              const u32 cfg = get_config(f, v0, v1, v2);
-              store_tess_info(splits + o, ci, v0, v1, v2, tri | (cfg << 16));
-            }
-          }
-          else
-          {
-            const u64 o = off[kCntParts] + (h == 0 ? __popc(bp0 & lt_mask) : __popc(bp0) + __popc(bp1 & lt_mask));
-            if(o < k.maxPartTriangles)
-            {
-              const u32 cfg = get_config(f, v0, v1, v2);
-              store_tess_info(parts + o, ci, v0, v1, v2, tri | (cfg << 16));
-            }
-          }
-        }
-        if(lane == 0)
-          s_fullInst[warp] = ~0u;
-      }
-    }
-    else if(lane == 0)
+    for(u32 i = 0; i < kScanItemsPerThread; i++)
     {
-      s_fullInst[warp] = ~0u;
+      if(first + i < n)
+      {
+        ClusterOffsets o;
+        o.part                = (u32)run[kCntParts];
+        o.split               = (u32)run[kCntSplits];
+        o.gen                 = (u32)run[kCntGen];
+        o.vert                = (u32)run[kCntVerts];
+        o.data                = run[kCntData];
+        cs.offsets[first + i] = o;
+      }
+      run[kCntParts] += cnt_parts(rec[i]);
+      run[kCntSplits] += cnt_splits(rec[i]);
+      run[kCntGen] += cnt_full(rec[i]);
+      run[kCntVerts] += cnt_verts(rec[i]);
+      run[kCntData] += rec[i].y;
     }
     __syncthreads();
-    // per-instance CLAS reference counts, one atomic per run of equal instances
-    if(threadIdx.x == 0)
-    {
-      u32 runInst = ~0u, runCount = 0;
-      for(int w = 0; w < W; w++)
-      {
-        u32 i = s_fullInst[w];
-        if(i == ~0u)
-          continue;
-        if(i != runInst)
-        {
-          if(runCount)
-            atomicAdd(&reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos)[runInst].clusterReferencesCount, runCount);
-          runInst  = i;
-          runCount = 0;
-        }
-        runCount++;
-      }
-      if(runCount)
-        atomicAdd(&reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos)[runInst].clusterReferencesCount, runCount);
-    }
-  }
-
-  // block-level statistics: one atomic each
-  for(int o = 16; o > 0; o >>= 1)
-  {
-    statFull += __shfl_xor_sync(0xFFFFFFFFu, statFull, o);
-    statTemp += __shfl_xor_sync(0xFFFFFFFFu, statTemp, o);
-    statTotalTris += __shfl_xor_sync(0xFFFFFFFFu, statTotalTris, o);
-  }
-  if(lane == 0)
-  {
-    if(statFull)
-      atomicAdd(&c.readback->numFullClusters, statFull);
-    if(statTemp)
-      atomicAdd(&b->tempInstantiateCounter, statTemp);
-    if(statTotalTris)
-      atomicAdd(&c.readback->numTotalTriangles, statTotalTris);
   }
 
   if(last_block_done(c, &s_flag))
@@ -393,11 +350,14 @@ __global__ void __launch_bounds__(W * 32) k_cluster_classify(StageCtx c)
     {
       if(numTiles)
       {
+        const u64 fullBefore     = b->genClusterCounter;
         b->partTriangleCounter   = (u32)c.scratch.totals[kCntParts];
         b->splitTriangleCounter  = (int32_t)(u32)c.scratch.totals[kCntSplits];
         b->genClusterCounter     = (u32)c.scratch.totals[kCntGen];
-        b->genClusterDataCounter = c.scratch.totals[kCntData];
         b->genVertexCounter      = (u32)c.scratch.totals[kCntVerts];
+        b->genClusterDataCounter = c.scratch.totals[kCntData];
+        // cluster_classify.comp.glsl:299 counts every full cluster, accepted or not
+        c.readback->numFullClusters += (u32)(c.scratch.totals[kCntGen] - fullBefore);
       }
       if(c.fuseSetup != kNoSetup)
         build_setup_apply(c, c.fuseSetup);
@@ -406,28 +366,191 @@ __global__ void __launch_bounds__(W * 32) k_cluster_classify(StageCtx c)
   }
 }
 
+// ---------------------------------------------------------------------------
+// write
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void store_tess_info(tc_TessTriangleInfo* dst, const tc_ClusterInfo& ci, u32 v0, u32 v1,
+                                                u32 v2, u32 tc)
+{
+  uint2* p = reinterpret_cast<uint2*>(dst);
+  p[0]     = make_uint2(ci.instanceID, ci.clusterID);
+  p[1]     = make_uint2(v0, v1);
+  p[2]     = make_uint2(v2, tc);
+}
+
+// part / split triangle from its per-triangle word (cluster_classify.comp.glsl:608-666)
+__device__ __forceinline__ void emit_triangle(tc_TessTriangleInfo* dst, const tc_ClusterInfo& ci, u32 tri, u32 word)
+{
+  u32       v0 = 0, v1 = TC_TESSTABLE_COORD_MAX, v2 = TC_TESSTABLE_COORD_MAX << 16;
+  const u32 rot = (word >> 16) & 3;
+  if(rot == 1)
+  {
+    u32 t = v0;
+    v0 = v1, v1 = v2, v2 = t;
+  }
+  else if(rot == 2)
+  {
+    u32 t = v2;
+    v2 = v1, v1 = v0, v0 = t;
+  }
+  store_tess_info(dst, ci, v0, v1, v2, tri | ((word & 0xFFFFu) << 16));
+}
+
+__global__ void __launch_bounds__(256) k_classify_write(StageCtx c, ClassifyScratch cs)
+{
+  __shared__ u32 s_range[2];
+  const u32 lane = threadIdx.x & 31;
+  if(threadIdx.x == 0)
+    window_range(c, s_range[0], s_range[1]);
+  __syncthreads();
+  const u32 begin = s_range[0];
+  const u32 n     = min(s_range[1] - s_range[0], c.scratch.itemCapacity);
+
+  tc_SceneBuilding*     b            = c.build;
+  const tc_caps&        k            = c.caps;
+  const tc_ClusterInfo* vis          = reinterpret_cast<const tc_ClusterInfo*>(b->visibleClusters);
+  const bool            haveTextures = c.numTextures > 0 && c.textures != nullptr;
+  const u64             maxData      = (u64)k.maxGeneratedClusterMegs * 1024ull * 1024ull;
+  tc_TessTriangleInfo*  splits       = reinterpret_cast<tc_TessTriangleInfo*>(b->splitTriangles);
+  tc_TessTriangleInfo*  parts        = reinterpret_cast<tc_TessTriangleInfo*>(b->partTriangles);
+  float*                gv           = reinterpret_cast<float*>(b->genVertices);
+  const u32             nwarps       = (gridDim.x * blockDim.x) >> 5;
+  const u32             ltm          = (1u << lane) - 1u;
+  u32                   statTris = 0, statTemp = 0;
+
+  for(u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nwarps)
+  {
+    const uint2          rec = cs.counts[v];
+    const ClusterOffsets off = cs.offsets[v];
+    const tc_ClusterInfo ci  = vis[begin + v];
+    if(cnt_full(rec))
+    {
+      // cluster_classify.comp.glsl:271-488: template instantiation of the full cluster
+      const u32  nv     = cnt_verts(rec);
+      const bool accept = !((u64)off.vert + nv > k.maxGeneratedVertices || (u64)off.gen + 1 > k.maxGeneratedClusters
+                            || off.data + rec.y > maxData);
+      if(!accept)
+        continue;
+      const tc_RenderInstance* in = c.instances + ci.instanceID;
+      const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
+      if(lane == 0)
+      {
+        // accepted instantiations form a prefix of the serial order, so the
+        // instantiation slot equals the generated-cluster slot
+        const u32                  tempOffset = off.gen;
+        tc_TemplateInstantiateInfo ti;
+        ti.clusterIdOffset        = 0;
+        ti.geometryIndexOffset    = 0;
+        ti.clusterTemplateAddress = __ldg(reinterpret_cast<const u64*>(in->clusterTemplateAdresses) + ci.clusterID);
+        ti.vertexBufferAddress    = b->genVertices + (u64)off.vert * 12ull;
+        ti.vertexBufferStride     = 12;
+        reinterpret_cast<tc_TemplateInstantiateInfo*>(b->tempInstantiations)[tempOffset] = ti;
+        reinterpret_cast<u32*>(b->tempInstanceIDs)[tempOffset]                          = ci.instanceID;
+        reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset]                     = b->genClusterData + off.data;
+        if((c.flags & TC_FLAG_WRITE_FULLCLUSTERS) && b->fullClusters)
+          reinterpret_cast<tc_ClusterInfo*>(b->fullClusters)[tempOffset] = ci;
+        atomicAdd(&reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos)[ci.instanceID].clusterReferencesCount, 1u);
+        statTemp += 1;
+        statTris += min((u32)cl.numTriangles, TC_MAX_CLUSTER_TRIANGLES);
+      }
+      // cluster_classify.comp.glsl:457-482: displaced cluster vertices
+      // texture descriptor held in registers (the vertex stores below may alias it)
+      tc_DisplacementTexture txd = {};
+      if(haveTextures && in->displacementIndex >= 0)
+      {
+        if((u32)in->displacementIndex < c.numTextures)
+          txd = c.textures[in->displacementIndex];
+        else if(lane == 0)
+          atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
+      }
+      const float iscale = in->displacementScale, ioffset = in->displacementOffset;
+      const float vscale = c.view->displacementScale, voffset = c.view->displacementOffset;
+      const float* pos = reinterpret_cast<const float*>(in->positions);
+      const float* nrm = reinterpret_cast<const float*>(in->normals);
+      const float* uvs = reinterpret_cast<const float*>(in->texcoords);
+      for(u32 i = lane; i < nv; i += 32)
+      {
+        const u32 vi = cl.firstLocalVertex + i;
+        f3        p  = ldg3(pos, vi);
+        if(txd.width != 0)
+        {
+          const float h = sample_bilinear(txd, ldg2(uvs, vi));
+          p             = displace(p, ldg3(nrm, vi), h, iscale, vscale, ioffset, voffset);
+        }
+        float* dst = gv + ((u64)off.vert + i) * 3;
+        dst[0]     = p.x;
+        dst[1]     = p.y;
+        dst[2]     = p.z;
+      }
+    }
+    else
+    {
+      // cluster_classify.comp.glsl:543-666: part and split triangles
+      const u32  nt  = cnt_parts(rec) + cnt_splits(rec);
+      const u32* tw  = cs.triWords + (u64)v * TC_MAX_CLUSTER_TRIANGLES;
+      const u32  w0  = lane < nt ? tw[lane] : 0u;
+      const u32  w1  = lane + 32 < nt ? tw[lane + 32] : 0u;
+      const bool s0  = lane < nt && (w0 >> 18) != 0, p0 = lane < nt && (w0 >> 18) == 0;
+      const bool s1  = lane + 32 < nt && (w1 >> 18) != 0, p1 = lane + 32 < nt && (w1 >> 18) == 0;
+      const u32  bs0 = __ballot_sync(0xFFFFFFFFu, s0), bp0 = __ballot_sync(0xFFFFFFFFu, p0);
+      const u32  bs1 = __ballot_sync(0xFFFFFFFFu, s1), bp1 = __ballot_sync(0xFFFFFFFFu, p1);
+      if(s0)
+      {
+        const u64 o = (u64)off.split + __popc(bs0 & ltm);
+        if(o < k.maxSplitTriangles)
+          emit_triangle(splits + o, ci, lane, w0);
+      }
+      else if(p0)
+      {
+        const u64 o = (u64)off.part + __popc(bp0 & ltm);
+        if(o < k.maxPartTriangles)
+          emit_triangle(parts + o, ci, lane, w0);
+      }
+      if(s1)
+      {
+        const u64 o = (u64)off.split + __popc(bs0) + __popc(bs1 & ltm);
+        if(o < k.maxSplitTriangles)
+          emit_triangle(splits + o, ci, lane + 32, w1);
+      }
+      else if(p1)
+      {
+        const u64 o = (u64)off.part + __popc(bp0) + __popc(bp1 & ltm);
+        if(o < k.maxPartTriangles)
+          emit_triangle(parts + o, ci, lane + 32, w1);
+      }
+    }
+  }
+
+  // statistics: one atomic each per warp
+  if(lane == 0)
+  {
+    if(statTemp)
+      atomicAdd(&b->tempInstantiateCounter, statTemp);
+    if(statTris)
+      atomicAdd(&c.readback->numTotalTriangles, statTris);
+  }
+}
+
 }  // namespace
 
-u32 classify_num_counters() { return kNumCounters; }
-
-cudaError_t launch_cluster_classify(const StageCtx& c, u32 warpsPerBlock, u32 grid, cudaStream_t s)
+cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
+                                    cudaStream_t s)
 {
-  switch(warpsPerBlock)
-  {
-    case 2:
-      k_cluster_classify<2><<<grid, 64, 0, s>>>(c);
-      break;
-    case 4:
-      k_cluster_classify<4><<<grid, 128, 0, s>>>(c);
-      break;
-    case 16:
-      k_cluster_classify<16><<<grid, 512, 0, s>>>(c);
-      break;
-    default:
-      k_cluster_classify<8><<<grid, 256, 0, s>>>(c);
-      break;
-  }
+  ClassifyScratch cs{buf.counts, buf.offsets, buf.triWords};
+  const u32       warpGrid = std::max(1u, std::min((maxClusters + 7) / 8, numSMs * 8));
+  k_classify_count<<<warpGrid, 256, 0, s>>>(c, cs);
+  cudaError_t e = cudaGetLastError();
+  if(e != cudaSuccess)
+    return e;
+  const u32 scanGrid = std::max(1u, std::min((maxClusters + kScanTile - 1) / kScanTile, numSMs * 4));
+  k_classify_scan<<<scanGrid, kScanBlock, 0, s>>>(c, cs);
+  if((e = cudaGetLastError()) != cudaSuccess)
+    return e;
+  k_classify_write<<<warpGrid, 256, 0, s>>>(c, cs);
   return cudaGetLastError();
 }
+
+u32 classify_scan_tiles(u32 maxClusters) { return (maxClusters + kScanTile - 1) / kScanTile; }
 
 }  // namespace tc

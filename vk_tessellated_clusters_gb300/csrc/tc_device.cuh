@@ -45,11 +45,11 @@ __device__ __forceinline__ f3    sub3(f3 a, f3 b) { return {a.x - b.x, a.y - b.y
 __device__ __forceinline__ float dot3(f3 a, f3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
 __device__ __forceinline__ float len3(f3 a) { return __fsqrt_rn(dot3(a, a)); }
 __device__ __forceinline__ float dist3(f3 a, f3 b) { return len3(sub3(a, b)); }
-// GLSL normalize(): v / length(v)
+// GLSL normalize(): v * (1 / length(v)) (one IEEE division, three multiplies)
 __device__ __forceinline__ f3 normalize3(f3 a)
 {
-  float l = len3(a);
-  return {__fdiv_rn(a.x, l), __fdiv_rn(a.y, l), __fdiv_rn(a.z, l)};
+  float r = __fdiv_rn(1.0f, len3(a));
+  return {a.x * r, a.y * r, a.z * r};
 }
 
 // (M * vec4(p, 1)).xyz, column-major M
@@ -223,8 +223,15 @@ __device__ __forceinline__ f3 cfg_vertex(const Table& t, const tc_TessTableEntry
 // filter weights.
 // ---------------------------------------------------------------------------
 
+// i mod n in [0, n); taps are almost always within one period of the range
 __device__ __forceinline__ int wrapi(int i, int n)
 {
+  if((unsigned)i < (unsigned)n)
+    return i;
+  if(i < 0 && i >= -n)
+    return i + n;
+  if(i >= n && i - n < n)
+    return i - n;
   int r = i % n;
   return r < 0 ? r + n : r;
 }
@@ -295,14 +302,17 @@ __device__ __forceinline__ f3 displace(f3 pos, f3 normal, float h, float instSca
 // memory-model helpers
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ void st_release_u64(u64* p, u64 v)
+// Look-back state words carry their value and flag in one 64-bit word and
+// nothing else is published through them, so relaxed (single-copy atomic)
+// accesses at GPU scope suffice: no fences on the polling path.
+__device__ __forceinline__ void st_relaxed_u64(u64* p, u64 v)
 {
-  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
-__device__ __forceinline__ u64 ld_acquire_u64(const u64* p)
+__device__ __forceinline__ u64 ld_relaxed_u64(const u64* p)
 {
   u64 v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
 __device__ __forceinline__ u32 ld_acquire_u32(const u32* p)
@@ -348,11 +358,11 @@ __device__ __forceinline__ u64 warp_lookback_exclusive(u64* state, u32 tile, u64
   if(tile == 0)
   {
     if(lane == 0)
-      st_release_u64(state, kLbPrefix | ((base + aggregate) & kLbValueMask));
+      st_relaxed_u64(state, kLbPrefix | ((base + aggregate) & kLbValueMask));
     return base;
   }
   if(lane == 0)
-    st_release_u64(state + tile, kLbAggregate | (aggregate & kLbValueMask));
+    st_relaxed_u64(state + tile, kLbAggregate | (aggregate & kLbValueMask));
   u64 excl  = 0;
   int start = (int)tile - 1;
   u32 spins = 0;
@@ -360,7 +370,7 @@ __device__ __forceinline__ u64 warp_lookback_exclusive(u64* state, u32 tile, u64
   {
     const int t = start - (int)lane;
     // window slots before tile 0 count as an empty inclusive prefix
-    u64 s = t >= 0 ? ld_acquire_u64(state + t) : kLbPrefix;
+    u64 s = t >= 0 ? ld_relaxed_u64(state + t) : kLbPrefix;
     while(__any_sync(0xFFFFFFFFu, (s & ~kLbValueMask) == 0))
     {
       if(++spins > kSpinLimit)
@@ -372,7 +382,7 @@ __device__ __forceinline__ u64 warp_lookback_exclusive(u64* state, u32 tile, u64
       }
       __nanosleep(32);
       if((s & ~kLbValueMask) == 0)
-        s = ld_acquire_u64(state + t);
+        s = ld_relaxed_u64(state + t);
     }
     const u32 pmask = __ballot_sync(0xFFFFFFFFu, (s & ~kLbValueMask) == kLbPrefix);
     u64       v     = s & kLbValueMask;
@@ -388,7 +398,7 @@ __device__ __forceinline__ u64 warp_lookback_exclusive(u64* state, u32 tile, u64
     start -= 32;
   }
   if(lane == 0)
-    st_release_u64(state + tile, kLbPrefix | ((excl + aggregate) & kLbValueMask));
+    st_relaxed_u64(state + tile, kLbPrefix | ((excl + aggregate) & kLbValueMask));
   return excl;
 }
 

@@ -3,17 +3,20 @@
 //
 // shaders/triangle_tess_template_instantiate.comp.glsl:126-373.
 //
-// GB300 mapping (HBM-write bound: 12 B per generated vertex dominates):
-//  * a tile is 32 part triangles; warp 0 reads them, computes the counts
-//    (generated clusters, CLAS bytes, vertices), orders them after all earlier
-//    tiles with a decoupled look-back and writes the 44 B of instantiation
-//    arguments per part;
-//  * per-part base data (positions, normalised normals, uvs, decoded
-//    barycentrics, table offsets) is staged once in shared memory;
-//  * all threads then generate the tile's vertices (flat index -> part by
-//    binary search), stage them in shared memory and write the tile's
-//    contiguous vertex range with aligned 16-byte stores (scalar stores only at
-//    the two unaligned ends).
+// GB300 mapping, two launches:
+//   alloc    : a scan over the part triangles (1024 per tile, decoupled
+//              look-back between tiles) assigns generated-cluster slots, CLAS
+//              bytes and vertex ranges in part order, applies the capacity test
+//              and writes the 44 B of instantiation arguments per part; the
+//              first vertex of each accepted part goes to scratch
+//   vertices : HBM-write bound (12 B per generated vertex dominates). One warp
+//              per 32 consecutive parts, whose vertices form one contiguous
+//              range: per-part base data staged once in shared memory, then the
+//              range is written as aligned 48-byte groups of four vertices
+//              (three 16-byte stores per lane), scalar stores only at the two
+//              unaligned ends. No block barriers, no cross-block waits.
+#include <algorithm>
+
 #include "tc_kernels.h"
 #include "tc_stage.cuh"
 
@@ -29,307 +32,207 @@ enum : int
   kNumCounters
 };
 
-constexpr int kPartsPerTile = 32;
-constexpr int kMaxTileVerts = kPartsPerTile * 78;  // 78 = largest config vertex count of an 11-segment table
+constexpr u32 kAllocBlock   = 256;
+constexpr u32 kAllocItems   = 4;
+constexpr u32 kAllocTile    = kAllocBlock * kAllocItems;
+constexpr u32 kVertexWarps  = 8;  // warps per block of the vertex kernel
+constexpr u32 kPartsPerWarp = 32;
 
-struct PartRecord
+static_assert(kAllocTile == kInstantiateTile, "allocation tile size");
+
+// parts of this launch: [0, part counter) or one run, narrowed to the instance window
+__device__ inline void part_range(const StageCtx& c, u32& lo, u32& hi)
 {
-  f3  p[3];
-  f3  n[3];
-  f2  uv[3];
-  f3  bb[3];
-  u32 firstVertex;
-  u32 cfg;
-  u32 texIndex;  // ~0 = no displacement
-  float scale, offset;
-};
-
-template <int B>
-__global__ void __launch_bounds__(B) k_triangle_instantiate(StageCtx c)
-{
-  __shared__ PartRecord s_part[kPartsPerTile];
-  __shared__ u32        s_vpre[kPartsPerTile + 1];  // vertex prefix within tile (accepted parts only)
-  __shared__ __align__(16) float s_stage[kMaxTileVerts * 3 + 4];
-  __shared__ u64 s_excl[kNumCounters];
-  __shared__ u64 s_agg[kNumCounters];
-  __shared__ u64 s_vbase;
-  __shared__ u32 s_tile, s_flag, s_range[2];
-
-  const u32         lane = threadIdx.x & 31;
-  const u32         warp = threadIdx.x >> 5;
-  tc_SceneBuilding* b    = c.build;
-  const tc_caps&    k    = c.caps;
-  const tc_TessTriangleInfo* parts = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
-
-  if(threadIdx.x == 0)
+  const tc_TessTriangleInfo* parts = reinterpret_cast<const tc_TessTriangleInfo*>(c.build->partTriangles);
+  lo                               = 0;
+  hi                               = min(c.build->partTriangleCounter, c.caps.maxPartTriangles);
+  if(c.run != kAllRuns)
   {
-    u32 lo = 0, hi = min(b->partTriangleCounter, c.caps.maxPartTriangles);
-    if(c.run != kAllRuns)
-    {
-      u32 rs = c.runStarts[c.run], re = c.runStarts[c.run + 1];
-      lo     = min(rs, hi);
-      hi     = min(max(re, rs), hi);
-    }
-    if(!whole_window(c))
-    {
-      auto get = [&](u32 i) { return parts[i].cluster.instanceID; };
-      u32  e   = lower_bound_instance(lo, hi, c.instEnd, get);
-      lo       = lower_bound_instance(lo, e, c.instBegin, get);
-      hi       = e;
-    }
-    s_range[0] = lo;
-    s_range[1] = hi;
+    const u32 rs = c.runStarts[c.run], re = c.runStarts[c.run + 1];
+    lo           = min(rs, hi);
+    hi           = min(max(re, rs), hi);
   }
+  if(!whole_window(c))
+  {
+    auto get = [&](u32 i) { return parts[i].cluster.instanceID; };
+    u32  e   = lower_bound_instance(lo, hi, c.instEnd, get);
+    lo       = lower_bound_instance(lo, e, c.instBegin, get);
+    hi       = e;
+  }
+}
+
+template <class T>
+__device__ __forceinline__ T warp_inclusive(T x, u32 lane)
+{
+#pragma unroll
+  for(int d = 1; d < 32; d <<= 1)
+  {
+    T y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+    if(lane >= (u32)d)
+      x += y;
+  }
+  return x;
+}
+
+// ---------------------------------------------------------------------------
+// alloc
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kAllocBlock) k_instantiate_alloc(StageCtx c, InstantiateBuffers ib)
+{
+  __shared__ u64 s_warp[33][kNumCounters];
+  __shared__ u64 s_excl[kNumCounters];
+  __shared__ u32 s_tile, s_flag, s_range[2];
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if(threadIdx.x == 0)
+    part_range(c, s_range[0], s_range[1]);
   __syncthreads();
-  const u32 begin = s_range[0], end = s_range[1];
-  u32 numTiles = (end - begin + kPartsPerTile - 1) / kPartsPerTile;
-  numTiles = clamp_tiles(c, numTiles);
+  const u32 begin    = s_range[0], n = s_range[1] - s_range[0];
+  const u32 numTiles = clamp_tiles(c, (n + kAllocTile - 1) / kAllocTile);
 
-  const bool haveTextures = c.numTextures > 0 && c.textures != nullptr;
-  const u64  maxData      = (u64)k.maxGeneratedClusterMegs * 1024ull * 1024ull;
-  const float viewScale   = c.view->displacementScale;
-  const float viewOffset  = c.view->displacementOffset;
-  float*      gv          = reinterpret_cast<float*>(b->genVertices);
-  const bool  aligned16   = (reinterpret_cast<uintptr_t>(gv) & 15) == 0;
-
-  u32 statTris = 0, statTemp = 0;
+  tc_SceneBuilding*          b        = c.build;
+  const tc_caps&             k        = c.caps;
+  const tc_TessTriangleInfo* parts    = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
+  const u64                  maxData  = (u64)k.maxGeneratedClusterMegs * 1024ull * 1024ull;
+  tc_BlasBuildInfo*          blas     = reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos);
+  u32                        statTris = 0, statTemp = 0;
 
   for(;;)
   {
     const u32 tile = next_tile(c, &s_tile);
     if(tile >= numTiles)
       break;
-
-    // ---- warp 0: read the tile's parts, per-part counts and their scans -----------
-    const u32           p     = begin + tile * kPartsPerTile + lane;
-    const bool          valid = warp == 0 && p < end;
-    tc_TessTriangleInfo info  = {};
-    u32                 cfg = 0, nv = 0, nt = 0;
-    u64                 ds = 0;
-    u32                 xv = 0;
-    u64                 xd = 0;
+    const u32 first = tile * kAllocTile + threadIdx.x * kAllocItems;
+    u32       inst[kAllocItems], cfg[kAllocItems], nv[kAllocItems], nt[kAllocItems], ds[kAllocItems];
+    u64       sum[kNumCounters] = {0, 0, 0};
+#pragma unroll
+    for(u32 i = 0; i < kAllocItems; i++)
+    {
+      inst[i] = ~0u;
+      cfg[i] = nv[i] = nt[i] = ds[i] = 0;
+      if(first + i < n)
+      {
+        const uint2* raw          = reinterpret_cast<const uint2*>(parts + begin + first + i);
+        inst[i]                   = raw[0].x;
+        cfg[i]                    = raw[2].y >> 16;
+        const tc_TessTableEntry e = table_entry(c.table, cfg[i]);
+        nv[i]                     = e.numVertices;
+        nt[i]                     = e.numTriangles;
+        ds[i]                     = __ldg(c.table.templateSizes + cfg_index(cfg[i]));
+        sum[kCntGen] += 1;
+        sum[kCntData] += ds[i];
+        sum[kCntVerts] += nv[i];
+      }
+    }
+    // block exclusive scan of the three counters
+    u64 inc[kNumCounters];
+#pragma unroll
+    for(int q = 0; q < kNumCounters; q++)
+    {
+      inc[q] = warp_inclusive<u64>(sum[q], lane);
+      if(lane == 31)
+        s_warp[warp][q] = inc[q];
+    }
+    __syncthreads();
     if(warp == 0)
     {
-      if(valid)
-      {
-        const uint2* raw                   = reinterpret_cast<const uint2*>(parts + p);
-        uint2        r0 = raw[0], r1 = raw[1], r2 = raw[2];
-        info.cluster                       = {r0.x, r0.y};
-        info.subTriangle.vtxEncoded[0]     = r1.x;
-        info.subTriangle.vtxEncoded[1]     = r1.y;
-        info.subTriangle.vtxEncoded[2]     = r2.x;
-        info.subTriangle.triangleID_config = r2.y;
-        cfg                                = r2.y >> 16;
-        const tc_TessTableEntry e          = table_entry(c.table, cfg);
-        nv                                 = e.numVertices;
-        nt                                 = e.numTriangles;
-        ds                                 = __ldg(c.table.templateSizes + cfg_index(cfg));
-      }
-      // warp scans (inclusive) of vertices (u32) and CLAS bytes (u64)
-      xv = nv;
-      xd = ds;
 #pragma unroll
-      for(int d = 1; d < 32; d <<= 1)
+      for(int q = 0; q < kNumCounters; q++)
       {
-        u32 yv = __shfl_up_sync(0xFFFFFFFFu, xv, d);
-        u64 yd = __shfl_up_sync(0xFFFFFFFFu, xd, d);
-        if(lane >= (u32)d)
-        {
-          xv += yv;
-          xd += yd;
-        }
-      }
-      if(lane == 31)
-      {
-        s_agg[kCntGen]   = min((u32)kPartsPerTile, end - (begin + tile * kPartsPerTile));
-        s_agg[kCntData]  = xd;
-        s_agg[kCntVerts] = xv;
+        u64 w = lane < nw ? s_warp[lane][q] : 0;
+        u64 s = warp_inclusive<u64>(w, lane);
+        __syncwarp();
+        if(lane < nw)
+          s_warp[lane][q] = s - w;
+        if(lane == 31)
+          s_warp[32][q] = s;
       }
     }
     __syncthreads();
-
-    // ---- look-back: warps 0..2, one counter each ------------------------------------
+    // look-back: warps 0..2, one counter each
     if(warp < kNumCounters)
     {
-      u64 base = 0;
+      const u32 q    = warp;
+      u64       base = 0;
       if(tile == 0)
-        base = warp == kCntGen ? b->genClusterCounter : (warp == kCntData ? b->genClusterDataCounter : b->genVertexCounter);
-      const u64 ex = warp_lookback_exclusive(c.scratch.lbState + (u64)warp * c.scratch.lbStride, tile, s_agg[warp], base,
-                                             c.errorWord);
+        base = q == kCntGen ? b->genClusterCounter : (q == kCntData ? b->genClusterDataCounter : b->genVertexCounter);
+      const u64 agg = s_warp[32][q];
+      const u64 ex = warp_lookback_exclusive(c.scratch.lbState + (u64)q * c.scratch.lbStride, tile, agg, base, c.errorWord);
       if(lane == 0)
       {
-        s_excl[warp] = ex;
+        s_excl[q] = ex;
         if(tile == numTiles - 1)
-          c.scratch.totals[warp] = ex + s_agg[warp];
+          c.scratch.totals[q] = ex + agg;
       }
     }
     __syncthreads();
-
-    // ---- warp 0: acceptance, instantiation arguments, per-part staging ---------------
-    if(warp == 0)
+    u64 genOffset    = s_excl[kCntGen] + s_warp[warp][kCntGen] + inc[kCntGen] - sum[kCntGen];
+    u64 dataOffset   = s_excl[kCntData] + s_warp[warp][kCntData] + inc[kCntData] - sum[kCntData];
+    u64 vertexOffset = s_excl[kCntVerts] + s_warp[warp][kCntVerts] + inc[kCntVerts] - sum[kCntVerts];
+    u32 runInst = ~0u, runCount = 0;
+#pragma unroll
+    for(u32 i = 0; i < kAllocItems; i++)
     {
-      const u64 genOffset    = s_excl[kCntGen] + lane;
-      const u64 dataOffset   = s_excl[kCntData] + (xd - ds);
-      const u64 vertexOffset = s_excl[kCntVerts] + (xv - nv);
-      // triangle_tess_template_instantiate.comp.glsl:160-167 capacity test
-      const bool accept = valid
-                          && !(vertexOffset + nv > k.maxGeneratedVertices || genOffset + 1 > k.maxGeneratedClusters
-                               || dataOffset + ds > maxData);
-      const u32 acceptMask = __ballot_sync(0xFFFFFFFFu, accept);
-      if(accept)
+      if(first + i < n)
       {
-        // accepted instantiations form a prefix of the serial order: slot == generated cluster index
-        const u32 tempOffset = (u32)genOffset;
-        tc_TemplateInstantiateInfo* dst = reinterpret_cast<tc_TemplateInstantiateInfo*>(b->tempInstantiations) + tempOffset;
-        const u64 tmpl  = __ldg(c.table.templateAddresses + cfg_index(cfg));
-        const u64 vaddr = b->genVertices + vertexOffset * 12ull;
-        const uint4 lo4 = make_uint4(p | (TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED << 30), 0u, (u32)tmpl, (u32)(tmpl >> 32));
-        const uint4 hi4 = make_uint4((u32)vaddr, (u32)(vaddr >> 32), 12u, 0u);
-        if((reinterpret_cast<uintptr_t>(dst) & 15) == 0)
+        const u32 p = begin + first + i;
+        // triangle_tess_template_instantiate.comp.glsl:160-167 capacity test
+        const bool accept = !(vertexOffset + nv[i] > k.maxGeneratedVertices || genOffset + 1 > k.maxGeneratedClusters
+                              || dataOffset + ds[i] > maxData);
+        if(accept)
         {
-          reinterpret_cast<uint4*>(dst)[0] = lo4;
-          reinterpret_cast<uint4*>(dst)[1] = hi4;
-        }
-        else
-        {
-          uint2* d2 = reinterpret_cast<uint2*>(dst);
-          d2[0]     = make_uint2(lo4.x, lo4.y);
-          d2[1]     = make_uint2(lo4.z, lo4.w);
-          d2[2]     = make_uint2(hi4.x, hi4.y);
-          d2[3]     = make_uint2(hi4.z, hi4.w);
-        }
-        reinterpret_cast<u32*>(b->tempInstanceIDs)[tempOffset]      = info.cluster.instanceID;
-        reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset] = b->genClusterData + dataOffset;
-        statTris += nt;
-      }
-      if(lane == 0)
-        statTemp += __popc(acceptMask);
-      // per-instance CLAS reference counts: one atomic per distinct instance in the warp
-      {
-        const u32 inst  = accept ? info.cluster.instanceID : 0xFFFFFFFFu;
-        const u32 peers = __match_any_sync(0xFFFFFFFFu, inst);
-        if(accept && (__ffs(peers) - 1) == (int)lane)
-          atomicAdd(&reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos)[inst].clusterReferencesCount, (u32)__popc(peers));
-      }
-      // staging of per-part vertex-generation inputs
-      const u32 nvAcc = accept ? nv : 0u;
-      u32       xa    = nvAcc;
-#pragma unroll
-      for(int d = 1; d < 32; d <<= 1)
-      {
-        u32 y = __shfl_up_sync(0xFFFFFFFFu, xa, d);
-        if(lane >= (u32)d)
-          xa += y;
-      }
-      if(lane == 0)
-      {
-        s_vpre[0] = 0;
-        s_vbase   = s_excl[kCntVerts];
-      }
-      s_vpre[lane + 1] = xa;
-      if(accept)
-      {
-        const tc_RenderInstance& in  = c.instances[info.cluster.instanceID];
-        const tc_Cluster         cl  = reinterpret_cast<const tc_Cluster*>(in.clusters)[info.cluster.clusterID];
-        const uint8_t*           lt  = reinterpret_cast<const uint8_t*>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
-        const u32                tri = info.subTriangle.triangleID_config & 0xFFFFu;
-        const float*             pos = reinterpret_cast<const float*>(in.positions);
-        const float*             nrm = reinterpret_cast<const float*>(in.normals);
-        const float*             uvs = reinterpret_cast<const float*>(in.texcoords);
-        PartRecord&              r   = s_part[lane];
-#pragma unroll
-        for(int v = 0; v < 3; v++)
-        {
-          const u32 vi = cl.firstLocalVertex + lt[tri * 3 + v];
-          r.bb[v]      = decode_bary(info.subTriangle.vtxEncoded[v]);
-          r.p[v]       = ldg3(pos, vi);
-          r.n[v]       = normalize3(ldg3(nrm, vi));  // :329
-          r.uv[v]      = ldg2(uvs, vi);
-        }
-        r.firstVertex = table_entry(c.table, cfg).firstVertex;
-        r.cfg         = cfg;
-        r.texIndex    = ~0u;
-        if(haveTextures && in.displacementIndex >= 0)
-        {
-          if((u32)in.displacementIndex < c.numTextures)
-            r.texIndex = (u32)in.displacementIndex;
+          // accepted instantiations form a prefix of the serial order: slot == generated cluster index
+          const u32 tempOffset = (u32)genOffset;
+          tc_TemplateInstantiateInfo* dst =
+              reinterpret_cast<tc_TemplateInstantiateInfo*>(b->tempInstantiations) + tempOffset;
+          const u64   tmpl  = __ldg(c.table.templateAddresses + cfg_index(cfg[i]));
+          const u64   vaddr = b->genVertices + vertexOffset * 12ull;
+          const uint4 lo4 = make_uint4(p | (TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED << 30), 0u, (u32)tmpl, (u32)(tmpl >> 32));
+          const uint4 hi4 = make_uint4((u32)vaddr, (u32)(vaddr >> 32), 12u, 0u);
+          if((reinterpret_cast<uintptr_t>(dst) & 15) == 0)
+          {
+            reinterpret_cast<uint4*>(dst)[0] = lo4;
+            reinterpret_cast<uint4*>(dst)[1] = hi4;
+          }
           else
-            atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
+          {
+            uint2* d2 = reinterpret_cast<uint2*>(dst);
+            d2[0]     = make_uint2(lo4.x, lo4.y);
+            d2[1]     = make_uint2(lo4.z, lo4.w);
+            d2[2]     = make_uint2(hi4.x, hi4.y);
+            d2[3]     = make_uint2(hi4.z, hi4.w);
+          }
+          reinterpret_cast<u32*>(b->tempInstanceIDs)[tempOffset]      = inst[i];
+          reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset] = b->genClusterData + dataOffset;
+          ib.vertexOffset[p]                                          = (u32)vertexOffset;
+          statTris += nt[i];
+          statTemp += 1;
+          if(inst[i] != runInst)
+          {
+            if(runCount)
+              atomicAdd(&blas[runInst].clusterReferencesCount, runCount);
+            runInst  = inst[i];
+            runCount = 0;
+          }
+          runCount++;
         }
-        r.scale  = in.displacementScale;
-        r.offset = in.displacementOffset;
-      }
-    }
-    __syncthreads();
-
-    // ---- all threads: vertex generation into shared staging -----------------------
-    const u32 tileVerts = s_vpre[kPartsPerTile];
-    const u64 vbase     = s_vbase;
-    const u32 shift     = aligned16 ? (u32)((vbase * 3) & 3) : 0u;
-    for(u32 j = threadIdx.x; j < tileVerts; j += B)
-    {
-      u32 lo = 0, hi = kPartsPerTile;  // last part with s_vpre[part] <= j
-      while(hi - lo > 1)
-      {
-        u32 mid = (lo + hi) >> 1;
-        if(s_vpre[mid] <= j)
-          lo = mid;
         else
-          hi = mid;
+          ib.vertexOffset[p] = ~0u;
       }
-      const PartRecord& r    = s_part[lo];
-      const u32         vert = j - s_vpre[lo];
-      // triangle_tess_template_instantiate.comp.glsl:343-371
-      f3 w = decode_bary(__ldg(c.table.vertices + r.firstVertex + vert));
-      if(cfg_flipped(r.cfg))
-      {
-        float s = w.x;
-        w.x     = w.y;
-        w.y     = s;
-      }
-      w        = interp3(r.bb[0], r.bb[1], r.bb[2], w);
-      f3 p     = interp3(r.p[0], r.p[1], r.p[2], w);
-      if(r.texIndex != ~0u)
-      {
-        const f3 n  = interp3(r.n[0], r.n[1], r.n[2], w);
-        const f2 uv = interp2(r.uv[0], r.uv[1], r.uv[2], w);
-        const float h = sample_bilinear(c.textures[r.texIndex], uv);
-        p = displace(p, n, h, r.scale, viewScale, r.offset, viewOffset);
-      }
-      if(aligned16)
-      {
-        float* d = s_stage + shift + 3 * j;
-        d[0]     = p.x;
-        d[1]     = p.y;
-        d[2]     = p.z;
-      }
-      else
-      {
-        float* d = gv + (vbase + j) * 3;
-        d[0]     = p.x;
-        d[1]     = p.y;
-        d[2]     = p.z;
-      }
+      genOffset += 1;
+      dataOffset += ds[i];
+      vertexOffset += nv[i];
     }
-    __syncthreads();
-
-    // ---- write-out: the tile's vertices are one contiguous range ----------------------
-    if(aligned16 && tileVerts)
+    // per-instance CLAS reference counts: threads of a warp holding the same
+    // instance combine their last runs, one atomic per distinct instance
     {
-      const u32 nf     = tileVerts * 3;
-      const u64 g0     = vbase * 3 - shift;  // float index of the 16-B aligned start
-      const u32 groups = (shift + nf + 3) / 4;
-      float4*   dst4   = reinterpret_cast<float4*>(gv + g0);
-      const float4* src4 = reinterpret_cast<const float4*>(s_stage);
-      for(u32 g = threadIdx.x; g < groups; g += B)
-      {
-        const u32 lo = g * 4, hi = lo + 4;
-        if(lo >= shift && hi <= shift + nf)
-          dst4[g] = src4[g];
-        else
-          for(u32 q = max(lo, shift); q < min(hi, shift + nf); q++)
-            gv[g0 + q] = s_stage[q];
-      }
+      const u32 key   = runCount ? runInst : 0xFFFFFFFFu;
+      const u32 peers = __match_any_sync(0xFFFFFFFFu, key);
+      u32       peerSum = 0;
+      for(u32 m = peers; m; m &= m - 1)
+        peerSum += __shfl_sync(peers, runCount, __ffs(m) - 1);
+      if(runCount && (__ffs(peers) - 1) == (int)lane)
+        atomicAdd(&blas[runInst].clusterReferencesCount, peerSum);
     }
     __syncthreads();
   }
@@ -364,22 +267,209 @@ __global__ void __launch_bounds__(B) k_triangle_instantiate(StageCtx c)
   }
 }
 
+// ---------------------------------------------------------------------------
+// vertices
+// ---------------------------------------------------------------------------
+
+struct PartRecord
+{
+  f3                     p[3];
+  f3                     n[3];
+  f2                     uv[3];
+  f3                     bb[3];
+  u32                    firstVertex;
+  u32                    cfg;
+  float                  scale, offset;
+  tc_DisplacementTexture tx;  // width == 0: no displacement
+};
+
+// triangle_tess_template_instantiate.comp.glsl:343-371 for vertex `vert` of the part in `r`
+__device__ __forceinline__ f3 gen_vertex(const Table& table, const PartRecord& r, u32 vert, float viewScale,
+                                         float viewOffset)
+{
+  f3 w = decode_bary(__ldg(table.vertices + r.firstVertex + vert));
+  if(cfg_flipped(r.cfg))
+  {
+    const float s = w.x;
+    w.x           = w.y;
+    w.y           = s;
+  }
+  w    = interp3(r.bb[0], r.bb[1], r.bb[2], w);
+  f3 p = interp3(r.p[0], r.p[1], r.p[2], w);
+  if(r.tx.width != 0)
+  {
+    const f3    n  = interp3(r.n[0], r.n[1], r.n[2], w);
+    const f2    uv = interp2(r.uv[0], r.uv[1], r.uv[2], w);
+    const float h  = sample_bilinear(r.tx, uv);
+    p              = displace(p, n, h, r.scale, viewScale, r.offset, viewOffset);
+  }
+  return p;
+}
+
+// last part whose first vertex (within the warp's range) is <= j
+__device__ __forceinline__ u32 part_of(const u32* vpre, u32 j)
+{
+  u32 lo = 0, hi = kPartsPerWarp;
+#pragma unroll
+  for(int s = 0; s < 5; s++)
+  {
+    const u32 mid = (lo + hi) >> 1;
+    if(vpre[mid] <= j)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(kVertexWarps * 32) k_instantiate_vertices(StageCtx c, InstantiateBuffers ib)
+{
+  __shared__ PartRecord s_part[kVertexWarps][kPartsPerWarp];
+  __shared__ u32        s_vpre[kVertexWarps][kPartsPerWarp + 1];
+  __shared__ u32        s_range[2];
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if(threadIdx.x == 0)
+    part_range(c, s_range[0], s_range[1]);
+  __syncthreads();
+  const u32 begin = s_range[0], n = s_range[1] - s_range[0];
+
+  const tc_SceneBuilding*    b            = c.build;
+  const tc_TessTriangleInfo* parts        = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
+  const bool                 haveTextures = c.numTextures > 0 && c.textures != nullptr;
+  float*                     gv           = reinterpret_cast<float*>(b->genVertices);
+  const bool                 aligned16    = (reinterpret_cast<uintptr_t>(gv) & 15) == 0;
+  const float                viewScale    = c.view->displacementScale;
+  const float                viewOffset   = c.view->displacementOffset;
+  const u32                  nwarps    = (gridDim.x * blockDim.x) >> 5;
+  const u32                  numChunks = (n + kPartsPerWarp - 1) / kPartsPerWarp;
+  PartRecord*                sp        = s_part[warp];
+  u32*                       vpre      = s_vpre[warp];
+
+  for(u32 chunk = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; chunk < numChunks; chunk += nwarps)
+  {
+    const u32  p        = begin + chunk * kPartsPerWarp + lane;
+    const u32  vo       = p < begin + n ? ib.vertexOffset[p] : ~0u;
+    const bool accepted = vo != ~0u;
+    // accepted parts form a prefix of the part order: nothing further to do
+    if(!__any_sync(0xFFFFFFFFu, accepted))
+      break;
+    u32 nv = 0;
+    if(accepted)
+    {
+      const uint2*             raw = reinterpret_cast<const uint2*>(parts + p);
+      const uint2              r0 = raw[0], r1 = raw[1], r2 = raw[2];
+      const u32                cfg = r2.y >> 16;
+      const u32                tri = r2.y & 0xFFFFu;
+      const tc_TessTableEntry  e   = table_entry(c.table, cfg);
+      const tc_RenderInstance& in  = c.instances[r0.x];
+      const tc_Cluster         cl  = reinterpret_cast<const tc_Cluster*>(in.clusters)[r0.y];
+      const uint8_t*           lt  = reinterpret_cast<const uint8_t*>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
+      const float*             pos = reinterpret_cast<const float*>(in.positions);
+      const float*             nrm = reinterpret_cast<const float*>(in.normals);
+      const float*             uvs = reinterpret_cast<const float*>(in.texcoords);
+      const u32                vtx[3] = {r1.x, r1.y, r2.x};
+      PartRecord&              r      = sp[lane];
+#pragma unroll
+      for(int v = 0; v < 3; v++)
+      {
+        const u32 vi = cl.firstLocalVertex + lt[tri * 3 + v];
+        r.bb[v]      = decode_bary(vtx[v]);
+        r.p[v]       = ldg3(pos, vi);
+        r.n[v]       = normalize3(ldg3(nrm, vi));  // :329
+        r.uv[v]      = ldg2(uvs, vi);
+      }
+      r.firstVertex = e.firstVertex;
+      r.cfg         = cfg;
+      r.tx          = {};
+      if(haveTextures && in.displacementIndex >= 0)
+      {
+        if((u32)in.displacementIndex < c.numTextures)
+          r.tx = c.textures[in.displacementIndex];
+        else
+          atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
+      }
+      r.scale  = in.displacementScale;
+      r.offset = in.displacementOffset;
+      nv       = e.numVertices;
+    }
+    const u32 inc  = warp_inclusive<u32>(nv, lane);
+    vpre[lane + 1] = inc;
+    if(lane == 0)
+      vpre[0] = 0;
+    const u32 total = __shfl_sync(0xFFFFFFFFu, inc, 31);
+    const u64 v0    = __shfl_sync(0xFFFFFFFFu, vo, 0);
+    __syncwarp();
+
+    const Table& table = c.table;
+    if(aligned16)
+    {
+      const u32 head   = min((4u - (u32)(v0 & 3)) & 3u, total);
+      const u32 groups = (total - head) / 4;
+      const u32 tail   = total - head - 4 * groups;
+      if(lane < head)
+      {
+        const u32 pi = part_of(vpre, lane);
+        const f3  q  = gen_vertex(table, sp[pi], lane - vpre[pi], viewScale, viewOffset);
+        float*    d  = gv + (v0 + lane) * 3;
+        d[0] = q.x, d[1] = q.y, d[2] = q.z;
+      }
+      for(u32 g = lane; g < groups; g += 32)
+      {
+        // four consecutive vertices, usually of one part: one lookup, then advance
+        const u32 j  = head + 4 * g;
+        u32       pi = part_of(vpre, j);
+        f3        q[4];
+#pragma unroll
+        for(u32 k = 0; k < 4; k++)
+        {
+          while(j + k >= vpre[pi + 1])
+            pi++;
+          q[k] = gen_vertex(table, sp[pi], j + k - vpre[pi], viewScale, viewOffset);
+        }
+        float4* d = reinterpret_cast<float4*>(gv + (v0 + j) * 3);
+        d[0]      = make_float4(q[0].x, q[0].y, q[0].z, q[1].x);
+        d[1]      = make_float4(q[1].y, q[1].z, q[2].x, q[2].y);
+        d[2]      = make_float4(q[2].z, q[3].x, q[3].y, q[3].z);
+      }
+      if(lane < tail)
+      {
+        const u32 j  = head + 4 * groups + lane;
+        const u32 pi = part_of(vpre, j);
+        const f3  q  = gen_vertex(table, sp[pi], j - vpre[pi], viewScale, viewOffset);
+        float*    d  = gv + (v0 + j) * 3;
+        d[0] = q.x, d[1] = q.y, d[2] = q.z;
+      }
+    }
+    else
+    {
+      for(u32 j = lane; j < total; j += 32)
+      {
+        const u32 pi = part_of(vpre, j);
+        const f3  q  = gen_vertex(table, sp[pi], j - vpre[pi], viewScale, viewOffset);
+        float*    d  = gv + (v0 + j) * 3;
+        d[0] = q.x, d[1] = q.y, d[2] = q.z;
+      }
+    }
+    __syncwarp();  // the warp's staging is rewritten by its next chunk
+  }
+}
+
 }  // namespace
 
-cudaError_t launch_triangle_instantiate(const StageCtx& c, u32 blockSize, u32 grid, cudaStream_t s)
+u32 instantiate_alloc_tiles(u32 maxParts) { return (maxParts + kAllocTile - 1) / kAllocTile; }
+
+cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
+                                        u32 vertexBlocksPerSM, cudaStream_t s)
 {
-  switch(blockSize)
-  {
-    case 128:
-      k_triangle_instantiate<128><<<grid, 128, 0, s>>>(c);
-      break;
-    case 512:
-      k_triangle_instantiate<512><<<grid, 512, 0, s>>>(c);
-      break;
-    default:
-      k_triangle_instantiate<256><<<grid, 256, 0, s>>>(c);
-      break;
-  }
+  const u32   allocGrid = std::max(1u, std::min(instantiate_alloc_tiles(maxParts), numSMs * 8));
+  k_instantiate_alloc<<<allocGrid, kAllocBlock, 0, s>>>(c, buf);
+  cudaError_t e = cudaGetLastError();
+  if(e != cudaSuccess)
+    return e;
+  const u32 chunks     = (maxParts + kPartsPerWarp - 1) / kPartsPerWarp;
+  const u32 vertexGrid = std::max(1u, std::min((chunks + kVertexWarps - 1) / kVertexWarps,
+                                               numSMs * std::max(1u, vertexBlocksPerSM)));
+  k_instantiate_vertices<<<vertexGrid, kVertexWarps * 32, 0, s>>>(c, buf);
   return cudaGetLastError();
 }
 

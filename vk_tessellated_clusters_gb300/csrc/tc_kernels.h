@@ -11,13 +11,38 @@ namespace tc {
 struct StageCtx;
 typedef uint32_t u32;
 
+// exclusive offsets of one visible cluster's appends
+struct ClusterOffsets
+{
+  u32                part, split, gen, vert;
+  unsigned long long data;
+};
+
+// cluster_classify scratch, per visible cluster of a launch's window
+struct ClassifyBuffers
+{
+  uint2*          counts;
+  ClusterOffsets* offsets;
+  u32*            triWords;  // 64 per cluster
+};
+
+// triangle_tess_template_instantiate scratch, per part triangle
+struct InstantiateBuffers
+{
+  u32* vertexOffset;  // first generated vertex of each accepted part, ~0 otherwise
+};
+
 cudaError_t launch_frame_begin(const StageCtx& c, u32 grid, cudaStream_t s);
 cudaError_t launch_instances_classify(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 cudaError_t launch_build_setup(const StageCtx& c, u32 mode, cudaStream_t s);
-cudaError_t launch_cluster_classify(const StageCtx& c, u32 warpsPerBlock, u32 grid, cudaStream_t s);
+cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
+                                    cudaStream_t s);
+u32         classify_scan_tiles(u32 maxClusters);
 cudaError_t launch_triangle_split(const StageCtx& c, u32 blockSize, u32 grid, cudaStream_t s);
-cudaError_t launch_triangle_instantiate(const StageCtx& c, u32 blockSize, u32 grid, cudaStream_t s);
+cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
+                                        u32 vertexBlocksPerSM, cudaStream_t s);
+u32         instantiate_alloc_tiles(u32 maxParts);
 cudaError_t launch_blas_setup_insertion(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 cudaError_t launch_blas_clusters_insert(const StageCtx& c, u32* segStart, u32* segEnd, u32 stride, u32 grid,
                                         cudaStream_t s);
@@ -27,8 +52,7 @@ cudaError_t launch_instantiate_backward(const StageCtx& c, const float* gradVert
 // tiles per launch for each stage (used to size the look-back scratch)
 constexpr u32 kInstanceTile     = 256;  // instances per tile (instances_classify, blas_setup)
 constexpr u32 kCullTile         = 256;  // clusters per tile
-constexpr u32 kClassifyMinWarps = 2;    // smallest clusters-per-tile variant
 constexpr u32 kSplitMinItems    = 16;   // smallest split items-per-tile variant
-constexpr u32 kInstantiateTile  = 32;   // part triangles per tile
+constexpr u32 kInstantiateTile  = 1024; // part triangles per allocation tile
 
 }  // namespace tc

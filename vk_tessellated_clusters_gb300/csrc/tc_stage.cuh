@@ -11,9 +11,11 @@ namespace tc {
 // counter and the totals the last tile publishes. Zeroed before every launch.
 struct LaunchScratch
 {
-  u64* lbState;   // [numCounters][lbStride]
-  u32  lbStride;  // max tiles per launch
-  u32  selfClean; // 1: the last block re-zeroes what the launch used (repeated launches on one slot)
+  u64* lbState;       // [numCounters][lbStride]
+  u32  lbStride;      // max tiles per launch
+  u32  selfClean;     // 1: the last block re-zeroes what the launch used (repeated launches on one slot)
+  u32  itemCapacity;  // capacity of the stage's per-item scratch arrays (items per launch)
+  u32  _pad;
   u32* ticket;
   u32* done;
   u64* totals;  // [numCounters] inclusive totals (base included) of the last tile

@@ -190,9 +190,12 @@ class FrameArgs(ctypes.Structure):
 
 
 class Schedule(ctypes.Structure):
-    _fields_ = [("classifyWarpsPerBlock", ctypes.c_uint32), ("splitBlockSize", ctypes.c_uint32),
-                ("instantiatePartsPerTile", ctypes.c_uint32), ("instantiateBlockSize", ctypes.c_uint32),
+    _fields_ = [("classifyBlocksPerSM", ctypes.c_uint32), ("splitBlockSize", ctypes.c_uint32),
+                ("vertexBlocksPerSM", ctypes.c_uint32), ("scanBlocksPerSM", ctypes.c_uint32),
                 ("blocksPerSM", ctypes.c_uint32), ("_pad", ctypes.c_uint32 * 3)]
+
+
+SCHEDULE_FIELDS = ("classifyBlocksPerSM", "splitBlockSize", "vertexBlocksPerSM", "scanBlocksPerSM", "blocksPerSM")
 
 
 class ContextDesc(ctypes.Structure):

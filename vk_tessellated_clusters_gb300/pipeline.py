@@ -70,16 +70,14 @@ class TessellationPipeline:
     def set_schedule(self, sched: dict) -> None:
         s = L.Schedule()
         cur = self.schedule()
-        for k in ("classifyWarpsPerBlock", "splitBlockSize", "instantiatePartsPerTile", "instantiateBlockSize",
-                  "blocksPerSM"):
+        for k in L.SCHEDULE_FIELDS:
             setattr(s, k, int(sched.get(k, cur[k])))
         native.check(self.lib.tc_set_schedule(self.ctx, ctypes.byref(s)), "tc_set_schedule")
 
     def schedule(self) -> dict:
         s = L.Schedule()
         native.check(self.lib.tc_get_schedule(self.ctx, ctypes.byref(s)), "tc_get_schedule")
-        return {k: getattr(s, k) for k in ("classifyWarpsPerBlock", "splitBlockSize", "instantiatePartsPerTile",
-                                           "instantiateBlockSize", "blocksPerSM")}
+        return {k: getattr(s, k) for k in L.SCHEDULE_FIELDS}
 
     def set_cameras(self, now: Camera | np.ndarray, last: Camera | np.ndarray | None = None) -> None:
         fc = now if isinstance(now, np.ndarray) else frame_constants(now)
