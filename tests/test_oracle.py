@@ -1,0 +1,239 @@
+"""The CPU oracle: known answers of the shader math, whole-frame invariants,
+golden digests, and its FP64 adjoint against finite differences."""
+import ctypes
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from tests.golden.cases import CASES, run_case, outputs_digest
+from vk_tessellated_clusters_gb300 import layouts as L
+from vk_tessellated_clusters_gb300 import scene as S
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ONE = L.TESSTABLE_COORD_MAX
+
+
+def lib():
+    from oracle.binding import lib as _lib
+    return _lib()
+
+
+def encode(w, u, v):
+    return lib().tco_encode_barycentrics(w, u, v)
+
+
+def decode(e):
+    out = (ctypes.c_float * 3)()
+    lib().tco_decode_barycentrics(e, out)
+    return tuple(out)
+
+
+def factors(a, b, c, eye=(0, 0, 0), near=0.01, h=1080.0, rate=0.25):
+    f3 = ctypes.c_float * 3
+    out = (ctypes.c_uint32 * 3)()
+    lib().tco_tess_factors(f3(*a), f3(*b), f3(*c), f3(*eye), near, h, rate, out)
+    return tuple(out)
+
+
+def get_config(f, tv=(0, 1, 2)):
+    ff = (ctypes.c_uint32 * 3)(*f)
+    t = (ctypes.c_uint32 * 3)(*tv)
+    c = lib().tco_get_config(ff, t)
+    return c, tuple(t)
+
+
+# ---------------------------------------------------------------------------
+# tessellation.glsl known answers
+# ---------------------------------------------------------------------------
+
+def test_encode_corners_and_midpoints():
+    assert encode(1, 0, 0) == 0
+    assert encode(0, 1, 0) == ONE
+    assert encode(0, 0, 1) == ONE << 16
+    assert encode(0.5, 0.5, 0) == ONE // 2
+    assert encode(0, 0.5, 0.5) == (ONE // 2) | ((ONE // 2) << 16)
+    # largest component is fixed up so the three sum to exactly 1 (tessellation.glsl:51-57)
+    e = encode(0.2, 0.7, 0.1)
+    u, v = e & 0xFFFF, e >> 16
+    assert v == int(0.1 * ONE + 0.5) and u == ONE - int(0.2 * ONE + 0.5) - v
+
+
+def test_decode_is_exact_and_inverts_encode():
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        u = int(rng.integers(0, ONE + 1))
+        v = int(rng.integers(0, ONE - u + 1))
+        w = decode(u | (v << 16))
+        assert w[1] == u / ONE and w[2] == v / ONE and w[0] == (1 - u / ONE) - v / ONE
+        assert encode(*w) == u | (v << 16)
+
+
+def test_tess_factor_known_answers():
+    # edge length 1 at distance 10: round(1/10 * 1080 * 0.25) = 27
+    assert factors((0, 0, 10), (1, 0, 10), (0, 1, 10), rate=0.25)[0] == 27
+    # clamped to [1, 32768]
+    assert factors((0, 0, 1000), (1e-4, 0, 1000), (0, 1e-4, 1000)) == (1, 1, 1)
+    assert factors((0, 0, 0.0), (5, 0, 0), (0, 5, 0), near=0.01)[0] == 32768
+    # distance uses the nearer endpoint of each edge and the near plane
+    f = factors((0, 0, 2), (1, 0, 20), (0, 1, 20), rate=1.0, h=100.0)
+    assert f[0] == round(math.dist((0, 0, 2), (1, 0, 20)) / 2 * 100)
+    # round half to even: 2.5 -> 2
+    assert factors((0, 0, 1), (0.025, 0, 1), (0, 0.025, 1), rate=1.0, h=100.0)[0] == 2
+
+
+def test_get_config_rotation_and_flip():
+    lk = lambda x, y, z: x + 16 * y + 256 * z - 273
+    c, tv = get_config((3, 2, 1))
+    assert c == lk(3, 2, 1) and tv == (0, 1, 2)
+    c, tv = get_config((1, 3, 2))   # max at y -> .yzx
+    assert c == lk(3, 2, 1) and tv == (1, 2, 0)
+    c, tv = get_config((2, 1, 3))   # max at z -> .zxy
+    assert c == lk(3, 2, 1) and tv == (2, 0, 1)
+    c, tv = get_config((3, 1, 2))   # z > y -> flipped
+    assert c == lk(3, 1, 2) | 0x8000
+    c, _ = get_config((2, 2, 1))    # tie: y checked first -> (2,1,2), flipped
+    assert c == lk(2, 1, 2) | 0x8000
+
+
+def test_split_factor_and_pass_count():
+    sf = lambda f, s: lib().tco_split_factor(f, s)
+    assert sf(12, 8) == 2 and sf(11, 8) == 1 and sf(100, 8) == 8 and sf(32768, 11) == 11 and sf(30, 2) == 2
+    for s in range(2, 12):
+        coord, n = ONE, 0
+        while coord > s:
+            coord //= s
+            n += 1
+        assert lib().tco_split_pass_count(s) == n
+    assert lib().tco_split_pass_count(8) == 4
+
+
+# ---------------------------------------------------------------------------
+# whole frames
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_golden_frame_digests(name, oracle):
+    with open(os.path.join(ROOT, "tests", "golden", "oracle_frames.json")) as f:
+        want = json.load(f)[name]
+    assert run_case(name, oracle) and outputs_digest(run_case(name, oracle)[2]) == want
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_frame_invariants(name, oracle):
+    sc, st, out = run_case(name, oracle)
+    e = oracle.entries
+    rb, b = out["readback"], out["build"]
+    ti = out["tempInstantiations"]
+    full = (ti["clusterIdOffset"] >> 30) == 0
+    parts = out["partTriangles"]
+    # every instantiation is accounted for; instantiation slots follow generation order
+    assert len(ti) == int(rb["numTempInstantiations"]) == int(b["tempInstantiateCounter"])
+    pidx = ti["clusterIdOffset"][~full] & 0x3FFFFFFF
+    assert np.array_equal(pidx, np.arange(len(pidx)))
+    # vertex ranges are contiguous and ordered
+    nvs = []
+    for j in range(len(ti)):
+        if full[j]:
+            fc = out["fullClusters"][j]
+            g = sc.geometries[sc.instances[fc["instanceID"]].geometry]
+            nvs.append(int(g.clusters[fc["clusterID"]]["numVertices"]))
+        else:
+            p = parts[ti["clusterIdOffset"][j] & 0x3FFFFFFF]
+            nvs.append(int(e[(p["triangleID_config"] >> 16) & 0x7FFF]["numVertices"]))
+    starts = ti["vertexBufferAddress"] // 12
+    assert np.array_equal(starts, np.concatenate([[0], np.cumsum(nvs)[:-1]]).astype(np.uint64))
+    assert len(out["genVertices"]) == sum(nvs) == int(rb["numGenVertices"])
+    # tessellated triangles = full cluster triangles + part pattern triangles
+    tris = sum(int(sc.geometries[sc.instances[fc["instanceID"]].geometry].clusters[fc["clusterID"]]["numTriangles"])
+               for fc in out["fullClusters"])
+    tris += int(e[(parts["triangleID_config"] >> 16) & 0x7FFF]["numTriangles"].astype(np.int64).sum())
+    assert tris == int(rb["numTotalTriangles"])
+    # BLAS lists: per-instance sections holding exactly that instance's CLAS, in instantiation order
+    bi = out["blasBuildInfos"]
+    refs = out["blasClusterAddresses"]
+    for i in range(len(sc.instances)):
+        mine = out["tempClusterAddresses"][out["tempInstanceIDs"] == i]
+        off = int(bi[i]["clusterReferences"]) // 8
+        assert bi[i]["clusterReferencesCount"] == len(mine) and bi[i]["clusterReferencesStride"] == 8
+        assert np.array_equal(refs[off:off + len(mine)], mine)
+    # part triangles: positively oriented sub-triangles inside the unit triangle
+    v = parts["vtxEncoded"].astype(np.int64)
+    u_, w_ = v & 0xFFFF, v >> 16
+    assert np.all(u_ + w_ <= ONE)
+    area = (u_[:, 1] - u_[:, 0]) * (w_[:, 2] - w_[:, 0]) - (w_[:, 1] - w_[:, 0]) * (u_[:, 2] - u_[:, 0])
+    assert np.all(area > 0)
+    # the split tree tiles each base triangle (up to the 2^-15 quantisation of deep levels)
+    key = parts["instanceID"].astype(np.int64) << 40 | parts["clusterID"].astype(np.int64) << 16 | (
+        parts["triangleID_config"] & 0xFFFF).astype(np.int64)
+    if int(b["splitWriteCounter"]) == 0:
+        # no splits: every part triangle is a whole base triangle
+        assert np.all(area == ONE * ONE)
+    sums = {}
+    for k_, a_ in zip(key.tolist(), area.tolist()):
+        sums[k_] = sums.get(k_, 0) + a_
+    rel = np.abs(np.array(list(sums.values())) / (ONE * ONE) - 1.0)
+    nothing_dropped = (int(rb["numPartTriangles"]) == len(parts)
+                       and int(rb["numSplitTriangles"]) <= st.caps["maxSplitTriangles"])
+    if nothing_dropped and len(parts):
+        assert rel.max() < 2e-3, rel.max()
+
+
+def test_fp32_vertices_close_to_fp64_twin(oracle):
+    sc, st, out = run_case("icosphere2_split", oracle)
+    ref = oracle.vertices_f64(st, len(out["genVertices"]))
+    err = np.abs(out["genVertices"].astype(np.float64) - ref).max()
+    assert err < 1e-5 * 2.1  # bounding-box diagonal of a unit sphere with displacement
+
+
+# ---------------------------------------------------------------------------
+# FP64 adjoint vs central differences (tessellation decisions frozen)
+# ---------------------------------------------------------------------------
+
+def test_fp64_adjoint_matches_finite_differences(oracle):
+    from oracle.binding import lib as olib
+    sc, st, out = run_case("icosphere2_split", oracle)
+    g = sc.geometries[0]
+    tex = sc.textures[0].texels.astype(np.float64)
+    P = g.positions.astype(np.float64).copy()
+    N = g.normals.astype(np.float64).copy()
+    T = tex.copy()
+    nverts = len(out["genVertices"])
+    rng = np.random.default_rng(3)
+    target = out["genVertices"].astype(np.float64) + rng.normal(0, 0.01, (nverts, 3))
+    pp = (ctypes.c_void_p * 1)(P.ctypes.data)
+    nn = (ctypes.c_void_p * 1)(N.ctypes.data)
+    tt = (ctypes.c_void_p * 1)(T.ctypes.data)
+
+    def loss():
+        v = np.zeros((nverts, 3))
+        olib().tco_generate_vertices_f64_params(ctypes.byref(oracle.table), ctypes.byref(st.args), pp, nn, tt,
+                                                v.ctypes.data)
+        return float(((v - target) ** 2).sum()), v
+
+    L0, v0 = loss()
+    grad_v = 2 * (v0 - target)
+    dP = np.zeros_like(P)
+    dN = np.zeros_like(N)
+    dT = np.zeros_like(T)
+    olib().tco_backward_f64(ctypes.byref(oracle.table), ctypes.byref(st.args), grad_v.ctypes.data,
+                            (ctypes.c_void_p * 1)(dP.ctypes.data), (ctypes.c_void_p * 1)(dN.ctypes.data),
+                            (ctypes.c_void_p * 1)(dT.ctypes.data))
+    h = 1e-3
+    picks = [("P", P, dP, i) for i in rng.choice(P.size, 8, replace=False)]
+    picks += [("N", N, dN, i) for i in rng.choice(N.size, 8, replace=False)]
+    touched = np.flatnonzero(dT.reshape(-1))
+    picks += [("T", T, dT, i) for i in rng.choice(touched, 8, replace=False)]
+    for name, arr, grad, i in picks:
+        flat = arr.reshape(-1)
+        old = flat[i]
+        flat[i] = old + h
+        lp, _ = loss()
+        flat[i] = old - h
+        lm, _ = loss()
+        flat[i] = old
+        fd = (lp - lm) / (2 * h)
+        an = grad.reshape(-1)[i]
+        assert abs(fd - an) <= 1e-4 * max(1.0, abs(fd)), (name, i, fd, an)

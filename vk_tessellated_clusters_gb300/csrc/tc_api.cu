@@ -362,7 +362,7 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, desc->device);
   ctx->numSMs   = (u32)std::max(1, sms);
-  ctx->schedule = {8, 256, 6, 8, 1, {0, 0, 0}};
+  ctx->schedule = {8, 256, 5, 8, 1, {0, 0, 0}};
   ctx->plan     = make_plan(*desc);
   if(cudaMalloc(&ctx->dScratch, ctx->plan.totalBytes) != cudaSuccess
      || cudaMemset(ctx->dScratch, 0, ctx->plan.totalBytes) != cudaSuccess)

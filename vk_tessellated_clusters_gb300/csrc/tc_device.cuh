@@ -277,12 +277,33 @@ __device__ __forceinline__ float sample_bilinear(const tc_DisplacementTexture& t
 {
   if(tx.width == 0 || tx.height == 0)
     return 0.0f;
-  Taps  b   = bilinear_taps(tx, uv);
-  float t00 = fetch_texel(tx, b.x0, b.y0);
-  float t10 = fetch_texel(tx, b.x1, b.y0);
-  float t01 = fetch_texel(tx, b.x0, b.y1);
-  float t11 = fetch_texel(tx, b.x1, b.y1);
-  float gx  = 1.0f - b.fx;
+  Taps      b  = bilinear_taps(tx, uv);
+  const u64 r0 = (u64)b.y0 * tx.width, r1 = (u64)b.y1 * tx.width;
+  float     t00, t10, t01, t11;
+  if(tx.format == TC_TEXEL_F16)
+  {
+    const unsigned short* t = reinterpret_cast<const unsigned short*>(tx.texels);
+    t00 = __half2float(__ushort_as_half(__ldg(t + r0 + b.x0)));
+    t10 = __half2float(__ushort_as_half(__ldg(t + r0 + b.x1)));
+    t01 = __half2float(__ushort_as_half(__ldg(t + r1 + b.x0)));
+    t11 = __half2float(__ushort_as_half(__ldg(t + r1 + b.x1)));
+  }
+  else if(tx.format == TC_TEXEL_F32)
+  {
+    const float* t = reinterpret_cast<const float*>(tx.texels);
+    t00 = __ldg(t + r0 + b.x0);
+    t10 = __ldg(t + r0 + b.x1);
+    t01 = __ldg(t + r1 + b.x0);
+    t11 = __ldg(t + r1 + b.x1);
+  }
+  else
+  {
+    t00 = fetch_texel(tx, b.x0, b.y0);
+    t10 = fetch_texel(tx, b.x1, b.y0);
+    t01 = fetch_texel(tx, b.x0, b.y1);
+    t11 = fetch_texel(tx, b.x1, b.y1);
+  }
+  float gx = 1.0f - b.fx;
   float top = gx * t00 + b.fx * t10;
   float bot = gx * t01 + b.fx * t11;
   return (1.0f - b.fy) * top + b.fy * bot;

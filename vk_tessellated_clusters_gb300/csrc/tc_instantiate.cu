@@ -10,7 +10,7 @@
 //              and writes the 44 B of instantiation arguments per part; the
 //              first vertex of each accepted part goes to scratch
 //   vertices : HBM-write bound (12 B per generated vertex dominates). One warp
-//              per 32 consecutive parts, whose vertices form one contiguous
+//              per 16 consecutive parts, whose vertices form one contiguous
 //              range: per-part base data staged once in shared memory, then the
 //              range is written as aligned 48-byte groups of four vertices
 //              (three 16-byte stores per lane), scalar stores only at the two
@@ -36,7 +36,7 @@ constexpr u32 kAllocBlock   = 256;
 constexpr u32 kAllocItems   = 4;
 constexpr u32 kAllocTile    = kAllocBlock * kAllocItems;
 constexpr u32 kVertexWarps  = 8;  // warps per block of the vertex kernel
-constexpr u32 kPartsPerWarp = 32;
+constexpr u32 kPartsPerWarp = 16;  // parts staged per warp and chunk (shared memory budget)
 
 static_assert(kAllocTile == kInstantiateTile, "allocation tile size");
 
@@ -309,9 +309,10 @@ __device__ __forceinline__ f3 gen_vertex(const Table& table, const PartRecord& r
 // last part whose first vertex (within the warp's range) is <= j
 __device__ __forceinline__ u32 part_of(const u32* vpre, u32 j)
 {
+  static_assert(kPartsPerWarp == 16, "binary search depth");
   u32 lo = 0, hi = kPartsPerWarp;
 #pragma unroll
-  for(int s = 0; s < 5; s++)
+  for(int s = 0; s < 4; s++)
   {
     const u32 mid = (lo + hi) >> 1;
     if(vpre[mid] <= j)
@@ -322,10 +323,11 @@ __device__ __forceinline__ u32 part_of(const u32* vpre, u32 j)
   return lo;
 }
 
-__global__ void __launch_bounds__(kVertexWarps * 32) k_instantiate_vertices(StageCtx c, InstantiateBuffers ib)
+__global__ void __launch_bounds__(kVertexWarps * 32, 5) k_instantiate_vertices(StageCtx c, InstantiateBuffers ib)
 {
   __shared__ PartRecord s_part[kVertexWarps][kPartsPerWarp];
   __shared__ u32        s_vpre[kVertexWarps][kPartsPerWarp + 1];
+  __shared__ __align__(16) float s_stage[kVertexWarps][32][12];  // one 4-vertex group per lane
   __shared__ u32        s_range[2];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if(threadIdx.x == 0)
@@ -348,7 +350,7 @@ __global__ void __launch_bounds__(kVertexWarps * 32) k_instantiate_vertices(Stag
   for(u32 chunk = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; chunk < numChunks; chunk += nwarps)
   {
     const u32  p        = begin + chunk * kPartsPerWarp + lane;
-    const u32  vo       = p < begin + n ? ib.vertexOffset[p] : ~0u;
+    const u32  vo       = (lane < kPartsPerWarp && p < begin + n) ? ib.vertexOffset[p] : ~0u;
     const bool accepted = vo != ~0u;
     // accepted parts form a prefix of the part order: nothing further to do
     if(!__any_sync(0xFFFFFFFFu, accepted))
@@ -392,62 +394,55 @@ __global__ void __launch_bounds__(kVertexWarps * 32) k_instantiate_vertices(Stag
       r.offset = in.displacementOffset;
       nv       = e.numVertices;
     }
-    const u32 inc  = warp_inclusive<u32>(nv, lane);
-    vpre[lane + 1] = inc;
+    const u32 inc = warp_inclusive<u32>(nv, lane);
+    if(lane < kPartsPerWarp)
+      vpre[lane + 1] = inc;
     if(lane == 0)
       vpre[0] = 0;
-    const u32 total = __shfl_sync(0xFFFFFFFFu, inc, 31);
+    const u32 total = __shfl_sync(0xFFFFFFFFu, inc, kPartsPerWarp - 1);
     const u64 v0    = __shfl_sync(0xFFFFFFFFu, vo, 0);
     __syncwarp();
 
-    const Table& table = c.table;
-    if(aligned16)
+    // Work items over the warp's vertex range [v0, v0 + total): single vertices
+    // up to the first 16-byte aligned vertex (v % 4 == 0), groups of four
+    // vertices (48 B = three aligned 16-byte stores), single vertices at the
+    // end. One copy of the vertex code; a group's vertices pass through the
+    // lane's own staging slots.
+    const u32 head   = aligned16 ? min((4u - (u32)(v0 & 3)) & 3u, total) : total;
+    const u32 groups = aligned16 ? (total - head) / 4 : 0;
+    const u32 items  = head + groups + (total - head - 4 * groups);
+    float*    stage  = s_stage[warp][lane];
+    for(u32 t = lane; t < items; t += 32)
     {
-      const u32 head   = min((4u - (u32)(v0 & 3)) & 3u, total);
-      const u32 groups = (total - head) / 4;
-      const u32 tail   = total - head - 4 * groups;
-      if(lane < head)
+      const bool grp   = t >= head && t < head + groups;
+      const u32  j     = t < head ? t : (grp ? head + 4 * (t - head) : t + 3 * groups);
+      const u32  count = grp ? 4u : 1u;
+      u32        pi    = part_of(vpre, j);
+#pragma unroll 1
+      for(u32 k = 0; k < count; k++)
       {
-        const u32 pi = part_of(vpre, lane);
-        const f3  q  = gen_vertex(table, sp[pi], lane - vpre[pi], viewScale, viewOffset);
-        float*    d  = gv + (v0 + lane) * 3;
-        d[0] = q.x, d[1] = q.y, d[2] = q.z;
-      }
-      for(u32 g = lane; g < groups; g += 32)
-      {
-        // four consecutive vertices, usually of one part: one lookup, then advance
-        const u32 j  = head + 4 * g;
-        u32       pi = part_of(vpre, j);
-        f3        q[4];
-#pragma unroll
-        for(u32 k = 0; k < 4; k++)
+        while(j + k >= vpre[pi + 1])
+          pi++;
+        const f3 q = gen_vertex(c.table, sp[pi], j + k - vpre[pi], viewScale, viewOffset);
+        if(grp)
         {
-          while(j + k >= vpre[pi + 1])
-            pi++;
-          q[k] = gen_vertex(table, sp[pi], j + k - vpre[pi], viewScale, viewOffset);
+          stage[3 * k + 0] = q.x;
+          stage[3 * k + 1] = q.y;
+          stage[3 * k + 2] = q.z;
         }
-        float4* d = reinterpret_cast<float4*>(gv + (v0 + j) * 3);
-        d[0]      = make_float4(q[0].x, q[0].y, q[0].z, q[1].x);
-        d[1]      = make_float4(q[1].y, q[1].z, q[2].x, q[2].y);
-        d[2]      = make_float4(q[2].z, q[3].x, q[3].y, q[3].z);
+        else
+        {
+          float* d = gv + (v0 + j) * 3;
+          d[0] = q.x, d[1] = q.y, d[2] = q.z;
+        }
       }
-      if(lane < tail)
+      if(grp)
       {
-        const u32 j  = head + 4 * groups + lane;
-        const u32 pi = part_of(vpre, j);
-        const f3  q  = gen_vertex(table, sp[pi], j - vpre[pi], viewScale, viewOffset);
-        float*    d  = gv + (v0 + j) * 3;
-        d[0] = q.x, d[1] = q.y, d[2] = q.z;
-      }
-    }
-    else
-    {
-      for(u32 j = lane; j < total; j += 32)
-      {
-        const u32 pi = part_of(vpre, j);
-        const f3  q  = gen_vertex(table, sp[pi], j - vpre[pi], viewScale, viewOffset);
-        float*    d  = gv + (v0 + j) * 3;
-        d[0] = q.x, d[1] = q.y, d[2] = q.z;
+        const float4* src = reinterpret_cast<const float4*>(stage);
+        float4*       d   = reinterpret_cast<float4*>(gv + (v0 + j) * 3);
+        d[0]              = src[0];
+        d[1]              = src[1];
+        d[2]              = src[2];
       }
     }
     __syncwarp();  // the warp's staging is rewritten by its next chunk
