@@ -557,6 +557,13 @@ typedef struct tc_GradTargets {
   uint64_t dNormals;
 } tc_GradTargets;
 
+/* Forward of the vertex generation of the last frame built in `args` with its
+ * tessellation decisions held fixed: regenerates genVertices of every accepted
+ * instantiation from the current positions / normals / texels (the forward of
+ * the differentiable path; bit-identical to the build's vertices for unchanged
+ * inputs). Requires TC_FLAG_WRITE_FULLCLUSTERS. */
+tc_status tc_generate_vertices(tc_context* ctx, const tc_frame_args* args, void* stream);
+
 /* Adjoint of the vertex generation of the last frame built in `args` (full
  * clusters and part triangles, tessellation decisions held fixed): scatters
  * dL/d(genVertices) into base positions, base normals and displacement texels.

@@ -1,0 +1,123 @@
+"""Differentiable displaced-vertex generation through torch.autograd.
+
+The tessellation decisions of a built frame (segment counts, configs, split
+tree, instantiation order) are piecewise constant in the inputs, so they are
+held fixed: the differentiable function maps base positions, base normals and
+displacement texels to the frame's generated vertices
+
+    part triangle : v = P(w) + normalize(N(w)) * (bilinear(tex, uv(w)) * s + o)
+    full cluster  : v = p + normalize(n) * (bilinear(tex, uv) * s + o)
+
+(triangle_tess_template_instantiate.comp.glsl:343-371,
+cluster_classify.comp.glsl:457-482), with forward tc_generate_vertices and
+backward tc_instantiate_backward (CUDA kernels). The parameters are views of
+the pipeline's own device buffers, so in-place updates (an optimiser step) are
+seen by the next frame.
+
+    frozen = FrozenFrame(pipe)               # after pipe.build(...) with FLAG_WRITE_FULLCLUSTERS
+    v = tessellate(frozen)                    # (num_vertices, 3) float32
+    loss = ((v - target) ** 2).sum(); loss.backward()
+    frozen.positions[0].grad, frozen.normals[0].grad, frozen.texels[0].grad
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import layouts as L
+
+
+class FrozenFrame:
+    def __init__(self, pipe):
+        import torch
+        self.torch = torch
+        if not (pipe.state.flags & L.FLAG_WRITE_FULLCLUSTERS):
+            raise ValueError("the frame must be built with FLAG_WRITE_FULLCLUSTERS")
+        self.pipe = pipe
+        torch.cuda.synchronize(pipe.device)
+        out = pipe.state
+        self.num_vertices = self._accepted_vertex_count()
+        scene = pipe.scene
+        res = out.res
+        self.positions = [self._view(b["positions"], g.positions.shape) for b, g in zip(res.geo, scene.geometries)]
+        self.normals = [self._view(b["normals"], g.normals.shape) for b, g in zip(res.geo, scene.geometries)]
+        self.texels = []
+        for buf, t in zip(res.tex, scene.textures):
+            if t.format != L.TEXEL_F32:
+                self.texels.append(None)  # only fp32 maps are differentiable parameters
+            else:
+                self.texels.append(buf.handle[:t.texels.nbytes].view(torch.float32).view(t.texels.shape))
+        for p in self.parameters():
+            p.requires_grad_(True)
+        self._inst_geo = np.array([i.geometry for i in scene.instances], np.int64)
+
+    def _view(self, buf, shape):
+        n = int(np.prod(shape))
+        return buf.handle[:4 * n].view(self.torch.float32).view(*shape)
+
+    def _accepted_vertex_count(self) -> int:
+        out = self.pipe.outputs()
+        return len(out["genVertices"])
+
+    def parameters(self) -> list:
+        return [p for p in self.positions + self.normals + self.texels if p is not None]
+
+    # ---- forward / backward on the C ABI ------------------------------------------------
+
+    def generate(self):
+        """Vertices of the frozen frame from the current parameters (a copy)."""
+        self.pipe.stage("generate_vertices")
+        return self.pipe.gen_vertices_tensor(self.num_vertices).clone()
+
+    def scatter_gradients(self, grad_vertices):
+        torch = self.torch
+        dev = grad_vertices.device
+        dP = [torch.zeros_like(p) for p in self.positions]
+        dN = [torch.zeros_like(n) for n in self.normals]
+        dT = [torch.zeros_like(t) if t is not None else None for t in self.texels]
+        tg = np.zeros(len(self._inst_geo), L.GradTargets)
+        tg["dPositions"] = [dP[g].data_ptr() for g in self._inst_geo]
+        tg["dNormals"] = [dN[g].data_ptr() for g in self._inst_geo]
+        targets = torch.from_numpy(tg.view(np.uint8).copy()).to(dev)
+        tex_ptrs = torch.tensor([t.data_ptr() if t is not None else 0 for t in dT] or [0], dtype=torch.int64,
+                                device=dev)
+        gv = grad_vertices.contiguous().float()
+        self.pipe.backward(gv.data_ptr(), targets.data_ptr(), tex_ptrs.data_ptr())
+        self.torch.cuda.current_stream(self.pipe.device).synchronize()
+        return dP, dN, dT
+
+
+class _Tessellate:
+    """torch.autograd.Function, built lazily so importing this module needs no torch."""
+    fn = None
+
+    @classmethod
+    def get(cls):
+        if cls.fn is None:
+            import torch
+
+            class TessellateFunction(torch.autograd.Function):
+                @staticmethod
+                def forward(ctx, frozen, *params):
+                    ctx.frozen = frozen
+                    return frozen.generate()
+
+                @staticmethod
+                def backward(ctx, grad):
+                    f = ctx.frozen
+                    dP, dN, dT = f.scatter_gradients(grad)
+                    grads = []
+                    for p, g in zip(f.positions, dP):
+                        grads.append(g)
+                    for n, g in zip(f.normals, dN):
+                        grads.append(g)
+                    for t, g in zip(f.texels, dT):
+                        if t is not None:
+                            grads.append(g)
+                    return (None, *grads)
+
+            cls.fn = TessellateFunction
+        return cls.fn
+
+
+def tessellate(frozen: FrozenFrame):
+    return _Tessellate.get().apply(frozen, *frozen.parameters())

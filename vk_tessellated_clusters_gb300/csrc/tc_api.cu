@@ -795,6 +795,19 @@ tc_status tc_instantiate_backward(tc_context* ctx, const tc_frame_args* a, uint6
   return TC_OK;
 }
 
+tc_status tc_generate_vertices(tc_context* ctx, const tc_frame_args* a, void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  if(!(a->flags & TC_FLAG_WRITE_FULLCLUSTERS))
+    return TC_ERR_INVALID_ARG;
+  StageCtx c = base_ctx(ctx, a);
+  TC_CHECK_CUDA(launch_generate_vertices(c, ctx->numSMs * 8, reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += 1;
+  return TC_OK;
+}
+
 tc_status tc_read_device_errors(tc_context* ctx, uint32_t* outBits, void* stream)
 {
   if(!ctx || !outBits)

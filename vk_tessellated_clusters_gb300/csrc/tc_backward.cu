@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(256) k_instantiate_backward(StageCtx c, const 
         const f3    n    = ldg3(reinterpret_cast<const float*>(in.normals), vi);
         const f2    uv   = ldg2(reinterpret_cast<const float*>(in.texcoords), vi);
         const float nl   = len3(n);
-        const f3    nh   = {__fdiv_rn(n.x, nl), __fdiv_rn(n.y, nl), __fdiv_rn(n.z, nl)};
+        const f3    nh   = normalize3(n);
         const float hraw = sample_bilinear(*tx, uv);
         const float h    = ((hraw * in.displacementScale) * viewScale + in.displacementOffset) + c.view->displacementOffset;
         const float dh   = dot3(nh, g);
@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(256) k_instantiate_backward(StageCtx c, const 
       float*       gtex = tx ? gradTexels[in.displacementIndex] : nullptr;
       const float  s    = in.displacementScale * viewScale;
       u32          vi[3];
-      f3           bb[3], p[3], nr[3], nh[3];
+      f3           bb[3], nr[3], nh[3];
       f2           uvb[3];
       float        nl[3];
 #pragma unroll
@@ -128,13 +128,11 @@ __global__ void __launch_bounds__(256) k_instantiate_backward(StageCtx c, const 
       {
         vi[k]  = cl.firstLocalVertex + lt[tri * 3 + k];
         bb[k]  = decode_bary(pi.subTriangle.vtxEncoded[k]);
-        p[k]   = ldg3(reinterpret_cast<const float*>(in.positions), vi[k]);
         nr[k]  = ldg3(reinterpret_cast<const float*>(in.normals), vi[k]);
         nl[k]  = len3(nr[k]);
-        nh[k]  = {__fdiv_rn(nr[k].x, nl[k]), __fdiv_rn(nr[k].y, nl[k]), __fdiv_rn(nr[k].z, nl[k])};
+        nh[k]  = normalize3(nr[k]);
         uvb[k] = ldg2(reinterpret_cast<const float*>(in.texcoords), vi[k]);
       }
-      (void)p;
       f3 dP[3]  = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
       f3 dNh[3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
       for(u32 v = lane; v < e.numVertices; v += 32)
@@ -161,7 +159,7 @@ __global__ void __launch_bounds__(256) k_instantiate_backward(StageCtx c, const 
         const f3    N    = interp3(nh[0], nh[1], nh[2], w);
         const f2    uv   = interp2(uvb[0], uvb[1], uvb[2], w);
         const float Nl   = len3(N);
-        const f3    m    = {__fdiv_rn(N.x, Nl), __fdiv_rn(N.y, Nl), __fdiv_rn(N.z, Nl)};
+        const f3    m    = normalize3(N);
         const float hraw = sample_bilinear(*tx, uv);
         const float h    = ((hraw * in.displacementScale) * viewScale + in.displacementOffset) + c.view->displacementOffset;
         const float dh   = dot3(m, g);
@@ -203,7 +201,101 @@ __global__ void __launch_bounds__(256) k_instantiate_backward(StageCtx c, const 
   }
 }
 
+// Forward of the same frozen frame: regenerates every accepted instantiation's
+// vertices with the arithmetic of the build kernels (bit-identical output).
+__global__ void __launch_bounds__(256) k_generate_vertices(StageCtx c)
+{
+  const u32         lane  = threadIdx.x & 31;
+  const u32         gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const u32         nwarp = (gridDim.x * blockDim.x) >> 5;
+  tc_SceneBuilding* b     = c.build;
+  const u32         temps = min(b->tempInstantiateCounter, c.caps.maxGeneratedClusters);
+  const tc_TemplateInstantiateInfo* ti    = reinterpret_cast<const tc_TemplateInstantiateInfo*>(b->tempInstantiations);
+  const tc_TessTriangleInfo*        parts = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
+  const tc_ClusterInfo*             fulls = reinterpret_cast<const tc_ClusterInfo*>(b->fullClusters);
+  const bool  haveTextures = c.numTextures > 0 && c.textures != nullptr;
+  const float vscale       = c.view->displacementScale, voffset = c.view->displacementOffset;
+  float*      gv           = reinterpret_cast<float*>(b->genVertices);
+
+  for(u32 j = gwarp; j < temps; j += nwarp)
+  {
+    const tc_TemplateInstantiateInfo info  = ti[j];
+    const u32                        mode  = info.clusterIdOffset >> 30;
+    const u64                        vbase = (info.vertexBufferAddress - b->genVertices) / 12;
+    if(mode == TC_RT_CLUSTER_MODE_FULL_CLUSTER)
+    {
+      if(!fulls)
+        continue;
+      const tc_ClusterInfo     ci = fulls[j];
+      const tc_RenderInstance& in = c.instances[ci.instanceID];
+      const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in.clusters)[ci.clusterID];
+      tc_DisplacementTexture   tx = {};
+      if(haveTextures && in.displacementIndex >= 0 && (u32)in.displacementIndex < c.numTextures)
+        tx = c.textures[in.displacementIndex];
+      const u32 nv = min((u32)cl.numVertices, TC_MAX_CLUSTER_VERTICES);
+      for(u32 v = lane; v < nv; v += 32)
+      {
+        const u32 vi = cl.firstLocalVertex + v;
+        f3        p  = ldg3(reinterpret_cast<const float*>(in.positions), vi);
+        if(tx.width != 0)
+        {
+          const float h = sample_bilinear(tx, ldg2(reinterpret_cast<const float*>(in.texcoords), vi));
+          p = displace(p, ldg3(reinterpret_cast<const float*>(in.normals), vi), h, in.displacementScale, vscale,
+                       in.displacementOffset, voffset);
+        }
+        float* d = gv + (vbase + v) * 3;
+        d[0] = p.x, d[1] = p.y, d[2] = p.z;
+      }
+    }
+    else
+    {
+      const tc_TessTriangleInfo pi  = parts[info.clusterIdOffset & 0x3FFFFFFFu];
+      const u32                 cfg = pi.subTriangle.triangleID_config >> 16;
+      const u32                 tri = pi.subTriangle.triangleID_config & 0xFFFFu;
+      const tc_RenderInstance&  in  = c.instances[pi.cluster.instanceID];
+      const tc_Cluster          cl  = reinterpret_cast<const tc_Cluster*>(in.clusters)[pi.cluster.clusterID];
+      const uint8_t*            lt  = reinterpret_cast<const uint8_t*>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
+      const tc_TessTableEntry   e   = table_entry(c.table, cfg);
+      tc_DisplacementTexture    tx  = {};
+      if(haveTextures && in.displacementIndex >= 0 && (u32)in.displacementIndex < c.numTextures)
+        tx = c.textures[in.displacementIndex];
+      f3 bb[3], p[3], nh[3];
+      f2 uvb[3];
+#pragma unroll
+      for(int k = 0; k < 3; k++)
+      {
+        const u32 vi = cl.firstLocalVertex + lt[tri * 3 + k];
+        bb[k]        = decode_bary(pi.subTriangle.vtxEncoded[k]);
+        p[k]         = ldg3(reinterpret_cast<const float*>(in.positions), vi);
+        nh[k]        = normalize3(ldg3(reinterpret_cast<const float*>(in.normals), vi));
+        uvb[k]       = ldg2(reinterpret_cast<const float*>(in.texcoords), vi);
+      }
+      for(u32 v = lane; v < e.numVertices; v += 32)
+      {
+        f3 w = cfg_vertex(c.table, e, cfg, v);
+        w    = interp3(bb[0], bb[1], bb[2], w);
+        f3 q = interp3(p[0], p[1], p[2], w);
+        if(tx.width != 0)
+        {
+          const f3    n  = interp3(nh[0], nh[1], nh[2], w);
+          const f2    uv = interp2(uvb[0], uvb[1], uvb[2], w);
+          const float h  = sample_bilinear(tx, uv);
+          q              = displace(q, n, h, in.displacementScale, vscale, in.displacementOffset, voffset);
+        }
+        float* d = gv + (vbase + v) * 3;
+        d[0] = q.x, d[1] = q.y, d[2] = q.z;
+      }
+    }
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_generate_vertices(const StageCtx& c, u32 grid, cudaStream_t s)
+{
+  k_generate_vertices<<<grid, 256, 0, s>>>(c);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_instantiate_backward(const StageCtx& c, const float* gradVertices, const tc_GradTargets* targets,
                                         float* const* gradTexels, u32 grid, cudaStream_t s)
