@@ -495,6 +495,8 @@ def backward_forward(torch, dev, local, reps=10):
 
     grad_v = 2 * (frozen.generate() - target)
     fwd_ms = timed(lambda: pipe.stage("generate_vertices"))
+    _, table = frozen.gradient_buffers(dev)
+    bwd_kernel_ms = timed(lambda: frozen.launch_backward(grad_v, table))
     bwd_ms = timed(lambda: frozen.scatter_gradients(grad_v))
     frame_ms = timed(lambda: pipe.build("graph"))
     # one autograd step end to end for the record
@@ -502,8 +504,10 @@ def backward_forward(torch, dev, local, reps=10):
     loss = ((v - target) ** 2).sum()
     loss.backward()
     res = {"workload": "icosphere 20,480 tris, 1024^2 fp32 value-noise map, decisions frozen, L = sum |v - t|^2",
-           "vertices": frozen.num_vertices, "forward_ms": fwd_ms, "backward_ms": bwd_ms, "frame_build_ms": frame_ms,
-           "backward_over_forward": bwd_ms / fwd_ms, "backward_over_frame_build": bwd_ms / frame_ms,
+           "vertices": frozen.num_vertices, "forward_ms": fwd_ms, "backward_kernel_ms": bwd_kernel_ms,
+           "backward_ms": bwd_ms, "frame_build_ms": frame_ms,
+           "backward_kernel_over_forward": bwd_kernel_ms / fwd_ms, "backward_over_forward": bwd_ms / fwd_ms,
+           "backward_over_frame_build": bwd_ms / frame_ms,
            "loss": float(loss.item()), "device_errors": pipe.device_errors(),
            "gradient_check": "tests/test_gpu_backward.py: rel. error vs FP64 adjoint <= 1e-4, 64-parameter central differences"}
     pipe.close()

@@ -49,6 +49,29 @@ class FrozenFrame:
         for p in self.parameters():
             p.requires_grad_(True)
         self._inst_geo = np.array([i.geometry for i in scene.instances], np.int64)
+        self._layout_gradients(scene)
+
+    def _layout_gradients(self, scene) -> None:
+        """All gradients of one backward live in one flat float32 buffer; the
+        kernel's pointer tables (per instance dPositions/dNormals, per map
+        texels) are stored once as byte offsets into it and rebased on the
+        device each call, so a backward needs no host-to-device copy."""
+        torch = self.torch
+        sizes = [p.numel() for p in self.positions] + [n.numel() for n in self.normals]
+        sizes += [t.numel() if t is not None else 0 for t in self.texels]
+        starts = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        self._grad_floats = int(starts[-1])
+        self._grad_starts = starts
+        ng = len(self.positions)
+        rel = np.zeros((len(self._inst_geo), 2), np.int64)
+        rel[:, 0] = 4 * starts[self._inst_geo]
+        rel[:, 1] = 4 * starts[ng + self._inst_geo]
+        tex = np.array([4 * starts[2 * ng + i] if t is not None else -1 for i, t in enumerate(self.texels)] or [-1],
+                       np.int64)
+        self._num_targets = rel.size
+        table = np.concatenate([rel.reshape(-1), tex])
+        self._rel_table = torch.from_numpy(table).to(self.pipe.device)
+        self._table_valid = self._rel_table >= 0
 
     def _view(self, buf, shape):
         n = int(np.prod(shape))
@@ -68,21 +91,29 @@ class FrozenFrame:
         self.pipe.stage("generate_vertices")
         return self.pipe.gen_vertices_tensor(self.num_vertices).clone()
 
-    def scatter_gradients(self, grad_vertices):
+    def gradient_buffers(self, device):
+        """A zeroed flat float32 gradient buffer and the kernel's pointer table
+        rebased onto it (both on `device`, enqueued on the current stream)."""
         torch = self.torch
-        dev = grad_vertices.device
-        dP = [torch.zeros_like(p) for p in self.positions]
-        dN = [torch.zeros_like(n) for n in self.normals]
-        dT = [torch.zeros_like(t) if t is not None else None for t in self.texels]
-        tg = np.zeros(len(self._inst_geo), L.GradTargets)
-        tg["dPositions"] = [dP[g].data_ptr() for g in self._inst_geo]
-        tg["dNormals"] = [dN[g].data_ptr() for g in self._inst_geo]
-        targets = torch.from_numpy(tg.view(np.uint8).copy()).to(dev)
-        tex_ptrs = torch.tensor([t.data_ptr() if t is not None else 0 for t in dT] or [0], dtype=torch.int64,
-                                device=dev)
-        gv = grad_vertices.contiguous().float()
-        self.pipe.backward(gv.data_ptr(), targets.data_ptr(), tex_ptrs.data_ptr())
-        self.torch.cuda.current_stream(self.pipe.device).synchronize()
+        flat = torch.zeros(self._grad_floats, dtype=torch.float32, device=device)
+        table = torch.where(self._table_valid, self._rel_table + flat.data_ptr(), torch.zeros_like(self._rel_table))
+        return flat, table
+
+    def launch_backward(self, grad_vertices, table) -> None:
+        """tc_instantiate_backward: accumulates dL/dv into the buffer `table` points at."""
+        self.pipe.backward(grad_vertices.data_ptr(), table.data_ptr(), table.data_ptr() + 8 * self._num_targets)
+
+    def scatter_gradients(self, grad_vertices):
+        """dL/dv -> (dPositions, dNormals, dTexels), lists parallel to the
+        parameters; all enqueued on the current stream, no synchronisation."""
+        flat, table = self.gradient_buffers(grad_vertices.device)
+        self.launch_backward(grad_vertices.contiguous().float(), table)
+        st = self._grad_starts
+        ng = len(self.positions)
+        views = [flat[st[i]:st[i + 1]] for i in range(len(st) - 1)]
+        dP = [views[i].view(p.shape) for i, p in enumerate(self.positions)]
+        dN = [views[ng + i].view(n.shape) for i, n in enumerate(self.normals)]
+        dT = [views[2 * ng + i].view(t.shape) if t is not None else None for i, t in enumerate(self.texels)]
         return dP, dN, dT
 
 
