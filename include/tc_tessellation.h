@@ -544,6 +544,30 @@ tc_status tc_blas_setup_insertion(tc_context* ctx, const tc_frame_args* args, vo
 /* shaders/blas_clusters_insert.comp.glsl:97-136 (template instantiations) */
 tc_status tc_blas_clusters_insert(tc_context* ctx, const tc_frame_args* args, void* stream);
 
+/* Largest instance count tc_blas_setup_insertion_noalloc accepts. */
+#define TC_NOALLOC_MAX_INSTANCES (1u << 20)
+
+/* No counterpart in the reference (whose Vulkan renderer allocates all its
+ * buffers up front): tc_blas_setup_insertion for callers that cannot allocate
+ * device memory, such as an application that owns every device byte through
+ * its own pool or imported allocations, or a real-time frame loop that cannot
+ * take cudaMalloc's implicit synchronisation; creating a tc_context allocates,
+ * so this entry point takes none. It reads args->build and args->readback only
+ * (the other pointers may be 0), with the same results as
+ * tc_blas_setup_insertion. It calls no cudaMalloc, cudaFree or allocating
+ * library routine: its look-back scratch is a fixed 33,024-byte __device__
+ * array of the library, held on every GPU that loads the library until the
+ * process exits.
+ *   - args->numInstances (which must equal SceneBuilding.numRenderInstances)
+ *     above TC_NOALLOC_MAX_INSTANCES: TC_ERR_CAPACITY, nothing launched.
+ *   - The first call on a device (the current device) resolves the array's
+ *     address with cudaGetSymbolAddress; make it before any stream capture.
+ *   - Every call shares the array and clears it (cudaMemsetAsync on `stream`)
+ *     before its launch; calls that overlap on the GPU race on it.
+ *   - deviceErrors: optional device word that receives TC_DEVERR_* bits
+ *     (atomic OR; 0 = not reported). */
+tc_status tc_blas_setup_insertion_noalloc(const tc_frame_args* args, uint32_t* deviceErrors, void* stream);
+
 /* Number of split passes the host issues for a split factor
  * (src/renderer_raytrace_clusters_tess.cpp:516-543). */
 uint32_t tc_split_pass_count(uint32_t splitFactor);

@@ -49,6 +49,7 @@ def _bind(lib):
         "tc_triangle_instantiate_run": (st, [vp, ctypes.POINTER(L.FrameArgs), u32, u32, u32, vp]),
         "tc_blas_setup_insertion": (st, [vp, ctypes.POINTER(L.FrameArgs), vp]),
         "tc_blas_clusters_insert": (st, [vp, ctypes.POINTER(L.FrameArgs), vp]),
+        "tc_blas_setup_insertion_noalloc": (st, [ctypes.POINTER(L.FrameArgs), vp, vp]),
         "tc_split_pass_count": (u32, [u32]),
         "tc_instantiate_backward": (st, [vp, ctypes.POINTER(L.FrameArgs), u64, u64, u64, vp]),
         "tc_generate_vertices": (st, [vp, ctypes.POINTER(L.FrameArgs), vp]),
@@ -69,7 +70,8 @@ def exported_symbols() -> list[str]:
         "tc_table_set_templates", "tc_set_schedule", "tc_get_schedule", "tc_frame_build", "tc_frame_build_graph",
         "tc_frame_build_plain", "tc_frame_begin", "tc_instances_classify", "tc_clusters_cull", "tc_build_setup",
         "tc_cluster_classify", "tc_triangle_split", "tc_triangle_instantiate", "tc_triangle_instantiate_run",
-        "tc_blas_setup_insertion", "tc_blas_clusters_insert", "tc_split_pass_count", "tc_instantiate_backward",
+        "tc_blas_setup_insertion", "tc_blas_clusters_insert", "tc_blas_setup_insertion_noalloc",
+        "tc_split_pass_count", "tc_instantiate_backward",
         "tc_generate_vertices",
         "tc_read_device_errors", "tc_launch_count",
     ]
