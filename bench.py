@@ -51,6 +51,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-extras", action="store_true", help="skip the plain-path and terrain measurements")
+    p.add_argument("--no-tune", action="store_true", help="keep the default launch schedule (no autotuning)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--profile-case", choices=["batched", "terrain"], default=None,
                    help="run only `warmup` + `steps` graph frames of one case (for ncu captures) and exit")
@@ -184,6 +185,20 @@ def run_reference(args):
 # GPU leg
 # ---------------------------------------------------------------------------
 
+def recorded_traffic(key: str):
+    """DRAM bytes (read + write) per launch of a stage, from the ncu capture
+    summarised in profiles/traffic.txt (lines `<case>/<stage> <bytes>`), or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) == 2 and parts[0] == key:
+                return int(parts[1])
+    return None
+
+
 def stage_sequence(pipe, n_inst):
     from vk_tessellated_clusters_gb300 import layouts as L
     seq = [("frame_begin", ()), ("instances_classify", ()), ("clusters_cull", (0, n_inst)),
@@ -242,10 +257,6 @@ def run_ours(args):
     caps = L.default_caps()
     flags = L.FLAG_CULLING
     pipe = TessellationPipeline(scene, caps, flags, device=local)
-    sched_path = os.path.join(ROOT, "profiles", "schedule_batched.json")
-    if os.path.exists(sched_path):
-        with open(sched_path) as f:
-            pipe.set_schedule(json.load(f)["schedule"])
 
     # all orbit frames' constants resident on the device; a step copies its pair in
     fcs = [S.frame_constants(S.camera_orbit(f)) for f in range(NUM_ORBIT_FRAMES)]
@@ -270,6 +281,12 @@ def run_ours(args):
     def read_tris():
         rb_host.copy_(pipe.state.readback.handle[:L.Readback.itemsize])
         return int(rb_host.numpy().view(L.Readback)[0]["numTotalTriangles"])
+
+    # ---- launch schedule: autotuned on six orbit frames (outside the timing) ---
+    tune_report = None
+    if not args.no_tune:
+        from vk_tessellated_clusters_gb300.autotune import autotune
+        _, tune_report = autotune(pipe, list(range(0, NUM_ORBIT_FRAMES, NUM_ORBIT_FRAMES // 6)), set_frame, flush)
 
     # ---- warm-up --------------------------------------------------------------
     for s in range(args.warmup):
@@ -348,10 +365,7 @@ def run_ours(args):
         roof = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg,
                 "launch_ms": means[dominant], "traffic": None}
-        tpath = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(tpath):
-            with open(tpath) as f:
-                roof["traffic"] = json.load(f).get(f"batched/{dominant}")
+        roof["traffic"] = recorded_traffic(f"batched/{dominant}")
     inst_alg = statistics.mean(M.instantiate_bytes(o, pipe.entries, scene) for o in outs)
     stage_gbs = {"cluster_classify": statistics.mean(M.classify_bytes(o, scene) for o in outs)
                  / (means["cluster_classify"] / 1e3) / 1e9,
@@ -364,7 +378,7 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "instances": 256, "base_triangles": scene.total_triangles,
                    "clusters": scene.total_clusters, "tessellated_tris_per_frame": statistics.mean(tris),
                    "l2": "flushed between timed frames (256 MiB write)", "mode": "CUDA graph, batched persistent stages",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "schedule": pipe.schedule(), "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": "tris/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": L.Readback.itemsize, "ms_per_step": statistics.mean(e2e_times)},
         "gpu_launches": gpu_launches,
@@ -373,6 +387,7 @@ def run_ours(args):
         "stages_ms": means,
         "stage_gbs": stage_gbs,
         "device_errors": errs,
+        "autotune": tune_report,
     }
 
     if not args.no_extras:
@@ -380,9 +395,11 @@ def run_ours(args):
         pipe.close()
         del pipe
         torch.cuda.empty_cache()
-        result["terrain"] = terrain_bandwidth(torch, dev, local, peak)
+        result["terrain"] = terrain_bandwidth(torch, dev, local, peak, tune=not args.no_tune)
         torch.cuda.empty_cache()
         result["backward_forward"] = backward_forward(torch, dev, local)
+        torch.cuda.empty_cache()
+        result["animation"] = animation_fwd_bwd(torch, dev, local, result["config"]["schedule"])
     if rank == 0:
         result["cpu_baseline"] = cpu_baseline(args)
         print(json.dumps(result))
@@ -414,8 +431,10 @@ def batched_vs_plain(pipe, torch, set_frame, flush, frames=(3, 17, 31)):
     return out
 
 
-def terrain_bandwidth(torch, dev, local, peak):
-    """Large bandwidth case: HBM GB/s of the instantiate kernel on the terrain."""
+def terrain_bandwidth(torch, dev, local, peak, tune=True):
+    """Large bandwidth case: HBM GB/s of the instantiate stage on the terrain,
+    with its own autotuned launch schedule (its split passes and vertex counts
+    differ from the batched scene's)."""
     from vk_tessellated_clusters_gb300 import layouts as L
     from vk_tessellated_clusters_gb300 import metrics as M
     from vk_tessellated_clusters_gb300 import scene as S
@@ -427,6 +446,10 @@ def terrain_bandwidth(torch, dev, local, peak):
     flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     pipe.build("graph")
     torch.cuda.synchronize()
+    tune_report = None
+    if tune:
+        from vk_tessellated_clusters_gb300.autotune import autotune
+        _, tune_report = autotune(pipe, [0, 0, 0], lambda f: None, lambda: flush_buf.fill_(1))
     stage_ms, outs = profile_stages(pipe, torch, [0, 0, 0], lambda f: None, lambda: flush_buf.fill_(1))
     means = {k: statistics.mean(v) for k, v in stage_ms.items()}
     o = outs[-1]
@@ -440,14 +463,18 @@ def terrain_bandwidth(torch, dev, local, peak):
            "generated_vertices": int(o["readback"]["numGenVertices"]),
            "stages_ms": means, "instantiate_algorithmic_bytes": alg, "instantiate_gbs": gbs,
            "instantiate_frac_of_peak": gbs / peak,
+           "schedule": pipe.schedule(), "autotune": tune_report,
            "frame_ms_graph": None}
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    flush_buf.fill_(1)
-    e0.record()
-    pipe.build("graph")
-    e1.record()
-    torch.cuda.synchronize()
-    res["frame_ms_graph"] = e0.elapsed_time(e1)
+    frame_ms = []
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush_buf.fill_(1)
+        e0.record()
+        pipe.build("graph")
+        e1.record()
+        torch.cuda.synchronize()
+        frame_ms.append(e0.elapsed_time(e1))
+    res["frame_ms_graph"] = statistics.median(frame_ms)
     res["tris_per_s"] = res["tessellated_tris"] / (res["frame_ms_graph"] / 1e3)
     res["device_errors"] = pipe.device_errors()
     pipe.close()
@@ -512,6 +539,107 @@ def backward_forward(torch, dev, local, reps=10):
            "gradient_check": "tests/test_gpu_backward.py: rel. error vs FP64 adjoint <= 1e-4, 64-parameter central differences"}
     pipe.close()
     return res
+
+
+def animation_fwd_bwd(torch, dev, local, schedule, frames=300, plain_frames=6):
+    """Batched differentiable animation: 1,024 instances of the four batched
+    meshes with seeded rigid motion (omega U[0,1] rad/s, speed U[0,2] units/s)
+    at 60 frames/s over `frames` frames, orbit camera, frustum culling. A
+    frame = this frame's instance records and camera copied in (device to
+    device), then one CUDA graph replay of the whole forward frame plus the
+    zeroing of the four 512^2 fp32 map gradients and the backward with
+    dL/dv = v (L = 0.5 * sum |v|^2). Latency per frame with CUDA events, L2
+    flushed between frames; the same frames through per-instance launches for
+    `plain_frames` frames."""
+    import numpy as np
+    from vk_tessellated_clusters_gb300 import layouts as L
+    from vk_tessellated_clusters_gb300 import scene as S
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    scene = S.scene_batched(1024)
+    caps = L.default_caps()
+    pipe = TessellationPipeline(scene, caps, L.FLAG_CULLING | L.FLAG_WRITE_FULLCLUSTERS, device=local)
+    if schedule:
+        pipe.set_schedule(schedule)
+    motion = S.animation_motion(len(scene.instances))
+    base_recs = pipe.state.res.instance_records
+    recs = np.repeat(base_recs[None], frames, axis=0)
+    for f in range(frames):
+        W = S.animated_worlds(scene, motion, f / 60.0)
+        recs[f]["worldMatrix"] = np.transpose(W, (0, 2, 1)).reshape(len(W), 16).astype(np.float32)
+    rec_bytes = base_recs.nbytes
+    recs_dev = torch.from_numpy(recs.view(np.uint8).reshape(frames, rec_bytes)).to(dev)
+    fcs = np.stack([np.frombuffer(S.frame_constants(S.camera_orbit(f % NUM_ORBIT_FRAMES)).tobytes(), np.uint8)
+                    for f in range(NUM_ORBIT_FRAMES)])
+    fc_dev = torch.from_numpy(fcs).to(dev)
+    FC = L.FrameConstants.itemsize
+    inst_t, view_t, last_t = pipe.state.res.instances.handle, pipe.state.view.handle, pipe.state.view_last.handle
+
+    def set_frame(f):
+        inst_t[:rec_bytes].copy_(recs_dev[f])
+        view_t[:FC].copy_(fc_dev[f % NUM_ORBIT_FRAMES])
+        last_t[:FC].copy_(fc_dev[(f - 1) % NUM_ORBIT_FRAMES])
+
+    map_floats = [t.texels.size for t in scene.textures]
+    grads = torch.zeros(sum(map_floats), dtype=torch.float32, device=dev)
+    starts = np.concatenate([[0], np.cumsum(map_floats)[:-1]])
+    tex_ptrs = torch.tensor([grads.data_ptr() + 4 * int(o) for o in starts], dtype=torch.int64, device=dev)
+    targets = torch.zeros(2 * len(scene.instances), dtype=torch.int64, device=dev)  # no position/normal grads
+    gv = pipe.state.gen_vertices.addr
+
+    def fwd_bwd(mode):
+        pipe.build(mode)
+        grads.zero_()
+        pipe.backward(gv, targets.data_ptr(), tex_ptrs.data_ptr())
+
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    rb = pipe.state.readback
+
+    # capture forward + gradient zeroing + backward as one graph
+    set_frame(0)
+    fwd_bwd("batched")
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        fwd_bwd("batched")
+    torch.cuda.synchronize()
+
+    def timed_frames(run, frame_ids):
+        lat, tris = [], []
+        for f in frame_ids:
+            flush_buf.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            set_frame(f)
+            run()
+            e1.record()
+            torch.cuda.synchronize()
+            lat.append(e0.elapsed_time(e1))
+            tris.append(int(rb.read(L.Readback, 1)[0]["numTotalTriangles"]))
+        return lat, tris
+
+    for f in range(3):  # warm-up
+        set_frame(f)
+        g.replay()
+    torch.cuda.synchronize()
+    lat, tris = timed_frames(g.replay, range(frames))
+    errs = pipe.device_errors()
+    plain_ids = list(range(0, frames, frames // plain_frames))[:plain_frames]
+    plat, ptris = timed_frames(lambda: fwd_bwd("plain"), plain_ids)
+    same = [tris[f] for f in plain_ids] == ptris
+    grad_norm = float(grads.norm().item())
+    pipe.close()
+    q = lambda v, p: float(np.percentile(np.asarray(v), p))
+    return {"workload": "1,024 instances of the 4 batched meshes (13.2M base tris), seeded rigid motion "
+                        "(omega U[0,1] rad/s, speed U[0,2] units/s, 60 frames/s), orbit camera 1920x1080, "
+                        "culling on; forward frame + backward into 4 x 512^2 fp32 maps, L = 0.5 sum |v|^2",
+            "frames": frames, "graph_p50_ms": q(lat, 50), "graph_p99_ms": q(lat, 99),
+            "graph_tris_per_s": sum(tris) / (sum(lat) / 1e3),
+            "tessellated_tris_per_frame": {"min": min(tris), "max": max(tris)},
+            "plain_frames": len(plat), "plain_p50_ms": q(plat, 50), "plain_p99_ms": q(plat, 99),
+            "plain_tris_per_s": sum(ptris) / (sum(plat) / 1e3),
+            "plain_over_graph_p50": q(plat, 50) / q([lat[f] for f in plain_ids], 50),
+            "plain_same_triangle_counts": same, "texel_grad_norm": grad_norm, "device_errors": errs,
+            "l2": "flushed between frames (256 MiB write)"}
 
 
 def cpu_baseline(args):

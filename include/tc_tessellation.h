@@ -436,10 +436,12 @@ typedef enum tc_status {
 /* Launch schedule: grid shapes per stage, picked by the autotuner
  * (vk_tessellated_clusters_gb300/autotune.py) or left at the defaults. */
 typedef struct tc_schedule {
-  uint32_t classifyBlocksPerSM; /* grid of the per-cluster classify kernels = SMs x this (256 threads) */
+  uint32_t classifyBlocksPerSM; /* grid of the per-cluster classify kernels = SMs x this (256 threads); 4 or less:
+                                 * 64 registers per thread, 5-7: 40, 8 and more: 32 */
   uint32_t splitBlockSize;      /* split tile: 128 (16 items), 256 or 512 (32 items) threads */
-  uint32_t vertexBlocksPerSM;   /* grid of the vertex-generation kernel = SMs x this (256 threads) */
-  uint32_t scanBlocksPerSM;     /* grid of the scan / allocation kernels = SMs x this */
+  uint32_t vertexBlocksPerSM;   /* grid of the vertex-generation kernel = SMs x this (256 threads); 4 or less: 64
+                                 * registers per thread, 5: 48, 6 and more: 40 (resident blocks per SM) */
+  uint32_t scanBlocksPerSM;     /* grid of the classify scan and instantiate allocation kernels = SMs x this */
   uint32_t blocksPerSM;         /* persistent grid of the split kernel = SMs x this x (512 / splitBlockSize) */
   uint32_t _pad[3];
 } tc_schedule;
@@ -485,7 +487,10 @@ tc_status tc_table_init(tc_context* ctx, const uint32_t* vertices, uint32_t numV
 tc_status tc_table_set_templates(tc_context* ctx, const uint64_t* templateAddresses, const uint32_t* instantiationSizes,
                                  void* stream);
 
-/* Launch schedule used by the calls below. */
+/* Launch schedule used by the calls below. Per-SM multipliers must lie in
+ * [1, 64] and splitBlockSize in {128, 256, 512} (else TC_ERR_INVALID_ARG).
+ * The schedule changes launch shapes only: outputs are identical for every
+ * valid schedule. */
 tc_status tc_set_schedule(tc_context* ctx, const tc_schedule* schedule);
 tc_status tc_get_schedule(const tc_context* ctx, tc_schedule* schedule);
 

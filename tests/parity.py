@@ -1,9 +1,12 @@
 """Comparison of two frames' outputs (GPU vs oracle, or GPU vs GPU).
 
-Integer/index outputs must be bit-exact. Generated vertex positions are
-compared bit-exactly too (both sides evaluate the same IEEE operations in the
-same order); the spec bar (|dp| <= 1e-5 * bbox diagonal) is asserted
-separately so a violation of either is reported distinctly.
+Integer/index outputs (counters, cluster lists, part and split records with
+their encoded barycentrics and configs, instantiation arguments, BLAS lists)
+must be bit-exact. Generated vertex positions: GPU vs GPU bit-exact (same
+kernels); GPU vs oracle within |dp| <= 1e-5 x the smallest mesh bounding-box
+diagonal (`vertex_tolerance`), because the GPU evaluates the part-triangle
+vertices in per-part affine form with fused multiply-adds while the oracle
+restates the reference's two-level interpolation without contraction.
 """
 from __future__ import annotations
 
@@ -29,7 +32,7 @@ def _first_diff(a: np.ndarray, b: np.ndarray):
     return (int(rows[0]), a[rows[0]], b[rows[0]], len(rows)) if rows.size else None
 
 
-def diff_outputs(got: dict, want: dict, fields=ARRAY_FIELDS) -> list[str]:
+def diff_outputs(got: dict, want: dict, fields=ARRAY_FIELDS, vertex_tol: float | None = None) -> list[str]:
     errs = []
     gb, wb = got["build"], want["build"]
     for f in COUNTER_FIELDS:
@@ -52,6 +55,13 @@ def diff_outputs(got: dict, want: dict, fields=ARRAY_FIELDS) -> list[str]:
     gv, wv = got["genVertices"], want["genVertices"]
     if gv.shape != wv.shape:
         errs.append(f"genVertices: shape {gv.shape} vs {wv.shape}")
+    elif vertex_tol is not None:
+        d = np.abs(gv.astype(np.float64) - wv.astype(np.float64)).max(axis=1) if len(gv) else np.zeros(0)
+        if not np.isfinite(gv).all():
+            errs.append("genVertices: non-finite values")
+        elif d.size and d.max() > vertex_tol:
+            bad = int(np.argmax(d))
+            errs.append(f"genVertices: max |d| {d.max():.3e} > {vertex_tol:.3e} at {bad}: got {gv[bad]} want {wv[bad]}")
     elif gv.tobytes() != wv.tobytes():
         bad = np.flatnonzero((gv != wv).any(axis=1))
         errs.append(f"genVertices: {bad.size} vertices differ bitwise, first {bad[0]}: got {gv[bad[0]]} want {wv[bad[0]]}, "
@@ -59,8 +69,8 @@ def diff_outputs(got: dict, want: dict, fields=ARRAY_FIELDS) -> list[str]:
     return errs
 
 
-def assert_same(got: dict, want: dict, what: str = "", fields=ARRAY_FIELDS) -> None:
-    errs = diff_outputs(got, want, fields)
+def assert_same(got: dict, want: dict, what: str = "", fields=ARRAY_FIELDS, vertex_tol: float | None = None) -> None:
+    errs = diff_outputs(got, want, fields, vertex_tol)
     assert not errs, (what + "\n" if what else "") + "\n".join(errs[:20])
 
 
@@ -75,3 +85,9 @@ def scene_diagonal(scene) -> float:
         lo = np.minimum(lo, g.lo)
         hi = np.maximum(hi, g.hi)
     return float(np.linalg.norm(hi - lo))
+
+
+def vertex_tolerance(scene) -> float:
+    """1e-5 x the smallest mesh bounding-box diagonal of the scene (positions
+    are in each mesh's object space)."""
+    return 1e-5 * min(float(np.linalg.norm(g.hi - g.lo)) for g in scene.geometries)

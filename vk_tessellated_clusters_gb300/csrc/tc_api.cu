@@ -286,7 +286,7 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   bind_slot(ctx, c, p.slotClassify, false);
   c.fuseSetup = TC_BUILD_SETUP_SPLIT;
   TC_CHECK_CUDA(launch_cluster_classify(c, classify_buffers(ctx), std::min(a->totalClusters, a->caps.maxVisibleClusters),
-                                        ctx->numSMs, s));
+                                        ctx->numSMs, sched.classifyBlocksPerSM, sched.scanBlocksPerSM, s));
 
   const u32 passes = split_passes(a->caps.splitFactor);
   const u32 sb     = split_block(sched);
@@ -301,7 +301,7 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   bind_slot(ctx, c, p.slotInstantiate, false);
   c.fuseSetup = TC_BUILD_SETUP_BUILD_BLAS;
   TC_CHECK_CUDA(launch_triangle_instantiate(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
-                                            std::max(1u, sched.vertexBlocksPerSM), s));
+                                            sched.scanBlocksPerSM, sched.vertexBlocksPerSM, s));
 
   bind_slot(ctx, c, p.slotBlas, false);
   c.fuseSetup = kNoSetup;
@@ -362,7 +362,7 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, desc->device);
   ctx->numSMs   = (u32)std::max(1, sms);
-  ctx->schedule = {8, 256, 5, 8, 1, {0, 0, 0}};
+  ctx->schedule = {8, 256, 4, 8, 1, {0, 0, 0}};
   ctx->plan     = make_plan(*desc);
   if(cudaMalloc(&ctx->dScratch, ctx->plan.totalBytes) != cudaSuccess
      || cudaMemset(ctx->dScratch, 0, ctx->plan.totalBytes) != cudaSuccess)
@@ -508,6 +508,13 @@ tc_status tc_set_schedule(tc_context* ctx, const tc_schedule* schedule)
 {
   if(!ctx || !schedule)
     return TC_ERR_INVALID_ARG;
+  const tc_schedule& q = *schedule;
+  const u32 perSM[] = {q.classifyBlocksPerSM, q.vertexBlocksPerSM, q.scanBlocksPerSM, q.blocksPerSM};
+  for(u32 v : perSM)
+    if(v < 1 || v > 64)
+      return TC_ERR_INVALID_ARG;
+  if(q.splitBlockSize != 128 && q.splitBlockSize != 256 && q.splitBlockSize != 512)
+    return TC_ERR_INVALID_ARG;
   ctx->schedule   = *schedule;
   ctx->graphValid = false;
   return TC_OK;
@@ -648,7 +655,8 @@ tc_status tc_cluster_classify(tc_context* ctx, const tc_frame_args* a, uint32_t 
   c.instEnd   = instanceEnd;
   bind_slot(ctx, c, ctx->plan.slotClassify, true);
   TC_CHECK_CUDA(launch_cluster_classify(c, classify_buffers(ctx), std::min(a->totalClusters, a->caps.maxVisibleClusters),
-                                        ctx->numSMs, reinterpret_cast<cudaStream_t>(stream)));
+                                        ctx->numSMs, ctx->schedule.classifyBlocksPerSM, ctx->schedule.scanBlocksPerSM,
+                                        reinterpret_cast<cudaStream_t>(stream)));
   ctx->launches += 3;
   return TC_OK;
 }
@@ -690,7 +698,7 @@ tc_status tc_triangle_instantiate_run(tc_context* ctx, const tc_frame_args* a, u
   c.run       = run;
   bind_slot(ctx, c, ctx->plan.slotInstantiate, true);
   TC_CHECK_CUDA(launch_triangle_instantiate(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
-                                            std::max(1u, ctx->schedule.vertexBlocksPerSM),
+                                            ctx->schedule.scanBlocksPerSM, ctx->schedule.vertexBlocksPerSM,
                                             reinterpret_cast<cudaStream_t>(stream)));
   ctx->launches += 2;
   return TC_OK;

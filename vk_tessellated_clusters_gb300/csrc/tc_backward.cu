@@ -19,6 +19,7 @@
 // global atomics.
 #include "tc_kernels.h"
 #include "tc_stage.cuh"
+#include "tc_vertex.cuh"
 
 namespace tc {
 
@@ -160,6 +161,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_instantiate_backward(StageCtx c
                                                                       const tc_GradTargets* targets,
                                                                       float* const* gradTexels)
 {
+  stage_prologue();
   __shared__ ChunkSmem sm;
   const u32         lane  = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const u32         gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -300,6 +302,8 @@ __global__ void __launch_bounds__(kWarps * 32) k_instantiate_backward(StageCtx c
 // vertices with the arithmetic of the build kernels (bit-identical output).
 __global__ void __launch_bounds__(256) k_generate_vertices(StageCtx c)
 {
+  stage_prologue();
+  __shared__ PartAffine s_aff[8];
   const u32         lane  = threadIdx.x & 31;
   const u32         gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const u32         nwarp = (gridDim.x * blockDim.x) >> 5;
@@ -344,42 +348,41 @@ __global__ void __launch_bounds__(256) k_generate_vertices(StageCtx c)
     }
     else
     {
+      // the affine vertex form of the build kernel (tc_vertex.cuh): identical bits
       const tc_TessTriangleInfo pi  = parts[info.clusterIdOffset & 0x3FFFFFFFu];
       const u32                 cfg = pi.subTriangle.triangleID_config >> 16;
-      const u32                 tri = pi.subTriangle.triangleID_config & 0xFFFFu;
-      const tc_RenderInstance&  in  = c.instances[pi.cluster.instanceID];
-      const tc_Cluster          cl  = reinterpret_cast<const tc_Cluster*>(in.clusters)[pi.cluster.clusterID];
-      const uint8_t*            lt  = reinterpret_cast<const uint8_t*>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
       const tc_TessTableEntry   e   = table_entry(c.table, cfg);
-      tc_DisplacementTexture    tx  = {};
-      if(haveTextures && in.displacementIndex >= 0 && (u32)in.displacementIndex < c.numTextures)
-        tx = c.textures[in.displacementIndex];
-      f3 bb[3], p[3], nh[3];
-      f2 uvb[3];
-#pragma unroll
-      for(int k = 0; k < 3; k++)
+      PartAffine&               r   = s_aff[threadIdx.x >> 5];
+      if(lane == 0)
       {
-        const u32 vi = cl.firstLocalVertex + lt[tri * 3 + k];
-        bb[k]        = decode_bary(pi.subTriangle.vtxEncoded[k]);
-        p[k]         = ldg3(reinterpret_cast<const float*>(in.positions), vi);
-        nh[k]        = normalize3(ldg3(reinterpret_cast<const float*>(in.normals), vi));
-        uvb[k]       = ldg2(reinterpret_cast<const float*>(in.texcoords), vi);
+        const u32                tri = pi.subTriangle.triangleID_config & 0xFFFFu;
+        const tc_RenderInstance& in  = c.instances[pi.cluster.instanceID];
+        const tc_Cluster         cl  = reinterpret_cast<const tc_Cluster*>(in.clusters)[pi.cluster.clusterID];
+        const uint8_t* lt = reinterpret_cast<const uint8_t*>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
+        tc_DisplacementTexture tx = {};
+        if(haveTextures && in.displacementIndex >= 0 && (u32)in.displacementIndex < c.numTextures)
+          tx = c.textures[in.displacementIndex];
+        f3 bp[3], bn[3];
+        f2 bt[3];
+#pragma unroll
+        for(int k = 0; k < 3; k++)
+        {
+          const u32 vi = cl.firstLocalVertex + lt[tri * 3 + k];
+          bp[k]        = ldg3(reinterpret_cast<const float*>(in.positions), vi);
+          bn[k]        = normalize3(ldg3(reinterpret_cast<const float*>(in.normals), vi));
+          bt[k]        = ldg2(reinterpret_cast<const float*>(in.texcoords), vi);
+        }
+        write_part_affine(r, pi.subTriangle.vtxEncoded, cfg_flipped(cfg), bp, bn, bt, e.firstVertex, tx,
+                          in.displacementScale * vscale, in.displacementOffset + voffset);
       }
+      __syncwarp();
       for(u32 v = lane; v < e.numVertices; v += 32)
       {
-        f3 w = cfg_vertex(c.table, e, cfg, v);
-        w    = interp3(bb[0], bb[1], bb[2], w);
-        f3 q = interp3(p[0], p[1], p[2], w);
-        if(tx.width != 0)
-        {
-          const f3    n  = interp3(nh[0], nh[1], nh[2], w);
-          const f2    uv = interp2(uvb[0], uvb[1], uvb[2], w);
-          const float h  = sample_bilinear(tx, uv);
-          q              = displace(q, n, h, in.displacementScale, vscale, in.displacementOffset, voffset);
-        }
-        float* d = gv + (vbase + v) * 3;
+        const f3 q = affine_vertex(r, __ldg(c.table.vertices + e.firstVertex + v));
+        float*   d = gv + (vbase + v) * 3;
         d[0] = q.x, d[1] = q.y, d[2] = q.z;
       }
+      __syncwarp();  // the record is rewritten by the warp's next part
     }
   }
 }
@@ -388,15 +391,13 @@ __global__ void __launch_bounds__(256) k_generate_vertices(StageCtx c)
 
 cudaError_t launch_generate_vertices(const StageCtx& c, u32 grid, cudaStream_t s)
 {
-  k_generate_vertices<<<grid, 256, 0, s>>>(c);
-  return cudaGetLastError();
+  return launch_pdl(k_generate_vertices, grid, 256, s, c);
 }
 
 cudaError_t launch_instantiate_backward(const StageCtx& c, const float* gradVertices, const tc_GradTargets* targets,
                                         float* const* gradTexels, u32 grid, cudaStream_t s)
 {
-  k_instantiate_backward<<<grid, 256, 0, s>>>(c, gradVertices, targets, gradTexels);
-  return cudaGetLastError();
+  return launch_pdl(k_instantiate_backward, grid, 256, s, c, gradVertices, targets, gradTexels);
 }
 
 }  // namespace tc

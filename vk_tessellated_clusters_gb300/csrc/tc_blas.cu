@@ -24,6 +24,7 @@ namespace {
 
 __global__ void k_blas_setup_insertion(StageCtx c)
 {
+  stage_prologue();
   __shared__ u32 s_tile, s_flag, s_warp[33];
   __shared__ u64 s_excl;
   tc_SceneBuilding* b        = c.build;
@@ -111,6 +112,7 @@ __device__ __forceinline__ u32 run_of(const Runs& r, u32 j)
 // segment tables: segStart/segEnd[run * stride + instance], zeroed beforehand
 __global__ void k_blas_segments(StageCtx c, u32* segStart, u32* segEnd, u32 stride)
 {
+  stage_prologue();
   __shared__ Runs s_runs;
   if(threadIdx.x == 0)
     load_runs(c, s_runs);
@@ -138,6 +140,7 @@ __global__ void k_blas_segments(StageCtx c, u32* segStart, u32* segEnd, u32 stri
 
 __global__ void k_blas_scatter(StageCtx c, const u32* segStart, const u32* segEnd, u32 stride)
 {
+  stage_prologue();
   __shared__ Runs s_runs;
   if(threadIdx.x == 0)
     load_runs(c, s_runs);
@@ -181,19 +184,16 @@ __global__ void k_blas_scatter(StageCtx c, const u32* segStart, const u32* segEn
 
 cudaError_t launch_blas_setup_insertion(const StageCtx& c, u32 grid, u32 block, cudaStream_t s)
 {
-  k_blas_setup_insertion<<<grid, block, 0, s>>>(c);
-  return cudaGetLastError();
+  return launch_pdl(k_blas_setup_insertion, grid, block, s, c);
 }
 
 cudaError_t launch_blas_clusters_insert(const StageCtx& c, u32* segStart, u32* segEnd, u32 stride, u32 grid,
                                         cudaStream_t s)
 {
-  k_blas_segments<<<grid, 256, 0, s>>>(c, segStart, segEnd, stride);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_pdl(k_blas_segments, grid, 256, s, c, segStart, segEnd, stride);
   if(e != cudaSuccess)
     return e;
-  k_blas_scatter<<<grid, 256, 0, s>>>(c, segStart, segEnd, stride);
-  return cudaGetLastError();
+  return launch_pdl(k_blas_scatter, grid, 256, s, c, segStart, segEnd, stride);
 }
 
 }  // namespace tc

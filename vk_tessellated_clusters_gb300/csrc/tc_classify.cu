@@ -118,8 +118,13 @@ __device__ __forceinline__ FactorParams factor_params(const StageCtx& c)
 // count
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(256) k_classify_count(StageCtx c, ClassifyScratch cs)
+// MinBlocks: resident 256-thread blocks per SM the registers are sized for
+// (4: 64 registers, 6: 40, 8: 32); more resident warps hide more of the
+// dependent-load latency per cluster at the cost of some spills.
+template <int MinBlocks>
+__global__ void __launch_bounds__(256, MinBlocks) k_classify_count(StageCtx c, ClassifyScratch cs)
 {
+  stage_prologue();
   __shared__ f3  s_vert[8][TC_MAX_CLUSTER_VERTICES];
   __shared__ u32 s_range[2];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -266,6 +271,7 @@ __device__ inline void block_scan5(u64 (&v)[kNumCounters], u64 (&tot)[kNumCounte
 
 __global__ void __launch_bounds__(kScanBlock) k_classify_scan(StageCtx c, ClassifyScratch cs)
 {
+  stage_prologue();
   __shared__ u64 s_warp[33][kNumCounters];
   __shared__ u64 s_excl[kNumCounters];
   __shared__ u32 s_tile, s_flag, s_range[2];
@@ -397,8 +403,10 @@ __device__ __forceinline__ void emit_triangle(tc_TessTriangleInfo* dst, const tc
   store_tess_info(dst, ci, v0, v1, v2, tri | ((word & 0xFFFFu) << 16));
 }
 
-__global__ void __launch_bounds__(256) k_classify_write(StageCtx c, ClassifyScratch cs)
+template <int MinBlocks>
+__global__ void __launch_bounds__(256, MinBlocks) k_classify_write(StageCtx c, ClassifyScratch cs)
 {
+  stage_prologue();
   __shared__ u32 s_range[2];
   const u32 lane = threadIdx.x & 31;
   if(threadIdx.x == 0)
@@ -419,7 +427,15 @@ __global__ void __launch_bounds__(256) k_classify_write(StageCtx c, ClassifyScra
   const u32             ltm          = (1u << lane) - 1u;
   u32                   statTris = 0, statTemp = 0;
 
-  for(u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nwarps)
+  // each warp takes a contiguous range of visible clusters (instance-sorted),
+  // so its full-cluster BLAS reference counts collapse into one atomic per
+  // instance it touches
+  const u32 gw   = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const u32 per  = (n + nwarps - 1) / nwarps;
+  const u32 vEnd = min(n, (gw + 1) * per);
+  u32       blasInst = 0xFFFFFFFFu, blasCount = 0;
+  tc_BlasBuildInfo* blas = reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos);
+  for(u32 v = gw * per; v < vEnd; v++)
   {
     const uint2          rec = cs.counts[v];
     const ClusterOffsets off = cs.offsets[v];
@@ -450,7 +466,14 @@ __global__ void __launch_bounds__(256) k_classify_write(StageCtx c, ClassifyScra
         reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset]                     = b->genClusterData + off.data;
         if((c.flags & TC_FLAG_WRITE_FULLCLUSTERS) && b->fullClusters)
           reinterpret_cast<tc_ClusterInfo*>(b->fullClusters)[tempOffset] = ci;
-        atomicAdd(&reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos)[ci.instanceID].clusterReferencesCount, 1u);
+        if(ci.instanceID != blasInst)
+        {
+          if(blasCount)
+            atomicAdd(&blas[blasInst].clusterReferencesCount, blasCount);
+          blasInst  = ci.instanceID;
+          blasCount = 0;
+        }
+        blasCount++;
         statTemp += 1;
         statTris += min((u32)cl.numTriangles, TC_MAX_CLUSTER_TRIANGLES);
       }
@@ -522,6 +545,8 @@ __global__ void __launch_bounds__(256) k_classify_write(StageCtx c, ClassifyScra
     }
   }
 
+  if(lane == 0 && blasCount)
+    atomicAdd(&blas[blasInst].clusterReferencesCount, blasCount);
   // statistics: one atomic each per warp
   if(lane == 0)
   {
@@ -535,20 +560,24 @@ __global__ void __launch_bounds__(256) k_classify_write(StageCtx c, ClassifyScra
 }  // namespace
 
 cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
-                                    cudaStream_t s)
+                                    u32 warpBlocksPerSM, u32 scanBlocksPerSM, cudaStream_t s)
 {
   ClassifyScratch cs{buf.counts, buf.offsets, buf.triWords};
-  const u32       warpGrid = std::max(1u, std::min((maxClusters + 7) / 8, numSMs * 8));
-  k_classify_count<<<warpGrid, 256, 0, s>>>(c, cs);
-  cudaError_t e = cudaGetLastError();
+  const u32 warpGrid = std::max(1u, std::min((maxClusters + 7) / 8, numSMs * std::max(1u, warpBlocksPerSM)));
+  // register budget from the requested residency: 4 or less -> 64, 5-7 -> 40, 8 and more -> 32
+  const int   occ = warpBlocksPerSM >= 8 ? 8 : (warpBlocksPerSM >= 5 ? 6 : 4);
+  cudaError_t e   = occ == 8   ? launch_pdl(k_classify_count<8>, warpGrid, 256, s, c, cs)
+                    : occ == 6 ? launch_pdl(k_classify_count<6>, warpGrid, 256, s, c, cs)
+                               : launch_pdl(k_classify_count<4>, warpGrid, 256, s, c, cs);
   if(e != cudaSuccess)
     return e;
-  const u32 scanGrid = std::max(1u, std::min((maxClusters + kScanTile - 1) / kScanTile, numSMs * 4));
-  k_classify_scan<<<scanGrid, kScanBlock, 0, s>>>(c, cs);
-  if((e = cudaGetLastError()) != cudaSuccess)
+  const u32 scanGrid =
+      std::max(1u, std::min((maxClusters + kScanTile - 1) / kScanTile, numSMs * std::max(1u, scanBlocksPerSM)));
+  if((e = launch_pdl(k_classify_scan, scanGrid, kScanBlock, s, c, cs)) != cudaSuccess)
     return e;
-  k_classify_write<<<warpGrid, 256, 0, s>>>(c, cs);
-  return cudaGetLastError();
+  return occ == 8   ? launch_pdl(k_classify_write<8>, warpGrid, 256, s, c, cs)
+         : occ == 6 ? launch_pdl(k_classify_write<6>, warpGrid, 256, s, c, cs)
+                    : launch_pdl(k_classify_write<4>, warpGrid, 256, s, c, cs);
 }
 
 u32 classify_scan_tiles(u32 maxClusters) { return (maxClusters + kScanTile - 1) / kScanTile; }

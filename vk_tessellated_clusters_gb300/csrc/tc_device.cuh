@@ -344,6 +344,25 @@ __device__ __forceinline__ u32 ld_acquire_u32(const u32* p)
 }
 
 // ---------------------------------------------------------------------------
+// Programmatic dependent launch. Every stage kernel is launched with
+// programmatic stream serialisation (launch_pdl in tc_stage.cuh): it may be
+// scheduled while its predecessor in the stream is still running, so its
+// launch latency and block start-up overlap the predecessor's tail. Each
+// kernel opens with stage_prologue(): it lets its own successor launch early
+// (the trigger fires once every block of this grid has started, so a waiting
+// successor never holds resources a not-yet-started block needs), then waits
+// for the full completion and memory visibility of its predecessor before it
+// touches global memory. Completion is transitive: a kernel completes only
+// after passing its own wait.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void stage_prologue()
+{
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// ---------------------------------------------------------------------------
 // Decoupled look-back (single-pass chained scan) over tiles. Gives every tile
 // the exclusive prefix of per-tile aggregates in tile order, so appends are
 // ordered exactly like a serial loop. Each state word holds a 62-bit value and
@@ -368,11 +387,16 @@ __device__ __forceinline__ u64 warp_sum_u64(u64 v)
 
 // Warp-cooperative look-back: all 32 lanes of one warp call it for one counter
 // and all receive the tile's exclusive prefix. Each step reads a window of the
-// 32 nearest predecessors at once (lane i reads tile - 1 - i), waits until all
-// of them have published, and either stops at the nearest inclusive prefix or
-// adds the 32 aggregates and moves the window back. `state` is this counter's
-// tile-state array; `base` (the counter value before this launch) is only used
-// by tile 0.
+// kLbWindow = 128 nearest predecessors at once (lane i reads tiles
+// tile - 1 - i - 32 k, k = 0..3: four independent loads per lane, one round
+// trip), waits until all of them have published, and either stops at the
+// nearest inclusive prefix or adds the aggregates and moves the window back.
+// The prefix frontier therefore advances 128 tiles per memory round trip.
+// `state` is this counter's tile-state array; `base` (the counter value before
+// this launch) is only used by tile 0.
+constexpr int kLbSlots  = 4;
+constexpr int kLbWindow = 32 * kLbSlots;
+
 __device__ __forceinline__ u64 warp_lookback_exclusive(u64* state, u32 tile, u64 aggregate, u64 base, u32* errorWord)
 {
   const u32 lane = threadIdx.x & 31;
@@ -389,34 +413,56 @@ __device__ __forceinline__ u64 warp_lookback_exclusive(u64* state, u32 tile, u64
   u32 spins = 0;
   for(;;)
   {
-    const int t = start - (int)lane;
-    // window slots before tile 0 count as an empty inclusive prefix
-    u64 s = t >= 0 ? ld_relaxed_u64(state + t) : kLbPrefix;
-    while(__any_sync(0xFFFFFFFFu, (s & ~kLbValueMask) == 0))
+    u64 s[kLbSlots];
+#pragma unroll
+    for(int k = 0; k < kLbSlots; k++)
     {
+      const int t = start - (int)lane - 32 * k;
+      // window slots before tile 0 count as an empty inclusive prefix
+      s[k] = t >= 0 ? ld_relaxed_u64(state + t) : kLbPrefix;
+    }
+    for(;;)
+    {
+      bool pending = false;
+#pragma unroll
+      for(int k = 0; k < kLbSlots; k++)
+        pending |= (s[k] & ~kLbValueMask) == 0;
+      if(!__any_sync(0xFFFFFFFFu, pending))
+        break;
       if(++spins > kSpinLimit)
       {
         if(lane == 0)
           atomicOr(errorWord, TC_DEVERR_LOOKBACK_TIMEOUT);
-        s = kLbPrefix;  // give up on this window
+#pragma unroll
+        for(int k = 0; k < kLbSlots; k++)
+          if((s[k] & ~kLbValueMask) == 0)
+            s[k] = kLbPrefix;  // give up on this window
         break;
       }
       __nanosleep(32);
-      if((s & ~kLbValueMask) == 0)
-        s = ld_relaxed_u64(state + t);
+#pragma unroll
+      for(int k = 0; k < kLbSlots; k++)
+        if((s[k] & ~kLbValueMask) == 0)
+          s[k] = ld_relaxed_u64(state + (start - (int)lane - 32 * k));
     }
-    const u32 pmask = __ballot_sync(0xFFFFFFFFu, (s & ~kLbValueMask) == kLbPrefix);
-    u64       v     = s & kLbValueMask;
-    if(pmask)
+    // nearest slot (smallest window index 32 k + lane) holding an inclusive prefix
+    int first = kLbWindow;
+#pragma unroll
+    for(int k = kLbSlots - 1; k >= 0; k--)
     {
-      const u32 first = __ffs(pmask) - 1;  // nearest predecessor holding an inclusive prefix
-      if(lane > first)
-        v = 0;
-      excl += warp_sum_u64(v);
-      break;
+      const u32 pmask = __ballot_sync(0xFFFFFFFFu, (s[k] & ~kLbValueMask) == kLbPrefix);
+      if(pmask)
+        first = 32 * k + __ffs(pmask) - 1;
     }
+    u64 v = 0;
+#pragma unroll
+    for(int k = 0; k < kLbSlots; k++)
+      if(32 * k + (int)lane <= first)
+        v += s[k] & kLbValueMask;
     excl += warp_sum_u64(v);
-    start -= 32;
+    if(first < kLbWindow)
+      break;
+    start -= kLbWindow;
   }
   if(lane == 0)
     st_relaxed_u64(state + tile, kLbPrefix | ((excl + aggregate) & kLbValueMask));

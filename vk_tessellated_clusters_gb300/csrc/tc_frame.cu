@@ -91,6 +91,7 @@ __device__ inline bool intersect_hiz(const Clip&, const Clip&) { return true; }
 
 __global__ void k_frame_begin(StageCtx c)
 {
+  stage_prologue();
   tc_SceneBuilding* b = c.build;
   if(blockIdx.x == 0)
   {
@@ -148,6 +149,7 @@ __global__ void k_frame_begin(StageCtx c)
 
 __global__ void k_instances_classify(StageCtx c)
 {
+  stage_prologue();
   __shared__ u32 s_tile, s_flag, s_warp[33];
   __shared__ u64 s_excl;
   const u32      n        = c.numInstances;
@@ -210,6 +212,7 @@ __global__ void k_instances_classify(StageCtx c)
 
 __global__ void k_clusters_cull(StageCtx c)
 {
+  stage_prologue();
   __shared__ u32 s_tile, s_flag, s_warp[33];
   __shared__ u64 s_excl;
   tc_SceneBuilding* b          = c.build;
@@ -293,6 +296,7 @@ __global__ void k_clusters_cull(StageCtx c)
 
 __global__ void k_build_setup(StageCtx c, u32 mode)
 {
+  stage_prologue();
   if(blockIdx.x == 0 && threadIdx.x == 0)
     build_setup_apply(c, mode);
 }
@@ -303,26 +307,22 @@ __global__ void k_build_setup(StageCtx c, u32 mode)
 
 cudaError_t launch_frame_begin(const StageCtx& c, u32 grid, cudaStream_t s)
 {
-  k_frame_begin<<<grid, 256, 0, s>>>(c);
-  return cudaGetLastError();
+  return launch_pdl(k_frame_begin, grid, 256, s, c);
 }
 
 cudaError_t launch_instances_classify(const StageCtx& c, u32 grid, u32 block, cudaStream_t s)
 {
-  k_instances_classify<<<grid, block, 0, s>>>(c);
-  return cudaGetLastError();
+  return launch_pdl(k_instances_classify, grid, block, s, c);
 }
 
 cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStream_t s)
 {
-  k_clusters_cull<<<grid, block, 0, s>>>(c);
-  return cudaGetLastError();
+  return launch_pdl(k_clusters_cull, grid, block, s, c);
 }
 
 cudaError_t launch_build_setup(const StageCtx& c, u32 mode, cudaStream_t s)
 {
-  k_build_setup<<<1, 32, 0, s>>>(c, mode);
-  return cudaGetLastError();
+  return launch_pdl(k_build_setup, 1, 32, s, c, mode);
 }
 
 }  // namespace tc

@@ -11,14 +11,15 @@
 //              first vertex of each accepted part goes to scratch
 //   vertices : HBM-write bound (12 B per generated vertex dominates). One warp
 //              per 16 consecutive parts, whose vertices form one contiguous
-//              range: per-part base data staged once in shared memory, then the
-//              range is written as aligned 48-byte groups of four vertices
-//              (three 16-byte stores per lane), scalar stores only at the two
-//              unaligned ends. No block barriers, no cross-block waits.
+//              range: each part's affine vertex form (tc_vertex.cuh, 128 B) is
+//              set up once in shared memory, then the lanes walk the range
+//              on consecutive vertices. No block barriers, no cross-block
+//              waits.
 #include <algorithm>
 
 #include "tc_kernels.h"
 #include "tc_stage.cuh"
+#include "tc_vertex.cuh"
 
 namespace tc {
 
@@ -80,9 +81,11 @@ __device__ __forceinline__ T warp_inclusive(T x, u32 lane)
 
 __global__ void __launch_bounds__(kAllocBlock) k_instantiate_alloc(StageCtx c, InstantiateBuffers ib)
 {
+  stage_prologue();
   __shared__ u64 s_warp[33][kNumCounters];
   __shared__ u64 s_excl[kNumCounters];
   __shared__ u32 s_tile, s_flag, s_range[2];
+  __shared__ u32 s_blasKey[kAllocBlock / 32][2], s_blasCnt[kAllocBlock / 32][2], s_stat[kAllocBlock / 32][2];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   if(threadIdx.x == 0)
     part_range(c, s_range[0], s_range[1]);
@@ -223,20 +226,66 @@ __global__ void __launch_bounds__(kAllocBlock) k_instantiate_alloc(StageCtx c, I
       dataOffset += ds[i];
       vertexOffset += nv[i];
     }
-    // per-instance CLAS reference counts: threads of a warp holding the same
-    // instance combine their last runs, one atomic per distinct instance
+    // Per-instance CLAS reference counts. Parts are instance-sorted within a
+    // run, so an instance's parts in this tile are (almost always) contiguous:
+    // threads of a warp holding the same instance combine their last runs;
+    // the warp's first and last instances go to shared memory and are merged
+    // across the block's warps, every other instance is added directly. One
+    // atomic per instance and tile instead of one per warp.
     {
-      const u32 key   = runCount ? runInst : 0xFFFFFFFFu;
-      const u32 peers = __match_any_sync(0xFFFFFFFFu, key);
-      u32       peerSum = 0;
+      const u32  key     = runCount ? runInst : 0xFFFFFFFFu;
+      const u32  peers   = __match_any_sync(0xFFFFFFFFu, key);
+      u32        peerSum = 0;
       for(u32 m = peers; m; m &= m - 1)
         peerSum += __shfl_sync(peers, runCount, __ffs(m) - 1);
-      if(runCount && (__ffs(peers) - 1) == (int)lane)
-        atomicAdd(&blas[runInst].clusterReferencesCount, peerSum);
+      const bool leader  = runCount && (__ffs(peers) - 1) == (int)lane;
+      const u32  holders = __ballot_sync(0xFFFFFFFFu, runCount != 0);
+      const u32  firstKey = holders ? __shfl_sync(0xFFFFFFFFu, key, __ffs(holders) - 1) : 0xFFFFFFFFu;
+      const u32  lastKey  = holders ? __shfl_sync(0xFFFFFFFFu, key, 31 - __clz(holders)) : 0xFFFFFFFFu;
+      if(lane == 0)
+      {
+        s_blasKey[warp][0] = firstKey;
+        s_blasKey[warp][1] = lastKey;
+        s_blasCnt[warp][0] = 0;
+        s_blasCnt[warp][1] = 0;
+      }
+      __syncwarp();
+      if(leader)
+      {
+        if(key == firstKey)
+          s_blasCnt[warp][0] = peerSum;
+        else if(key == lastKey)
+          s_blasCnt[warp][1] = peerSum;
+        else
+          atomicAdd(&blas[runInst].clusterReferencesCount, peerSum);
+      }
+    }
+    __syncthreads();
+    if(threadIdx.x == 0)
+    {
+      u32 curKey = 0xFFFFFFFFu, curCnt = 0;
+      for(u32 w = 0; w < nw; w++)
+        for(u32 e = 0; e < 2; e++)
+        {
+          const u32 k = s_blasKey[w][e], n = s_blasCnt[w][e];
+          if(n == 0)
+            continue;
+          if(k != curKey)
+          {
+            if(curCnt)
+              atomicAdd(&blas[curKey].clusterReferencesCount, curCnt);
+            curKey = k;
+            curCnt = 0;
+          }
+          curCnt += n;
+        }
+      if(curCnt)
+        atomicAdd(&blas[curKey].clusterReferencesCount, curCnt);
     }
     __syncthreads();
   }
 
+  // statistics: one atomic each per block
   for(int o = 16; o > 0; o >>= 1)
   {
     statTris += __shfl_xor_sync(0xFFFFFFFFu, statTris, o);
@@ -244,10 +293,19 @@ __global__ void __launch_bounds__(kAllocBlock) k_instantiate_alloc(StageCtx c, I
   }
   if(lane == 0)
   {
-    if(statTris)
-      atomicAdd(&c.readback->numTotalTriangles, statTris);
-    if(statTemp)
-      atomicAdd(&b->tempInstantiateCounter, statTemp);
+    s_stat[warp][0] = statTris;
+    s_stat[warp][1] = statTemp;
+  }
+  __syncthreads();
+  if(threadIdx.x == 0)
+  {
+    u32 t = 0, q = 0;
+    for(u32 w = 0; w < nw; w++)
+      t += s_stat[w][0], q += s_stat[w][1];
+    if(t)
+      atomicAdd(&c.readback->numTotalTriangles, t);
+    if(q)
+      atomicAdd(&b->tempInstantiateCounter, q);
   }
 
   if(last_block_done(c, &s_flag))
@@ -271,63 +329,13 @@ __global__ void __launch_bounds__(kAllocBlock) k_instantiate_alloc(StageCtx c, I
 // vertices
 // ---------------------------------------------------------------------------
 
-struct PartRecord
+// MinBlocks: resident blocks per SM the register allocation is sized for
+// (4: 64 registers, 5: 48, 6: 40); picked from the schedule's vertexBlocksPerSM.
+template <int MinBlocks>
+__global__ void __launch_bounds__(kVertexWarps * 32, MinBlocks) k_instantiate_vertices(StageCtx c, InstantiateBuffers ib)
 {
-  f3                     p[3];
-  f3                     n[3];
-  f2                     uv[3];
-  f3                     bb[3];
-  u32                    firstVertex;
-  u32                    cfg;
-  float                  scale, offset;
-  tc_DisplacementTexture tx;  // width == 0: no displacement
-};
-
-// triangle_tess_template_instantiate.comp.glsl:343-371 for vertex `vert` of the part in `r`
-__device__ __forceinline__ f3 gen_vertex(const Table& table, const PartRecord& r, u32 vert, float viewScale,
-                                         float viewOffset)
-{
-  f3 w = decode_bary(__ldg(table.vertices + r.firstVertex + vert));
-  if(cfg_flipped(r.cfg))
-  {
-    const float s = w.x;
-    w.x           = w.y;
-    w.y           = s;
-  }
-  w    = interp3(r.bb[0], r.bb[1], r.bb[2], w);
-  f3 p = interp3(r.p[0], r.p[1], r.p[2], w);
-  if(r.tx.width != 0)
-  {
-    const f3    n  = interp3(r.n[0], r.n[1], r.n[2], w);
-    const f2    uv = interp2(r.uv[0], r.uv[1], r.uv[2], w);
-    const float h  = sample_bilinear(r.tx, uv);
-    p              = displace(p, n, h, r.scale, viewScale, r.offset, viewOffset);
-  }
-  return p;
-}
-
-// last part whose first vertex (within the warp's range) is <= j
-__device__ __forceinline__ u32 part_of(const u32* vpre, u32 j)
-{
-  static_assert(kPartsPerWarp == 16, "binary search depth");
-  u32 lo = 0, hi = kPartsPerWarp;
-#pragma unroll
-  for(int s = 0; s < 4; s++)
-  {
-    const u32 mid = (lo + hi) >> 1;
-    if(vpre[mid] <= j)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  return lo;
-}
-
-__global__ void __launch_bounds__(kVertexWarps * 32, 5) k_instantiate_vertices(StageCtx c, InstantiateBuffers ib)
-{
-  __shared__ PartRecord s_part[kVertexWarps][kPartsPerWarp];
-  __shared__ u32        s_vpre[kVertexWarps][kPartsPerWarp + 1];
-  __shared__ __align__(16) float s_stage[kVertexWarps][32][12];  // one 4-vertex group per lane
+  stage_prologue();
+  __shared__ PartAffine s_part[kVertexWarps][kPartsPerWarp];
   __shared__ u32        s_range[2];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if(threadIdx.x == 0)
@@ -339,13 +347,11 @@ __global__ void __launch_bounds__(kVertexWarps * 32, 5) k_instantiate_vertices(S
   const tc_TessTriangleInfo* parts        = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
   const bool                 haveTextures = c.numTextures > 0 && c.textures != nullptr;
   float*                     gv           = reinterpret_cast<float*>(b->genVertices);
-  const bool                 aligned16    = (reinterpret_cast<uintptr_t>(gv) & 15) == 0;
   const float                viewScale    = c.view->displacementScale;
   const float                viewOffset   = c.view->displacementOffset;
-  const u32                  nwarps    = (gridDim.x * blockDim.x) >> 5;
-  const u32                  numChunks = (n + kPartsPerWarp - 1) / kPartsPerWarp;
-  PartRecord*                sp        = s_part[warp];
-  u32*                       vpre      = s_vpre[warp];
+  const u32                  nwarps       = (gridDim.x * blockDim.x) >> 5;
+  const u32                  numChunks    = (n + kPartsPerWarp - 1) / kPartsPerWarp;
+  PartAffine*                sp           = s_part[warp];
 
   for(u32 chunk = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; chunk < numChunks; chunk += nwarps)
   {
@@ -369,83 +375,70 @@ __global__ void __launch_bounds__(kVertexWarps * 32, 5) k_instantiate_vertices(S
       const float*             pos = reinterpret_cast<const float*>(in.positions);
       const float*             nrm = reinterpret_cast<const float*>(in.normals);
       const float*             uvs = reinterpret_cast<const float*>(in.texcoords);
-      const u32                vtx[3] = {r1.x, r1.y, r2.x};
-      PartRecord&              r      = sp[lane];
+      const u32                corner[3] = {r1.x, r1.y, r2.x};
+      f3                       bp[3], bn[3];
+      f2                       bt[3];
 #pragma unroll
       for(int v = 0; v < 3; v++)
       {
         const u32 vi = cl.firstLocalVertex + lt[tri * 3 + v];
-        r.bb[v]      = decode_bary(vtx[v]);
-        r.p[v]       = ldg3(pos, vi);
-        r.n[v]       = normalize3(ldg3(nrm, vi));  // :329
-        r.uv[v]      = ldg2(uvs, vi);
+        bp[v]        = ldg3(pos, vi);
+        bn[v]        = normalize3(ldg3(nrm, vi));  // :329
+        bt[v]        = ldg2(uvs, vi);
       }
-      r.firstVertex = e.firstVertex;
-      r.cfg         = cfg;
-      r.tx          = {};
+      tc_DisplacementTexture tx = {};
       if(haveTextures && in.displacementIndex >= 0)
       {
         if((u32)in.displacementIndex < c.numTextures)
-          r.tx = c.textures[in.displacementIndex];
+          tx = c.textures[in.displacementIndex];
         else
           atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
       }
-      r.scale  = in.displacementScale;
-      r.offset = in.displacementOffset;
+      write_part_affine(sp[lane], corner, cfg_flipped(cfg), bp, bn, bt, e.firstVertex, tx,
+                        in.displacementScale * viewScale, in.displacementOffset + viewOffset);
       nv       = e.numVertices;
     }
-    const u32 inc = warp_inclusive<u32>(nv, lane);
-    if(lane < kPartsPerWarp)
-      vpre[lane + 1] = inc;
-    if(lane == 0)
-      vpre[0] = 0;
+    const u32 inc   = warp_inclusive<u32>(nv, lane);
+    const u32 start = inc - nv;  // first vertex of this lane's part within the chunk
     const u32 total = __shfl_sync(0xFFFFFFFFu, inc, kPartsPerWarp - 1);
     const u64 v0    = __shfl_sync(0xFFFFFFFFu, vo, 0);
     __syncwarp();
+    if(total == 0)
+      continue;
 
-    // Work items over the warp's vertex range [v0, v0 + total): single vertices
-    // up to the first 16-byte aligned vertex (v % 4 == 0), groups of four
-    // vertices (48 B = three aligned 16-byte stores), single vertices at the
-    // end. One copy of the vertex code; a group's vertices pass through the
-    // lane's own staging slots.
-    const u32 head   = aligned16 ? min((4u - (u32)(v0 & 3)) & 3u, total) : total;
-    const u32 groups = aligned16 ? (total - head) / 4 : 0;
-    const u32 items  = head + groups + (total - head - 4 * groups);
-    float*    stage  = s_stage[warp][lane];
-    for(u32 t = lane; t < items; t += 32)
+    // Lanes take consecutive vertices (lanes of one step share one to three
+    // part records: broadcast reads); each vertex is three 4-byte stores. A
+    // lane's part: the parts starting at or before the step's first vertex,
+    // plus those starting inside the step up to the lane (one bit each).
+    const bool owner = lane < kPartsPerWarp && nv > 0;
+    for(u32 base = 0; base < total; base += 32)
     {
-      const bool grp   = t >= head && t < head + groups;
-      const u32  j     = t < head ? t : (grp ? head + 4 * (t - head) : t + 3 * groups);
-      const u32  count = grp ? 4u : 1u;
-      u32        pi    = part_of(vpre, j);
-#pragma unroll 1
-      for(u32 k = 0; k < count; k++)
+      const u32 before = __popc(__ballot_sync(0xFFFFFFFFu, owner && start <= base));
+      const u32 inside = __reduce_or_sync(0xFFFFFFFFu, (owner && start > base && start < base + 32) ? 1u << (start - base) : 0u);
+      const u32 pi     = before - 1 + __popc(inside & ((2u << lane) - 2u));
+      const u32 pstart = __shfl_sync(0xFFFFFFFFu, start, pi & 31);
+      const u32 jj     = base + lane;
+      const PartAffine& r = sp[pi];
+      // the step's records usually share one kind: then a branch-free specialisation
+      const u32 kind  = affine_kind_of(r);
+      const u32 kind0 = __shfl_sync(0xFFFFFFFFu, kind, 0);
+      const u32 kw    = __all_sync(0xFFFFFFFFu, kind == kind0) ? kind0 : ~0u;
+      if(jj < total)
       {
-        while(j + k >= vpre[pi + 1])
-          pi++;
-        const f3 q = gen_vertex(c.table, sp[pi], j + k - vpre[pi], viewScale, viewOffset);
-        if(grp)
+        const u32 tv = __ldg(c.table.vertices + affine_first_vertex(r) + (jj - pstart));
+        f3        q;
+        switch(kw)
         {
-          stage[3 * k + 0] = q.x;
-          stage[3 * k + 1] = q.y;
-          stage[3 * k + 2] = q.z;
+          case affine_kind(TC_TEXEL_F16, true): q = affine_vertex_k<affine_kind(TC_TEXEL_F16, true)>(r, tv); break;
+          case affine_kind(TC_TEXEL_F32, true): q = affine_vertex_k<affine_kind(TC_TEXEL_F32, true)>(r, tv); break;
+          case kAffineFlat: q = affine_vertex_k<kAffineFlat>(r, tv); break;
+          default: q = affine_vertex_k<~0u>(r, tv); break;
         }
-        else
-        {
-          float* d = gv + (v0 + j) * 3;
-          d[0] = q.x, d[1] = q.y, d[2] = q.z;
-        }
-      }
-      if(grp)
-      {
-        const float4* src = reinterpret_cast<const float4*>(stage);
-        float4*       d   = reinterpret_cast<float4*>(gv + (v0 + j) * 3);
-        d[0]              = src[0];
-        d[1]              = src[1];
-        d[2]              = src[2];
+        float* d = gv + 3 * (v0 + jj);
+        d[0] = q.x, d[1] = q.y, d[2] = q.z;
       }
     }
-    __syncwarp();  // the warp's staging is rewritten by its next chunk
+    __syncwarp();  // the warp's part records are rewritten by its next chunk
   }
 }
 
@@ -454,18 +447,20 @@ __global__ void __launch_bounds__(kVertexWarps * 32, 5) k_instantiate_vertices(S
 u32 instantiate_alloc_tiles(u32 maxParts) { return (maxParts + kAllocTile - 1) / kAllocTile; }
 
 cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
-                                        u32 vertexBlocksPerSM, cudaStream_t s)
+                                        u32 allocBlocksPerSM, u32 vertexBlocksPerSM, cudaStream_t s)
 {
-  const u32   allocGrid = std::max(1u, std::min(instantiate_alloc_tiles(maxParts), numSMs * 8));
-  k_instantiate_alloc<<<allocGrid, kAllocBlock, 0, s>>>(c, buf);
-  cudaError_t e = cudaGetLastError();
+  const u32 allocGrid = std::max(1u, std::min(instantiate_alloc_tiles(maxParts), numSMs * std::max(1u, allocBlocksPerSM)));
+  cudaError_t e = launch_pdl(k_instantiate_alloc, allocGrid, kAllocBlock, s, c, buf);
   if(e != cudaSuccess)
     return e;
   const u32 chunks     = (maxParts + kPartsPerWarp - 1) / kPartsPerWarp;
   const u32 vertexGrid = std::max(1u, std::min((chunks + kVertexWarps - 1) / kVertexWarps,
                                                numSMs * std::max(1u, vertexBlocksPerSM)));
-  k_instantiate_vertices<<<vertexGrid, kVertexWarps * 32, 0, s>>>(c, buf);
-  return cudaGetLastError();
+  if(vertexBlocksPerSM >= 6)
+    return launch_pdl(k_instantiate_vertices<6>, vertexGrid, kVertexWarps * 32, s, c, buf);
+  if(vertexBlocksPerSM == 5)
+    return launch_pdl(k_instantiate_vertices<5>, vertexGrid, kVertexWarps * 32, s, c, buf);
+  return launch_pdl(k_instantiate_vertices<4>, vertexGrid, kVertexWarps * 32, s, c, buf);
 }
 
 }  // namespace tc

@@ -37,11 +37,11 @@ cudaError_t launch_instances_classify(const StageCtx& c, u32 grid, u32 block, cu
 cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 cudaError_t launch_build_setup(const StageCtx& c, u32 mode, cudaStream_t s);
 cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
-                                    cudaStream_t s);
+                                    u32 warpBlocksPerSM, u32 scanBlocksPerSM, cudaStream_t s);
 u32         classify_scan_tiles(u32 maxClusters);
 cudaError_t launch_triangle_split(const StageCtx& c, u32 blockSize, u32 grid, cudaStream_t s);
 cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
-                                        u32 vertexBlocksPerSM, cudaStream_t s);
+                                        u32 allocBlocksPerSM, u32 vertexBlocksPerSM, cudaStream_t s);
 u32         instantiate_alloc_tiles(u32 maxParts);
 cudaError_t launch_blas_setup_insertion(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 cudaError_t launch_blas_clusters_insert(const StageCtx& c, u32* segStart, u32* segEnd, u32 stride, u32 grid,

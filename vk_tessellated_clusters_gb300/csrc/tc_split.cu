@@ -92,6 +92,7 @@ __device__ __forceinline__ Child make_child(const Table& table, const SplitItem&
 template <int T, int B>
 __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
 {
+  stage_prologue();
   static_assert(T <= B && T <= 32, "tile items are set up by warp 0");
   constexpr u32 kMaxChildren = T * kMaxChildrenPerItem;
   constexpr u32 kMaxChunks   = (kMaxChildren + B - 1) / B;
@@ -345,16 +346,12 @@ cudaError_t launch_triangle_split(const StageCtx& c, u32 blockSize, u32 grid, cu
   switch(blockSize)
   {
     case 128:
-      k_triangle_split<16, 128><<<grid, 128, 0, s>>>(c);
-      break;
+      return launch_pdl(k_triangle_split<16, 128>, grid, 128, s, c);
     case 512:
-      k_triangle_split<32, 512><<<grid, 512, 0, s>>>(c);
-      break;
+      return launch_pdl(k_triangle_split<32, 512>, grid, 512, s, c);
     default:
-      k_triangle_split<32, 256><<<grid, 256, 0, s>>>(c);
-      break;
+      return launch_pdl(k_triangle_split<32, 256>, grid, 256, s, c);
   }
-  return cudaGetLastError();
 }
 
 }  // namespace tc

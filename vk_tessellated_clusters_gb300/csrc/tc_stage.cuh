@@ -7,6 +7,24 @@
 
 namespace tc {
 
+// Host side of the programmatic dependent launch (see stage_prologue): a
+// kernel launch on `s` that may overlap the tail of the previous kernel.
+template <typename... Params, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(Params...), u32 grid, u32 block, cudaStream_t s, Args... args)
+{
+  cudaLaunchConfig_t  cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.gridDim                                        = dim3(grid);
+  cfg.blockDim                                       = dim3(block);
+  cfg.dynamicSmemBytes                               = 0;
+  cfg.stream                                         = s;
+  cfg.attrs                                          = attr;
+  cfg.numAttrs                                       = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<Params>(args)...);
+}
+
 // Per-launch scratch: look-back tile states, the tile ticket, the "blocks done"
 // counter and the totals the last tile publishes. Zeroed before every launch.
 struct LaunchScratch

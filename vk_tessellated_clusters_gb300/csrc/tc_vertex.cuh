@@ -1,0 +1,197 @@
+// tc_vertex.cuh — displaced vertex of a part triangle in per-part affine form.
+//
+// The reference (triangle_tess_template_instantiate.comp.glsl:343-371) maps
+// each table vertex w of the config through the part's sub-triangle corners
+// bb_k into base-triangle barycentrics, interpolates position, normalised
+// normal and uv with them, samples the displacement map and displaces along
+// the renormalised normal. Both interpolations are linear, so for a table
+// vertex w = (1 - a - b, a, b) every attribute is
+//
+//     A(w) = A_0 + a (A_1 - A_0) + b (A_2 - A_0),   A_k = sum_j C_k[j] attr_j
+//
+// with C_k the sub-triangle corners (a flipped config swaps C_0 and C_1, the
+// same as swapping w.x and w.y). A_k are evaluated once per part; a vertex then
+// costs three fused multiply-adds per component. The result equals the
+// reference's two-level evaluation up to rounding (a few ulps of the
+// coordinates), inside the |dp| <= 1e-5 x bounding-box-diagonal tolerance the
+// positions are held to; integer outputs are unaffected.
+//
+// Bilinear displacement: mip 0, REPEAT, texel centres at (i + 0.5) / size,
+// fp32 weights, texels through read-only loads (one path for fp32, fp16 and
+// unorm16 maps).
+#pragma once
+
+#include "tc_device.cuh"
+
+namespace tc {
+
+// Nine 16-byte words read with vector loads from shared memory; the 144-byte
+// stride puts consecutive records of an array in different bank groups.
+struct __align__(16) PartAffine
+{
+  float4 q[9];
+  // q[0] = P0.xyz, E1.x       P0 = position at corner 0, E1 = P1 - P0, E2 = P2 - P0
+  // q[1] = E1.yz, E2.xy
+  // q[2] = E2.z, N0.xyz       N = interpolated normalised base normals
+  // q[3] = F1.xyz, F2.x       F1 = N1 - N0, F2 = N2 - N0
+  // q[4] = F2.yz, T0.xy       T = uv
+  // q[5] = G1.xy, G2.xy       G1 = T1 - T0, G2 = T2 - T0
+  // q[6] = scale, offset, firstVertex (bits), kind (bits; see affine_kind)
+  // q[7] = texels lo, texels hi, width, height (bits; width 0 = no displacement)
+  // q[8] = width, height (as floats), width - 1, height - 1 (bits; the wrap
+  //        masks of power-of-two sizes)
+};
+
+// Record kinds (q[6].w): what the vertex needs beyond the interpolated position.
+enum : u32
+{
+  kAffineFlat     = 0,  // no displacement map
+  kAffineZeroMap  = 1,  // map of height 0: displaced by the offsets only
+  kAffineTextured = 2,  // 2 + 2 * format + (1 if both sizes are powers of two)
+};
+
+__host__ __device__ constexpr u32 affine_kind(u32 format, bool pow2) { return kAffineTextured + 2 * format + (pow2 ? 1 : 0); }
+
+__device__ __forceinline__ f3 fma3(float s, f3 a, f3 b)
+{
+  return {__fmaf_rn(s, a.x, b.x), __fmaf_rn(s, a.y, b.y), __fmaf_rn(s, a.z, b.z)};
+}
+
+// sum_j c[j] v_j
+__device__ __forceinline__ f3 bary3(f3 c, f3 v0, f3 v1, f3 v2) { return fma3(c.z, v2, fma3(c.y, v1, {c.x * v0.x, c.x * v0.y, c.x * v0.z})); }
+__device__ __forceinline__ f2 bary2(f3 c, f2 v0, f2 v1, f2 v2)
+{
+  return {__fmaf_rn(c.z, v2.x, __fmaf_rn(c.y, v1.x, c.x * v0.x)), __fmaf_rn(c.z, v2.y, __fmaf_rn(c.y, v1.y, c.x * v0.y))};
+}
+
+// Per-part set-up, written straight into `r` (normally shared memory) word by
+// word. `corner` are the sub-triangle's encoded corners
+// (TessTriangleInfo.vtxEncoded), p / nh / uv the base triangle's positions,
+// normalised normals and uvs; `scale` / `offset` the combined displacement
+// scale (instance x view) and offset (instance + view).
+__device__ __forceinline__ void write_part_affine(PartAffine& r, const u32 corner[3], bool flipped, const f3 p[3],
+                                                  const f3 nh[3], const f2 uv[3], u32 firstVertex,
+                                                  const tc_DisplacementTexture& tx, float scale, float offset)
+{
+  f3 c0 = decode_bary(corner[0]), c1 = decode_bary(corner[1]), c2 = decode_bary(corner[2]);
+  if(flipped)
+  {
+    const f3 t = c0;
+    c0         = c1;
+    c1         = t;
+  }
+  const u32 w = tx.width;
+  const u32 h    = tx.height;
+  const bool pow2 = w != 0 && h != 0 && (w & (w - 1)) == 0 && (h & (h - 1)) == 0;
+  // formats other than fp16 / unorm16 read as fp32, as in every other sampling path
+  const u32 fmt  = tx.format == TC_TEXEL_F16 || tx.format == TC_TEXEL_UNORM16 ? tx.format : TC_TEXEL_F32;
+  const u32 kind = w == 0 ? kAffineFlat : (h == 0 ? kAffineZeroMap : affine_kind(fmt, pow2));
+  r.q[6]          = make_float4(scale, offset, __uint_as_float(firstVertex), __uint_as_float(kind));
+  r.q[7]      = w ? make_float4(__uint_as_float((u32)tx.texels), __uint_as_float((u32)(tx.texels >> 32)),
+                                __uint_as_float(w), __uint_as_float(tx.height))
+                  : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  r.q[8]      = make_float4(__uint2float_rn(w), __uint2float_rn(h), __uint_as_float(w - 1), __uint_as_float(h - 1));
+  {
+    const f3 P0 = bary3(c0, p[0], p[1], p[2]);
+    const f3 E1 = sub3(bary3(c1, p[0], p[1], p[2]), P0);
+    r.q[0]      = make_float4(P0.x, P0.y, P0.z, E1.x);
+    const f3 E2 = sub3(bary3(c2, p[0], p[1], p[2]), P0);
+    r.q[1]      = make_float4(E1.y, E1.z, E2.x, E2.y);
+    r.q[2].x    = E2.z;
+  }
+  if(w == 0)
+    return;
+  const f3 N0 = bary3(c0, nh[0], nh[1], nh[2]);
+  r.q[2]      = make_float4(r.q[2].x, N0.x, N0.y, N0.z);
+  const f3 F1 = sub3(bary3(c1, nh[0], nh[1], nh[2]), N0);
+  const f3 F2 = sub3(bary3(c2, nh[0], nh[1], nh[2]), N0);
+  r.q[3]      = make_float4(F1.x, F1.y, F1.z, F2.x);
+  const f2 T0 = bary2(c0, uv[0], uv[1], uv[2]), T1 = bary2(c1, uv[0], uv[1], uv[2]), T2 = bary2(c2, uv[0], uv[1], uv[2]);
+  r.q[4]      = make_float4(F2.y, F2.z, T0.x, T0.y);
+  r.q[5]      = make_float4(T1.x - T0.x, T1.y - T0.y, T2.x - T0.x, T2.y - T0.y);
+}
+
+template <u32 Format>
+__device__ __forceinline__ float texel_at(u64 texels, u64 i)
+{
+  if(Format == TC_TEXEL_F16)
+    return __half2float(__ushort_as_half(__ldg(reinterpret_cast<const unsigned short*>(texels) + i)));
+  if(Format == TC_TEXEL_F32)
+    return __ldg(reinterpret_cast<const float*>(texels) + i);
+  return __uint2float_rn(__ldg(reinterpret_cast<const unsigned short*>(texels) + i)) * (1.0f / 65535.0f);
+}
+
+// bilinear sample at (u, v) of the map described by q7 and q8
+template <u32 Format, bool Pow2>
+__device__ __forceinline__ float affine_sample(float4 q7, float4 q8, float u, float v)
+{
+  const u32   w = __float_as_uint(q7.z), h = __float_as_uint(q7.w);
+  const float x = __fmaf_rn(u, q8.x, -0.5f), y = __fmaf_rn(v, q8.y, -0.5f);
+  const float xf = floorf(x), yf = floorf(y);
+  const float fx = x - xf, fy = y - yf;
+  const int   ix = __float2int_rz(xf), iy = __float2int_rz(yf);
+  int         x0, x1, y0, y1;
+  if(Pow2)
+  {
+    const int mx = (int)__float_as_uint(q8.z), my = (int)__float_as_uint(q8.w);
+    x0 = ix & mx, x1 = (ix + 1) & mx, y0 = iy & my, y1 = (iy + 1) & my;
+  }
+  else
+  {
+    x0 = wrapi(ix, (int)w), x1 = wrapi(ix + 1, (int)w), y0 = wrapi(iy, (int)h), y1 = wrapi(iy + 1, (int)h);
+  }
+  const u64   texels = (u64)__float_as_uint(q7.x) | ((u64)__float_as_uint(q7.y) << 32);
+  const u32   r0 = (u32)y0 * w, r1 = (u32)y1 * w;  // maps hold fewer than 2^32 texels
+  const float t00 = texel_at<Format>(texels, r0 + (u32)x0), t10 = texel_at<Format>(texels, r0 + (u32)x1);
+  const float t01 = texel_at<Format>(texels, r1 + (u32)x0), t11 = texel_at<Format>(texels, r1 + (u32)x1);
+  const float top = __fmaf_rn(fx, t10 - t00, t00), bot = __fmaf_rn(fx, t11 - t01, t01);
+  return __fmaf_rn(fy, bot - top, top);
+}
+
+__device__ __forceinline__ u32 affine_kind_of(const PartAffine& r) { return __float_as_uint(r.q[6].w); }
+
+// Vertex `tableVertex` (an encoded table barycentric) of the part in `r`, for
+// a record of kind Kind (~0u: any kind, resolved at run time).
+template <u32 Kind>
+__device__ __forceinline__ f3 affine_vertex_k(const PartAffine& r, u32 tableVertex)
+{
+  const float  a  = __uint2float_rn(tableVertex & 0xFFFFu) * (1.0f / 32768.0f);
+  const float  b  = __uint2float_rn(tableVertex >> 16) * (1.0f / 32768.0f);
+  const float4 q0 = r.q[0], q1 = r.q[1], q2 = r.q[2];
+  f3           P  = {__fmaf_rn(b, q1.z, __fmaf_rn(a, q0.w, q0.x)), __fmaf_rn(b, q1.w, __fmaf_rn(a, q1.x, q0.y)),
+                     __fmaf_rn(b, q2.x, __fmaf_rn(a, q1.y, q0.z))};
+  const u32    kind = Kind == ~0u ? affine_kind_of(r) : Kind;
+  if(kind == kAffineFlat)
+    return P;
+  const float4 q3 = r.q[3], q4 = r.q[4], q5 = r.q[5], q6 = r.q[6];
+  const f3     N  = {__fmaf_rn(b, q3.w, __fmaf_rn(a, q3.x, q2.y)), __fmaf_rn(b, q4.x, __fmaf_rn(a, q3.y, q2.z)),
+                     __fmaf_rn(b, q4.y, __fmaf_rn(a, q3.z, q2.w))};
+  const float  u  = __fmaf_rn(b, q5.z, __fmaf_rn(a, q5.x, q4.z));
+  const float  v  = __fmaf_rn(b, q5.w, __fmaf_rn(a, q5.y, q4.w));
+  float        hraw = 0.0f;
+  switch(kind)
+  {
+    case affine_kind(TC_TEXEL_F32, true): hraw = affine_sample<TC_TEXEL_F32, true>(r.q[7], r.q[8], u, v); break;
+    case affine_kind(TC_TEXEL_F32, false): hraw = affine_sample<TC_TEXEL_F32, false>(r.q[7], r.q[8], u, v); break;
+    case affine_kind(TC_TEXEL_F16, true): hraw = affine_sample<TC_TEXEL_F16, true>(r.q[7], r.q[8], u, v); break;
+    case affine_kind(TC_TEXEL_F16, false): hraw = affine_sample<TC_TEXEL_F16, false>(r.q[7], r.q[8], u, v); break;
+    case affine_kind(TC_TEXEL_UNORM16, true): hraw = affine_sample<TC_TEXEL_UNORM16, true>(r.q[7], r.q[8], u, v); break;
+    case affine_kind(TC_TEXEL_UNORM16, false):
+      hraw = affine_sample<TC_TEXEL_UNORM16, false>(r.q[7], r.q[8], u, v);
+      break;
+    default: break;  // kAffineZeroMap: samples as 0
+  }
+  // displace along the renormalised interpolated normal
+  const float height = __fmaf_rn(hraw, q6.x, q6.y);
+  const float k      = height * rsqrtf(__fmaf_rn(N.z, N.z, __fmaf_rn(N.y, N.y, N.x * N.x)));
+  return fma3(k, N, P);
+}
+
+__device__ __forceinline__ f3 affine_vertex(const PartAffine& r, u32 tableVertex)
+{
+  return affine_vertex_k<~0u>(r, tableVertex);
+}
+
+__device__ __forceinline__ u32 affine_first_vertex(const PartAffine& r) { return __float_as_uint(r.q[6].z); }
+
+}  // namespace tc

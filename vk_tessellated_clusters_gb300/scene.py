@@ -516,6 +516,36 @@ def scene_batched(num_instances: int = 256, seed: int = 1, map_size: int = 512, 
     return Scene("batched", geos, insts, texs)
 
 
+def animation_motion(num_instances: int, seed: int = 3):
+    """Seeded rigid motion per instance: a random rotation axis with angular
+    speed U[0, 1] rad/s, and a random direction with speed U[0, 2] units/s."""
+    rng = np.random.default_rng(seed)
+    axes = rng.normal(size=(num_instances, 3))
+    axes /= np.linalg.norm(axes, axis=1, keepdims=True)
+    omega = rng.random(num_instances)
+    dirs = rng.normal(size=(num_instances, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    velocity = dirs * (2.0 * rng.random(num_instances))[:, None]
+    return axes, omega, velocity
+
+
+def animated_worlds(scene: "Scene", motion, t: float) -> np.ndarray:
+    """World matrices (n, 4, 4) at time t: each instance spins about its own
+    origin (axis, omega * t) and translates by velocity * t."""
+    axes, omega, velocity = motion
+    base = np.stack([i.world for i in scene.instances])
+    ang = omega * t
+    c, s_, k = np.cos(ang)[:, None, None], np.sin(ang)[:, None, None], axes
+    K = np.zeros((len(k), 3, 3))
+    K[:, 0, 1], K[:, 0, 2], K[:, 1, 0] = -k[:, 2], k[:, 1], k[:, 2]
+    K[:, 1, 2], K[:, 2, 0], K[:, 2, 1] = -k[:, 0], -k[:, 1], k[:, 0]
+    R = np.eye(3)[None] + s_ * K + (1 - c) * (K @ K)  # Rodrigues
+    W = base.copy()
+    W[:, :3, :3] = R @ base[:, :3, :3]
+    W[:, :3, 3] = base[:, :3, 3] + velocity * t
+    return W
+
+
 def camera_orbit(frame: int, num_frames: int = 60, radius: float = 30.0, center=(20.0, 20.0, 20.0),
                  height: float = 10.0, tess_rate_pixels: float = 4.0) -> Camera:
     a = 2 * np.pi * frame / num_frames
