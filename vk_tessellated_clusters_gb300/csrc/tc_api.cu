@@ -29,9 +29,9 @@ struct SlotPlan
 constexpr size_t kCtrlBytes = 8 + 8 * kMaxCounters;
 
 // kernels of a batched frame besides the split passes: frame_begin,
-// instances_classify, clusters_cull, classify (3), instantiate (2), blas setup,
+// instances_classify, clusters_cull, classify (3), instantiate (4), blas setup,
 // blas insert (2)
-constexpr uint64_t kFrameFixedLaunches = 11;
+constexpr uint64_t kFrameFixedLaunches = 13;
 
 struct Plan
 {
@@ -700,7 +700,7 @@ tc_status tc_triangle_instantiate_run(tc_context* ctx, const tc_frame_args* a, u
   TC_CHECK_CUDA(launch_triangle_instantiate(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
                                             ctx->schedule.scanBlocksPerSM, ctx->schedule.vertexBlocksPerSM,
                                             reinterpret_cast<cudaStream_t>(stream)));
-  ctx->launches += 2;
+  ctx->launches += 4;
   return TC_OK;
 }
 

@@ -394,8 +394,9 @@ __device__ __forceinline__ u64 warp_sum_u64(u64 v)
 // The prefix frontier therefore advances 128 tiles per memory round trip.
 // `state` is this counter's tile-state array; `base` (the counter value before
 // this launch) is only used by tile 0.
-constexpr int kLbSlots  = 4;
-constexpr int kLbWindow = 32 * kLbSlots;
+constexpr int kLbSlots      = 4;
+constexpr int kLbWindow     = 32 * kLbSlots;
+constexpr u32 kLbEagerPolls = 64;
 
 __device__ __forceinline__ u64 warp_lookback_exclusive(u64* state, u32 tile, u64 aggregate, u64 base, u32* errorWord)
 {
@@ -439,7 +440,10 @@ __device__ __forceinline__ u64 warp_lookback_exclusive(u64* state, u32 tile, u64
             s[k] = kLbPrefix;  // give up on this window
         break;
       }
-      __nanosleep(32);
+      // predecessors usually publish within a few hundred nanoseconds: poll
+      // back to back at first, then back off
+      if(spins > kLbEagerPolls)
+        __nanosleep(spins > 4 * kLbEagerPolls ? 256 : 32);
 #pragma unroll
       for(int k = 0; k < kLbSlots; k++)
         if((s[k] & ~kLbValueMask) == 0)

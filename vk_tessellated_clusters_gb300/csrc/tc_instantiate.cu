@@ -3,18 +3,24 @@
 //
 // shaders/triangle_tess_template_instantiate.comp.glsl:126-373.
 //
-// GB300 mapping, two launches:
-//   alloc    : a scan over the part triangles (1024 per tile, decoupled
-//              look-back between tiles) assigns generated-cluster slots, CLAS
-//              bytes and vertex ranges in part order, applies the capacity test
-//              and writes the 44 B of instantiation arguments per part; the
-//              first vertex of each accepted part goes to scratch
-//   vertices : HBM-write bound (12 B per generated vertex dominates). One warp
-//              per 16 consecutive parts, whose vertices form one contiguous
-//              range: each part's affine vertex form (tc_vertex.cuh, 128 B) is
-//              set up once in shared memory, then the lanes walk the range
-//              on consecutive vertices. No block barriers, no cross-block
-//              waits.
+// GB300 mapping, four launches; the first three work on tiles of 1024 part
+// triangles (striped: item i of thread t is part tile * 1024 + i * 256 + t,
+// so every load and store instruction of a warp touches 32 consecutive parts):
+//   tile_sums : per tile, the CLAS bytes and vertex counts of its parts
+//               (reads the config word of each part only).
+//   tile_scan : one block turns the tile sums into each tile's exclusive
+//               offsets (plus the counters' values before the launch) and
+//               advances the counters: the serial order of the reference's
+//               allocation without any cross-block waiting.
+//   args      : per tile, the parts' offsets (block scan + tile offset), the
+//               capacity test, the 44 B of instantiation arguments per part,
+//               the first generated vertex of each part (scratch), CLAS
+//               reference counts and statistics.
+//   vertices  : HBM-write bound (12 B per generated vertex). One warp per 16
+//               consecutive parts (spread over the whole grid): every part's
+//               affine vertex form (tc_vertex.cuh) is set up once in shared
+//               memory, then the lanes walk the chunk's contiguous vertex
+//               range on consecutive vertices.
 #include <algorithm>
 
 #include "tc_kernels.h"
@@ -25,21 +31,19 @@ namespace tc {
 
 namespace {
 
-enum : int
-{
-  kCntGen = 0,
-  kCntData,
-  kCntVerts,
-  kNumCounters
-};
-
-constexpr u32 kAllocBlock   = 256;
-constexpr u32 kAllocItems   = 4;
-constexpr u32 kAllocTile    = kAllocBlock * kAllocItems;
-constexpr u32 kVertexWarps  = 8;  // warps per block of the vertex kernel
+constexpr u32 kBlock        = 256;
+constexpr u32 kItems        = 4;
+constexpr u32 kTile         = kBlock * kItems;
+constexpr u32 kWarps        = kBlock / 32;
 constexpr u32 kPartsPerWarp = 16;  // parts staged per warp and chunk (shared memory budget)
+constexpr u32 kScanBlock    = 1024;
 
-static_assert(kAllocTile == kInstantiateTile, "allocation tile size");
+static_assert(kTile == kInstantiateTile, "allocation tile size");
+
+// CLAS bytes and vertex counts travel packed as (bytes << 20) | vertices: a
+// tile holds at most 1024 x 78 < 2^20 vertices and 1024 x 2^32 bytes.
+constexpr u32 kPackShift = 20;
+constexpr u64 kPackMask  = (1ull << kPackShift) - 1;
 
 // parts of this launch: [0, part counter) or one run, narrowed to the instance window
 __device__ inline void part_range(const StageCtx& c, u32& lo, u32& hi)
@@ -75,173 +79,284 @@ __device__ __forceinline__ T warp_inclusive(T x, u32 lane)
   return x;
 }
 
+__device__ __forceinline__ u32 part_cfg(const tc_TessTriangleInfo* parts, u32 p)
+{
+  return __ldg(&parts[p].subTriangle.triangleID_config) >> 16;
+}
+
+__device__ __forceinline__ u64 part_packed(const StageCtx& c, u32 cfg)
+{
+  return ((u64)__ldg(c.table.templateSizes + cfg_index(cfg)) << kPackShift) | table_entry(c.table, cfg).numVertices;
+}
+
+// Scratch of the instantiate slot: lbState[tile] = packed tile sum,
+// lbState[stride + tile] / lbState[2 * stride + tile] = the tile's exclusive
+// CLAS-byte / vertex offset, totals[0] = generated-cluster counter before the
+// launch.
+
 // ---------------------------------------------------------------------------
-// alloc
+// tile sums
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kAllocBlock) k_instantiate_alloc(StageCtx c, InstantiateBuffers ib)
+__global__ void __launch_bounds__(kBlock) k_instantiate_tile_sums(StageCtx c)
 {
   stage_prologue();
-  __shared__ u64 s_warp[33][kNumCounters];
-  __shared__ u64 s_excl[kNumCounters];
-  __shared__ u32 s_tile, s_flag, s_range[2];
-  __shared__ u32 s_blasKey[kAllocBlock / 32][2], s_blasCnt[kAllocBlock / 32][2], s_stat[kAllocBlock / 32][2];
-  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __shared__ u64 s_warp[kWarps];
+  __shared__ u32 s_range[2];
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if(threadIdx.x == 0)
     part_range(c, s_range[0], s_range[1]);
   __syncthreads();
-  const u32 begin    = s_range[0], n = s_range[1] - s_range[0];
-  const u32 numTiles = clamp_tiles(c, (n + kAllocTile - 1) / kAllocTile);
-
-  tc_SceneBuilding*          b        = c.build;
-  const tc_caps&             k        = c.caps;
-  const tc_TessTriangleInfo* parts    = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
-  const u64                  maxData  = (u64)k.maxGeneratedClusterMegs * 1024ull * 1024ull;
-  tc_BlasBuildInfo*          blas     = reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos);
-  u32                        statTris = 0, statTemp = 0;
-
-  for(;;)
+  const u32                  begin    = s_range[0], n = s_range[1] - s_range[0];
+  const u32                  numTiles = clamp_tiles(c, (n + kTile - 1) / kTile);
+  const tc_TessTriangleInfo* parts    = reinterpret_cast<const tc_TessTriangleInfo*>(c.build->partTriangles);
+  for(u32 tile = blockIdx.x; tile < numTiles; tile += gridDim.x)
   {
-    const u32 tile = next_tile(c, &s_tile);
-    if(tile >= numTiles)
-      break;
-    const u32 first = tile * kAllocTile + threadIdx.x * kAllocItems;
-    u32       inst[kAllocItems], cfg[kAllocItems], nv[kAllocItems], nt[kAllocItems], ds[kAllocItems];
-    u64       sum[kNumCounters] = {0, 0, 0};
+    u64 sum = 0;
 #pragma unroll
-    for(u32 i = 0; i < kAllocItems; i++)
+    for(u32 i = 0; i < kItems; i++)
     {
-      inst[i] = ~0u;
-      cfg[i] = nv[i] = nt[i] = ds[i] = 0;
-      if(first + i < n)
-      {
-        const uint2* raw          = reinterpret_cast<const uint2*>(parts + begin + first + i);
-        inst[i]                   = raw[0].x;
-        cfg[i]                    = raw[2].y >> 16;
-        const tc_TessTableEntry e = table_entry(c.table, cfg[i]);
-        nv[i]                     = e.numVertices;
-        nt[i]                     = e.numTriangles;
-        ds[i]                     = __ldg(c.table.templateSizes + cfg_index(cfg[i]));
-        sum[kCntGen] += 1;
-        sum[kCntData] += ds[i];
-        sum[kCntVerts] += nv[i];
-      }
+      const u32 q = tile * kTile + i * kBlock + threadIdx.x;
+      if(q < n)
+        sum += part_packed(c, part_cfg(parts, begin + q));
     }
-    // block exclusive scan of the three counters
-    u64 inc[kNumCounters];
 #pragma unroll
-    for(int q = 0; q < kNumCounters; q++)
+    for(int o = 16; o > 0; o >>= 1)
+      sum += __shfl_xor_sync(0xFFFFFFFFu, sum, o);
+    if(lane == 0)
+      s_warp[warp] = sum;
+    __syncthreads();
+    if(threadIdx.x == 0)
     {
-      inc[q] = warp_inclusive<u64>(sum[q], lane);
-      if(lane == 31)
-        s_warp[warp][q] = inc[q];
+      u64 t = 0;
+      for(u32 w = 0; w < kWarps; w++)
+        t += s_warp[w];
+      c.scratch.lbState[tile] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// tile scan (one block)
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kScanBlock) k_instantiate_tile_scan(StageCtx c)
+{
+  stage_prologue();
+  __shared__ u64 s_warpData[32], s_warpVerts[32];
+  __shared__ u32 s_range[2];
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  tc_SceneBuilding* b = c.build;
+  if(threadIdx.x == 0)
+    part_range(c, s_range[0], s_range[1]);
+  __syncthreads();
+  const u32 n        = s_range[1] - s_range[0];
+  const u32 numTiles = clamp_tiles(c, (n + kTile - 1) / kTile);
+  const u32 stride   = c.scratch.lbStride;
+  u64 carryData = b->genClusterDataCounter, carryVerts = b->genVertexCounter;
+  const u32 genBase = b->genClusterCounter;
+  for(u32 t0 = 0; t0 < numTiles; t0 += kScanBlock)
+  {
+    const u32 t = t0 + threadIdx.x;
+    const u64 v = t < numTiles ? c.scratch.lbState[t] : 0ull;
+    u64       d = v >> kPackShift, vx = v & kPackMask;
+    u64       id = warp_inclusive<u64>(d, lane), iv = warp_inclusive<u64>(vx, lane);
+    if(lane == 31)
+    {
+      s_warpData[warp]  = id;
+      s_warpVerts[warp] = iv;
     }
     __syncthreads();
     if(warp == 0)
     {
-#pragma unroll
-      for(int q = 0; q < kNumCounters; q++)
-      {
-        u64 w = lane < nw ? s_warp[lane][q] : 0;
-        u64 s = warp_inclusive<u64>(w, lane);
-        __syncwarp();
-        if(lane < nw)
-          s_warp[lane][q] = s - w;
-        if(lane == 31)
-          s_warp[32][q] = s;
-      }
+      const u64 wd = s_warpData[lane], wv = s_warpVerts[lane];
+      const u64 sd = warp_inclusive<u64>(wd, lane), sv = warp_inclusive<u64>(wv, lane);
+      s_warpData[lane]  = sd - wd;
+      s_warpVerts[lane] = sv - wv;
     }
     __syncthreads();
-    // look-back: warps 0..2, one counter each
-    if(warp < kNumCounters)
+    const u64 exData  = carryData + s_warpData[warp] + id - d;
+    const u64 exVerts = carryVerts + s_warpVerts[warp] + iv - vx;
+    if(t < numTiles)
     {
-      const u32 q    = warp;
-      u64       base = 0;
-      if(tile == 0)
-        base = q == kCntGen ? b->genClusterCounter : (q == kCntData ? b->genClusterDataCounter : b->genVertexCounter);
-      const u64 agg = s_warp[32][q];
-      const u64 ex = warp_lookback_exclusive(c.scratch.lbState + (u64)q * c.scratch.lbStride, tile, agg, base, c.errorWord);
-      if(lane == 0)
-      {
-        s_excl[q] = ex;
-        if(tile == numTiles - 1)
-          c.scratch.totals[q] = ex + agg;
-      }
+      c.scratch.lbState[stride + t]     = exData;
+      c.scratch.lbState[2 * stride + t] = exVerts;
+    }
+    // the last thread holds the inclusive total of this round
+    const u64 lastData  = __shfl_sync(0xFFFFFFFFu, exData + d, 31);
+    const u64 lastVerts = __shfl_sync(0xFFFFFFFFu, exVerts + vx, 31);
+    __syncthreads();
+    if(threadIdx.x == kScanBlock - 1)
+    {
+      s_warpData[0]  = lastData;
+      s_warpVerts[0] = lastVerts;
     }
     __syncthreads();
-    u64 genOffset    = s_excl[kCntGen] + s_warp[warp][kCntGen] + inc[kCntGen] - sum[kCntGen];
-    u64 dataOffset   = s_excl[kCntData] + s_warp[warp][kCntData] + inc[kCntData] - sum[kCntData];
-    u64 vertexOffset = s_excl[kCntVerts] + s_warp[warp][kCntVerts] + inc[kCntVerts] - sum[kCntVerts];
-    u32 runInst = ~0u, runCount = 0;
-#pragma unroll
-    for(u32 i = 0; i < kAllocItems; i++)
+    carryData  = s_warpData[0];
+    carryVerts = s_warpVerts[0];
+    __syncthreads();
+  }
+  if(threadIdx.x == 0)
+  {
+    c.scratch.totals[0] = genBase;
+    if(numTiles)
     {
-      if(first + i < n)
+      // the reference's counters count every attempt, accepted or not
+      b->genClusterCounter     = genBase + min(n, numTiles * kTile);
+      b->genClusterDataCounter = carryData;
+      b->genVertexCounter      = (u32)carryVerts;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// write: arguments, counts, vertices
+// ---------------------------------------------------------------------------
+
+template <u32 Kind>
+__device__ __forceinline__ void chunk_vertices(const StageCtx& c, const PartAffine* sp, u32 owner, u32 start,
+                                               u32 total, float* dst)
+{
+  const u32 lane = threadIdx.x & 31;
+  for(u32 base = 0; base < total; base += 32)
+  {
+    // lane's part: those starting at or before the step's first vertex, plus
+    // those starting inside the step up to the lane (one bit each)
+    const u32         before = __popc(__ballot_sync(0xFFFFFFFFu, owner && start <= base));
+    const u32         inside = __reduce_or_sync(0xFFFFFFFFu,
+                                                (owner && start > base && start < base + 32) ? 1u << (start - base) : 0u);
+    const u32         pi     = before - 1 + __popc(inside & ((2u << lane) - 2u));
+    const u32         pstart = __shfl_sync(0xFFFFFFFFu, start, pi & 31);
+    const u32         jj     = base + lane;
+    const PartAffine& r      = sp[pi];
+    if(jj < total)
+    {
+      const f3 q = affine_vertex_k<Kind>(r, __ldg(c.table.vertices + affine_first_vertex(r) + (jj - pstart)));
+      float*   d = dst + 3 * (u64)jj;
+      d[0] = q.x, d[1] = q.y, d[2] = q.z;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock, 4) k_instantiate_args(StageCtx c, InstantiateBuffers ib)
+{
+  stage_prologue();
+  __shared__ u64        s_rowWarp[kItems][kWarps];  // per row and warp: packed warp totals
+  __shared__ u32        s_flag, s_range[2];
+  __shared__ u32        s_blasKey[kWarps][2], s_blasCnt[kWarps][2], s_stat[kWarps][2];
+  const u32         lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  tc_SceneBuilding* b    = c.build;
+  if(threadIdx.x == 0)
+    part_range(c, s_range[0], s_range[1]);
+  __syncthreads();
+  const u32 begin    = s_range[0], n = s_range[1] - s_range[0];
+  const u32 numTiles = clamp_tiles(c, (n + kTile - 1) / kTile);
+  const u32 stride   = c.scratch.lbStride;
+  const u64 genBase  = c.scratch.totals[0];
+
+  const tc_caps&             k            = c.caps;
+  const tc_TessTriangleInfo* parts        = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
+  const u64                  maxData      = (u64)k.maxGeneratedClusterMegs * 1024ull * 1024ull;
+  tc_BlasBuildInfo*          blas         = reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos);
+  u32                        statTris = 0, statTemp = 0;
+
+  for(u32 tile = blockIdx.x; tile < numTiles; tile += gridDim.x)
+  {
+    // ---- offsets: block scan of the packed counts, row by row ----------------
+    u32 inst[kItems], cfg[kItems];
+    u64 own[kItems], incl[kItems];
+#pragma unroll
+    for(u32 i = 0; i < kItems; i++)
+    {
+      const u32 q = tile * kTile + i * kBlock + threadIdx.x;
+      inst[i] = ~0u, cfg[i] = 0, own[i] = 0;
+      if(q < n)
       {
-        const u32 p = begin + first + i;
-        // triangle_tess_template_instantiate.comp.glsl:160-167 capacity test
-        const bool accept = !(vertexOffset + nv[i] > k.maxGeneratedVertices || genOffset + 1 > k.maxGeneratedClusters
-                              || dataOffset + ds[i] > maxData);
-        if(accept)
-        {
-          // accepted instantiations form a prefix of the serial order: slot == generated cluster index
-          const u32 tempOffset = (u32)genOffset;
-          tc_TemplateInstantiateInfo* dst =
-              reinterpret_cast<tc_TemplateInstantiateInfo*>(b->tempInstantiations) + tempOffset;
-          const u64   tmpl  = __ldg(c.table.templateAddresses + cfg_index(cfg[i]));
-          const u64   vaddr = b->genVertices + vertexOffset * 12ull;
-          const uint4 lo4 = make_uint4(p | (TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED << 30), 0u, (u32)tmpl, (u32)(tmpl >> 32));
-          const uint4 hi4 = make_uint4((u32)vaddr, (u32)(vaddr >> 32), 12u, 0u);
-          if((reinterpret_cast<uintptr_t>(dst) & 15) == 0)
-          {
-            reinterpret_cast<uint4*>(dst)[0] = lo4;
-            reinterpret_cast<uint4*>(dst)[1] = hi4;
-          }
-          else
-          {
-            uint2* d2 = reinterpret_cast<uint2*>(dst);
-            d2[0]     = make_uint2(lo4.x, lo4.y);
-            d2[1]     = make_uint2(lo4.z, lo4.w);
-            d2[2]     = make_uint2(hi4.x, hi4.y);
-            d2[3]     = make_uint2(hi4.z, hi4.w);
-          }
-          reinterpret_cast<u32*>(b->tempInstanceIDs)[tempOffset]      = inst[i];
-          reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset] = b->genClusterData + dataOffset;
-          ib.vertexOffset[p]                                          = (u32)vertexOffset;
-          statTris += nt[i];
-          statTemp += 1;
-          if(inst[i] != runInst)
-          {
-            if(runCount)
-              atomicAdd(&blas[runInst].clusterReferencesCount, runCount);
-            runInst  = inst[i];
-            runCount = 0;
-          }
-          runCount++;
-        }
-        else
-          ib.vertexOffset[p] = ~0u;
+        const uint2* raw = reinterpret_cast<const uint2*>(parts + begin + q);
+        inst[i]          = raw[0].x;
+        cfg[i]           = raw[2].y >> 16;
+        own[i]           = part_packed(c, cfg[i]);
       }
-      genOffset += 1;
-      dataOffset += ds[i];
-      vertexOffset += nv[i];
+      incl[i] = warp_inclusive<u64>(own[i], lane);
+      if(lane == 31)
+        s_rowWarp[i][warp] = incl[i];
+    }
+    __syncthreads();
+    const u64 tileData = c.scratch.lbState[stride + tile], tileVerts = c.scratch.lbState[2 * stride + tile];
+    u64       rowBase = 0;
+    u32       runInst = ~0u, runCount = 0;
+#pragma unroll
+    for(u32 i = 0; i < kItems; i++)
+    {
+      u64 before = 0, total = 0;
+      for(u32 w = 0; w < kWarps; w++)
+      {
+        const u64 v = s_rowWarp[i][w];
+        before += w < warp ? v : 0ull;
+        total += v;
+      }
+      const u64 within = rowBase + before + incl[i] - own[i];
+      rowBase += total;
+      const u32 q = tile * kTile + i * kBlock + threadIdx.x;
+      if(q >= n)
+        continue;
+      const u32  p            = begin + q;
+      const u32  nv           = (u32)(own[i] & kPackMask);
+      const u32  ds           = (u32)(own[i] >> kPackShift);
+      const u64  genOffset    = genBase + q;
+      const u64  dataOffset   = tileData + (within >> kPackShift);
+      const u64  vertexOffset = tileVerts + (within & kPackMask);
+      // triangle_tess_template_instantiate.comp.glsl:160-167 capacity test
+      const bool accept = !(vertexOffset + nv > k.maxGeneratedVertices || genOffset + 1 > k.maxGeneratedClusters
+                            || dataOffset + ds > maxData);
+      ib.vertexOffset[p] = accept ? (u32)vertexOffset : ~0u;
+      if(!accept)
+        continue;
+      // accepted instantiations form a prefix of the serial order: slot == generated cluster index
+      const u32                   tempOffset = (u32)genOffset;
+      tc_TemplateInstantiateInfo* dst = reinterpret_cast<tc_TemplateInstantiateInfo*>(b->tempInstantiations) + tempOffset;
+      const u64   tmpl  = __ldg(c.table.templateAddresses + cfg_index(cfg[i]));
+      const u64   vaddr = b->genVertices + vertexOffset * 12ull;
+      const uint4 lo4   = make_uint4(p | (TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED << 30), 0u, (u32)tmpl, (u32)(tmpl >> 32));
+      const uint4 hi4   = make_uint4((u32)vaddr, (u32)(vaddr >> 32), 12u, 0u);
+      if((reinterpret_cast<uintptr_t>(dst) & 15) == 0)
+      {
+        reinterpret_cast<uint4*>(dst)[0] = lo4;
+        reinterpret_cast<uint4*>(dst)[1] = hi4;
+      }
+      else
+      {
+        uint2* d2 = reinterpret_cast<uint2*>(dst);
+        d2[0]     = make_uint2(lo4.x, lo4.y);
+        d2[1]     = make_uint2(lo4.z, lo4.w);
+        d2[2]     = make_uint2(hi4.x, hi4.y);
+        d2[3]     = make_uint2(hi4.z, hi4.w);
+      }
+      reinterpret_cast<u32*>(b->tempInstanceIDs)[tempOffset]      = inst[i];
+      reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset] = b->genClusterData + dataOffset;
+      statTris += table_entry(c.table, cfg[i]).numTriangles;
+      statTemp += 1;
+      if(inst[i] != runInst)
+      {
+        if(runCount)
+          atomicAdd(&blas[runInst].clusterReferencesCount, runCount);
+        runInst  = inst[i];
+        runCount = 0;
+      }
+      runCount++;
     }
     // Per-instance CLAS reference counts. Parts are instance-sorted within a
     // run, so an instance's parts in this tile are (almost always) contiguous:
-    // threads of a warp holding the same instance combine their last runs;
-    // the warp's first and last instances go to shared memory and are merged
-    // across the block's warps, every other instance is added directly. One
-    // atomic per instance and tile instead of one per warp.
+    // a warp sums its threads' last runs per distinct instance; its first and
+    // last instances go to shared memory and are merged across the block's
+    // warps, every other instance is added directly. About one atomic per
+    // instance and tile.
     {
-      const u32  key     = runCount ? runInst : 0xFFFFFFFFu;
-      const u32  peers   = __match_any_sync(0xFFFFFFFFu, key);
-      u32        peerSum = 0;
-      for(u32 m = peers; m; m &= m - 1)
-        peerSum += __shfl_sync(peers, runCount, __ffs(m) - 1);
-      const bool leader  = runCount && (__ffs(peers) - 1) == (int)lane;
-      const u32  holders = __ballot_sync(0xFFFFFFFFu, runCount != 0);
-      const u32  firstKey = holders ? __shfl_sync(0xFFFFFFFFu, key, __ffs(holders) - 1) : 0xFFFFFFFFu;
-      const u32  lastKey  = holders ? __shfl_sync(0xFFFFFFFFu, key, 31 - __clz(holders)) : 0xFFFFFFFFu;
+      const u32 key      = runCount ? runInst : 0xFFFFFFFFu;
+      const u32 holders  = __ballot_sync(0xFFFFFFFFu, runCount != 0);
+      const u32 firstKey = holders ? __shfl_sync(0xFFFFFFFFu, key, __ffs(holders) - 1) : 0xFFFFFFFFu;
+      const u32 lastKey  = holders ? __shfl_sync(0xFFFFFFFFu, key, 31 - __clz(holders)) : 0xFFFFFFFFu;
       if(lane == 0)
       {
         s_blasKey[warp][0] = firstKey;
@@ -250,42 +365,51 @@ __global__ void __launch_bounds__(kAllocBlock) k_instantiate_alloc(StageCtx c, I
         s_blasCnt[warp][1] = 0;
       }
       __syncwarp();
-      if(leader)
+      for(u32 remaining = holders; remaining;)
       {
-        if(key == firstKey)
-          s_blasCnt[warp][0] = peerSum;
-        else if(key == lastKey)
-          s_blasCnt[warp][1] = peerSum;
-        else
-          atomicAdd(&blas[runInst].clusterReferencesCount, peerSum);
+        const int src = __ffs(remaining) - 1;
+        const u32 gk  = __shfl_sync(0xFFFFFFFFu, key, src);
+        const u32 sum = __reduce_add_sync(0xFFFFFFFFu, key == gk ? runCount : 0u);
+        remaining &= ~__ballot_sync(0xFFFFFFFFu, key == gk);
+        if((int)lane == src)
+        {
+          if(gk == firstKey)
+            s_blasCnt[warp][0] = sum;
+          else if(gk == lastKey)
+            s_blasCnt[warp][1] = sum;
+          else
+            atomicAdd(&blas[gk].clusterReferencesCount, sum);
+        }
       }
     }
     __syncthreads();
     if(threadIdx.x == 0)
     {
       u32 curKey = 0xFFFFFFFFu, curCnt = 0;
-      for(u32 w = 0; w < nw; w++)
+      for(u32 w = 0; w < kWarps; w++)
         for(u32 e = 0; e < 2; e++)
         {
-          const u32 k = s_blasKey[w][e], n = s_blasCnt[w][e];
-          if(n == 0)
+          const u32 kk = s_blasKey[w][e], cnt = s_blasCnt[w][e];
+          if(cnt == 0)
             continue;
-          if(k != curKey)
+          if(kk != curKey)
           {
             if(curCnt)
               atomicAdd(&blas[curKey].clusterReferencesCount, curCnt);
-            curKey = k;
+            curKey = kk;
             curCnt = 0;
           }
-          curCnt += n;
+          curCnt += cnt;
         }
       if(curCnt)
         atomicAdd(&blas[curKey].clusterReferencesCount, curCnt);
     }
-    __syncthreads();
+
+    __syncthreads();  // s_rowWarp and the count merge are rewritten by the next tile
   }
 
   // statistics: one atomic each per block
+#pragma unroll
   for(int o = 16; o > 0; o >>= 1)
   {
     statTris += __shfl_xor_sync(0xFFFFFFFFu, statTris, o);
@@ -300,7 +424,7 @@ __global__ void __launch_bounds__(kAllocBlock) k_instantiate_alloc(StageCtx c, I
   if(threadIdx.x == 0)
   {
     u32 t = 0, q = 0;
-    for(u32 w = 0; w < nw; w++)
+    for(u32 w = 0; w < kWarps; w++)
       t += s_stat[w][0], q += s_stat[w][1];
     if(t)
       atomicAdd(&c.readback->numTotalTriangles, t);
@@ -310,18 +434,11 @@ __global__ void __launch_bounds__(kAllocBlock) k_instantiate_alloc(StageCtx c, I
 
   if(last_block_done(c, &s_flag))
   {
-    if(threadIdx.x == 0)
-    {
-      if(numTiles)
-      {
-        b->genClusterCounter     = (u32)c.scratch.totals[kCntGen];
-        b->genClusterDataCounter = c.scratch.totals[kCntData];
-        b->genVertexCounter      = (u32)c.scratch.totals[kCntVerts];
-      }
-      if(c.fuseSetup != kNoSetup)
-        build_setup_apply(c, c.fuseSetup);
-    }
-    scratch_release(c, numTiles, kNumCounters);
+    if(threadIdx.x == 0 && c.fuseSetup != kNoSetup)
+      build_setup_apply(c, c.fuseSetup);
+    // done counter back to zero for a reused slot (nothing else needs clearing)
+    if(threadIdx.x == 0 && c.scratch.selfClean)
+      *c.scratch.done = 0;
   }
 }
 
@@ -332,10 +449,10 @@ __global__ void __launch_bounds__(kAllocBlock) k_instantiate_alloc(StageCtx c, I
 // MinBlocks: resident blocks per SM the register allocation is sized for
 // (4: 64 registers, 5: 48, 6: 40); picked from the schedule's vertexBlocksPerSM.
 template <int MinBlocks>
-__global__ void __launch_bounds__(kVertexWarps * 32, MinBlocks) k_instantiate_vertices(StageCtx c, InstantiateBuffers ib)
+__global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_vertices(StageCtx c, InstantiateBuffers ib)
 {
   stage_prologue();
-  __shared__ PartAffine s_part[kVertexWarps][kPartsPerWarp];
+  __shared__ PartAffine s_part[kWarps][kPartsPerWarp];
   __shared__ u32        s_range[2];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if(threadIdx.x == 0)
@@ -361,7 +478,7 @@ __global__ void __launch_bounds__(kVertexWarps * 32, MinBlocks) k_instantiate_ve
     // accepted parts form a prefix of the part order: nothing further to do
     if(!__any_sync(0xFFFFFFFFu, accepted))
       break;
-    u32 nv = 0;
+    u32 nv = 0, kind = 0;
     if(accepted)
     {
       const uint2*             raw = reinterpret_cast<const uint2*>(parts + p);
@@ -396,47 +513,29 @@ __global__ void __launch_bounds__(kVertexWarps * 32, MinBlocks) k_instantiate_ve
       }
       write_part_affine(sp[lane], corner, cfg_flipped(cfg), bp, bn, bt, e.firstVertex, tx,
                         in.displacementScale * viewScale, in.displacementOffset + viewOffset);
-      nv       = e.numVertices;
+      nv   = e.numVertices;
+      kind = affine_kind_of(sp[lane]);
     }
-    const u32 inc   = warp_inclusive<u32>(nv, lane);
-    const u32 start = inc - nv;  // first vertex of this lane's part within the chunk
-    const u32 total = __shfl_sync(0xFFFFFFFFu, inc, kPartsPerWarp - 1);
-    const u64 v0    = __shfl_sync(0xFFFFFFFFu, vo, 0);
-    __syncwarp();
-    if(total == 0)
-      continue;
-
-    // Lanes take consecutive vertices (lanes of one step share one to three
-    // part records: broadcast reads); each vertex is three 4-byte stores. A
-    // lane's part: the parts starting at or before the step's first vertex,
-    // plus those starting inside the step up to the lane (one bit each).
+    const u32  inc   = warp_inclusive<u32>(nv, lane);
+    const u32  start = inc - nv;  // first vertex of this lane's part within the chunk
+    const u32  total = __shfl_sync(0xFFFFFFFFu, inc, kPartsPerWarp - 1);
+    const u32  v0    = __shfl_sync(0xFFFFFFFFu, vo, 0);
     const bool owner = lane < kPartsPerWarp && nv > 0;
-    for(u32 base = 0; base < total; base += 32)
+    // one specialisation for the whole chunk when its parts share a map kind
+    const u32 kind0 = __shfl_sync(0xFFFFFFFFu, kind, 0);
+    const u32 kw    = __all_sync(0xFFFFFFFFu, !owner || kind == kind0) ? kind0 : ~0u;
+    __syncwarp();
+    float* dst = gv + 3 * (u64)v0;
+    switch(kw)
     {
-      const u32 before = __popc(__ballot_sync(0xFFFFFFFFu, owner && start <= base));
-      const u32 inside = __reduce_or_sync(0xFFFFFFFFu, (owner && start > base && start < base + 32) ? 1u << (start - base) : 0u);
-      const u32 pi     = before - 1 + __popc(inside & ((2u << lane) - 2u));
-      const u32 pstart = __shfl_sync(0xFFFFFFFFu, start, pi & 31);
-      const u32 jj     = base + lane;
-      const PartAffine& r = sp[pi];
-      // the step's records usually share one kind: then a branch-free specialisation
-      const u32 kind  = affine_kind_of(r);
-      const u32 kind0 = __shfl_sync(0xFFFFFFFFu, kind, 0);
-      const u32 kw    = __all_sync(0xFFFFFFFFu, kind == kind0) ? kind0 : ~0u;
-      if(jj < total)
-      {
-        const u32 tv = __ldg(c.table.vertices + affine_first_vertex(r) + (jj - pstart));
-        f3        q;
-        switch(kw)
-        {
-          case affine_kind(TC_TEXEL_F16, true): q = affine_vertex_k<affine_kind(TC_TEXEL_F16, true)>(r, tv); break;
-          case affine_kind(TC_TEXEL_F32, true): q = affine_vertex_k<affine_kind(TC_TEXEL_F32, true)>(r, tv); break;
-          case kAffineFlat: q = affine_vertex_k<kAffineFlat>(r, tv); break;
-          default: q = affine_vertex_k<~0u>(r, tv); break;
-        }
-        float* d = gv + 3 * (v0 + jj);
-        d[0] = q.x, d[1] = q.y, d[2] = q.z;
-      }
+      case affine_kind(TC_TEXEL_F16, true):
+        chunk_vertices<affine_kind(TC_TEXEL_F16, true)>(c, sp, owner, start, total, dst);
+        break;
+      case affine_kind(TC_TEXEL_F32, true):
+        chunk_vertices<affine_kind(TC_TEXEL_F32, true)>(c, sp, owner, start, total, dst);
+        break;
+      case kAffineFlat: chunk_vertices<kAffineFlat>(c, sp, owner, start, total, dst); break;
+      default: chunk_vertices<~0u>(c, sp, owner, start, total, dst); break;
     }
     __syncwarp();  // the warp's part records are rewritten by its next chunk
   }
@@ -444,23 +543,27 @@ __global__ void __launch_bounds__(kVertexWarps * 32, MinBlocks) k_instantiate_ve
 
 }  // namespace
 
-u32 instantiate_alloc_tiles(u32 maxParts) { return (maxParts + kAllocTile - 1) / kAllocTile; }
+u32 instantiate_alloc_tiles(u32 maxParts) { return (maxParts + kTile - 1) / kTile; }
 
 cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
-                                        u32 allocBlocksPerSM, u32 vertexBlocksPerSM, cudaStream_t s)
+                                        u32 scanBlocksPerSM, u32 vertexBlocksPerSM, cudaStream_t s)
 {
-  const u32 allocGrid = std::max(1u, std::min(instantiate_alloc_tiles(maxParts), numSMs * std::max(1u, allocBlocksPerSM)));
-  cudaError_t e = launch_pdl(k_instantiate_alloc, allocGrid, kAllocBlock, s, c, buf);
+  const u32   tiles    = std::max(1u, instantiate_alloc_tiles(maxParts));
+  const u32   tileGrid = std::max(1u, std::min(tiles, numSMs * std::max(1u, scanBlocksPerSM)));
+  cudaError_t e        = launch_pdl(k_instantiate_tile_sums, tileGrid, kBlock, s, c);
   if(e != cudaSuccess)
     return e;
+  if((e = launch_pdl(k_instantiate_tile_scan, 1u, kScanBlock, s, c)) != cudaSuccess)
+    return e;
+  if((e = launch_pdl(k_instantiate_args, tileGrid, kBlock, s, c, buf)) != cudaSuccess)
+    return e;
   const u32 chunks     = (maxParts + kPartsPerWarp - 1) / kPartsPerWarp;
-  const u32 vertexGrid = std::max(1u, std::min((chunks + kVertexWarps - 1) / kVertexWarps,
-                                               numSMs * std::max(1u, vertexBlocksPerSM)));
+  const u32 vertexGrid = std::max(1u, std::min((chunks + kWarps - 1) / kWarps, numSMs * std::max(1u, vertexBlocksPerSM)));
   if(vertexBlocksPerSM >= 6)
-    return launch_pdl(k_instantiate_vertices<6>, vertexGrid, kVertexWarps * 32, s, c, buf);
+    return launch_pdl(k_instantiate_vertices<6>, vertexGrid, kBlock, s, c, buf);
   if(vertexBlocksPerSM == 5)
-    return launch_pdl(k_instantiate_vertices<5>, vertexGrid, kVertexWarps * 32, s, c, buf);
-  return launch_pdl(k_instantiate_vertices<4>, vertexGrid, kVertexWarps * 32, s, c, buf);
+    return launch_pdl(k_instantiate_vertices<5>, vertexGrid, kBlock, s, c, buf);
+  return launch_pdl(k_instantiate_vertices<4>, vertexGrid, kBlock, s, c, buf);
 }
 
 }  // namespace tc

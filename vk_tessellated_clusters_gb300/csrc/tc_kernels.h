@@ -26,12 +26,6 @@ struct ClassifyBuffers
   u32*            triWords;  // 64 per cluster
 };
 
-// triangle_tess_template_instantiate scratch, per part triangle
-struct InstantiateBuffers
-{
-  u32* vertexOffset;  // first generated vertex of each accepted part, ~0 otherwise
-};
-
 cudaError_t launch_frame_begin(const StageCtx& c, u32 grid, cudaStream_t s);
 cudaError_t launch_instances_classify(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
@@ -40,8 +34,16 @@ cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& bu
                                     u32 warpBlocksPerSM, u32 scanBlocksPerSM, cudaStream_t s);
 u32         classify_scan_tiles(u32 maxClusters);
 cudaError_t launch_triangle_split(const StageCtx& c, u32 blockSize, u32 grid, cudaStream_t s);
+// triangle_tess_template_instantiate scratch, per part triangle
+struct InstantiateBuffers
+{
+  u32* vertexOffset;  // first generated vertex of each accepted part, ~0 otherwise
+};
+
+// four launches (tile sums, tile scan, args, vertices); the slot needs 3 state rows of
+// instantiate_alloc_tiles(maxParts)
 cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
-                                        u32 allocBlocksPerSM, u32 vertexBlocksPerSM, cudaStream_t s);
+                                        u32 scanBlocksPerSM, u32 vertexBlocksPerSM, cudaStream_t s);
 u32         instantiate_alloc_tiles(u32 maxParts);
 cudaError_t launch_blas_setup_insertion(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 cudaError_t launch_blas_clusters_insert(const StageCtx& c, u32* segStart, u32* segEnd, u32 stride, u32 grid,
@@ -54,6 +56,6 @@ cudaError_t launch_instantiate_backward(const StageCtx& c, const float* gradVert
 constexpr u32 kInstanceTile     = 256;  // instances per tile (instances_classify, blas_setup)
 constexpr u32 kCullTile         = 256;  // clusters per tile
 constexpr u32 kSplitMinItems    = 16;   // smallest split items-per-tile variant
-constexpr u32 kInstantiateTile  = 1024; // part triangles per allocation tile
+constexpr u32 kInstantiateTile  = 1024; // part triangles per instantiate tile
 
 }  // namespace tc
