@@ -529,7 +529,9 @@ tc_status tc_build_setup(tc_context* ctx, const tc_frame_args* args, uint32_t mo
 tc_status tc_cluster_classify(tc_context* ctx, const tc_frame_args* args, uint32_t instanceBegin, uint32_t instanceEnd,
                               void* stream);
 /* shaders/triangle_split.comp.glsl:598-632: one pass over the current split level
- * (SceneBuilding.splitPassStart/End) restricted to instances [instanceBegin, instanceEnd) */
+ * (SceneBuilding.splitPassStart/End) restricted to instances [instanceBegin, instanceEnd).
+ * The split items must come from this context's tc_cluster_classify / earlier passes of
+ * the same frame: they keep their base triangle's world positions in context scratch. */
 tc_status tc_triangle_split(tc_context* ctx, const tc_frame_args* args, uint32_t instanceBegin, uint32_t instanceEnd,
                             void* stream);
 /* shaders/triangle_tess_template_instantiate.comp.glsl:126-373 over all part

@@ -47,6 +47,7 @@ struct Plan
   u32    classifyCap; // clusters the classify scratch holds
   size_t clsCountsOffset, clsOffsetsOffset, clsTriWordsOffset;
   size_t partVertexOffset;  // u32 per part triangle
+  size_t splitBaseOffset;   // 9 floats per split item: its base triangle's world positions
   size_t instOffset;  // instance cluster prefix (u32 x maxInstances+1)
   size_t errOffset;   // device error word
   size_t totalBytes;
@@ -163,6 +164,8 @@ Plan make_plan(const tc_context_desc& d)
   off                 = align_up(off + (size_t)p.classifyCap * TC_MAX_CLUSTER_TRIANGLES * 4, 256);
   p.partVertexOffset  = off;
   off                 = align_up(off + (size_t)std::max(1u, k.maxPartTriangles) * 4, 256);
+  p.splitBaseOffset   = off;
+  off                 = align_up(off + (size_t)std::max(1u, k.maxSplitTriangles) * 36, 256);
   p.totalBytes        = off;
   return p;
 }
@@ -214,6 +217,7 @@ StageCtx base_ctx(tc_context* ctx, const tc_frame_args* a)
   c.errorWord               = reinterpret_cast<u32*>(ctx->dScratch + ctx->plan.errOffset);
   c.runStarts               = reinterpret_cast<u32*>(ctx->dScratch + ctx->plan.runOffset);
   c.instClusterStart        = reinterpret_cast<u32*>(ctx->dScratch + ctx->plan.instOffset);
+  c.splitBase               = reinterpret_cast<float*>(ctx->dScratch + ctx->plan.splitBaseOffset);
   c.instBegin               = 0;
   c.instEnd                 = a->numInstances;
   c.fuseSetup               = kNoSetup;

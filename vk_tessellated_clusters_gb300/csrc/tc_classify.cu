@@ -160,32 +160,32 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_count(StageCtx c, C
     u32 simple = nt;  // cluster_classify.comp.glsl:203-211: invisible instance, no tessellation
     if(!culled)
     {
-      // cluster_classify.comp.glsl:180-198 object-space vertices, then 217-246 factors
+      // cluster_classify.comp.glsl:180-198 vertices, then 217-246 factors; each
+      // vertex is taken to world space once here (the same operations the
+      // shader applies per triangle corner, so the same bits)
       const float* pos = reinterpret_cast<const float*>(in->positions);
-      for(u32 i = lane; i < nv; i += 32)
-        s_vert[warp][i] = ldg3(pos, cl.firstLocalVertex + i);
-      float m[16];
+      float        m[16];
 #pragma unroll
       for(int j = 0; j < 16; j++)
         m[j] = __ldg(in->worldMatrix.m + j);
+      for(u32 i = lane; i < nv; i += 32)
+        s_vert[warp][i] = xform_point(m, ldg3(pos, cl.firstLocalVertex + i));
       __syncwarp();
       // indices are masked to the staged range: a malformed index reads a wrong
       // vertex of the same cluster, never outside shared memory
       const uint8_t* lt = reinterpret_cast<const uint8_t*>(in->clusterLocalTriangles) + cl.firstLocalTriangle;
       if(lane < nt)
       {
-        const uint3 f = tess_factors(xform_point(m, s_vert[warp][lt[lane * 3 + 0] & 63u]),
-                                     xform_point(m, s_vert[warp][lt[lane * 3 + 1] & 63u]),
-                                     xform_point(m, s_vert[warp][lt[lane * 3 + 2] & 63u]), fp);
+        const uint3 f = tess_factors(s_vert[warp][lt[lane * 3 + 0] & 63u], s_vert[warp][lt[lane * 3 + 1] & 63u],
+                                     s_vert[warp][lt[lane * 3 + 2] & 63u], fp);
         m0 = max(max(f.x, f.y), f.z);
         w0 = classify_triangle(f, sf);
       }
       if(lane + 32 < nt)
       {
         const u32   t = lane + 32;
-        const uint3 f = tess_factors(xform_point(m, s_vert[warp][lt[t * 3 + 0] & 63u]),
-                                     xform_point(m, s_vert[warp][lt[t * 3 + 1] & 63u]),
-                                     xform_point(m, s_vert[warp][lt[t * 3 + 2] & 63u]), fp);
+        const uint3 f = tess_factors(s_vert[warp][lt[t * 3 + 0] & 63u], s_vert[warp][lt[t * 3 + 1] & 63u],
+                                     s_vert[warp][lt[t * 3 + 2] & 63u], fp);
         m1 = max(max(f.x, f.y), f.z);
         w1 = classify_triangle(f, sf);
       }
@@ -403,11 +403,26 @@ __device__ __forceinline__ void emit_triangle(tc_TessTriangleInfo* dst, const tc
   store_tess_info(dst, ci, v0, v1, v2, tri | ((word & 0xFFFFu) << 16));
 }
 
+// what the vertex walk of a full cluster needs (phase 2 of k_classify_write)
+struct FullRecord
+{
+  const float*           pos;
+  const float*           nrm;
+  const float*           uvs;
+  u32                    first;  // firstLocalVertex
+  float                  iscale, ioffset;
+  u32                    vo;     // first generated vertex
+  u32                    nv;     // vertex count
+  u32                    _pad;
+  tc_DisplacementTexture tx;
+};
+
 template <int MinBlocks>
 __global__ void __launch_bounds__(256, MinBlocks) k_classify_write(StageCtx c, ClassifyScratch cs)
 {
   stage_prologue();
-  __shared__ u32 s_range[2];
+  __shared__ u32        s_range[2];
+  __shared__ FullRecord s_full[8][32];
   const u32 lane = threadIdx.x & 31;
   if(threadIdx.x == 0)
     window_range(c, s_range[0], s_range[1]);
@@ -433,81 +448,15 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_write(StageCtx c, C
   const u32 gw   = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const u32 per  = (n + nwarps - 1) / nwarps;
   const u32 vEnd = min(n, (gw + 1) * per);
-  u32       blasInst = 0xFFFFFFFFu, blasCount = 0;
   tc_BlasBuildInfo* blas = reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos);
+  // ---- phase 1: part and split triangles, one cluster at a time ---------------
   for(u32 v = gw * per; v < vEnd; v++)
   {
-    const uint2          rec = cs.counts[v];
+    const uint2 rec = cs.counts[v];
+    if(cnt_full(rec))
+      continue;  // phase 2
     const ClusterOffsets off = cs.offsets[v];
     const tc_ClusterInfo ci  = vis[begin + v];
-    if(cnt_full(rec))
-    {
-      // cluster_classify.comp.glsl:271-488: template instantiation of the full cluster
-      const u32  nv     = cnt_verts(rec);
-      const bool accept = !((u64)off.vert + nv > k.maxGeneratedVertices || (u64)off.gen + 1 > k.maxGeneratedClusters
-                            || off.data + rec.y > maxData);
-      if(!accept)
-        continue;
-      const tc_RenderInstance* in = c.instances + ci.instanceID;
-      const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
-      if(lane == 0)
-      {
-        // accepted instantiations form a prefix of the serial order, so the
-        // instantiation slot equals the generated-cluster slot
-        const u32                  tempOffset = off.gen;
-        tc_TemplateInstantiateInfo ti;
-        ti.clusterIdOffset        = 0;
-        ti.geometryIndexOffset    = 0;
-        ti.clusterTemplateAddress = __ldg(reinterpret_cast<const u64*>(in->clusterTemplateAdresses) + ci.clusterID);
-        ti.vertexBufferAddress    = b->genVertices + (u64)off.vert * 12ull;
-        ti.vertexBufferStride     = 12;
-        reinterpret_cast<tc_TemplateInstantiateInfo*>(b->tempInstantiations)[tempOffset] = ti;
-        reinterpret_cast<u32*>(b->tempInstanceIDs)[tempOffset]                          = ci.instanceID;
-        reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset]                     = b->genClusterData + off.data;
-        if((c.flags & TC_FLAG_WRITE_FULLCLUSTERS) && b->fullClusters)
-          reinterpret_cast<tc_ClusterInfo*>(b->fullClusters)[tempOffset] = ci;
-        if(ci.instanceID != blasInst)
-        {
-          if(blasCount)
-            atomicAdd(&blas[blasInst].clusterReferencesCount, blasCount);
-          blasInst  = ci.instanceID;
-          blasCount = 0;
-        }
-        blasCount++;
-        statTemp += 1;
-        statTris += min((u32)cl.numTriangles, TC_MAX_CLUSTER_TRIANGLES);
-      }
-      // cluster_classify.comp.glsl:457-482: displaced cluster vertices
-      // texture descriptor held in registers (the vertex stores below may alias it)
-      tc_DisplacementTexture txd = {};
-      if(haveTextures && in->displacementIndex >= 0)
-      {
-        if((u32)in->displacementIndex < c.numTextures)
-          txd = c.textures[in->displacementIndex];
-        else if(lane == 0)
-          atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
-      }
-      const float iscale = in->displacementScale, ioffset = in->displacementOffset;
-      const float vscale = c.view->displacementScale, voffset = c.view->displacementOffset;
-      const float* pos = reinterpret_cast<const float*>(in->positions);
-      const float* nrm = reinterpret_cast<const float*>(in->normals);
-      const float* uvs = reinterpret_cast<const float*>(in->texcoords);
-      for(u32 i = lane; i < nv; i += 32)
-      {
-        const u32 vi = cl.firstLocalVertex + i;
-        f3        p  = ldg3(pos, vi);
-        if(txd.width != 0)
-        {
-          const float h = sample_bilinear(txd, ldg2(uvs, vi));
-          p             = displace(p, ldg3(nrm, vi), h, iscale, vscale, ioffset, voffset);
-        }
-        float* dst = gv + ((u64)off.vert + i) * 3;
-        dst[0]     = p.x;
-        dst[1]     = p.y;
-        dst[2]     = p.z;
-      }
-    }
-    else
     {
       // cluster_classify.comp.glsl:543-666: part and split triangles
       const u32  nt  = cnt_parts(rec) + cnt_splits(rec);
@@ -518,11 +467,40 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_write(StageCtx c, C
       const bool s1  = lane + 32 < nt && (w1 >> 18) != 0, p1 = lane + 32 < nt && (w1 >> 18) == 0;
       const u32  bs0 = __ballot_sync(0xFFFFFFFFu, s0), bp0 = __ballot_sync(0xFFFFFFFFu, p0);
       const u32  bs1 = __ballot_sync(0xFFFFFFFFu, s1), bp1 = __ballot_sync(0xFFFFFFFFu, p1);
+      // split items also carry their base triangle's world positions (read by
+      // every split pass instead of the instance / cluster / vertex chain)
+      const tc_RenderInstance* in  = nullptr;
+      tc_Cluster               cl  = {};
+      float                    m[16];
+      if(bs0 | bs1)
+      {
+        in = c.instances + ci.instanceID;
+        cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
+#pragma unroll
+        for(int j = 0; j < 16; j++)
+          m[j] = __ldg(in->worldMatrix.m + j);
+      }
+      auto split_base = [&](u64 o, u32 tri) {
+        if(!c.splitBase)
+          return;
+        const uint8_t* lt  = reinterpret_cast<const uint8_t*>(in->clusterLocalTriangles) + cl.firstLocalTriangle;
+        const float*   pos = reinterpret_cast<const float*>(in->positions);
+        float*         d   = c.splitBase + 9 * o;
+#pragma unroll
+        for(int vv = 0; vv < 3; vv++)
+        {
+          const f3 wp = xform_point(m, ldg3(pos, cl.firstLocalVertex + lt[tri * 3 + vv]));
+          d[3 * vv + 0] = wp.x, d[3 * vv + 1] = wp.y, d[3 * vv + 2] = wp.z;
+        }
+      };
       if(s0)
       {
         const u64 o = (u64)off.split + __popc(bs0 & ltm);
         if(o < k.maxSplitTriangles)
+        {
           emit_triangle(splits + o, ci, lane, w0);
+          split_base(o, lane);
+        }
       }
       else if(p0)
       {
@@ -534,7 +512,10 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_write(StageCtx c, C
       {
         const u64 o = (u64)off.split + __popc(bs0) + __popc(bs1 & ltm);
         if(o < k.maxSplitTriangles)
+        {
           emit_triangle(splits + o, ci, lane + 32, w1);
+          split_base(o, lane + 32);
+        }
       }
       else if(p1)
       {
@@ -545,9 +526,128 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_write(StageCtx c, C
     }
   }
 
-  if(lane == 0 && blasCount)
-    atomicAdd(&blas[blasInst].clusterReferencesCount, blasCount);
+  // ---- phase 2: full clusters of the range, 32 at a time ----------------------
+  // cluster_classify.comp.glsl:271-488: instantiation arguments (one lane per
+  // cluster, so the instance / cluster loads of 32 clusters overlap), then the
+  // clusters' displaced vertices (:457-482), which are contiguous in
+  // genVertices, walked on consecutive lanes.
+  FullRecord* rec = s_full[threadIdx.x >> 5];
+  for(u32 v0 = gw * per; v0 < vEnd; v0 += 32)
+  {
+    const u32 v    = v0 + lane;
+    bool       full = false;
+    u32        nv = 0;
+    u32        inst = 0xFFFFFFFFu;
+    FullRecord fr;
+    if(v < vEnd)
+    {
+      const uint2 r = cs.counts[v];
+      if(cnt_full(r))
+      {
+        const ClusterOffsets off = cs.offsets[v];
+        nv                       = cnt_verts(r);
+        full = !((u64)off.vert + nv > k.maxGeneratedVertices || (u64)off.gen + 1 > k.maxGeneratedClusters
+                 || off.data + r.y > maxData);
+        if(full)
+        {
+          const tc_ClusterInfo     ci = vis[begin + v];
+          const tc_RenderInstance* in = c.instances + ci.instanceID;
+          const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
+          // accepted instantiations form a prefix of the serial order, so the
+          // instantiation slot equals the generated-cluster slot
+          const u32                  tempOffset = off.gen;
+          tc_TemplateInstantiateInfo ti;
+          ti.clusterIdOffset        = 0;
+          ti.geometryIndexOffset    = 0;
+          ti.clusterTemplateAddress = __ldg(reinterpret_cast<const u64*>(in->clusterTemplateAdresses) + ci.clusterID);
+          ti.vertexBufferAddress    = b->genVertices + (u64)off.vert * 12ull;
+          ti.vertexBufferStride     = 12;
+          reinterpret_cast<tc_TemplateInstantiateInfo*>(b->tempInstantiations)[tempOffset] = ti;
+          reinterpret_cast<u32*>(b->tempInstanceIDs)[tempOffset]                          = ci.instanceID;
+          reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset]                     = b->genClusterData + off.data;
+          if((c.flags & TC_FLAG_WRITE_FULLCLUSTERS) && b->fullClusters)
+            reinterpret_cast<tc_ClusterInfo*>(b->fullClusters)[tempOffset] = ci;
+          statTemp += 1;
+          statTris += min((u32)cl.numTriangles, TC_MAX_CLUSTER_TRIANGLES);
+          inst     = ci.instanceID;
+          fr.vo    = off.vert;
+          fr.nv    = nv;
+          fr.pos   = reinterpret_cast<const float*>(in->positions);
+          fr.nrm   = reinterpret_cast<const float*>(in->normals);
+          fr.uvs   = reinterpret_cast<const float*>(in->texcoords);
+          fr.first = cl.firstLocalVertex;
+          fr.tx    = {};
+          if(haveTextures && in->displacementIndex >= 0)
+          {
+            if((u32)in->displacementIndex < c.numTextures)
+              fr.tx = c.textures[in->displacementIndex];
+            else
+              atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
+          }
+          fr.iscale  = in->displacementScale;
+          fr.ioffset = in->displacementOffset;
+        }
+      }
+    }
+    const u32 fm = __ballot_sync(0xFFFFFFFFu, full);
+    if(fm == 0)
+      continue;
+    // records packed in lane order: record r belongs to the r-th full cluster
+    if(full)
+      rec[__popc(fm & ltm)] = fr;
+    // CLAS reference counts: one atomic per distinct instance of the batch
+    for(u32 remaining = fm; remaining;)
+    {
+      const int src = __ffs(remaining) - 1;
+      const u32 gk  = __shfl_sync(0xFFFFFFFFu, inst, src);
+      const u32 sum = __popc(__ballot_sync(0xFFFFFFFFu, full && inst == gk));
+      remaining &= ~__ballot_sync(0xFFFFFFFFu, full && inst == gk);
+      if((int)lane == src)
+        atomicAdd(&blas[gk].clusterReferencesCount, sum);
+    }
+    __syncwarp();
+    // per record (lane r < nrec): first vertex within the batch and vertex count
+    const u32 nrec   = __popc(fm);
+    const u32 vBase  = rec[0].vo;
+    const u32 rStart = lane < nrec ? rec[lane].vo - vBase : 0u;
+    const u32 rCount = lane < nrec ? rec[lane].nv : 0u;
+    const u32 rEnd   = __shfl_sync(0xFFFFFFFFu, rStart + rCount, nrec - 1);
+    const bool  owner  = lane < nrec;
+    const float vscale = c.view->displacementScale, voffset = c.view->displacementOffset;
+    for(u32 base = 0; base < rEnd; base += 32)
+    {
+      const u32 before = __popc(__ballot_sync(0xFFFFFFFFu, owner && rStart <= base));
+      const u32 inside = __reduce_or_sync(0xFFFFFFFFu,
+                                          (owner && rStart > base && rStart < base + 32) ? 1u << (rStart - base) : 0u);
+      const u32 ri     = before - 1 + __popc(inside & ((2u << lane) - 2u));
+      const u32 rs     = __shfl_sync(0xFFFFFFFFu, rStart, ri & 31);
+      const u32 jj     = base + lane;
+      if(jj < rEnd)
+      {
+        const FullRecord& fr = rec[ri];
+        const u32         vi = fr.first + (jj - rs);
+        f3                p  = ldg3(fr.pos, vi);
+        if(fr.tx.width != 0)
+        {
+          const float h = sample_bilinear(fr.tx, ldg2(fr.uvs, vi));
+          p             = displace(p, ldg3(fr.nrm, vi), h, fr.iscale, vscale, fr.ioffset, voffset);
+        }
+        float* dst = gv + ((u64)vBase + jj) * 3;
+        dst[0]     = p.x;
+        dst[1]     = p.y;
+        dst[2]     = p.z;
+      }
+    }
+    __syncwarp();  // records are rewritten by the next batch
+  }
+
   // statistics: one atomic each per warp
+#pragma unroll
+  for(int o = 16; o > 0; o >>= 1)
+  {
+    statTemp += __shfl_xor_sync(0xFFFFFFFFu, statTemp, o);
+    statTris += __shfl_xor_sync(0xFFFFFFFFu, statTris, o);
+  }
   if(lane == 0)
   {
     if(statTemp)

@@ -10,10 +10,15 @@
 // GB300 mapping: a tile is T parent items; their children are laid out flat
 // across the block (block scan of child counts, binary search child -> parent,
 // the same packing the reference does per subgroup, triangle_split.comp.glsl:350-472).
-// Pass 1 classifies every child and counts; a decoupled look-back orders the
-// tile's appends after all earlier tiles; pass 2 recomputes the children (pure
-// ALU on L1-resident table and parent data) and writes them in (parent, child)
-// order. Persistent grid, tiles from a ticket.
+// Pass 1 classifies every child, keeps it in shared memory and counts per
+// (chunk, warp); one warp turns the counts into offsets and a decoupled
+// look-back orders the tile's appends after all earlier tiles; pass 2 writes
+// the children in (parent, child) order (recomputing them only when a tile
+// has more than 64 children per item, i.e. split factors above 8), with no
+// block barrier inside either pass. Split items carry their base
+// triangle's world positions in a side array, so a tile's set-up is one load
+// level instead of the instance / cluster / index / vertex chain. Persistent
+// grid, tiles from a ticket.
 #include "tc_kernels.h"
 #include "tc_stage.cuh"
 
@@ -96,11 +101,18 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
   static_assert(T <= B && T <= 32, "tile items are set up by warp 0");
   constexpr u32 kMaxChildren = T * kMaxChildrenPerItem;
   constexpr u32 kMaxChunks   = (kMaxChildren + B - 1) / B;
+  constexpr u32 kW           = B / 32;
+  constexpr u32 kSlots       = kMaxChunks * kW;  // (chunk, warp) count slots, in serial order
+  static_assert(kSlots <= 128, "one warp scans the count slots, four per lane");
 
+  // pass 1 keeps its children for pass 2 when they fit (always for split
+  // factors up to 8: at most 64 children per item)
+  constexpr u32 kCacheChildren = T * 64;
+  __shared__ uint4     s_child[kCacheChildren];      // vtx[3], tc
+  __shared__ u32       s_splitMask[kSlots];          // per (chunk, warp): which lanes' children are split items
   __shared__ SplitItem s_item[T];
   __shared__ u32       s_pre[T + 1];
-  __shared__ u32       s_chunkCnt[kMaxChunks][kNumCounters];  // exclusive per chunk after the scan
-  __shared__ u32       s_warpCnt[B / 32][kNumCounters];
+  __shared__ u32       s_cnt[kNumCounters][kSlots];  // per (chunk, warp): count, then exclusive offset within the tile
   __shared__ u64       s_excl[kNumCounters];
   __shared__ u32       s_tile, s_flag, s_range[2];
 
@@ -135,6 +147,21 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
   fp.viewportH = c.view->viewportf.y;
   fp.tessRate  = c.view->tessRate;
   const u32 sf = clamp_split_factor(k.splitFactor);
+  const u32 ltm = (1u << lane) - 1u;
+
+  // parent of child j: last item with s_pre[item] <= j
+  auto parent_of = [&](u32 j) {
+    u32 lo = 0, hi = T;
+    while(hi - lo > 1)
+    {
+      const u32 mid = (lo + hi) >> 1;
+      if(s_pre[mid] <= j)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    return lo;
+  };
 
   for(;;)
   {
@@ -150,7 +177,8 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
       u32        n     = 0;
       if(valid)
       {
-        // triangle_split.comp.glsl:146-180 fillBaseVertices
+        // triangle_split.comp.glsl:146-180 fillBaseVertices; the base
+        // triangle's world positions travel with the item (splitBase)
         const uint2* raw = reinterpret_cast<const uint2*>(queue + item);
         uint2        r0 = raw[0], r1 = raw[1], r2 = raw[2];
         SplitItem    it;
@@ -159,19 +187,29 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
         it.vtx[1] = r1.y;
         it.vtx[2] = r2.x;
         it.tc     = r2.y;
-        const tc_TessTableEntry  e  = table_entry(c.table, it.tc >> 16);
-        const tc_RenderInstance& in = c.instances[it.ci.instanceID];
-        const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in.clusters)[it.ci.clusterID];
-        const uint8_t*           lt = reinterpret_cast<const uint8_t*>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
-        const u32                tri = it.tc & 0xFFFFu;
-        const float*             pos = reinterpret_cast<const float*>(in.positions);
-        float                    m[16];
+        const tc_TessTableEntry e = table_entry(c.table, it.tc >> 16);
+        if(c.splitBase)
+        {
+          const float* sb = c.splitBase + 9 * (u64)item;
 #pragma unroll
-        for(int j = 0; j < 16; j++)
-          m[j] = __ldg(in.worldMatrix.m + j);
+          for(int v = 0; v < 3; v++)
+            it.bp[v] = {__ldg(sb + 3 * v), __ldg(sb + 3 * v + 1), __ldg(sb + 3 * v + 2)};
+        }
+        else
+        {
+          const tc_RenderInstance& in  = c.instances[it.ci.instanceID];
+          const tc_Cluster         cl  = reinterpret_cast<const tc_Cluster*>(in.clusters)[it.ci.clusterID];
+          const uint8_t*           lt  = reinterpret_cast<const uint8_t*>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
+          const u32                tri = it.tc & 0xFFFFu;
+          const float*             pos = reinterpret_cast<const float*>(in.positions);
+          float                    m[16];
 #pragma unroll
-        for(int v = 0; v < 3; v++)
-          it.bp[v] = xform_point(m, ldg3(pos, cl.firstLocalVertex + lt[tri * 3 + v]));
+          for(int j = 0; j < 16; j++)
+            m[j] = __ldg(in.worldMatrix.m + j);
+#pragma unroll
+          for(int v = 0; v < 3; v++)
+            it.bp[v] = xform_point(m, ldg3(pos, cl.firstLocalVertex + lt[tri * 3 + v]));
+        }
         it.firstTriangle = e.firstTriangle;
         it.firstVertex   = e.firstVertex;
         n                = min((u32)e.numTriangles, kMaxChildrenPerItem);
@@ -192,67 +230,71 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
         s_pre[0] = 0;
     }
     __syncthreads();
-    const u32 numChildren = s_pre[T];
-    const u32 numChunks   = (numChildren + B - 1) / B;
+    const u32  numChildren = s_pre[T];
+    const u32  numChunks   = (numChildren + B - 1) / B;
+    const bool cached      = numChildren <= kCacheChildren;
 
-    // ---- pass 1: classify children, count per chunk -------------------------
+    // ---- pass 1: classify children; every warp counts its own slots ---------
     for(u32 ch = 0; ch < numChunks; ch++)
     {
-      const u32 j     = ch * B + threadIdx.x;
+      const u32  j     = ch * B + threadIdx.x;
       const bool valid = j < numChildren;
-      bool       split = false, part = false;
+      bool       split = false;
       if(valid)
       {
-        u32 lo = 0, hi = T;  // last item with s_pre[item] <= j
-        while(hi - lo > 1)
-        {
-          u32 mid = (lo + hi) >> 1;
-          if(s_pre[mid] <= j)
-            lo = mid;
-          else
-            hi = mid;
-        }
-        const Child child = make_child(c.table, s_item[lo], j - s_pre[lo], fp, sf);
+        const u32   it    = parent_of(j);
+        const Child child = make_child(c.table, s_item[it], j - s_pre[it], fp, sf);
         split             = child.split;
-        part              = !child.split;
+        if(cached)
+          s_child[j] = make_uint4(child.vtx[0], child.vtx[1], child.vtx[2], child.tc);
       }
-      const u32 bs = __ballot_sync(0xFFFFFFFFu, split), bp = __ballot_sync(0xFFFFFFFFu, part);
+      const u32 bs = __ballot_sync(0xFFFFFFFFu, valid && split), bp = __ballot_sync(0xFFFFFFFFu, valid && !split);
       if(lane == 0)
       {
-        s_warpCnt[warp][kCntSplit] = __popc(bs);
-        s_warpCnt[warp][kCntPart]  = __popc(bp);
+        s_cnt[kCntSplit][ch * kW + warp] = __popc(bs);
+        s_cnt[kCntPart][ch * kW + warp]  = __popc(bp);
+        s_splitMask[ch * kW + warp]      = bs;
       }
-      __syncthreads();
-      if(threadIdx.x < kNumCounters)
-      {
-        u32 s = 0;
-        for(u32 w = 0; w < B / 32; w++)
-          s += s_warpCnt[w][threadIdx.x];
-        s_chunkCnt[ch][threadIdx.x] = s;
-      }
-      __syncthreads();
     }
+    __syncthreads();
 
-    // ---- tile totals, look-back ------------------------------------------------
+    // ---- slot offsets within the tile, tile totals, look-back ------------------
     if(warp < kNumCounters)
     {
-      const u32 q   = warp;
-      u32       agg = 0;
-      for(u32 ch = 0; ch < numChunks; ch++)
-        agg += s_chunkCnt[ch][q];
-      u64 base = 0;
+      const u32 q     = warp;
+      const u32 slots = numChunks * kW;
+      u32       v[4], sum = 0;
+#pragma unroll
+      for(int r = 0; r < 4; r++)
+      {
+        const u32 i = lane * 4 + r;
+        v[r]        = i < slots ? s_cnt[q][i] : 0u;
+        sum += v[r];
+      }
+      u32 incl = sum;
+#pragma unroll
+      for(int d = 1; d < 32; d <<= 1)
+      {
+        const u32 y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if(lane >= (u32)d)
+          incl += y;
+      }
+      u32 run = incl - sum;
+#pragma unroll
+      for(int r = 0; r < 4; r++)
+      {
+        const u32 i = lane * 4 + r;
+        if(i < slots)
+          s_cnt[q][i] = run;
+        run += v[r];
+      }
+      const u32 agg = __shfl_sync(0xFFFFFFFFu, incl, 31);
+      u64       base = 0;
       if(tile == 0)
         base = q == kCntSplit ? b->splitWriteCounter : b->partTriangleCounter;
       const u64 ex = warp_lookback_exclusive(c.scratch.lbState + (u64)q * c.scratch.lbStride, tile, agg, base, c.errorWord);
       if(lane == 0)
       {
-        u32 run = 0;
-        for(u32 ch = 0; ch < numChunks; ch++)
-        {
-          u32 v              = s_chunkCnt[ch][q];
-          s_chunkCnt[ch][q]  = run;  // exclusive within tile
-          run += v;
-        }
         s_excl[q] = ex;
         if(tile == numTiles - 1)
           c.scratch.totals[q] = ex + agg;
@@ -260,57 +302,49 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
     }
     __syncthreads();
 
-    // ---- pass 2: recompute and write ---------------------------------------------
+    // ---- pass 2: write, from pass 1's children or recomputed (no block barriers)
     for(u32 ch = 0; ch < numChunks; ch++)
     {
-      const u32 j     = ch * B + threadIdx.x;
+      const u32  j     = ch * B + threadIdx.x;
       const bool valid = j < numChildren;
       Child      child;
       u32        item = 0;
       child.split     = false;
       if(valid)
       {
-        u32 lo = 0, hi = T;
-        while(hi - lo > 1)
+        item = parent_of(j);
+        if(cached)
         {
-          u32 mid = (lo + hi) >> 1;
-          if(s_pre[mid] <= j)
-            lo = mid;
-          else
-            hi = mid;
+          const uint4 cc = s_child[j];
+          child.vtx[0] = cc.x, child.vtx[1] = cc.y, child.vtx[2] = cc.z, child.tc = cc.w;
+          child.split  = (s_splitMask[ch * kW + warp] >> lane) & 1u;
         }
-        item  = lo;
-        child = make_child(c.table, s_item[lo], j - s_pre[lo], fp, sf);
+        else
+          child = make_child(c.table, s_item[item], j - s_pre[item], fp, sf);
       }
       const bool split = valid && child.split, part = valid && !child.split;
       const u32  bs = __ballot_sync(0xFFFFFFFFu, split), bp = __ballot_sync(0xFFFFFFFFu, part);
-      if(lane == 0)
-      {
-        s_warpCnt[warp][kCntSplit] = __popc(bs);
-        s_warpCnt[warp][kCntPart]  = __popc(bp);
-      }
-      __syncthreads();
-      u32 wsplit = 0, wpart = 0;
-      for(u32 w = 0; w < warp; w++)
-      {
-        wsplit += s_warpCnt[w][kCntSplit];
-        wpart += s_warpCnt[w][kCntPart];
-      }
-      const u32 ltm = (1u << lane) - 1u;
       if(split)
       {
-        const u64 o = s_excl[kCntSplit] + s_chunkCnt[ch][kCntSplit] + wsplit + __popc(bs & ltm);
+        const u64 o = s_excl[kCntSplit] + s_cnt[kCntSplit][ch * kW + warp] + __popc(bs & ltm);
         if(o < k.maxSplitTriangles)
         {
           uint2* dst = reinterpret_cast<uint2*>(queue + o);
           dst[0]     = make_uint2(s_item[item].ci.instanceID, s_item[item].ci.clusterID);
           dst[1]     = make_uint2(child.vtx[0], child.vtx[1]);
           dst[2]     = make_uint2(child.vtx[2], child.tc);
+          if(c.splitBase)
+          {
+            float* d = c.splitBase + 9 * o;
+#pragma unroll
+            for(int v = 0; v < 3; v++)
+              d[3 * v] = s_item[item].bp[v].x, d[3 * v + 1] = s_item[item].bp[v].y, d[3 * v + 2] = s_item[item].bp[v].z;
+          }
         }
       }
       else if(part)
       {
-        const u64 o = s_excl[kCntPart] + s_chunkCnt[ch][kCntPart] + wpart + __popc(bp & ltm);
+        const u64 o = s_excl[kCntPart] + s_cnt[kCntPart][ch * kW + warp] + __popc(bp & ltm);
         if(o < k.maxPartTriangles)
         {
           uint2* dst = reinterpret_cast<uint2*>(reinterpret_cast<tc_TessTriangleInfo*>(b->partTriangles) + o);
@@ -319,8 +353,8 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
           dst[2]     = make_uint2(child.vtx[2], child.tc);
         }
       }
-      __syncthreads();
     }
+    __syncthreads();  // s_item, s_pre and s_cnt are rewritten by the next tile
   }
 
   if(last_block_done(c, &s_flag))

@@ -56,6 +56,7 @@ struct StageCtx
   u32*                          errorWord;
   u32*                          runStarts;         // [kMaxRuns + 2]: part counter at each run start, then full-cluster count
   u32*                          instClusterStart;  // [numInstances + 1] exclusive prefix of numClusters
+  float*                        splitBase;         // [maxSplitTriangles][9]: world positions of each split item's base triangle
   LaunchScratch                 scratch;
   u32                           instBegin;  // instance window [instBegin, instEnd)
   u32                           instEnd;
