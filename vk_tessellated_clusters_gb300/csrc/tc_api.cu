@@ -29,14 +29,15 @@ struct SlotPlan
 constexpr size_t kCtrlBytes = 8 + 8 * kMaxCounters;
 
 // kernels of a batched frame besides the split passes: frame_begin,
-// instances_classify, clusters_cull, classify (3), instantiate (4), blas setup,
-// blas insert (2)
-constexpr uint64_t kFrameFixedLaunches = 13;
+// instances_classify, clusters_cull, classify (3), instantiate (4, twice: the
+// first part run overlapped with the split passes, then the others), blas
+// setup, blas insert (2)
+constexpr uint64_t kFrameFixedLaunches = 17;
 
 struct Plan
 {
   // slot indices
-  u32 slotInstances, slotCull, slotClassify, slotSplit0, slotInstantiate, slotBlas;
+  u32 slotInstances, slotCull, slotClassify, slotSplit0, slotInstantiate, slotInstantiate0, slotBlas;
   u32 numSlots;
   std::vector<SlotPlan> slots;
   size_t frameBytes;  // zeroed once per batched frame (all slots + segment tables)
@@ -80,6 +81,12 @@ struct tc_context
   // scratch
   Plan     plan;
   uint8_t* dScratch = nullptr;
+
+  // second stream of the batched frame: the first part run's instantiation
+  // overlaps the split passes (fork / join through the two events)
+  cudaStream_t side    = nullptr;
+  cudaEvent_t  evFork  = nullptr;
+  cudaEvent_t  evJoin  = nullptr;
 
   // graph cache
   cudaGraphExec_t graphExec = nullptr;
@@ -134,6 +141,7 @@ Plan make_plan(const tc_context_desc& d)
   for(u32 i = 1; i < passes; i++)
     add(ceil_div(k.maxSplitTriangles, kSplitMinItems), 2);
   p.slotInstantiate = add(instantiate_alloc_tiles(k.maxPartTriangles), 3);
+  p.slotInstantiate0 = add(instantiate_alloc_tiles(k.maxPartTriangles), 3);
   p.slotBlas        = add(ceil_div(d.maxInstances, kInstanceTile), 1);
   p.numSlots        = (u32)p.slots.size();
   size_t off        = 0;
@@ -292,6 +300,22 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   TC_CHECK_CUDA(launch_cluster_classify(c, classify_buffers(ctx), std::min(a->totalClusters, a->caps.maxVisibleClusters),
                                         ctx->numSMs, sched.classifyBlocksPerSM, sched.scanBlocksPerSM, s));
 
+  // The parts classify produced (run 0) come first in the instantiation order
+  // and their offsets depend on nothing the split passes do: they are
+  // instantiated on the side stream while the (latency-bound) split passes
+  // run, the other runs after both.
+  TC_CHECK_CUDA(cudaEventRecord(ctx->evFork, s));
+  TC_CHECK_CUDA(cudaStreamWaitEvent(ctx->side, ctx->evFork, 0));
+  {
+    StageCtx c0 = c;
+    bind_slot(ctx, c0, p.slotInstantiate0, false);
+    c0.fuseSetup = kNoSetup;
+    c0.run       = 0;
+    TC_CHECK_CUDA(launch_triangle_instantiate(c0, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
+                                              sched.scanBlocksPerSM, sched.vertexBlocksPerSM, ctx->side));
+  }
+  TC_CHECK_CUDA(cudaEventRecord(ctx->evJoin, ctx->side));
+
   const u32 passes = split_passes(a->caps.splitFactor);
   const u32 sb     = split_block(sched);
   for(u32 q = 0; q < passes; q++)
@@ -302,13 +326,16 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
         c, sb, persistent_grid(ctx, ceil_div(a->caps.maxSplitTriangles, split_items_per_tile(sb)), bpsm * (512 / sb)), s));
   }
 
+  TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evJoin, 0));
   bind_slot(ctx, c, p.slotInstantiate, false);
   c.fuseSetup = TC_BUILD_SETUP_BUILD_BLAS;
+  c.run       = kRunsAfterFirst;
   TC_CHECK_CUDA(launch_triangle_instantiate(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
                                             sched.scanBlocksPerSM, sched.vertexBlocksPerSM, s));
 
   bind_slot(ctx, c, p.slotBlas, false);
   c.fuseSetup = kNoSetup;
+  c.run       = kAllRuns;
   TC_CHECK_CUDA(launch_blas_setup_insertion(c, std::max(1u, ceil_div(a->numInstances, kInstanceTile)), kInstanceTile, s));
 
   u32* seg = reinterpret_cast<u32*>(ctx->dScratch + p.segOffset);
@@ -366,12 +393,26 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, desc->device);
   ctx->numSMs   = (u32)std::max(1, sms);
+  if(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess
+     || cudaEventCreateWithFlags(&ctx->evFork, cudaEventDisableTiming) != cudaSuccess
+     || cudaEventCreateWithFlags(&ctx->evJoin, cudaEventDisableTiming) != cudaSuccess)
+  {
+    if(ctx->evFork)
+      cudaEventDestroy(ctx->evFork);
+    if(ctx->side)
+      cudaStreamDestroy(ctx->side);
+    delete ctx;
+    return TC_ERR_CUDA;
+  }
   ctx->schedule = {8, 256, 4, 8, 1, {0, 0, 0}};
   ctx->plan     = make_plan(*desc);
   if(cudaMalloc(&ctx->dScratch, ctx->plan.totalBytes) != cudaSuccess
      || cudaMemset(ctx->dScratch, 0, ctx->plan.totalBytes) != cudaSuccess)
   {
     cudaFree(ctx->dScratch);
+    cudaEventDestroy(ctx->evFork);
+    cudaEventDestroy(ctx->evJoin);
+    cudaStreamDestroy(ctx->side);
     delete ctx;
     return TC_ERR_CUDA;
   }
@@ -395,6 +436,12 @@ tc_status tc_context_destroy(tc_context* ctx)
   cudaFree(ctx->dTemplateSizes);
   cudaFree(ctx->dTable);
   cudaFree(ctx->dScratch);
+  if(ctx->evFork)
+    cudaEventDestroy(ctx->evFork);
+  if(ctx->evJoin)
+    cudaEventDestroy(ctx->evJoin);
+  if(ctx->side)
+    cudaStreamDestroy(ctx->side);
   delete ctx;
   return TC_OK;
 }

@@ -45,17 +45,26 @@ static_assert(kTile == kInstantiateTile, "allocation tile size");
 constexpr u32 kPackShift = 20;
 constexpr u64 kPackMask  = (1ull << kPackShift) - 1;
 
-// parts of this launch: [0, part counter) or one run, narrowed to the instance window
+// parts of this launch: [0, part counter), every run after the first, or one
+// run, narrowed to the instance window. A single run is bounded by the run
+// table alone: the first run's instantiation may run while the split passes
+// still append to the part counter.
 __device__ inline void part_range(const StageCtx& c, u32& lo, u32& hi)
 {
   const tc_TessTriangleInfo* parts = reinterpret_cast<const tc_TessTriangleInfo*>(c.build->partTriangles);
+  const u32                  cap   = c.caps.maxPartTriangles;
   lo                               = 0;
-  hi                               = min(c.build->partTriangleCounter, c.caps.maxPartTriangles);
-  if(c.run != kAllRuns)
+  if(c.run == kAllRuns || c.run == kRunsAfterFirst)
+  {
+    hi = min(c.build->partTriangleCounter, cap);
+    if(c.run == kRunsAfterFirst)
+      lo = min(c.runStarts[1], hi);
+  }
+  else
   {
     const u32 rs = c.runStarts[c.run], re = c.runStarts[c.run + 1];
-    lo           = min(rs, hi);
-    hi           = min(max(re, rs), hi);
+    lo           = min(rs, cap);
+    hi           = min(max(re, rs), cap);
   }
   if(!whole_window(c))
   {

@@ -64,8 +64,9 @@ struct StageCtx
   u32                           run;        // instantiate: part run index or kAllRuns
 };
 
-constexpr u32 kNoSetup  = 0xFFFFFFFFu;
-constexpr u32 kAllRuns  = 0xFFFFFFFFu;
+constexpr u32 kNoSetup        = 0xFFFFFFFFu;
+constexpr u32 kAllRuns        = 0xFFFFFFFFu;
+constexpr u32 kRunsAfterFirst = 0xFFFFFFFEu;  // instantiate: every run but the first (the split passes' parts)
 constexpr u32 kMaxRuns  = 16;
 
 __device__ __forceinline__ u32 clamp_split_factor(u32 sf) { return max(2u, min(sf, TC_TESSTABLE_SIZE)); }
