@@ -58,6 +58,21 @@ def parse_args():
     return p.parse_args()
 
 
+def replica_totals(seconds: float, tris: float, device):
+    """Whole-job figures of N independent replicas (the path does not shard:
+    every rank builds its own frames): the slowest rank's time and the sum of
+    all ranks' tessellated triangles. Only these two numbers are exchanged."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return seconds, tris
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    n = torch.tensor([tris], dtype=torch.float64, device=device)
+    dist.all_reduce(n)
+    return float(t.item()), float(n.item())
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -317,12 +332,7 @@ def run_ours(args):
         torch.distributed.barrier()
     t_total = sum(times) / 1e3
     tris_total = float(sum(tris))
-    if world > 1:
-        tt = torch.tensor([t_total], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        nt = torch.tensor([tris_total], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(nt)
-        t_total, tris_total = float(tt.item()), float(nt.item())
+    t_total, tris_total = replica_totals(t_total, tris_total, dev)
     value = tris_total / t_total
     errs = pipe.device_errors()
 
@@ -459,6 +469,7 @@ def terrain_bandwidth(torch, dev, local, peak, tune=True):
                        "camera 10 deg grazing at height 2, 3840x2160, 4 px/segment",
            "tessellated_tris": int(o["readback"]["numTotalTriangles"]),
            "part_triangles": int(o["readback"]["numPartTriangles"]),
+           "classify_part_triangles": M.classify_parts_written(o),
            "split_triangles": int(o["readback"]["numSplitTriangles"]),
            "generated_vertices": int(o["readback"]["numGenVertices"]),
            "stages_ms": means, "instantiate_algorithmic_bytes": alg, "instantiate_gbs": gbs,
