@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(256) k_generate_vertices(StageCtx c)
         {
           const u32 vi = cl.firstLocalVertex + lt[tri * 3 + k];
           bp[k]        = ldg3(reinterpret_cast<const float*>(in.positions), vi);
-          bn[k]        = normalize3(ldg3(reinterpret_cast<const float*>(in.normals), vi));
+          bn[k]        = ldg3(reinterpret_cast<const float*>(in.normals), vi);
           bt[k]        = ldg2(reinterpret_cast<const float*>(in.texcoords), vi);
         }
         write_part_affine(r, pi.subTriangle.vtxEncoded, cfg_flipped(cfg), bp, bn, bt, e.firstVertex, tx,

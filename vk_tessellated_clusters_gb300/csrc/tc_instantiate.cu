@@ -35,7 +35,7 @@ constexpr u32 kBlock        = 256;
 constexpr u32 kItems        = 4;
 constexpr u32 kTile         = kBlock * kItems;
 constexpr u32 kWarps        = kBlock / 32;
-constexpr u32 kPartsPerWarp = 16;  // parts staged per warp and chunk (shared memory budget)
+constexpr u32 kPartsPerWarp = 32;  // parts staged per warp and chunk: one per lane
 constexpr u32 kScanBlock    = 1024;
 
 static_assert(kTile == kInstantiateTile, "allocation tile size");
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_vertices(Stag
       {
         const u32 vi = cl.firstLocalVertex + lt[tri * 3 + v];
         bp[v]        = ldg3(pos, vi);
-        bn[v]        = normalize3(ldg3(nrm, vi));  // :329
+        bn[v]        = ldg3(nrm, vi);  // normalised in write_part_affine (:329)
         bt[v]        = ldg2(uvs, vi);
       }
       tc_DisplacementTexture tx = {};

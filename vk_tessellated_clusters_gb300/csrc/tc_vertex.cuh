@@ -64,13 +64,21 @@ __device__ __forceinline__ f2 bary2(f3 c, f2 v0, f2 v1, f2 v2)
   return {__fmaf_rn(c.z, v2.x, __fmaf_rn(c.y, v1.x, c.x * v0.x)), __fmaf_rn(c.z, v2.y, __fmaf_rn(c.y, v1.y, c.x * v0.y))};
 }
 
+// normalize(v) as v * rsqrt(dot(v, v)) (hardware reciprocal square root)
+__device__ __forceinline__ f3 normalize_fast(f3 v)
+{
+  const float k = rsqrtf(__fmaf_rn(v.z, v.z, __fmaf_rn(v.y, v.y, v.x * v.x)));
+  return {v.x * k, v.y * k, v.z * k};
+}
+
 // Per-part set-up, written straight into `r` (normally shared memory) word by
 // word. `corner` are the sub-triangle's encoded corners
-// (TessTriangleInfo.vtxEncoded), p / nh / uv the base triangle's positions,
-// normalised normals and uvs; `scale` / `offset` the combined displacement
-// scale (instance x view) and offset (instance + view).
+// (TessTriangleInfo.vtxEncoded), p / n / uv the base triangle's positions,
+// normals (normalised here, triangle_tess_template_instantiate.comp.glsl:329)
+// and uvs; `scale` / `offset` the combined displacement scale (instance x
+// view) and offset (instance + view).
 __device__ __forceinline__ void write_part_affine(PartAffine& r, const u32 corner[3], bool flipped, const f3 p[3],
-                                                  const f3 nh[3], const f2 uv[3], u32 firstVertex,
+                                                  const f3 n[3], const f2 uv[3], u32 firstVertex,
                                                   const tc_DisplacementTexture& tx, float scale, float offset)
 {
   f3 c0 = decode_bary(corner[0]), c1 = decode_bary(corner[1]), c2 = decode_bary(corner[2]);
@@ -101,7 +109,8 @@ __device__ __forceinline__ void write_part_affine(PartAffine& r, const u32 corne
   }
   if(w == 0)
     return;
-  const f3 N0 = bary3(c0, nh[0], nh[1], nh[2]);
+  const f3 nh[3] = {normalize_fast(n[0]), normalize_fast(n[1]), normalize_fast(n[2])};
+  const f3 N0    = bary3(c0, nh[0], nh[1], nh[2]);
   r.q[2]      = make_float4(r.q[2].x, N0.x, N0.y, N0.z);
   const f3 F1 = sub3(bary3(c1, nh[0], nh[1], nh[2]), N0);
   const f3 F2 = sub3(bary3(c2, nh[0], nh[1], nh[2]), N0);
