@@ -269,6 +269,13 @@ u32 frame_begin_grid(const tc_context* ctx, const tc_frame_args* a)
   return std::max(1u, std::min(ctx->numSMs * 2, ceil_div((u64)a->caps.maxSplitTriangles * 6, 256)));
 }
 
+// blas_clusters_insert: two instantiations per thread (the lookups per
+// element are dependent loads; many resident warps hide them)
+u32 insert_grid(const tc_context* ctx, const tc_frame_args* a)
+{
+  return std::max(ctx->numSMs * 4, std::min(ceil_div(a->caps.maxGeneratedClusters, 512), 1u << 16));
+}
+
 u32 split_block(const tc_schedule& s)
 {
   u32 b = s.splitBlockSize;
@@ -339,7 +346,7 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   TC_CHECK_CUDA(launch_blas_setup_insertion(c, std::max(1u, ceil_div(a->numInstances, kInstanceTile)), kInstanceTile, s));
 
   u32* seg = reinterpret_cast<u32*>(ctx->dScratch + p.segOffset);
-  TC_CHECK_CUDA(launch_blas_clusters_insert(c, seg, seg + (size_t)p.segStride * p.segRows, p.segStride, ctx->numSMs * 4, s));
+  TC_CHECK_CUDA(launch_blas_clusters_insert(c, seg, seg + (size_t)p.segStride * p.segRows, p.segStride, insert_grid(ctx, a), s));
 
   ctx->launches += kFrameFixedLaunches + passes;
   return TC_OK;
@@ -787,7 +794,7 @@ tc_status tc_blas_clusters_insert(tc_context* ctx, const tc_frame_args* a, void*
   u32*         seg = reinterpret_cast<u32*>(ctx->dScratch + p.segOffset);
   TC_CHECK_CUDA(cudaMemsetAsync(seg, 0, (size_t)p.segStride * p.segRows * 4 * 2, s));
   StageCtx c = base_ctx(ctx, a);
-  TC_CHECK_CUDA(launch_blas_clusters_insert(c, seg, seg + (size_t)p.segStride * p.segRows, p.segStride, ctx->numSMs * 4, s));
+  TC_CHECK_CUDA(launch_blas_clusters_insert(c, seg, seg + (size_t)p.segStride * p.segRows, p.segStride, insert_grid(ctx, a), s));
   ctx->launches += 2;
   return TC_OK;
 }

@@ -13,10 +13,9 @@
 //
 // Gradients scattered: dL/dp, dL/dn (per base vertex) and dL/dtexel (the four
 // bilinear taps). Full clusters: one warp per instantiation, one lane per
-// vertex, direct atomics. Part triangles: 16 per warp; the warp walks their
-// concatenated vertices, sums per (part, base vertex) in shared memory and
-// adds them to the base vertex with one atomic per component; texel taps use
-// global atomics.
+// vertex, direct atomics. Part triangles: one lane per instantiation; it sums
+// the per-base-vertex terms of its vertices in registers and adds them with
+// one atomic per component; texel taps use global atomics.
 #include "tc_kernels.h"
 #include "tc_stage.cuh"
 #include "tc_vertex.cuh"
@@ -41,115 +40,7 @@ __device__ __forceinline__ void atomic_add3(float* base, u64 index, f3 v)
   atomicAdd(base + 3 * index + 2, v.z);
 }
 
-// ---------------------------------------------------------------------------
-// part instantiations are processed in chunks of 16 per warp: their vertices
-// are contiguous, so the warp walks the flattened vertex range with all lanes
-// busy (a part has ~4-80 vertices), the per-part data staged in shared memory
-// ---------------------------------------------------------------------------
-
-constexpr u32 kWarps      = 8;
-constexpr u32 kChunkParts = 16;
-
-struct PartRec
-{
-  f3                     bb[3];
-  f3                     nh[3];  // normalised base normals
-  f2                     uv[3];
-  float                  nl[3];  // base normal lengths
-  u32                    vi[3];
-  u32                    firstVertex, cfg, inst;
-  u32                    vbase;  // first generated vertex
-  float                  iscale, ioffset;
-  float*                 gtex;   // texel gradient of the instance's map (or null)
-  tc_DisplacementTexture tx;     // width == 0: no displacement
-};
-
-struct ChunkSmem
-{
-  PartRec rec[kWarps][kChunkParts];
-  u32     vpre[kWarps][kChunkParts + 1];
-  float   acc[kWarps][kChunkParts][3][6];  // per part and base vertex: dP xyz, d(normalised normal) xyz
-};
-
-// Loads the warp's chunk [first, first + 16) of part instantiations into
-// shared memory; returns the chunk's vertex count.
-__device__ __forceinline__ u32 load_chunk(const StageCtx& c, float* const* gradTexels, u32 first, u32 end, PartRec* rec,
-                                          u32* vpre)
-{
-  const u32                         lane  = threadIdx.x & 31;
-  const tc_SceneBuilding*           b     = c.build;
-  const tc_TemplateInstantiateInfo* ti    = reinterpret_cast<const tc_TemplateInstantiateInfo*>(b->tempInstantiations);
-  const tc_TessTriangleInfo*        parts = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
-  const u32                         j     = first + lane;
-  u32                               nv    = 0;
-  if(lane < kChunkParts && j < end)
-  {
-    const tc_TemplateInstantiateInfo info = ti[j];
-    const tc_TessTriangleInfo pi  = parts[info.clusterIdOffset & 0x3FFFFFFFu];
-    const u32                 cfg = pi.subTriangle.triangleID_config >> 16;
-    const u32                 tri = pi.subTriangle.triangleID_config & 0xFFFFu;
-    const tc_RenderInstance&  in  = c.instances[pi.cluster.instanceID];
-    const tc_Cluster          cl  = reinterpret_cast<const tc_Cluster*>(in.clusters)[pi.cluster.clusterID];
-    const uint8_t*            lt  = reinterpret_cast<const uint8_t*>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
-    const tc_TessTableEntry   e   = table_entry(c.table, cfg);
-    PartRec&                  r   = rec[lane];
-#pragma unroll
-    for(int k = 0; k < 3; k++)
-    {
-      const u32 vi = cl.firstLocalVertex + lt[tri * 3 + k];
-      const f3  n  = ldg3(reinterpret_cast<const float*>(in.normals), vi);
-      r.vi[k]      = vi;
-      r.bb[k]      = decode_bary(pi.subTriangle.vtxEncoded[k]);
-      r.nl[k]      = len3(n);
-      r.nh[k]      = normalize3(n);
-      r.uv[k]      = ldg2(reinterpret_cast<const float*>(in.texcoords), vi);
-    }
-    r.firstVertex = e.firstVertex;
-    r.cfg         = cfg;
-    r.inst        = pi.cluster.instanceID;
-    r.vbase       = (u32)((info.vertexBufferAddress - b->genVertices) / 12);
-    r.iscale      = in.displacementScale;
-    r.ioffset     = in.displacementOffset;
-    r.tx          = {};
-    r.gtex        = nullptr;
-    if(c.numTextures > 0 && c.textures != nullptr && in.displacementIndex >= 0
-       && (u32)in.displacementIndex < c.numTextures)
-    {
-      r.tx   = c.textures[in.displacementIndex];
-      r.gtex = r.tx.width ? gradTexels[in.displacementIndex] : nullptr;
-    }
-    nv = e.numVertices;
-  }
-  u32 x = nv;
-#pragma unroll
-  for(int d = 1; d < 32; d <<= 1)
-  {
-    u32 y = __shfl_up_sync(0xFFFFFFFFu, x, d);
-    if(lane >= (u32)d)
-      x += y;
-  }
-  if(lane < kChunkParts)
-    vpre[lane + 1] = x;
-  if(lane == 0)
-    vpre[0] = 0;
-  __syncwarp();
-  return __shfl_sync(0xFFFFFFFFu, x, kChunkParts - 1);
-}
-
-__device__ __forceinline__ u32 chunk_part_of(const u32* vpre, u32 t)
-{
-  u32 lo = 0, hi = kChunkParts;
-#pragma unroll
-  for(int s = 0; s < 4; s++)
-  {
-    const u32 mid = (lo + hi) >> 1;
-    if(vpre[mid] <= t)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  return lo;
-}
+constexpr u32 kWarps = 8;
 
 // number of leading full-cluster instantiations (they precede all parts)
 __device__ __forceinline__ u32 full_count(const StageCtx& c, u32 temps)
@@ -157,13 +48,12 @@ __device__ __forceinline__ u32 full_count(const StageCtx& c, u32 temps)
   return min(c.runStarts[kMaxRuns + 1], temps);
 }
 
-__global__ void __launch_bounds__(kWarps * 32) k_instantiate_backward(StageCtx c, const float* gradVertices,
+__global__ void __launch_bounds__(kWarps * 32, 2) k_instantiate_backward(StageCtx c, const float* gradVertices,
                                                                       const tc_GradTargets* targets,
                                                                       float* const* gradTexels)
 {
   stage_prologue();
-  __shared__ ChunkSmem sm;
-  const u32         lane  = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const u32         lane  = threadIdx.x & 31;
   const u32         gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const u32         nwarp = (gridDim.x * blockDim.x) >> 5;
   tc_SceneBuilding* b     = c.build;
@@ -216,85 +106,93 @@ __global__ void __launch_bounds__(kWarps * 32) k_instantiate_backward(StageCtx c
     }
   }
 
-  // part triangles (triangle_tess_template_instantiate.comp.glsl:343-371), 16 per warp
-  PartRec* rec  = sm.rec[warp];
-  u32*     vpre = sm.vpre[warp];
-  float(*acc)[3][6] = sm.acc[warp];
-  const u32 nparts  = temps - nfull;
-  for(u32 chunk = gwarp; chunk * kChunkParts < nparts; chunk += nwarp)
+  // part triangles (triangle_tess_template_instantiate.comp.glsl:343-371): one
+  // lane per part instantiation walks its vertices (3-78) and sums the
+  // per-base-vertex terms in registers; one atomic per component and base
+  // vertex at the end, no shared-memory traffic
+  const tc_TessTriangleInfo* parts = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
+  const u32                  gtid  = blockIdx.x * blockDim.x + threadIdx.x;
+  const u32                  nthr  = gridDim.x * blockDim.x;
+  for(u32 j = nfull + gtid; j < temps; j += nthr)
   {
-    const u32 first = nfull + chunk * kChunkParts;
-    const u32 total = load_chunk(c, gradTexels, first, temps, rec, vpre);
-    for(u32 t = lane; t < kChunkParts * 3 * 6; t += 32)
-      (&acc[0][0][0])[t] = 0.0f;
-    __syncwarp();
-    for(u32 t = lane; t < total; t += 32)
+    const tc_TemplateInstantiateInfo info = ti[j];
+    const u64                 vbase = (info.vertexBufferAddress - b->genVertices) / 12;
+    const tc_TessTriangleInfo pi    = parts[info.clusterIdOffset & 0x3FFFFFFFu];
+    const u32                 cfg   = pi.subTriangle.triangleID_config >> 16;
+    const u32                 tri   = pi.subTriangle.triangleID_config & 0xFFFFu;
+    const tc_RenderInstance&  in    = c.instances[pi.cluster.instanceID];
+    const tc_Cluster          cl    = reinterpret_cast<const tc_Cluster*>(in.clusters)[pi.cluster.clusterID];
+    const uint8_t*            lt    = reinterpret_cast<const uint8_t*>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
+    const tc_TessTableEntry   e     = table_entry(c.table, cfg);
+    const tc_GradTargets      gt    = targets[pi.cluster.instanceID];
+    tc_DisplacementTexture    tx    = {};
+    if(haveTextures && in.displacementIndex >= 0 && (u32)in.displacementIndex < c.numTextures)
+      tx = c.textures[in.displacementIndex];
+    float* const gtex = tx.width ? gradTexels[in.displacementIndex] : nullptr;
+    const float  s    = in.displacementScale * viewScale;
+    u32          vi[3];
+    f3           bb[3], nh[3];
+    f2           uvb[3];
+    float        nl[3];
+#pragma unroll
+    for(int k = 0; k < 3; k++)
     {
-      const u32      pi = chunk_part_of(vpre, t);
-      const PartRec& r  = rec[pi];
-      const u32      v  = t - vpre[pi];
-      f3             w  = decode_bary(__ldg(c.table.vertices + r.firstVertex + v));
-      if(cfg_flipped(r.cfg))
+      vi[k]      = cl.firstLocalVertex + lt[tri * 3 + k];
+      bb[k]      = decode_bary(pi.subTriangle.vtxEncoded[k]);
+      const f3 n = ldg3(reinterpret_cast<const float*>(in.normals), vi[k]);
+      nl[k]      = len3(n);
+      nh[k]      = normalize3(n);
+      uvb[k]     = ldg2(reinterpret_cast<const float*>(in.texcoords), vi[k]);
+    }
+    f3 dP[3]  = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    f3 dNh[3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for(u32 v = 0; v < e.numVertices; v++)
+    {
+      f3 w = decode_bary(__ldg(c.table.vertices + e.firstVertex + v));
+      if(cfg_flipped(cfg))
       {
         const float x = w.x;
         w.x           = w.y;
         w.y           = x;
       }
-      w                 = interp3(r.bb[0], r.bb[1], r.bb[2], w);
-      const f3    g     = ldg3(gradVertices, (u64)r.vbase + v);
+      w                 = interp3(bb[0], bb[1], bb[2], w);
+      const f3    g     = ldg3(gradVertices, vbase + v);
       const float wk[3] = {w.x, w.y, w.z};
 #pragma unroll
       for(int k = 0; k < 3; k++)
-      {
-        atomicAdd(&acc[pi][k][0], wk[k] * g.x);
-        atomicAdd(&acc[pi][k][1], wk[k] * g.y);
-        atomicAdd(&acc[pi][k][2], wk[k] * g.z);
-      }
-      if(r.tx.width == 0)
+        dP[k] = {dP[k].x + wk[k] * g.x, dP[k].y + wk[k] * g.y, dP[k].z + wk[k] * g.z};
+      if(tx.width == 0)
         continue;
-      const f3    N    = interp3(r.nh[0], r.nh[1], r.nh[2], w);
-      const f2    uv   = interp2(r.uv[0], r.uv[1], r.uv[2], w);
+      const f3    N    = interp3(nh[0], nh[1], nh[2], w);
+      const f2    uv   = interp2(uvb[0], uvb[1], uvb[2], w);
       const float Nl   = len3(N);
       const f3    m    = normalize3(N);
-      const float hraw = sample_bilinear(r.tx, uv);
-      const float h    = ((hraw * r.iscale) * viewScale + r.ioffset) + viewOffset;
+      const float hraw = sample_bilinear(tx, uv);
+      const float h    = ((hraw * in.displacementScale) * viewScale + in.displacementOffset) + viewOffset;
       const float dh   = dot3(m, g);
       // d normalize(N) / dN = (I - m m^T) / |N|
       const float kN = h / Nl;
       const f3    gN = {kN * (g.x - m.x * dh), kN * (g.y - m.y * dh), kN * (g.z - m.z * dh)};
 #pragma unroll
       for(int k = 0; k < 3; k++)
-      {
-        atomicAdd(&acc[pi][k][3], wk[k] * gN.x);
-        atomicAdd(&acc[pi][k][4], wk[k] * gN.y);
-        atomicAdd(&acc[pi][k][5], wk[k] * gN.z);
-      }
-      if(r.gtex)
-        scatter_texels(r.gtex, r.tx, bilinear_taps(r.tx, uv), dh * (r.iscale * viewScale));
+        dNh[k] = {dNh[k].x + wk[k] * gN.x, dNh[k].y + wk[k] * gN.y, dNh[k].z + wk[k] * gN.z};
+      if(gtex)
+        scatter_texels(gtex, tx, bilinear_taps(tx, uv), dh * s);
     }
-    __syncwarp();
-    // one lane per (part, base vertex): the chunk's sums go out with 6 atomics
-    const u32 nchunk = min(kChunkParts, temps - first);
-    for(u32 t = lane; t < nchunk * 3; t += 32)
+#pragma unroll
+    for(int k = 0; k < 3; k++)
     {
-      const u32            pi = t / 3, k = t % 3;
-      const PartRec&       r  = rec[pi];
-      const tc_GradTargets gt = targets[r.inst];
-      const f3             dp = {acc[pi][k][0], acc[pi][k][1], acc[pi][k][2]};
       if(gt.dPositions)
-        atomic_add3(reinterpret_cast<float*>(gt.dPositions), r.vi[k], dp);
-      if(r.tx.width && gt.dNormals)
+        atomic_add3(reinterpret_cast<float*>(gt.dPositions), vi[k], dP[k]);
+      if(tx.width && gt.dNormals)
       {
         // d normalize(n_k) / dn_k = (I - nh nh^T) / |n_k|
-        const f3    dnh = {acc[pi][k][3], acc[pi][k][4], acc[pi][k][5]};
-        const f3    nh  = r.nh[k];
-        const float d   = dot3(nh, dnh);
-        const float rr  = 1.0f / r.nl[k];
-        const f3    dn  = {rr * (dnh.x - nh.x * d), rr * (dnh.y - nh.y * d), rr * (dnh.z - nh.z * d)};
-        atomic_add3(reinterpret_cast<float*>(gt.dNormals), r.vi[k], dn);
+        const float d  = dot3(nh[k], dNh[k]);
+        const float rr = 1.0f / nl[k];
+        const f3    dn = {rr * (dNh[k].x - nh[k].x * d), rr * (dNh[k].y - nh[k].y * d), rr * (dNh[k].z - nh[k].z * d)};
+        atomic_add3(reinterpret_cast<float*>(gt.dNormals), vi[k], dn);
       }
     }
-    __syncwarp();
   }
 }
 

@@ -126,6 +126,7 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_count(StageCtx c, C
 {
   stage_prologue();
   __shared__ f3  s_vert[8][TC_MAX_CLUSTER_VERTICES];
+  __shared__ f2  s_dist[8][TC_MAX_CLUSTER_VERTICES];  // per vertex: distance to the view position, its reciprocal
   __shared__ u32 s_range[2];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if(threadIdx.x == 0)
@@ -137,6 +138,7 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_count(StageCtx c, C
   const tc_SceneBuilding* b       = c.build;
   const tc_ClusterInfo*   vis     = reinterpret_cast<const tc_ClusterInfo*>(b->visibleClusters);
   const FactorParams      fp      = factor_params(c);
+  const float             rNear   = __fdiv_rn(1.0f, fp.nearPlane);
   const bool              culling = (c.flags & TC_FLAG_CULLING) != 0;
   const u32               sf      = clamp_split_factor(c.caps.splitFactor);
   const u32               nwarps  = (gridDim.x * blockDim.x) >> 5;
@@ -169,23 +171,32 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_count(StageCtx c, C
       for(int j = 0; j < 16; j++)
         m[j] = __ldg(in->worldMatrix.m + j);
       for(u32 i = lane; i < nv; i += 32)
-        s_vert[warp][i] = xform_point(m, ldg3(pos, cl.firstLocalVertex + i));
+      {
+        const f3    w = xform_point(m, ldg3(pos, cl.firstLocalVertex + i));
+        const float d = dist3(w, fp.viewPos);
+        s_vert[warp][i] = w;
+        s_dist[warp][i] = {d, __fdiv_rn(1.0f, d)};
+      }
       __syncwarp();
       // indices are masked to the staged range: a malformed index reads a wrong
       // vertex of the same cluster, never outside shared memory
       const uint8_t* lt = reinterpret_cast<const uint8_t*>(in->clusterLocalTriangles) + cl.firstLocalTriangle;
       if(lane < nt)
       {
-        const uint3 f = tess_factors(s_vert[warp][lt[lane * 3 + 0] & 63u], s_vert[warp][lt[lane * 3 + 1] & 63u],
-                                     s_vert[warp][lt[lane * 3 + 2] & 63u], fp);
+        const u32   i0 = lt[lane * 3 + 0] & 63u, i1 = lt[lane * 3 + 1] & 63u, i2 = lt[lane * 3 + 2] & 63u;
+        const f2    d0 = s_dist[warp][i0], d1 = s_dist[warp][i1], d2 = s_dist[warp][i2];
+        const uint3 f  = tess_factors_hoisted(s_vert[warp][i0], s_vert[warp][i1], s_vert[warp][i2], d0.x, d1.x, d2.x,
+                                              d0.y, d1.y, d2.y, rNear, fp);
         m0 = max(max(f.x, f.y), f.z);
         w0 = classify_triangle(f, sf);
       }
       if(lane + 32 < nt)
       {
         const u32   t = lane + 32;
-        const uint3 f = tess_factors(s_vert[warp][lt[t * 3 + 0] & 63u], s_vert[warp][lt[t * 3 + 1] & 63u],
-                                     s_vert[warp][lt[t * 3 + 2] & 63u], fp);
+        const u32   i0 = lt[t * 3 + 0] & 63u, i1 = lt[t * 3 + 1] & 63u, i2 = lt[t * 3 + 2] & 63u;
+        const f2    d0 = s_dist[warp][i0], d1 = s_dist[warp][i1], d2 = s_dist[warp][i2];
+        const uint3 f  = tess_factors_hoisted(s_vert[warp][i0], s_vert[warp][i1], s_vert[warp][i2], d0.x, d1.x, d2.x,
+                                              d0.y, d1.y, d2.y, rNear, fp);
         m1 = max(max(f.x, f.y), f.z);
         w1 = classify_triangle(f, sf);
       }

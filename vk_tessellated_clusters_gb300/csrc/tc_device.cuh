@@ -139,6 +139,31 @@ __device__ __forceinline__ uint3 tess_factors(f3 a, f3 b, f3 c, const FactorPara
   return f;
 }
 
+// tess_factors with the per-vertex work hoisted: d_k = |p_k - viewPos| and
+// r_k = 1 / d_k (IEEE division) computed once per vertex, rNear = 1 / nearPlane.
+// Division is monotonic, so 1 / max(near, min(d_a, d_b)) is exactly the
+// reciprocal of whichever of near, d_a, d_b the max/min selects: the same bits
+// as tess_factors.
+__device__ __forceinline__ float rcp_of_clamped_min(float da, float db, float ra, float rb, float nearPlane, float rNear)
+{
+  const float m  = fminf(da, db);
+  const float rm = da <= db ? ra : rb;
+  return nearPlane > m ? rNear : rm;
+}
+
+__device__ __forceinline__ uint3 tess_factors_hoisted(f3 a, f3 b, f3 c, float da, float db, float dc, float ra, float rb,
+                                                      float rc, float rNear, const FactorParams& fp)
+{
+  const float sx = rcp_of_clamped_min(da, db, ra, rb, fp.nearPlane, rNear);
+  const float sy = rcp_of_clamped_min(db, dc, rb, rc, fp.nearPlane, rNear);
+  const float sz = rcp_of_clamped_min(dc, da, rc, ra, fp.nearPlane, rNear);
+  uint3       f;
+  f.x = round_clamp_factor(dist3(a, b), sx, fp);
+  f.y = round_clamp_factor(dist3(b, c), sy, fp);
+  f.z = round_clamp_factor(dist3(c, a), sz, fp);
+  return f;
+}
+
 // tessellation.glsl:101-104
 __device__ __forceinline__ u32 split_factor1(u32 f, u32 sf) { return min((f + TC_TESSTABLE_SIZE - 1) / TC_TESSTABLE_SIZE, sf); }
 
