@@ -531,11 +531,29 @@ def backward_forward(torch, dev, local, reps=10):
                 ts.append(e0.elapsed_time(e1))
         return statistics.median(ts)
 
+    def timed_back_to_back(fn, n=20):
+        """Device time per call with `n` calls enqueued back to back (the host
+        runs ahead, so launch latency is hidden as in a training loop)."""
+        ts = []
+        for i in range(reps // 2 + 2):
+            flush_buf.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(n):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            if i >= 2:
+                ts.append(e0.elapsed_time(e1) / n)
+        return statistics.median(ts)
+
     grad_v = 2 * (frozen.generate() - target)
     fwd_ms = timed(lambda: pipe.stage("generate_vertices"))
     _, table = frozen.gradient_buffers(dev)
     bwd_kernel_ms = timed(lambda: frozen.launch_backward(grad_v, table))
     bwd_ms = timed(lambda: frozen.scatter_gradients(grad_v))
+    fwd_b2b = timed_back_to_back(lambda: frozen.generate())
+    bwd_b2b = timed_back_to_back(lambda: frozen.scatter_gradients(grad_v))
     frame_ms = timed(lambda: pipe.build("graph"))
     # one autograd step end to end for the record
     v = tessellate(frozen)
@@ -545,6 +563,8 @@ def backward_forward(torch, dev, local, reps=10):
            "vertices": frozen.num_vertices, "forward_ms": fwd_ms, "backward_kernel_ms": bwd_kernel_ms,
            "backward_ms": bwd_ms, "frame_build_ms": frame_ms,
            "backward_kernel_over_forward": bwd_kernel_ms / fwd_ms, "backward_over_forward": bwd_ms / fwd_ms,
+           "forward_autograd_back_to_back_ms": fwd_b2b, "backward_autograd_back_to_back_ms": bwd_b2b,
+           "backward_over_forward_back_to_back": bwd_b2b / fwd_b2b,
            "backward_over_frame_build": bwd_ms / frame_ms,
            "loss": float(loss.item()), "device_errors": pipe.device_errors(),
            "gradient_check": "tests/test_gpu_backward.py: rel. error vs FP64 adjoint <= 1e-4, 64-parameter central differences"}

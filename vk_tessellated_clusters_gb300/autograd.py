@@ -54,8 +54,8 @@ class FrozenFrame:
     def _layout_gradients(self, scene) -> None:
         """All gradients of one backward live in one flat float32 buffer; the
         kernel's pointer tables (per instance dPositions/dNormals, per map
-        texels) are stored once as byte offsets into it and rebased on the
-        device each call, so a backward needs no host-to-device copy."""
+        texels) point into it once and for all, so a backward is a zero fill,
+        the kernel and one copy out, with no host-to-device transfer."""
         torch = self.torch
         sizes = [p.numel() for p in self.positions] + [n.numel() for n in self.normals]
         sizes += [t.numel() if t is not None else 0 for t in self.texels]
@@ -69,9 +69,13 @@ class FrozenFrame:
         tex = np.array([4 * starts[2 * ng + i] if t is not None else -1 for i, t in enumerate(self.texels)] or [-1],
                        np.int64)
         self._num_targets = rel.size
+        # one persistent gradient buffer and its pointer table (built once);
+        # every backward zeroes it, accumulates into it and hands out a copy
+        self._flat = torch.zeros(self._grad_floats, dtype=torch.float32, device=self.pipe.device)
+        base = self._flat.data_ptr()
         table = np.concatenate([rel.reshape(-1), tex])
-        self._rel_table = torch.from_numpy(table).to(self.pipe.device)
-        self._table_valid = self._rel_table >= 0
+        table = np.where(table >= 0, table + base, 0).astype(np.int64)
+        self._table = torch.from_numpy(table).to(self.pipe.device)
 
     def _view(self, buf, shape):
         n = int(np.prod(shape))
@@ -91,13 +95,11 @@ class FrozenFrame:
         self.pipe.stage("generate_vertices")
         return self.pipe.gen_vertices_tensor(self.num_vertices).clone()
 
-    def gradient_buffers(self, device):
-        """A zeroed flat float32 gradient buffer and the kernel's pointer table
-        rebased onto it (both on `device`, enqueued on the current stream)."""
-        torch = self.torch
-        flat = torch.zeros(self._grad_floats, dtype=torch.float32, device=device)
-        table = torch.where(self._table_valid, self._rel_table + flat.data_ptr(), torch.zeros_like(self._rel_table))
-        return flat, table
+    def gradient_buffers(self, device=None):
+        """The persistent flat float32 gradient buffer, zeroed (enqueued on the
+        current stream), and the kernel's pointer table into it."""
+        self._flat.zero_()
+        return self._flat, self._table
 
     def launch_backward(self, grad_vertices, table) -> None:
         """tc_instantiate_backward: accumulates dL/dv into the buffer `table` points at."""
@@ -106,8 +108,9 @@ class FrozenFrame:
     def scatter_gradients(self, grad_vertices):
         """dL/dv -> (dPositions, dNormals, dTexels), lists parallel to the
         parameters; all enqueued on the current stream, no synchronisation."""
-        flat, table = self.gradient_buffers(grad_vertices.device)
+        buf, table = self.gradient_buffers()
         self.launch_backward(grad_vertices.contiguous().float(), table)
+        flat = buf.clone()
         st = self._grad_starts
         ng = len(self.positions)
         views = [flat[st[i]:st[i + 1]] for i in range(len(st) - 1)]
