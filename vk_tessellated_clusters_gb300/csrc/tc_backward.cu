@@ -229,17 +229,18 @@ __global__ void __launch_bounds__(256) k_generate_vertices(StageCtx c)
       tc_DisplacementTexture   tx = {};
       if(haveTextures && in.displacementIndex >= 0 && (u32)in.displacementIndex < c.numTextures)
         tx = c.textures[in.displacementIndex];
-      const u32 nv = min((u32)cl.numVertices, TC_MAX_CLUSTER_VERTICES);
+      // the build's full-cluster vertex function (tc_vertex.cuh): identical bits
+      const MapDesc map    = make_map_desc(tx);
+      const float   scale  = in.displacementScale * vscale;
+      const float   offset = in.displacementOffset + voffset;
+      const u32     nv     = min((u32)cl.numVertices, TC_MAX_CLUSTER_VERTICES);
       for(u32 v = lane; v < nv; v += 32)
       {
         const u32 vi = cl.firstLocalVertex + v;
         f3        p  = ldg3(reinterpret_cast<const float*>(in.positions), vi);
-        if(tx.width != 0)
-        {
-          const float h = sample_bilinear(tx, ldg2(reinterpret_cast<const float*>(in.texcoords), vi));
-          p = displace(p, ldg3(reinterpret_cast<const float*>(in.normals), vi), h, in.displacementScale, vscale,
-                       in.displacementOffset, voffset);
-        }
+        if(map.kind != kAffineFlat)
+          p = full_vertex_k<~0u>(p, ldg3(reinterpret_cast<const float*>(in.normals), vi),
+                                 ldg2(reinterpret_cast<const float*>(in.texcoords), vi), map, scale, offset);
         float* d = gv + (vbase + v) * 3;
         d[0] = p.x, d[1] = p.y, d[2] = p.z;
       }

@@ -18,6 +18,7 @@
 
 #include "tc_kernels.h"
 #include "tc_stage.cuh"
+#include "tc_vertex.cuh"
 
 namespace tc {
 
@@ -417,16 +418,46 @@ __device__ __forceinline__ void emit_triangle(tc_TessTriangleInfo* dst, const tc
 // what the vertex walk of a full cluster needs (phase 2 of k_classify_write)
 struct FullRecord
 {
-  const float*           pos;
-  const float*           nrm;
-  const float*           uvs;
-  u32                    first;  // firstLocalVertex
-  float                  iscale, ioffset;
-  u32                    vo;     // first generated vertex
-  u32                    nv;     // vertex count
-  u32                    _pad;
-  tc_DisplacementTexture tx;
+  MapDesc      map;
+  const float* pos;
+  const float* nrm;
+  const float* uvs;
+  u32          first;  // firstLocalVertex
+  float        scale;  // instance x view displacement scale
+  float        offset; // instance + view displacement offset
+  u32          vo;     // first generated vertex
+  u32          nv;     // vertex count
 };
+
+// the vertex walk over a batch of full clusters (records in `rec`), for
+// records of map kind Kind (~0u: any)
+template <u32 Kind>
+__device__ __forceinline__ void full_steps(const FullRecord* rec, bool owner, u32 rStart, u32 rEnd, float* dst)
+{
+  const u32 lane = threadIdx.x & 31;
+#pragma unroll 2  // two steps in flight: their loads overlap
+  for(u32 base = 0; base < rEnd; base += 32)
+  {
+    const u32 before = __popc(__ballot_sync(0xFFFFFFFFu, owner && rStart <= base));
+    const u32 inside = __reduce_or_sync(0xFFFFFFFFu,
+                                        (owner && rStart > base && rStart < base + 32) ? 1u << (rStart - base) : 0u);
+    const u32 ri     = before - 1 + __popc(inside & ((2u << lane) - 2u));
+    const u32 rs     = __shfl_sync(0xFFFFFFFFu, rStart, ri & 31);
+    const u32 jj     = base + lane;
+    if(jj < rEnd)
+    {
+      const FullRecord& fr = rec[ri];
+      const u32         vi = fr.first + (jj - rs);
+      f3                p  = ldg3(fr.pos, vi);
+      if(Kind != kAffineFlat)
+        p = full_vertex_k<Kind>(p, ldg3(fr.nrm, vi), ldg2(fr.uvs, vi), fr.map, fr.scale, fr.offset);
+      float* d = dst + (u64)jj * 3;
+      d[0]     = p.x;
+      d[1]     = p.y;
+      d[2]     = p.z;
+    }
+  }
+}
 
 template <int MinBlocks>
 __global__ void __launch_bounds__(256, MinBlocks) k_classify_write(StageCtx c, ClassifyScratch cs)
@@ -587,16 +618,17 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_write(StageCtx c, C
           fr.nrm   = reinterpret_cast<const float*>(in->normals);
           fr.uvs   = reinterpret_cast<const float*>(in->texcoords);
           fr.first = cl.firstLocalVertex;
-          fr.tx    = {};
+          tc_DisplacementTexture tx = {};
           if(haveTextures && in->displacementIndex >= 0)
           {
             if((u32)in->displacementIndex < c.numTextures)
-              fr.tx = c.textures[in->displacementIndex];
+              tx = c.textures[in->displacementIndex];
             else
               atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
           }
-          fr.iscale  = in->displacementScale;
-          fr.ioffset = in->displacementOffset;
+          fr.map    = make_map_desc(tx);
+          fr.scale  = in->displacementScale * c.view->displacementScale;
+          fr.offset = in->displacementOffset + c.view->displacementOffset;
         }
       }
     }
@@ -623,31 +655,18 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_write(StageCtx c, C
     const u32 rStart = lane < nrec ? rec[lane].vo - vBase : 0u;
     const u32 rCount = lane < nrec ? rec[lane].nv : 0u;
     const u32 rEnd   = __shfl_sync(0xFFFFFFFFu, rStart + rCount, nrec - 1);
-    const bool  owner  = lane < nrec;
-    const float vscale = c.view->displacementScale, voffset = c.view->displacementOffset;
-    for(u32 base = 0; base < rEnd; base += 32)
+    const bool owner = lane < nrec;
+    // one specialisation when the batch's clusters share a map kind
+    const u32 kind  = owner ? rec[lane].map.kind : 0u;
+    const u32 kind0 = rec[0].map.kind;
+    const u32 kw    = __all_sync(0xFFFFFFFFu, !owner || kind == kind0) ? kind0 : ~0u;
+    float*    dst   = gv + (u64)vBase * 3;
+    switch(kw)
     {
-      const u32 before = __popc(__ballot_sync(0xFFFFFFFFu, owner && rStart <= base));
-      const u32 inside = __reduce_or_sync(0xFFFFFFFFu,
-                                          (owner && rStart > base && rStart < base + 32) ? 1u << (rStart - base) : 0u);
-      const u32 ri     = before - 1 + __popc(inside & ((2u << lane) - 2u));
-      const u32 rs     = __shfl_sync(0xFFFFFFFFu, rStart, ri & 31);
-      const u32 jj     = base + lane;
-      if(jj < rEnd)
-      {
-        const FullRecord& fr = rec[ri];
-        const u32         vi = fr.first + (jj - rs);
-        f3                p  = ldg3(fr.pos, vi);
-        if(fr.tx.width != 0)
-        {
-          const float h = sample_bilinear(fr.tx, ldg2(fr.uvs, vi));
-          p             = displace(p, ldg3(fr.nrm, vi), h, fr.iscale, vscale, fr.ioffset, voffset);
-        }
-        float* dst = gv + ((u64)vBase + jj) * 3;
-        dst[0]     = p.x;
-        dst[1]     = p.y;
-        dst[2]     = p.z;
-      }
+      case affine_kind(TC_TEXEL_F32, true): full_steps<affine_kind(TC_TEXEL_F32, true)>(rec, owner, rStart, rEnd, dst); break;
+      case affine_kind(TC_TEXEL_F16, true): full_steps<affine_kind(TC_TEXEL_F16, true)>(rec, owner, rStart, rEnd, dst); break;
+      case kAffineFlat: full_steps<kAffineFlat>(rec, owner, rStart, rEnd, dst); break;
+      default: full_steps<~0u>(rec, owner, rStart, rEnd, dst); break;
     }
     __syncwarp();  // records are rewritten by the next batch
   }

@@ -228,6 +228,7 @@ __device__ __forceinline__ void chunk_vertices(const StageCtx& c, const PartAffi
                                                u32 total, float* dst)
 {
   const u32 lane = threadIdx.x & 31;
+  #pragma unroll 2  // two steps in flight: their loads overlap
   for(u32 base = 0; base < total; base += 32)
   {
     // lane's part: those starting at or before the step's first vertex, plus
@@ -567,7 +568,10 @@ cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuff
   if((e = launch_pdl(k_instantiate_args, tileGrid, kBlock, s, c, buf)) != cudaSuccess)
     return e;
   const u32 chunks     = (maxParts + kPartsPerWarp - 1) / kPartsPerWarp;
-  const u32 vertexGrid = std::max(1u, std::min((chunks + kWarps - 1) / kWarps, numSMs * std::max(1u, vertexBlocksPerSM)));
+  // one chunk per warp (blocks retire as they finish, so a concurrent branch's
+  // blocks find room); vertexBlocksPerSM picks the register budget
+  const u32 vertexGrid = std::max(1u, std::min((chunks + kWarps - 1) / kWarps, 1u << 20));
+  (void)numSMs;
   if(vertexBlocksPerSM >= 6)
     return launch_pdl(k_instantiate_vertices<6>, vertexGrid, kBlock, s, c, buf);
   if(vertexBlocksPerSM == 5)

@@ -377,14 +377,17 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
 
 cudaError_t launch_triangle_split(const StageCtx& c, u32 blockSize, u32 grid, cudaStream_t s)
 {
+  // the split passes are the latency-critical branch of the frame: their
+  // blocks take precedence over the concurrent instantiation's
+  const int prio = high_launch_priority();
   switch(blockSize)
   {
     case 128:
-      return launch_pdl(k_triangle_split<16, 128>, grid, 128, s, c);
+      return launch_pdl_prio(k_triangle_split<16, 128>, grid, 128, prio, s, c);
     case 512:
-      return launch_pdl(k_triangle_split<32, 512>, grid, 512, s, c);
+      return launch_pdl_prio(k_triangle_split<32, 512>, grid, 512, prio, s, c);
     default:
-      return launch_pdl(k_triangle_split<32, 256>, grid, 256, s, c);
+      return launch_pdl_prio(k_triangle_split<32, 256>, grid, 256, prio, s, c);
   }
 }
 

@@ -10,19 +10,38 @@ namespace tc {
 // Host side of the programmatic dependent launch (see stage_prologue): a
 // kernel launch on `s` that may overlap the tail of the previous kernel.
 template <typename... Params, typename... Args>
-inline cudaError_t launch_pdl(void (*kernel)(Params...), u32 grid, u32 block, cudaStream_t s, Args... args)
+inline cudaError_t launch_pdl_prio(void (*kernel)(Params...), u32 grid, u32 block, int priority, cudaStream_t s,
+                                   Args... args)
 {
   cudaLaunchConfig_t  cfg = {};
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
+  attr[1].id                                         = cudaLaunchAttributePriority;
+  attr[1].val.priority                               = priority;
   cfg.gridDim                                        = dim3(grid);
   cfg.blockDim                                       = dim3(block);
   cfg.dynamicSmemBytes                               = 0;
   cfg.stream                                         = s;
   cfg.attrs                                          = attr;
-  cfg.numAttrs                                       = 1;
+  cfg.numAttrs                                       = priority != 0 ? 2 : 1;
   return cudaLaunchKernelEx(&cfg, kernel, static_cast<Params>(args)...);
+}
+
+template <typename... Params, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(Params...), u32 grid, u32 block, cudaStream_t s, Args... args)
+{
+  return launch_pdl_prio(kernel, grid, block, 0, s, args...);
+}
+
+// The device's highest launch priority (latency-critical kernels that share
+// the GPU with a concurrent branch of the frame).
+inline int high_launch_priority()
+{
+  int least = 0, greatest = 0;
+  if(cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess)
+    return 0;
+  return greatest;
 }
 
 // Per-launch scratch: look-back tile states, the tile ticket, the "blocks done"

@@ -52,6 +52,31 @@ enum : u32
 
 __host__ __device__ constexpr u32 affine_kind(u32 format, bool pow2) { return kAffineTextured + 2 * format + (pow2 ? 1 : 0); }
 
+// A displacement map as the vertex code reads it: q7 = texels lo, texels hi,
+// width, height (bits); q8 = width, height (floats), width - 1, height - 1
+// (bits; the wrap masks of power-of-two sizes); kind = affine_kind(format, pow2),
+// kAffineFlat without a map, kAffineZeroMap for a map of height 0.
+struct MapDesc
+{
+  float4 q7, q8;
+  u32    kind;
+};
+
+__device__ __forceinline__ MapDesc make_map_desc(const tc_DisplacementTexture& tx)
+{
+  MapDesc   m;
+  const u32 w = tx.width, h = tx.height;
+  m.q7 = w ? make_float4(__uint_as_float((u32)tx.texels), __uint_as_float((u32)(tx.texels >> 32)), __uint_as_float(w),
+                         __uint_as_float(h))
+           : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  m.q8 = make_float4(__uint2float_rn(w), __uint2float_rn(h), __uint_as_float(w - 1), __uint_as_float(h - 1));
+  const bool pow2 = w != 0 && h != 0 && (w & (w - 1)) == 0 && (h & (h - 1)) == 0;
+  // formats other than fp16 / unorm16 read as fp32, as in every other sampling path
+  const u32 fmt = tx.format == TC_TEXEL_F16 || tx.format == TC_TEXEL_UNORM16 ? tx.format : TC_TEXEL_F32;
+  m.kind        = w == 0 ? kAffineFlat : (h == 0 ? kAffineZeroMap : affine_kind(fmt, pow2));
+  return m;
+}
+
 __device__ __forceinline__ f3 fma3(float s, f3 a, f3 b)
 {
   return {__fmaf_rn(s, a.x, b.x), __fmaf_rn(s, a.y, b.y), __fmaf_rn(s, a.z, b.z)};
@@ -88,17 +113,11 @@ __device__ __forceinline__ void write_part_affine(PartAffine& r, const u32 corne
     c0         = c1;
     c1         = t;
   }
-  const u32 w = tx.width;
-  const u32 h    = tx.height;
-  const bool pow2 = w != 0 && h != 0 && (w & (w - 1)) == 0 && (h & (h - 1)) == 0;
-  // formats other than fp16 / unorm16 read as fp32, as in every other sampling path
-  const u32 fmt  = tx.format == TC_TEXEL_F16 || tx.format == TC_TEXEL_UNORM16 ? tx.format : TC_TEXEL_F32;
-  const u32 kind = w == 0 ? kAffineFlat : (h == 0 ? kAffineZeroMap : affine_kind(fmt, pow2));
-  r.q[6]          = make_float4(scale, offset, __uint_as_float(firstVertex), __uint_as_float(kind));
-  r.q[7]      = w ? make_float4(__uint_as_float((u32)tx.texels), __uint_as_float((u32)(tx.texels >> 32)),
-                                __uint_as_float(w), __uint_as_float(tx.height))
-                  : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  r.q[8]      = make_float4(__uint2float_rn(w), __uint2float_rn(h), __uint_as_float(w - 1), __uint_as_float(h - 1));
+  const u32     w = tx.width;
+  const MapDesc m = make_map_desc(tx);
+  r.q[6]          = make_float4(scale, offset, __uint_as_float(firstVertex), __uint_as_float(m.kind));
+  r.q[7]          = m.q7;
+  r.q[8]          = m.q8;
   {
     const f3 P0 = bary3(c0, p[0], p[1], p[2]);
     const f3 E1 = sub3(bary3(c1, p[0], p[1], p[2]), P0);
@@ -159,6 +178,36 @@ __device__ __forceinline__ float affine_sample(float4 q7, float4 q8, float u, fl
 
 __device__ __forceinline__ u32 affine_kind_of(const PartAffine& r) { return __float_as_uint(r.q[6].w); }
 
+// bilinear sample of a textured kind (0 for kAffineZeroMap)
+__device__ __forceinline__ float sample_kind(u32 kind, float4 q7, float4 q8, float u, float v)
+{
+  switch(kind)
+  {
+    case affine_kind(TC_TEXEL_F32, true): return affine_sample<TC_TEXEL_F32, true>(q7, q8, u, v);
+    case affine_kind(TC_TEXEL_F32, false): return affine_sample<TC_TEXEL_F32, false>(q7, q8, u, v);
+    case affine_kind(TC_TEXEL_F16, true): return affine_sample<TC_TEXEL_F16, true>(q7, q8, u, v);
+    case affine_kind(TC_TEXEL_F16, false): return affine_sample<TC_TEXEL_F16, false>(q7, q8, u, v);
+    case affine_kind(TC_TEXEL_UNORM16, true): return affine_sample<TC_TEXEL_UNORM16, true>(q7, q8, u, v);
+    case affine_kind(TC_TEXEL_UNORM16, false): return affine_sample<TC_TEXEL_UNORM16, false>(q7, q8, u, v);
+    default: return 0.0f;
+  }
+}
+
+// Displaced vertex of a full cluster (cluster_classify.comp.glsl:457-482):
+// p + normalize(n) * (bilinear(uv) * scale + offset), sampled and
+// renormalised like the part vertices (Kind ~0u: resolved at run time).
+template <u32 Kind>
+__device__ __forceinline__ f3 full_vertex_k(f3 p, f3 n, f2 uv, const MapDesc& m, float scale, float offset)
+{
+  const u32 kind = Kind == ~0u ? m.kind : Kind;
+  if(kind == kAffineFlat)
+    return p;
+  const float hraw   = sample_kind(kind, m.q7, m.q8, uv.x, uv.y);
+  const float height = __fmaf_rn(hraw, scale, offset);
+  const float k      = height * rsqrtf(__fmaf_rn(n.z, n.z, __fmaf_rn(n.y, n.y, n.x * n.x)));
+  return fma3(k, n, p);
+}
+
 // Vertex `tableVertex` (an encoded table barycentric) of the part in `r`, for
 // a record of kind Kind (~0u: any kind, resolved at run time).
 template <u32 Kind>
@@ -177,19 +226,7 @@ __device__ __forceinline__ f3 affine_vertex_k(const PartAffine& r, u32 tableVert
                      __fmaf_rn(b, q4.y, __fmaf_rn(a, q3.z, q2.w))};
   const float  u  = __fmaf_rn(b, q5.z, __fmaf_rn(a, q5.x, q4.z));
   const float  v  = __fmaf_rn(b, q5.w, __fmaf_rn(a, q5.y, q4.w));
-  float        hraw = 0.0f;
-  switch(kind)
-  {
-    case affine_kind(TC_TEXEL_F32, true): hraw = affine_sample<TC_TEXEL_F32, true>(r.q[7], r.q[8], u, v); break;
-    case affine_kind(TC_TEXEL_F32, false): hraw = affine_sample<TC_TEXEL_F32, false>(r.q[7], r.q[8], u, v); break;
-    case affine_kind(TC_TEXEL_F16, true): hraw = affine_sample<TC_TEXEL_F16, true>(r.q[7], r.q[8], u, v); break;
-    case affine_kind(TC_TEXEL_F16, false): hraw = affine_sample<TC_TEXEL_F16, false>(r.q[7], r.q[8], u, v); break;
-    case affine_kind(TC_TEXEL_UNORM16, true): hraw = affine_sample<TC_TEXEL_UNORM16, true>(r.q[7], r.q[8], u, v); break;
-    case affine_kind(TC_TEXEL_UNORM16, false):
-      hraw = affine_sample<TC_TEXEL_UNORM16, false>(r.q[7], r.q[8], u, v);
-      break;
-    default: break;  // kAffineZeroMap: samples as 0
-  }
+  const float hraw = sample_kind(kind, r.q[7], r.q[8], u, v);
   // displace along the renormalised interpolated normal
   const float height = __fmaf_rn(hraw, q6.x, q6.y);
   const float k      = height * rsqrtf(__fmaf_rn(N.z, N.z, __fmaf_rn(N.y, N.y, N.x * N.x)));
