@@ -441,7 +441,7 @@ typedef struct tc_schedule {
   uint32_t splitBlockSize;      /* split tile: 128 (16 items), 256 or 512 (32 items) threads */
   uint32_t vertexBlocksPerSM;   /* register budget of the vertex-generation kernel (one 32-part chunk per warp):
                                  * 4 or less: 64 registers per thread, 5: 48, 6 and more: 40 */
-  uint32_t scanBlocksPerSM;     /* grid of the classify scan and instantiate allocation kernels = SMs x this */
+  uint32_t scanBlocksPerSM;     /* grid of the instantiate allocation kernels (tile sums, arguments) = SMs x this */
   uint32_t blocksPerSM;         /* persistent grid of the split kernel = SMs x this x (512 / splitBlockSize) */
   uint32_t _pad[3];
 } tc_schedule;

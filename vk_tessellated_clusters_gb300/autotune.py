@@ -1,8 +1,8 @@
 """Launch-schedule autotuner for the batched frame.
 
 The schedule (tc_schedule) sets the launch shapes of the persistent stages:
-grid multipliers of the classify warp kernels, of the classify scan and the
-instantiate allocation, of the vertex-generation kernel, the split tile size
+grid multipliers of the classify warp kernels and of the instantiate
+allocation, the vertex kernel's register budget, the split tile size
 (128 threads x 16 items, 256 or 512 threads x 32 items) and the split grid.
 Outputs do not depend on it (every allocation is a prefix sum in a fixed
 order), so tuning is a pure timing search.

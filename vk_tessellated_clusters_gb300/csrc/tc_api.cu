@@ -29,10 +29,10 @@ struct SlotPlan
 constexpr size_t kCtrlBytes = 8 + 8 * kMaxCounters;
 
 // kernels of a batched frame besides the split passes: frame_begin,
-// instances_classify, clusters_cull, classify (3), instantiate (4, twice: the
+// instances_classify, clusters_cull, classify (2), instantiate (4, twice: the
 // first part run overlapped with the split passes, then the others), blas
 // setup, blas insert (2)
-constexpr uint64_t kFrameFixedLaunches = 17;
+constexpr uint64_t kFrameFixedLaunches = 16;
 
 struct Plan
 {
@@ -46,7 +46,7 @@ struct Plan
   u32    segRows;     // runs
   size_t runOffset;   // run starts (u32 x kMaxRuns+2)
   u32    classifyCap; // clusters the classify scratch holds
-  size_t clsCountsOffset, clsOffsetsOffset, clsTriWordsOffset;
+  size_t clsCountsOffset, clsTriWordsOffset, clsBlockSumsOffset;
   size_t partVertexOffset;  // u32 per part triangle
   size_t splitBaseOffset;   // 9 floats per split item: its base triangle's world positions
   size_t instOffset;  // instance cluster prefix (u32 x maxInstances+1)
@@ -136,7 +136,7 @@ Plan make_plan(const tc_context_desc& d)
   p.slotInstances   = add(ceil_div(d.maxInstances, kInstanceTile), 1);
   p.slotCull        = add(ceil_div(d.maxTotalClusters, kCullTile), 1);
   p.classifyCap     = (u32)std::max<u64>(1, std::min<u64>(k.maxVisibleClusters, d.maxTotalClusters));
-  p.slotClassify    = add(classify_scan_tiles(p.classifyCap), kMaxCounters);
+  p.slotClassify    = add(1, kMaxCounters);  // unused by classify's kernels (kept for the per-instance bind)
   p.slotSplit0      = add(ceil_div(k.maxSplitTriangles, kSplitMinItems), 2);
   for(u32 i = 1; i < passes; i++)
     add(ceil_div(k.maxSplitTriangles, kSplitMinItems), 2);
@@ -166,10 +166,10 @@ Plan make_plan(const tc_context_desc& d)
   // per-item scratch (written before it is read every launch; never zeroed)
   p.clsCountsOffset   = off;
   off                 = align_up(off + (size_t)p.classifyCap * 8, 256);
-  p.clsOffsetsOffset  = off;
-  off                 = align_up(off + (size_t)p.classifyCap * sizeof(ClusterOffsets), 256);
   p.clsTriWordsOffset = off;
   off                 = align_up(off + (size_t)p.classifyCap * TC_MAX_CLUSTER_TRIANGLES * 4, 256);
+  p.clsBlockSumsOffset = off;  // block sums, then the counter bases
+  off = align_up(off + ((size_t)classify_max_blocks(p.classifyCap) + 1) * sizeof(ClusterOffsets), 256);
   p.partVertexOffset  = off;
   off                 = align_up(off + (size_t)std::max(1u, k.maxPartTriangles) * 4, 256);
   p.splitBaseOffset   = off;
@@ -249,8 +249,9 @@ ClassifyBuffers classify_buffers(tc_context* ctx)
 {
   const Plan& p = ctx->plan;
   return {reinterpret_cast<uint2*>(ctx->dScratch + p.clsCountsOffset),
-          reinterpret_cast<ClusterOffsets*>(ctx->dScratch + p.clsOffsetsOffset),
-          reinterpret_cast<u32*>(ctx->dScratch + p.clsTriWordsOffset)};
+          reinterpret_cast<u32*>(ctx->dScratch + p.clsTriWordsOffset),
+          reinterpret_cast<ClusterOffsets*>(ctx->dScratch + p.clsBlockSumsOffset),
+          reinterpret_cast<ClusterOffsets*>(ctx->dScratch + p.clsBlockSumsOffset) + classify_max_blocks(p.classifyCap)};
 }
 
 InstantiateBuffers instantiate_buffers(tc_context* ctx)
@@ -305,7 +306,7 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   bind_slot(ctx, c, p.slotClassify, false);
   c.fuseSetup = TC_BUILD_SETUP_SPLIT;
   TC_CHECK_CUDA(launch_cluster_classify(c, classify_buffers(ctx), std::min(a->totalClusters, a->caps.maxVisibleClusters),
-                                        ctx->numSMs, sched.classifyBlocksPerSM, sched.scanBlocksPerSM, s));
+                                        ctx->numSMs, sched.classifyBlocksPerSM, s));
 
   // The parts classify produced (run 0) come first in the instantiation order
   // and their offsets depend on nothing the split passes do: they are
@@ -713,9 +714,9 @@ tc_status tc_cluster_classify(tc_context* ctx, const tc_frame_args* a, uint32_t 
   c.instEnd   = instanceEnd;
   bind_slot(ctx, c, ctx->plan.slotClassify, true);
   TC_CHECK_CUDA(launch_cluster_classify(c, classify_buffers(ctx), std::min(a->totalClusters, a->caps.maxVisibleClusters),
-                                        ctx->numSMs, ctx->schedule.classifyBlocksPerSM, ctx->schedule.scanBlocksPerSM,
+                                        ctx->numSMs, ctx->schedule.classifyBlocksPerSM,
                                         reinterpret_cast<cudaStream_t>(stream)));
-  ctx->launches += 3;
+  ctx->launches += 2;
   return TC_OK;
 }
 

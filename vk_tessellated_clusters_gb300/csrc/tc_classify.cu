@@ -3,17 +3,21 @@
 //
 // shaders/cluster_classify.comp.glsl:150-666 (RT target, plain path).
 //
-// GB300 mapping, three launches per stage so that the heavy kernels have no
-// block-wide barriers and no cross-block waits:
-//   count : one warp per cluster (<= 64 triangles, two per lane), vertices
-//           staged in shared memory; segment counts, configs and the
-//           cluster's counts (part / split triangles, full-cluster vertices,
-//           CLAS bytes) go to scratch
-//   scan  : exclusive scan of those counts over the clusters in visible order
-//           (512 clusters per tile, decoupled look-back between tiles), so
-//           every offset equals what a serial loop over the clusters gives
-//   write : one warp per cluster again; part / split triangles, instantiation
-//           arguments and the displaced full-cluster vertices at their offsets
+// GB300 mapping, two launches per stage, neither with a cross-block wait or a
+// last-block step. Block b of the grid owns the contiguous range of visible
+// clusters [b * per, (b + 1) * per), the same range in both launches:
+//   count : the block's warps take its clusters in turn, one cluster per warp
+//           (<= 64 triangles, two per lane), vertices staged in shared
+//           memory; segment counts, configs and the cluster's counts (part /
+//           split triangles, full-cluster vertices, CLAS bytes) go to
+//           scratch, the block's sums to one record per block
+//   write : every block adds up the sums of the blocks before it (the
+//           counters' values before the launch included), then scans its own
+//           clusters' counts in shared memory, so every offset equals what a
+//           serial loop over the clusters gives; part / split triangles,
+//           instantiation arguments and the displaced full-cluster vertices go
+//           to those offsets, and the grid's last block writes the counters'
+//           new totals
 #include <algorithm>
 
 #include "tc_kernels.h"
@@ -24,9 +28,8 @@ namespace tc {
 
 namespace {
 
-constexpr u32 kScanItemsPerThread = 2;
-constexpr u32 kScanBlock          = 256;
-constexpr u32 kScanTile           = kScanItemsPerThread * kScanBlock;  // clusters per scan tile
+constexpr u32 kBlock = 256;  // threads of the count and write blocks
+constexpr u32 kWarps = kBlock / 32;
 
 enum : int
 {
@@ -85,10 +88,19 @@ __device__ __forceinline__ u32 classify_triangle(uint3 f, u32 sf)
 
 struct ClassifyScratch
 {
-  uint2*          counts;    // per visible cluster of the window
-  ClusterOffsets* offsets;   // per visible cluster of the window
-  u32*            triWords;  // 64 per visible cluster
+  uint2*          counts;     // per visible cluster of the window
+  u32*            triWords;   // 64 per visible cluster
+  ClusterOffsets* blockSums;  // per block of the grid
+  ClusterOffsets* bases;      // the counters before the launch
 };
+
+// the contiguous range of visible clusters block `blk` of `nb` owns
+__device__ __forceinline__ void block_range(u32 n, u32 blk, u32 nb, u32& v0, u32& v1)
+{
+  const u32 per = (n + nb - 1) / nb;
+  v0            = min(n, blk * per);
+  v1            = min(n, v0 + per);
+}
 
 // visible clusters of the instance window (visibleClusters is sorted by instance)
 __device__ inline void window_range(const StageCtx& c, u32& lo, u32& hi)
@@ -116,18 +128,98 @@ __device__ __forceinline__ FactorParams factor_params(const StageCtx& c)
 }
 
 // ---------------------------------------------------------------------------
+// scans
+// ---------------------------------------------------------------------------
+
+template <class T>
+__device__ __forceinline__ T warp_inclusive(T x, u32 lane)
+{
+#pragma unroll
+  for(int d = 1; d < 32; d <<= 1)
+  {
+    T y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+    if(lane >= (u32)d)
+      x += y;
+  }
+  return x;
+}
+
+// block-wide exclusive scan of kNumCounters values per thread
+__device__ inline void block_scan5(u64 (&v)[kNumCounters], u64 (&tot)[kNumCounters], u64 (*s_warp)[kNumCounters])
+{
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  u64       inc[kNumCounters];
+#pragma unroll
+  for(int q = 0; q < kNumCounters; q++)
+  {
+    inc[q] = warp_inclusive<u64>(v[q], lane);
+    if(lane == 31)
+      s_warp[warp][q] = inc[q];
+  }
+  __syncthreads();
+  if(warp == 0)
+  {
+#pragma unroll
+    for(int q = 0; q < kNumCounters; q++)
+    {
+      u64 w = lane < nw ? s_warp[lane][q] : 0;
+      u64 s = warp_inclusive<u64>(w, lane);
+      __syncwarp();
+      if(lane < nw)
+        s_warp[lane][q] = s - w;
+      if(lane == 31)
+        s_warp[32][q] = s;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for(int q = 0; q < kNumCounters; q++)
+  {
+    tot[q] = s_warp[32][q];
+    v[q]   = s_warp[warp][q] + inc[q] - v[q];
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
 // count
 // ---------------------------------------------------------------------------
+
+// The offsets at which block `blockIdx.x` of the write launch starts: the
+// counters' values before the launch plus the sums of all blocks before it.
+__device__ inline void block_prefix(const ClassifyScratch& cs, u64 (&pre)[kNumCounters],
+                                    u64 (*s_warp)[kNumCounters])
+{
+  u64 x[kNumCounters] = {0, 0, 0, 0, 0};
+  for(u32 i = threadIdx.x; i < blockIdx.x; i += blockDim.x)
+  {
+    const ClusterOffsets o = cs.blockSums[i];
+    x[kCntParts] += o.part;
+    x[kCntSplits] += o.split;
+    x[kCntGen] += o.gen;
+    x[kCntVerts] += o.vert;
+    x[kCntData] += o.data;
+  }
+  u64 tot[kNumCounters];
+  block_scan5(x, tot, s_warp);
+  const ClusterOffsets b0 = *cs.bases;
+  pre[kCntParts]          = b0.part + tot[kCntParts];
+  pre[kCntSplits]         = b0.split + tot[kCntSplits];
+  pre[kCntGen]            = b0.gen + tot[kCntGen];
+  pre[kCntVerts]          = b0.vert + tot[kCntVerts];
+  pre[kCntData]           = b0.data + tot[kCntData];
+}
 
 // MinBlocks: resident 256-thread blocks per SM the registers are sized for
 // (4: 64 registers, 6: 40, 8: 32); more resident warps hide more of the
 // dependent-load latency per cluster at the cost of some spills.
 template <int MinBlocks>
-__global__ void __launch_bounds__(256, MinBlocks) k_classify_count(StageCtx c, ClassifyScratch cs)
+__global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c, ClassifyScratch cs)
 {
   stage_prologue();
-  __shared__ f3  s_vert[8][TC_MAX_CLUSTER_VERTICES];
-  __shared__ f2  s_dist[8][TC_MAX_CLUSTER_VERTICES];  // per vertex: distance to the view position, its reciprocal
+  __shared__ f3  s_vert[kWarps][TC_MAX_CLUSTER_VERTICES];
+  __shared__ f2  s_dist[kWarps][TC_MAX_CLUSTER_VERTICES];  // per vertex: distance to the view position, its reciprocal
+  __shared__ u64 s_wsum[kWarps][kNumCounters];
   __shared__ u32 s_range[2];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if(threadIdx.x == 0)
@@ -142,9 +234,19 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_count(StageCtx c, C
   const float             rNear   = __fdiv_rn(1.0f, fp.nearPlane);
   const bool              culling = (c.flags & TC_FLAG_CULLING) != 0;
   const u32               sf      = clamp_split_factor(c.caps.splitFactor);
-  const u32               nwarps  = (gridDim.x * blockDim.x) >> 5;
+  u32                     vBegin, vEnd;
+  block_range(n, blockIdx.x, gridDim.x, vBegin, vEnd);
+  if(blockIdx.x == 0 && threadIdx.x == 0)  // the offsets continue from the counters' current values
+    *cs.bases = {b->partTriangleCounter, (u32)b->splitTriangleCounter, b->genClusterCounter, b->genVertexCounter,
+                 b->genClusterDataCounter};
+  if(lane == 0)
+  {
+#pragma unroll
+    for(int q = 0; q < kNumCounters; q++)
+      s_wsum[warp][q] = 0;  // lane 0 accumulates the range's counts here
+  }
 
-  for(u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nwarps)
+  for(u32 v = vBegin + warp; v < vEnd; v += kWarps)
   {
     const tc_ClusterInfo     ci = vis[begin + v];
     const tc_RenderInstance* in = c.instances + ci.instanceID;
@@ -223,164 +325,30 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_count(StageCtx c, C
       const u32 data =
           full ? __ldg(reinterpret_cast<const u32*>(in->clusterTemplateInstantiatonSizes) + ci.clusterID) : 0u;
       cs.counts[v] = pack_counts(parts, splits, full, nv, data);
+      s_wsum[warp][kCntParts] += parts;
+      s_wsum[warp][kCntSplits] += splits;
+      s_wsum[warp][kCntGen] += full ? 1u : 0u;
+      s_wsum[warp][kCntVerts] += full ? nv : 0u;
+      s_wsum[warp][kCntData] += data;
     }
   }
-}
 
-// ---------------------------------------------------------------------------
-// scan
-// ---------------------------------------------------------------------------
-
-template <class T>
-__device__ __forceinline__ T warp_inclusive(T x, u32 lane)
-{
-#pragma unroll
-  for(int d = 1; d < 32; d <<= 1)
-  {
-    T y = __shfl_up_sync(0xFFFFFFFFu, x, d);
-    if(lane >= (u32)d)
-      x += y;
-  }
-  return x;
-}
-
-// block-wide exclusive scan of kNumCounters values per thread
-__device__ inline void block_scan5(u64 (&v)[kNumCounters], u64 (&tot)[kNumCounters], u64 (*s_warp)[kNumCounters])
-{
-  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  u64       inc[kNumCounters];
-#pragma unroll
-  for(int q = 0; q < kNumCounters; q++)
-  {
-    inc[q] = warp_inclusive<u64>(v[q], lane);
-    if(lane == 31)
-      s_warp[warp][q] = inc[q];
-  }
+  // the block's sums, for the write launch's block prefixes
   __syncthreads();
   if(warp == 0)
   {
+    u64 x[kNumCounters];
 #pragma unroll
     for(int q = 0; q < kNumCounters; q++)
     {
-      u64 w = lane < nw ? s_warp[lane][q] : 0;
-      u64 s = warp_inclusive<u64>(w, lane);
-      __syncwarp();
-      if(lane < nw)
-        s_warp[lane][q] = s - w;
-      if(lane == 31)
-        s_warp[32][q] = s;
-    }
-  }
-  __syncthreads();
+      x[q] = lane < kWarps ? s_wsum[lane][q] : 0ull;
 #pragma unroll
-  for(int q = 0; q < kNumCounters; q++)
-  {
-    tot[q] = s_warp[32][q];
-    v[q]   = s_warp[warp][q] + inc[q] - v[q];
-  }
-  __syncthreads();
-}
-
-__global__ void __launch_bounds__(kScanBlock) k_classify_scan(StageCtx c, ClassifyScratch cs)
-{
-  stage_prologue();
-  __shared__ u64 s_warp[33][kNumCounters];
-  __shared__ u64 s_excl[kNumCounters];
-  __shared__ u32 s_tile, s_flag, s_range[2];
-  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if(threadIdx.x == 0)
-    window_range(c, s_range[0], s_range[1]);
-  __syncthreads();
-  const u32 n        = min(s_range[1] - s_range[0], c.scratch.itemCapacity);
-  u32       numTiles = (n + kScanTile - 1) / kScanTile;
-  numTiles           = clamp_tiles(c, numTiles);
-  tc_SceneBuilding* b = c.build;
-
-  for(;;)
-  {
-    const u32 tile = next_tile(c, &s_tile);
-    if(tile >= numTiles)
-      break;
-    const u32 first = tile * kScanTile + threadIdx.x * kScanItemsPerThread;
-    uint2     rec[kScanItemsPerThread];
-    u64       sum[kNumCounters] = {0, 0, 0, 0, 0};
-#pragma unroll
-    for(u32 i = 0; i < kScanItemsPerThread; i++)
-    {
-      rec[i] = first + i < n ? cs.counts[first + i] : make_uint2(0, 0);
-      sum[kCntParts] += cnt_parts(rec[i]);
-      sum[kCntSplits] += cnt_splits(rec[i]);
-      sum[kCntGen] += cnt_full(rec[i]);
-      sum[kCntVerts] += cnt_verts(rec[i]);
-      sum[kCntData] += rec[i].y;
+      for(int o = kWarps / 2; o > 0; o >>= 1)
+        x[q] += __shfl_xor_sync(0xFFFFFFFFu, x[q], o);
     }
-    u64 tot[kNumCounters];
-    block_scan5(sum, tot, s_warp);
-    if(warp < kNumCounters)
-    {
-      const u32 q    = warp;
-      u64       base = 0;
-      if(tile == 0)
-        base = q == kCntParts    ? b->partTriangleCounter
-               : q == kCntSplits ? (u64)(u32)b->splitTriangleCounter
-               : q == kCntGen    ? b->genClusterCounter
-               : q == kCntVerts  ? b->genVertexCounter
-                                 : b->genClusterDataCounter;
-      const u64 ex =
-          warp_lookback_exclusive(c.scratch.lbState + (u64)q * c.scratch.lbStride, tile, tot[q], base, c.errorWord);
-      if(lane == 0)
-      {
-        s_excl[q] = ex;
-        if(tile == numTiles - 1)
-          c.scratch.totals[q] = ex + tot[q];
-      }
-    }
-    __syncthreads();
-    u64 run[kNumCounters];
-#pragma unroll
-    for(int q = 0; q < kNumCounters; q++)
-      run[q] = s_excl[q] + sum[q];
-#pragma unroll
-    for(u32 i = 0; i < kScanItemsPerThread; i++)
-    {
-      if(first + i < n)
-      {
-        ClusterOffsets o;
-        o.part                = (u32)run[kCntParts];
-        o.split               = (u32)run[kCntSplits];
-        o.gen                 = (u32)run[kCntGen];
-        o.vert                = (u32)run[kCntVerts];
-        o.data                = run[kCntData];
-        cs.offsets[first + i] = o;
-      }
-      run[kCntParts] += cnt_parts(rec[i]);
-      run[kCntSplits] += cnt_splits(rec[i]);
-      run[kCntGen] += cnt_full(rec[i]);
-      run[kCntVerts] += cnt_verts(rec[i]);
-      run[kCntData] += rec[i].y;
-    }
-    __syncthreads();
-  }
-
-  if(last_block_done(c, &s_flag))
-  {
-    if(threadIdx.x == 0)
-    {
-      if(numTiles)
-      {
-        const u64 fullBefore     = b->genClusterCounter;
-        b->partTriangleCounter   = (u32)c.scratch.totals[kCntParts];
-        b->splitTriangleCounter  = (int32_t)(u32)c.scratch.totals[kCntSplits];
-        b->genClusterCounter     = (u32)c.scratch.totals[kCntGen];
-        b->genVertexCounter      = (u32)c.scratch.totals[kCntVerts];
-        b->genClusterDataCounter = c.scratch.totals[kCntData];
-        // cluster_classify.comp.glsl:299 counts every full cluster, accepted or not
-        c.readback->numFullClusters += (u32)(c.scratch.totals[kCntGen] - fullBefore);
-      }
-      if(c.fuseSetup != kNoSetup)
-        build_setup_apply(c, c.fuseSetup);
-    }
-    scratch_release(c, numTiles, kNumCounters);
+    if(lane == 0)
+      cs.blockSums[blockIdx.x] = {(u32)x[kCntParts], (u32)x[kCntSplits], (u32)x[kCntGen], (u32)x[kCntVerts],
+                                  x[kCntData]};
   }
 }
 
@@ -460,12 +428,15 @@ __device__ __forceinline__ void full_steps(const FullRecord* rec, bool owner, u3
 }
 
 template <int MinBlocks>
-__global__ void __launch_bounds__(256, MinBlocks) k_classify_write(StageCtx c, ClassifyScratch cs)
+__global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c, ClassifyScratch cs)
 {
   stage_prologue();
-  __shared__ u32        s_range[2];
-  __shared__ FullRecord s_full[8][32];
-  const u32 lane = threadIdx.x & 31;
+  __shared__ u32            s_range[2];
+  __shared__ FullRecord     s_full[kWarps][32];
+  __shared__ u64            s_warp[33][kNumCounters];
+  __shared__ ClusterOffsets s_off[kBlock];  // offsets of the chunk's clusters
+  __shared__ uint2          s_cnt[kBlock];  // counts of the chunk's clusters
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if(threadIdx.x == 0)
     window_range(c, s_range[0], s_range[1]);
   __syncthreads();
@@ -480,195 +451,220 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_write(StageCtx c, C
   tc_TessTriangleInfo*  splits       = reinterpret_cast<tc_TessTriangleInfo*>(b->splitTriangles);
   tc_TessTriangleInfo*  parts        = reinterpret_cast<tc_TessTriangleInfo*>(b->partTriangles);
   float*                gv           = reinterpret_cast<float*>(b->genVertices);
-  const u32             nwarps       = (gridDim.x * blockDim.x) >> 5;
+  tc_BlasBuildInfo*     blas         = reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos);
   const u32             ltm          = (1u << lane) - 1u;
   u32                   statTris = 0, statTemp = 0;
 
-  // each warp takes a contiguous range of visible clusters (instance-sorted),
-  // so its full-cluster BLAS reference counts collapse into one atomic per
-  // instance it touches
-  const u32 gw   = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const u32 per  = (n + nwarps - 1) / nwarps;
-  const u32 vEnd = min(n, (gw + 1) * per);
-  tc_BlasBuildInfo* blas = reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos);
-  // ---- phase 1: part and split triangles, one cluster at a time ---------------
-  for(u32 v = gw * per; v < vEnd; v++)
-  {
-    const uint2 rec = cs.counts[v];
-    if(cnt_full(rec))
-      continue;  // phase 2
-    const ClusterOffsets off = cs.offsets[v];
-    const tc_ClusterInfo ci  = vis[begin + v];
-    {
-      // cluster_classify.comp.glsl:543-666: part and split triangles
-      const u32  nt  = cnt_parts(rec) + cnt_splits(rec);
-      const u32* tw  = cs.triWords + (u64)v * TC_MAX_CLUSTER_TRIANGLES;
-      const u32  w0  = lane < nt ? tw[lane] : 0u;
-      const u32  w1  = lane + 32 < nt ? tw[lane + 32] : 0u;
-      const bool s0  = lane < nt && (w0 >> 18) != 0, p0 = lane < nt && (w0 >> 18) == 0;
-      const bool s1  = lane + 32 < nt && (w1 >> 18) != 0, p1 = lane + 32 < nt && (w1 >> 18) == 0;
-      const u32  bs0 = __ballot_sync(0xFFFFFFFFu, s0), bp0 = __ballot_sync(0xFFFFFFFFu, p0);
-      const u32  bs1 = __ballot_sync(0xFFFFFFFFu, s1), bp1 = __ballot_sync(0xFFFFFFFFu, p1);
-      // split items also carry their base triangle's world positions (read by
-      // every split pass instead of the instance / cluster / vertex chain)
-      const tc_RenderInstance* in  = nullptr;
-      tc_Cluster               cl  = {};
-      float                    m[16];
-      if(bs0 | bs1)
-      {
-        in = c.instances + ci.instanceID;
-        cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
-#pragma unroll
-        for(int j = 0; j < 16; j++)
-          m[j] = __ldg(in->worldMatrix.m + j);
-      }
-      auto split_base = [&](u64 o, u32 tri) {
-        if(!c.splitBase)
-          return;
-        const uint8_t* lt  = reinterpret_cast<const uint8_t*>(in->clusterLocalTriangles) + cl.firstLocalTriangle;
-        const float*   pos = reinterpret_cast<const float*>(in->positions);
-        float*         d   = c.splitBase + 9 * o;
-#pragma unroll
-        for(int vv = 0; vv < 3; vv++)
-        {
-          const f3 wp = xform_point(m, ldg3(pos, cl.firstLocalVertex + lt[tri * 3 + vv]));
-          d[3 * vv + 0] = wp.x, d[3 * vv + 1] = wp.y, d[3 * vv + 2] = wp.z;
-        }
-      };
-      if(s0)
-      {
-        const u64 o = (u64)off.split + __popc(bs0 & ltm);
-        if(o < k.maxSplitTriangles)
-        {
-          emit_triangle(splits + o, ci, lane, w0);
-          split_base(o, lane);
-        }
-      }
-      else if(p0)
-      {
-        const u64 o = (u64)off.part + __popc(bp0 & ltm);
-        if(o < k.maxPartTriangles)
-          emit_triangle(parts + o, ci, lane, w0);
-      }
-      if(s1)
-      {
-        const u64 o = (u64)off.split + __popc(bs0) + __popc(bs1 & ltm);
-        if(o < k.maxSplitTriangles)
-        {
-          emit_triangle(splits + o, ci, lane + 32, w1);
-          split_base(o, lane + 32);
-        }
-      }
-      else if(p1)
-      {
-        const u64 o = (u64)off.part + __popc(bp0) + __popc(bp1 & ltm);
-        if(o < k.maxPartTriangles)
-          emit_triangle(parts + o, ci, lane + 32, w1);
-      }
-    }
-  }
+  u64 pre[kNumCounters];  // offsets of the next chunk's first cluster
+  block_prefix(cs, pre, s_warp);
+  u32 vBegin, vEnd;
+  block_range(n, blockIdx.x, gridDim.x, vBegin, vEnd);
+  FullRecord* rec = s_full[warp];
 
-  // ---- phase 2: full clusters of the range, 32 at a time ----------------------
-  // cluster_classify.comp.glsl:271-488: instantiation arguments (one lane per
-  // cluster, so the instance / cluster loads of 32 clusters overlap), then the
-  // clusters' displaced vertices (:457-482), which are contiguous in
-  // genVertices, walked on consecutive lanes.
-  FullRecord* rec = s_full[threadIdx.x >> 5];
-  for(u32 v0 = gw * per; v0 < vEnd; v0 += 32)
+  for(u32 c0 = vBegin; c0 < vEnd; c0 += kBlock)
   {
-    const u32 v    = v0 + lane;
-    bool       full = false;
-    u32        nv = 0;
-    u32        inst = 0xFFFFFFFFu;
-    FullRecord fr;
-    if(v < vEnd)
+    // exclusive scan of the chunk's counts, in cluster order
+    const u32 len = min(kBlock, vEnd - c0);
     {
-      const uint2 r = cs.counts[v];
-      if(cnt_full(r))
+      const uint2 r = threadIdx.x < len ? cs.counts[c0 + threadIdx.x] : make_uint2(0, 0);
+      u64 x[kNumCounters] = {cnt_parts(r), cnt_splits(r), cnt_full(r), cnt_verts(r), r.y};
+      u64 tot[kNumCounters];
+      block_scan5(x, tot, s_warp);
+      s_cnt[threadIdx.x] = r;
+      s_off[threadIdx.x] = {(u32)(pre[kCntParts] + x[kCntParts]), (u32)(pre[kCntSplits] + x[kCntSplits]),
+                            (u32)(pre[kCntGen] + x[kCntGen]), (u32)(pre[kCntVerts] + x[kCntVerts]),
+                            pre[kCntData] + x[kCntData]};
+#pragma unroll
+      for(int q = 0; q < kNumCounters; q++)
+        pre[q] += tot[q];
+    }
+    __syncthreads();
+    // each warp takes a contiguous part of the chunk (instance-sorted), so its
+    // full-cluster BLAS reference counts collapse into one atomic per instance
+    // it touches and its full clusters' vertices are contiguous
+    const u32 perW = (len + kWarps - 1) / kWarps;
+    const u32 lo = min(len, warp * perW), hi = min(len, lo + perW);
+
+    // ---- phase 1: part and split triangles, one cluster at a time -------------
+    for(u32 i = lo; i < hi; i++)
+    {
+      const uint2 cnt = s_cnt[i];
+      if(cnt_full(cnt))
+        continue;  // phase 2 (no part or split triangles)
+      const u32 v = c0 + i, offPart = s_off[i].part, offSplit = s_off[i].split;
+      const tc_ClusterInfo ci = vis[begin + v];
       {
-        const ClusterOffsets off = cs.offsets[v];
-        nv                       = cnt_verts(r);
-        full = !((u64)off.vert + nv > k.maxGeneratedVertices || (u64)off.gen + 1 > k.maxGeneratedClusters
-                 || off.data + r.y > maxData);
-        if(full)
+        // cluster_classify.comp.glsl:543-666: part and split triangles
+        const u32  nt  = cnt_parts(cnt) + cnt_splits(cnt);
+        const u32* tw  = cs.triWords + (u64)v * TC_MAX_CLUSTER_TRIANGLES;
+        const u32  w0  = lane < nt ? tw[lane] : 0u;
+        const u32  w1  = lane + 32 < nt ? tw[lane + 32] : 0u;
+        const bool s0  = lane < nt && (w0 >> 18) != 0, p0 = lane < nt && (w0 >> 18) == 0;
+        const bool s1  = lane + 32 < nt && (w1 >> 18) != 0, p1 = lane + 32 < nt && (w1 >> 18) == 0;
+        const u32  bs0 = __ballot_sync(0xFFFFFFFFu, s0), bp0 = __ballot_sync(0xFFFFFFFFu, p0);
+        const u32  bs1 = __ballot_sync(0xFFFFFFFFu, s1), bp1 = __ballot_sync(0xFFFFFFFFu, p1);
+        // split items also carry their base triangle's world positions (read by
+        // every split pass instead of the instance / cluster / vertex chain)
+        const tc_RenderInstance* in  = nullptr;
+        tc_Cluster               cl  = {};
+        float                    m[16];
+        if(bs0 | bs1)
         {
-          const tc_ClusterInfo     ci = vis[begin + v];
-          const tc_RenderInstance* in = c.instances + ci.instanceID;
-          const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
-          // accepted instantiations form a prefix of the serial order, so the
-          // instantiation slot equals the generated-cluster slot
-          const u32                  tempOffset = off.gen;
-          tc_TemplateInstantiateInfo ti;
-          ti.clusterIdOffset        = 0;
-          ti.geometryIndexOffset    = 0;
-          ti.clusterTemplateAddress = __ldg(reinterpret_cast<const u64*>(in->clusterTemplateAdresses) + ci.clusterID);
-          ti.vertexBufferAddress    = b->genVertices + (u64)off.vert * 12ull;
-          ti.vertexBufferStride     = 12;
-          reinterpret_cast<tc_TemplateInstantiateInfo*>(b->tempInstantiations)[tempOffset] = ti;
-          reinterpret_cast<u32*>(b->tempInstanceIDs)[tempOffset]                          = ci.instanceID;
-          reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset]                     = b->genClusterData + off.data;
-          if((c.flags & TC_FLAG_WRITE_FULLCLUSTERS) && b->fullClusters)
-            reinterpret_cast<tc_ClusterInfo*>(b->fullClusters)[tempOffset] = ci;
-          statTemp += 1;
-          statTris += min((u32)cl.numTriangles, TC_MAX_CLUSTER_TRIANGLES);
-          inst     = ci.instanceID;
-          fr.vo    = off.vert;
-          fr.nv    = nv;
-          fr.pos   = reinterpret_cast<const float*>(in->positions);
-          fr.nrm   = reinterpret_cast<const float*>(in->normals);
-          fr.uvs   = reinterpret_cast<const float*>(in->texcoords);
-          fr.first = cl.firstLocalVertex;
-          tc_DisplacementTexture tx = {};
-          if(haveTextures && in->displacementIndex >= 0)
+          in = c.instances + ci.instanceID;
+          cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
+#pragma unroll
+          for(int j = 0; j < 16; j++)
+            m[j] = __ldg(in->worldMatrix.m + j);
+        }
+        auto split_base = [&](u64 o, u32 tri) {
+          if(!c.splitBase)
+            return;
+          const uint8_t* lt  = reinterpret_cast<const uint8_t*>(in->clusterLocalTriangles) + cl.firstLocalTriangle;
+          const float*   pos = reinterpret_cast<const float*>(in->positions);
+          float*         d   = c.splitBase + 9 * o;
+#pragma unroll
+          for(int vv = 0; vv < 3; vv++)
           {
-            if((u32)in->displacementIndex < c.numTextures)
-              tx = c.textures[in->displacementIndex];
-            else
-              atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
+            const f3 wp = xform_point(m, ldg3(pos, cl.firstLocalVertex + lt[tri * 3 + vv]));
+            d[3 * vv + 0] = wp.x, d[3 * vv + 1] = wp.y, d[3 * vv + 2] = wp.z;
           }
-          fr.map    = make_map_desc(tx);
-          fr.scale  = in->displacementScale * c.view->displacementScale;
-          fr.offset = in->displacementOffset + c.view->displacementOffset;
+        };
+        if(s0)
+        {
+          const u64 o = (u64)offSplit + __popc(bs0 & ltm);
+          if(o < k.maxSplitTriangles)
+          {
+            emit_triangle(splits + o, ci, lane, w0);
+            split_base(o, lane);
+          }
+        }
+        else if(p0)
+        {
+          const u64 o = (u64)offPart + __popc(bp0 & ltm);
+          if(o < k.maxPartTriangles)
+            emit_triangle(parts + o, ci, lane, w0);
+        }
+        if(s1)
+        {
+          const u64 o = (u64)offSplit + __popc(bs0) + __popc(bs1 & ltm);
+          if(o < k.maxSplitTriangles)
+          {
+            emit_triangle(splits + o, ci, lane + 32, w1);
+            split_base(o, lane + 32);
+          }
+        }
+        else if(p1)
+        {
+          const u64 o = (u64)offPart + __popc(bp0) + __popc(bp1 & ltm);
+          if(o < k.maxPartTriangles)
+            emit_triangle(parts + o, ci, lane + 32, w1);
         }
       }
     }
-    const u32 fm = __ballot_sync(0xFFFFFFFFu, full);
-    if(fm == 0)
-      continue;
-    // records packed in lane order: record r belongs to the r-th full cluster
-    if(full)
-      rec[__popc(fm & ltm)] = fr;
-    // CLAS reference counts: one atomic per distinct instance of the batch
-    for(u32 remaining = fm; remaining;)
+
+    // ---- phase 2: full clusters of the warp's part, 32 at a time ---------------
+    // cluster_classify.comp.glsl:271-488: instantiation arguments (one lane per
+    // cluster, so the instance / cluster loads of 32 clusters overlap), then the
+    // clusters' displaced vertices (:457-482), which are contiguous in
+    // genVertices, walked on consecutive lanes.
+    for(u32 i0 = lo; i0 < hi; i0 += 32)
     {
-      const int src = __ffs(remaining) - 1;
-      const u32 gk  = __shfl_sync(0xFFFFFFFFu, inst, src);
-      const u32 sum = __popc(__ballot_sync(0xFFFFFFFFu, full && inst == gk));
-      remaining &= ~__ballot_sync(0xFFFFFFFFu, full && inst == gk);
-      if((int)lane == src)
-        atomicAdd(&blas[gk].clusterReferencesCount, sum);
+      const u32  i    = i0 + lane;
+      bool       full = false;
+      u32        nv   = 0;
+      u32        inst = 0xFFFFFFFFu;
+      FullRecord fr;
+      if(i < hi)
+      {
+        const uint2 r = s_cnt[i];
+        if(cnt_full(r))
+        {
+          const ClusterOffsets off = s_off[i];
+          const u32            v   = c0 + i;
+          nv                       = cnt_verts(r);
+          full = !((u64)off.vert + nv > k.maxGeneratedVertices || (u64)off.gen + 1 > k.maxGeneratedClusters
+                   || off.data + r.y > maxData);
+          if(full)
+          {
+            const tc_ClusterInfo     ci = vis[begin + v];
+            const tc_RenderInstance* in = c.instances + ci.instanceID;
+            const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
+            // accepted instantiations form a prefix of the serial order, so the
+            // instantiation slot equals the generated-cluster slot
+            const u32                  tempOffset = off.gen;
+            tc_TemplateInstantiateInfo ti;
+            ti.clusterIdOffset        = 0;
+            ti.geometryIndexOffset    = 0;
+            ti.clusterTemplateAddress = __ldg(reinterpret_cast<const u64*>(in->clusterTemplateAdresses) + ci.clusterID);
+            ti.vertexBufferAddress    = b->genVertices + (u64)off.vert * 12ull;
+            ti.vertexBufferStride     = 12;
+            reinterpret_cast<tc_TemplateInstantiateInfo*>(b->tempInstantiations)[tempOffset] = ti;
+            reinterpret_cast<u32*>(b->tempInstanceIDs)[tempOffset]                          = ci.instanceID;
+            reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset]                     = b->genClusterData + off.data;
+            if((c.flags & TC_FLAG_WRITE_FULLCLUSTERS) && b->fullClusters)
+              reinterpret_cast<tc_ClusterInfo*>(b->fullClusters)[tempOffset] = ci;
+            statTemp += 1;
+            statTris += min((u32)cl.numTriangles, TC_MAX_CLUSTER_TRIANGLES);
+            inst     = ci.instanceID;
+            fr.vo    = off.vert;
+            fr.nv    = nv;
+            fr.pos   = reinterpret_cast<const float*>(in->positions);
+            fr.nrm   = reinterpret_cast<const float*>(in->normals);
+            fr.uvs   = reinterpret_cast<const float*>(in->texcoords);
+            fr.first = cl.firstLocalVertex;
+            tc_DisplacementTexture tx = {};
+            if(haveTextures && in->displacementIndex >= 0)
+            {
+              if((u32)in->displacementIndex < c.numTextures)
+                tx = c.textures[in->displacementIndex];
+              else
+                atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
+            }
+            fr.map    = make_map_desc(tx);
+            fr.scale  = in->displacementScale * c.view->displacementScale;
+            fr.offset = in->displacementOffset + c.view->displacementOffset;
+          }
+        }
+      }
+      const u32 fm = __ballot_sync(0xFFFFFFFFu, full);
+      if(fm == 0)
+        continue;
+      // records packed in lane order: record r belongs to the r-th full cluster
+      if(full)
+        rec[__popc(fm & ltm)] = fr;
+      // CLAS reference counts: one atomic per distinct instance of the batch
+      for(u32 remaining = fm; remaining;)
+      {
+        const int src = __ffs(remaining) - 1;
+        const u32 gk  = __shfl_sync(0xFFFFFFFFu, inst, src);
+        const u32 sum = __popc(__ballot_sync(0xFFFFFFFFu, full && inst == gk));
+        remaining &= ~__ballot_sync(0xFFFFFFFFu, full && inst == gk);
+        if((int)lane == src)
+          atomicAdd(&blas[gk].clusterReferencesCount, sum);
+      }
+      __syncwarp();
+      // per record (lane r < nrec): first vertex within the batch and vertex count
+      const u32 nrec   = __popc(fm);
+      const u32 vBase  = rec[0].vo;
+      const u32 rStart = lane < nrec ? rec[lane].vo - vBase : 0u;
+      const u32 rCount = lane < nrec ? rec[lane].nv : 0u;
+      const u32 rEnd   = __shfl_sync(0xFFFFFFFFu, rStart + rCount, nrec - 1);
+      const bool owner = lane < nrec;
+      // one specialisation when the batch's clusters share a map kind
+      const u32 kind  = owner ? rec[lane].map.kind : 0u;
+      const u32 kind0 = rec[0].map.kind;
+      const u32 kw    = __all_sync(0xFFFFFFFFu, !owner || kind == kind0) ? kind0 : ~0u;
+      float*    dst   = gv + (u64)vBase * 3;
+      switch(kw)
+      {
+        case affine_kind(TC_TEXEL_F32, true): full_steps<affine_kind(TC_TEXEL_F32, true)>(rec, owner, rStart, rEnd, dst); break;
+        case affine_kind(TC_TEXEL_F16, true): full_steps<affine_kind(TC_TEXEL_F16, true)>(rec, owner, rStart, rEnd, dst); break;
+        case kAffineFlat: full_steps<kAffineFlat>(rec, owner, rStart, rEnd, dst); break;
+        default: full_steps<~0u>(rec, owner, rStart, rEnd, dst); break;
+      }
+      __syncwarp();  // records are rewritten by the next batch
     }
-    __syncwarp();
-    // per record (lane r < nrec): first vertex within the batch and vertex count
-    const u32 nrec   = __popc(fm);
-    const u32 vBase  = rec[0].vo;
-    const u32 rStart = lane < nrec ? rec[lane].vo - vBase : 0u;
-    const u32 rCount = lane < nrec ? rec[lane].nv : 0u;
-    const u32 rEnd   = __shfl_sync(0xFFFFFFFFu, rStart + rCount, nrec - 1);
-    const bool owner = lane < nrec;
-    // one specialisation when the batch's clusters share a map kind
-    const u32 kind  = owner ? rec[lane].map.kind : 0u;
-    const u32 kind0 = rec[0].map.kind;
-    const u32 kw    = __all_sync(0xFFFFFFFFu, !owner || kind == kind0) ? kind0 : ~0u;
-    float*    dst   = gv + (u64)vBase * 3;
-    switch(kw)
-    {
-      case affine_kind(TC_TEXEL_F32, true): full_steps<affine_kind(TC_TEXEL_F32, true)>(rec, owner, rStart, rEnd, dst); break;
-      case affine_kind(TC_TEXEL_F16, true): full_steps<affine_kind(TC_TEXEL_F16, true)>(rec, owner, rStart, rEnd, dst); break;
-      case kAffineFlat: full_steps<kAffineFlat>(rec, owner, rStart, rEnd, dst); break;
-      default: full_steps<~0u>(rec, owner, rStart, rEnd, dst); break;
-    }
-    __syncwarp();  // records are rewritten by the next batch
+    __syncthreads();  // s_off / s_cnt are rewritten by the next chunk
   }
 
   // statistics: one atomic each per warp
@@ -685,31 +681,47 @@ __global__ void __launch_bounds__(256, MinBlocks) k_classify_write(StageCtx c, C
     if(statTris)
       atomicAdd(&c.readback->numTotalTriangles, statTris);
   }
+
+  // the last block's running offsets are the totals; no block reads the
+  // counters after count took their values
+  if(blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
+  {
+    if(n)
+    {
+      const ClusterOffsets b0  = *cs.bases;
+      b->partTriangleCounter   = (u32)pre[kCntParts];
+      b->splitTriangleCounter  = (int32_t)(u32)pre[kCntSplits];
+      b->genClusterCounter     = (u32)pre[kCntGen];
+      b->genVertexCounter      = (u32)pre[kCntVerts];
+      b->genClusterDataCounter = pre[kCntData];
+      // cluster_classify.comp.glsl:299 counts every full cluster, accepted or not
+      c.readback->numFullClusters += (u32)pre[kCntGen] - b0.gen;
+    }
+    if(c.fuseSetup != kNoSetup)
+      build_setup_apply(c, c.fuseSetup);
+  }
 }
 
 }  // namespace
 
 cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
-                                    u32 warpBlocksPerSM, u32 scanBlocksPerSM, cudaStream_t s)
+                                    u32 warpBlocksPerSM, cudaStream_t s)
 {
-  ClassifyScratch cs{buf.counts, buf.offsets, buf.triWords};
-  const u32 warpGrid = std::max(1u, std::min((maxClusters + 7) / 8, numSMs * std::max(1u, warpBlocksPerSM)));
+  ClassifyScratch cs{buf.counts, buf.triWords, buf.blockSums, buf.bases};
+  // both launches use this grid: the blocks' cluster ranges must agree
+  const u32 grid = std::max(1u, std::min(classify_max_blocks(maxClusters), numSMs * std::max(1u, warpBlocksPerSM)));
   // register budget from the requested residency: 4 or less -> 64, 5-7 -> 40, 8 and more -> 32
   const int   occ = warpBlocksPerSM >= 8 ? 8 : (warpBlocksPerSM >= 5 ? 6 : 4);
-  cudaError_t e   = occ == 8   ? launch_pdl(k_classify_count<8>, warpGrid, 256, s, c, cs)
-                    : occ == 6 ? launch_pdl(k_classify_count<6>, warpGrid, 256, s, c, cs)
-                               : launch_pdl(k_classify_count<4>, warpGrid, 256, s, c, cs);
+  cudaError_t e   = occ == 8   ? launch_pdl(k_classify_count<8>, grid, kBlock, s, c, cs)
+                    : occ == 6 ? launch_pdl(k_classify_count<6>, grid, kBlock, s, c, cs)
+                               : launch_pdl(k_classify_count<4>, grid, kBlock, s, c, cs);
   if(e != cudaSuccess)
     return e;
-  const u32 scanGrid =
-      std::max(1u, std::min((maxClusters + kScanTile - 1) / kScanTile, numSMs * std::max(1u, scanBlocksPerSM)));
-  if((e = launch_pdl(k_classify_scan, scanGrid, kScanBlock, s, c, cs)) != cudaSuccess)
-    return e;
-  return occ == 8   ? launch_pdl(k_classify_write<8>, warpGrid, 256, s, c, cs)
-         : occ == 6 ? launch_pdl(k_classify_write<6>, warpGrid, 256, s, c, cs)
-                    : launch_pdl(k_classify_write<4>, warpGrid, 256, s, c, cs);
+  return occ == 8   ? launch_pdl(k_classify_write<8>, grid, kBlock, s, c, cs)
+         : occ == 6 ? launch_pdl(k_classify_write<6>, grid, kBlock, s, c, cs)
+                    : launch_pdl(k_classify_write<4>, grid, kBlock, s, c, cs);
 }
 
-u32 classify_scan_tiles(u32 maxClusters) { return (maxClusters + kScanTile - 1) / kScanTile; }
+u32 classify_max_blocks(u32 maxClusters) { return std::max(1u, (maxClusters + kWarps - 1) / kWarps); }
 
 }  // namespace tc

@@ -17,13 +17,16 @@ struct ClusterOffsets
   u32                part, split, gen, vert;
   unsigned long long data;
 };
+static_assert(sizeof(ClusterOffsets) == 24, "ClusterOffsets: three 8-byte words");
 
-// cluster_classify scratch, per visible cluster of a launch's window
+// cluster_classify scratch: per visible cluster of a launch's window, and per
+// block of the classify grid (each block owns a contiguous range of clusters)
 struct ClassifyBuffers
 {
   uint2*          counts;
-  ClusterOffsets* offsets;
-  u32*            triWords;  // 64 per cluster
+  u32*            triWords;   // 64 per cluster
+  ClusterOffsets* blockSums;  // per block: the sums of its clusters' counts
+  ClusterOffsets* bases;      // one: the counters before the launch
 };
 
 cudaError_t launch_frame_begin(const StageCtx& c, u32 grid, cudaStream_t s);
@@ -31,8 +34,8 @@ cudaError_t launch_instances_classify(const StageCtx& c, u32 grid, u32 block, cu
 cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 cudaError_t launch_build_setup(const StageCtx& c, u32 mode, cudaStream_t s);
 cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
-                                    u32 warpBlocksPerSM, u32 scanBlocksPerSM, cudaStream_t s);
-u32         classify_scan_tiles(u32 maxClusters);
+                                    u32 warpBlocksPerSM, cudaStream_t s);
+u32         classify_max_blocks(u32 maxClusters);
 cudaError_t launch_triangle_split(const StageCtx& c, u32 blockSize, u32 grid, cudaStream_t s);
 // triangle_tess_template_instantiate scratch, per part triangle
 struct InstantiateBuffers

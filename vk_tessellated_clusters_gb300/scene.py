@@ -21,6 +21,55 @@ import numpy as np
 
 from . import layouts as L
 
+
+def _libm(fn, *xs) -> np.ndarray:
+    """Elementwise libm function. numpy's SIMD kernels for some
+    transcendental functions (arctan2, arccos, arcsin) round differently on
+    hosts with and without AVX-512, which would make the generated scenes,
+    and every output digest over them, depend on the machine."""
+    return np.vectorize(fn, otypes=[np.float64])(*xs)
+
+
+# The small linear algebra below is written out with a fixed operation order
+# (separate IEEE multiplies and adds) instead of BLAS / LAPACK, whose kernels
+# use FMA or other summation orders depending on the host CPU.
+def _norm3(v) -> float:
+    x, y, z = (float(t) for t in v)
+    return math.sqrt(x * x + y * y + z * z)
+
+
+def _dot3(a, b) -> float:
+    return float(a[0]) * float(b[0]) + float(a[1]) * float(b[1]) + float(a[2]) * float(b[2])
+
+
+def _row_norms(v: np.ndarray) -> np.ndarray:
+    """Euclidean norms of the rows of an (n, 3) array, in the array's dtype."""
+    sq = v * v
+    return np.sqrt(sq[:, 0] + sq[:, 1] + sq[:, 2])
+
+
+def _mm(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Matrix product over the last two axes (batched), terms summed in k order."""
+    out = a[..., :, 0, None] * b[..., 0, None, :]
+    for k in range(1, a.shape[-1]):
+        out = out + a[..., :, k, None] * b[..., k, None, :]
+    return out
+
+
+def _inv4(m: np.ndarray) -> np.ndarray:
+    """4x4 inverse by cofactors (adjugate / determinant), in Python floats."""
+    a = [[float(m[i, j]) for j in range(4)] for i in range(4)]
+
+    def minor(r, c):
+        rows = [i for i in range(4) if i != r]
+        cols = [j for j in range(4) if j != c]
+        (p, q, t), (u, v, w), (x, y, z) = ([a[i][j] for j in cols] for i in rows)
+        return p * (v * z - w * y) - q * (u * z - w * x) + t * (u * y - v * x)
+
+    cof = [[(-1.0 if (i + j) & 1 else 1.0) * minor(i, j) for j in range(4)] for i in range(4)]
+    det = a[0][0] * cof[0][0] + a[0][1] * cof[0][1] + a[0][2] * cof[0][2] + a[0][3] * cof[0][3]
+    return np.array([[cof[j][i] / det for j in range(4)] for i in range(4)])
+
 MAX_CLUSTER_TRIANGLES = 64
 MAX_CLUSTER_VERTICES = 64
 
@@ -45,7 +94,7 @@ def icosphere(subdivisions: int, radius: float = 1.0) -> Mesh:
     f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
          (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
          (8, 6, 7), (9, 8, 1)]
-    verts = [np.array(p, dtype=np.float64) / np.linalg.norm(p) for p in v]
+    verts = [np.array(p, dtype=np.float64) / _norm3(p) for p in v]
     faces = [tuple(x) for x in f]
     for _ in range(subdivisions):
         cache: dict = {}
@@ -54,7 +103,7 @@ def icosphere(subdivisions: int, radius: float = 1.0) -> Mesh:
             key = (a, b) if a < b else (b, a)
             if key not in cache:
                 m = verts[a] + verts[b]
-                verts.append(m / np.linalg.norm(m))
+                verts.append(m / _norm3(m))
                 cache[key] = len(verts) - 1
             return cache[key]
 
@@ -66,8 +115,8 @@ def icosphere(subdivisions: int, radius: float = 1.0) -> Mesh:
     P = np.array(verts) * radius
     N = np.array(verts)
     # spherical mapping
-    u = np.arctan2(N[:, 2], N[:, 0]) / (2 * np.pi) + 0.5
-    vv = np.arccos(np.clip(N[:, 1], -1, 1)) / np.pi
+    u = _libm(math.atan2, N[:, 2], N[:, 0]) / (2 * np.pi) + 0.5
+    vv = _libm(math.acos, np.clip(N[:, 1], -1, 1)) / np.pi
     return Mesh(P, N, np.stack([u, vv], 1), np.array(faces, dtype=np.int64))
 
 
@@ -75,9 +124,10 @@ def torus(R: float = 1.0, r: float = 0.3, nu: int = 128, nv: int = 48) -> Mesh:
     i, j = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
     a = 2 * np.pi * i / nu
     b = 2 * np.pi * j / nv
-    cx, cz = np.cos(a), np.sin(a)
-    P = np.stack([(R + r * np.cos(b)) * cx, r * np.sin(b), (R + r * np.cos(b)) * cz], -1).reshape(-1, 3)
-    N = np.stack([np.cos(b) * cx, np.sin(b), np.cos(b) * cz], -1).reshape(-1, 3)
+    cx, cz = _libm(math.cos, a), _libm(math.sin, a)
+    cb, sb = _libm(math.cos, b), _libm(math.sin, b)
+    P = np.stack([(R + r * cb) * cx, r * sb, (R + r * cb) * cz], -1).reshape(-1, 3)
+    N = np.stack([cb * cx, sb, cb * cz], -1).reshape(-1, 3)
     UV = np.stack([i / nu, j / nv], -1).reshape(-1, 2).astype(np.float64)
     idx = lambda a_, b_: (a_ % nu) * nv + (b_ % nv)
     q00, q10, q01, q11 = idx(i, j), idx(i + 1, j), idx(i, j + 1), idx(i + 1, j + 1)
@@ -282,7 +332,7 @@ def _finish(pos, nrm, uv, lt, cl, num_tris, geometry_id) -> Geometry:
     bb["hi"] = hi
     tri_cluster = np.repeat(np.arange(nc), cl["numTriangles"].astype(np.int64))
     gidx = lt.reshape(-1, 3).astype(np.int64) + cl["firstLocalVertex"][tri_cluster].astype(np.int64)[:, None]
-    e = np.stack([np.linalg.norm(pos[gidx[:, k]] - pos[gidx[:, (k + 1) % 3]], axis=1) for k in range(3)], 1)
+    e = np.stack([_row_norms(pos[gidx[:, k]] - pos[gidx[:, (k + 1) % 3]]) for k in range(3)], 1)
     emin = np.full(nc, np.inf, np.float32)
     emax = np.zeros(nc, np.float32)
     np.minimum.at(emin, tri_cluster, e.min(1).astype(np.float32))
@@ -352,20 +402,21 @@ def translate_rotate_scale(t, q, s) -> np.ndarray:
 
 def random_unit_quaternion(rng) -> np.ndarray:
     u1, u2, u3 = rng.random(3)
-    return np.array([np.sqrt(1 - u1) * np.sin(2 * np.pi * u2), np.sqrt(1 - u1) * np.cos(2 * np.pi * u2),
-                     np.sqrt(u1) * np.sin(2 * np.pi * u3), np.sqrt(u1) * np.cos(2 * np.pi * u3)])[[3, 0, 1, 2]]
+    u1, u2, u3 = float(u1), float(u2), float(u3)
+    return np.array([math.sqrt(1 - u1) * math.sin(2 * math.pi * u2), math.sqrt(1 - u1) * math.cos(2 * math.pi * u2),
+                     math.sqrt(u1) * math.sin(2 * math.pi * u3), math.sqrt(u1) * math.cos(2 * math.pi * u3)])[[3, 0, 1, 2]]
 
 
 def look_at(eye, center, up) -> np.ndarray:
     eye, center, up = (np.asarray(v, np.float64) for v in (eye, center, up))
     f = center - eye
-    f /= np.linalg.norm(f)
+    f /= _norm3(f)
     s = np.cross(f, up)
-    s /= np.linalg.norm(s)
+    s /= _norm3(s)
     u = np.cross(s, f)
     M = np.eye(4)
     M[0, :3], M[1, :3], M[2, :3] = s, u, -f
-    M[0, 3], M[1, 3], M[2, 3] = -s @ eye, -u @ eye, f @ eye
+    M[0, 3], M[1, 3], M[2, 3] = -_dot3(s, eye), -_dot3(u, eye), _dot3(f, eye)
     return M
 
 
@@ -401,14 +452,14 @@ def frame_constants(cam: Camera) -> np.ndarray:
     P = perspective_rh_zo(math.radians(cam.fovy_deg), cam.width / cam.height, cam.near, cam.far)
     P[1, 1] *= -1  # projection[1][1] *= -1
     V = look_at(cam.eye, cam.center, cam.up)
-    VP = P @ V
+    VP = _mm(P, V)
+    Vi = _inv4(V)
     fc["projMatrix"] = mat_colmajor(P)
-    fc["projMatrixI"] = mat_colmajor(np.linalg.inv(P))
+    fc["projMatrixI"] = mat_colmajor(_inv4(P))
     fc["viewProjMatrix"] = mat_colmajor(VP)
-    fc["viewProjMatrixI"] = mat_colmajor(np.linalg.inv(VP))
+    fc["viewProjMatrixI"] = mat_colmajor(_inv4(VP))
     fc["viewMatrix"] = mat_colmajor(V)
-    fc["viewMatrixI"] = mat_colmajor(np.linalg.inv(V))
-    Vi = np.linalg.inv(V)
+    fc["viewMatrixI"] = mat_colmajor(Vi)
     fc["viewPos"] = np.append(Vi[:3, 3], 1.0).astype(np.float32)
     fc["viewDir"] = np.append(-Vi[:3, 2], 0.0).astype(np.float32)
     fc["viewPlane"] = fc["viewDir"]
@@ -521,10 +572,10 @@ def animation_motion(num_instances: int, seed: int = 3):
     speed U[0, 1] rad/s, and a random direction with speed U[0, 2] units/s."""
     rng = np.random.default_rng(seed)
     axes = rng.normal(size=(num_instances, 3))
-    axes /= np.linalg.norm(axes, axis=1, keepdims=True)
+    axes /= _row_norms(axes)[:, None]
     omega = rng.random(num_instances)
     dirs = rng.normal(size=(num_instances, 3))
-    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    dirs /= _row_norms(dirs)[:, None]
     velocity = dirs * (2.0 * rng.random(num_instances))[:, None]
     return axes, omega, velocity
 
@@ -535,21 +586,21 @@ def animated_worlds(scene: "Scene", motion, t: float) -> np.ndarray:
     axes, omega, velocity = motion
     base = np.stack([i.world for i in scene.instances])
     ang = omega * t
-    c, s_, k = np.cos(ang)[:, None, None], np.sin(ang)[:, None, None], axes
+    c, s_, k = _libm(math.cos, ang)[:, None, None], _libm(math.sin, ang)[:, None, None], axes
     K = np.zeros((len(k), 3, 3))
     K[:, 0, 1], K[:, 0, 2], K[:, 1, 0] = -k[:, 2], k[:, 1], k[:, 2]
     K[:, 1, 2], K[:, 2, 0], K[:, 2, 1] = -k[:, 0], -k[:, 1], k[:, 0]
-    R = np.eye(3)[None] + s_ * K + (1 - c) * (K @ K)  # Rodrigues
+    R = np.eye(3)[None] + s_ * K + (1 - c) * _mm(K, K)  # Rodrigues
     W = base.copy()
-    W[:, :3, :3] = R @ base[:, :3, :3]
+    W[:, :3, :3] = _mm(R, base[:, :3, :3])
     W[:, :3, 3] = base[:, :3, 3] + velocity * t
     return W
 
 
 def camera_orbit(frame: int, num_frames: int = 60, radius: float = 30.0, center=(20.0, 20.0, 20.0),
                  height: float = 10.0, tess_rate_pixels: float = 4.0) -> Camera:
-    a = 2 * np.pi * frame / num_frames
-    eye = (center[0] + radius * np.cos(a), center[1] + height, center[2] + radius * np.sin(a))
+    a = 2 * math.pi * frame / num_frames
+    eye = (center[0] + radius * math.cos(a), center[1] + height, center[2] + radius * math.sin(a))
     return Camera(eye=eye, center=center, fovy_deg=45.0, width=1920, height=1080, near=0.01, far=1000.0,
                   tess_rate_pixels=tess_rate_pixels)
 
@@ -564,6 +615,7 @@ def scene_terrain(n: int = 1024, extent: float = 1024.0, map_size: int = 4096, o
 
 def camera_terrain(extent: float = 1024.0, height: float = 2.0, pitch_deg: float = 10.0) -> Camera:
     eye = np.array([0.0, height, 0.0])
-    d = np.array([np.cos(np.radians(pitch_deg)) * 0.0, -np.sin(np.radians(pitch_deg)), np.cos(np.radians(pitch_deg))])
+    p = math.radians(pitch_deg)
+    d = np.array([math.cos(p) * 0.0, -math.sin(p), math.cos(p)])
     return Camera(eye=tuple(eye), center=tuple(eye + d * 10.0), fovy_deg=45.0, width=3840, height=2160, near=0.01,
                   far=4 * extent, tess_rate_pixels=4.0)
