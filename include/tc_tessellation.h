@@ -443,7 +443,10 @@ typedef struct tc_schedule {
                                  * 4 or less: 64 registers per thread, 5: 48, 6 and more: 40 */
   uint32_t scanBlocksPerSM;     /* grid of the instantiate allocation kernels (tile sums, arguments) = SMs x this */
   uint32_t blocksPerSM;         /* persistent grid of the split kernel = SMs x this x (512 / splitBlockSize) */
-  uint32_t _pad[3];
+  uint32_t fullVertexBlocksPerSM; /* grid of the full-cluster vertex kernel = SMs x this (at most 4 resident);
+                                   * it runs beside the rest of the frame (fewer blocks leave room for it);
+                                   * 0: the default (4) */
+  uint32_t _pad[2];
 } tc_schedule;
 
 typedef struct tc_context_desc {

@@ -2,7 +2,9 @@
 
 The schedule (tc_schedule) sets the launch shapes of the persistent stages:
 grid multipliers of the classify warp kernels and of the instantiate
-allocation, the vertex kernel's register budget, the split tile size
+allocation, the vertex kernel's register budget, the grid of the
+full-cluster vertex kernel (which runs beside the rest of the frame), the
+split tile size
 (128 threads x 16 items, 256 or 512 threads x 32 items) and the split grid.
 Outputs do not depend on it (every allocation is a prefix sum in a fixed
 order), so tuning is a pure timing search.
@@ -25,6 +27,7 @@ SPACE = {
     "splitBlockSize": (128, 256, 512),
     "blocksPerSM": (1, 2, 4),
     "vertexBlocksPerSM": (3, 4, 5, 6),
+    "fullVertexBlocksPerSM": (1, 2, 3, 4),
 }
 
 

@@ -29,10 +29,12 @@ struct SlotPlan
 constexpr size_t kCtrlBytes = 8 + 8 * kMaxCounters;
 
 // kernels of a batched frame besides the split passes: frame_begin,
-// instances_classify, clusters_cull, classify (2), instantiate (4, twice: the
+// instances_classify, clusters_cull, classify (3), instantiate (4, twice: the
 // first part run overlapped with the split passes, then the others), blas
 // setup, blas insert (2)
-constexpr uint64_t kFrameFixedLaunches = 16;
+constexpr uint64_t kFrameFixedLaunches = 17;
+
+constexpr u32 kDefaultFullVertexBlocksPerSM = 4;
 
 struct Plan
 {
@@ -46,7 +48,7 @@ struct Plan
   u32    segRows;     // runs
   size_t runOffset;   // run starts (u32 x kMaxRuns+2)
   u32    classifyCap; // clusters the classify scratch holds
-  size_t clsCountsOffset, clsTriWordsOffset, clsBlockSumsOffset;
+  size_t clsCountsOffset, clsTriWordsOffset, clsBlockSumsOffset, clsFullRecsOffset;
   size_t partVertexOffset;  // u32 per part triangle
   size_t splitBaseOffset;   // 9 floats per split item: its base triangle's world positions
   size_t instOffset;  // instance cluster prefix (u32 x maxInstances+1)
@@ -84,9 +86,11 @@ struct tc_context
 
   // second stream of the batched frame: the first part run's instantiation
   // overlaps the split passes (fork / join through the two events)
-  cudaStream_t side    = nullptr;
+  cudaStream_t side    = nullptr;  // the first part run's instantiation
+  cudaStream_t side2   = nullptr;  // the full clusters' vertices
   cudaEvent_t  evFork  = nullptr;
   cudaEvent_t  evJoin  = nullptr;
+  cudaEvent_t  evJoin2 = nullptr;
 
   // graph cache
   cudaGraphExec_t graphExec = nullptr;
@@ -170,6 +174,8 @@ Plan make_plan(const tc_context_desc& d)
   off                 = align_up(off + (size_t)p.classifyCap * TC_MAX_CLUSTER_TRIANGLES * 4, 256);
   p.clsBlockSumsOffset = off;  // block sums, then the counter bases
   off = align_up(off + ((size_t)classify_max_blocks(p.classifyCap) + 1) * sizeof(ClusterOffsets), 256);
+  p.clsFullRecsOffset = off;  // per full cluster, then the slot range
+  off = align_up(off + (size_t)p.classifyCap * 8 + 8, 256);
   p.partVertexOffset  = off;
   off                 = align_up(off + (size_t)std::max(1u, k.maxPartTriangles) * 4, 256);
   p.splitBaseOffset   = off;
@@ -251,7 +257,9 @@ ClassifyBuffers classify_buffers(tc_context* ctx)
   return {reinterpret_cast<uint2*>(ctx->dScratch + p.clsCountsOffset),
           reinterpret_cast<u32*>(ctx->dScratch + p.clsTriWordsOffset),
           reinterpret_cast<ClusterOffsets*>(ctx->dScratch + p.clsBlockSumsOffset),
-          reinterpret_cast<ClusterOffsets*>(ctx->dScratch + p.clsBlockSumsOffset) + classify_max_blocks(p.classifyCap)};
+          reinterpret_cast<ClusterOffsets*>(ctx->dScratch + p.clsBlockSumsOffset) + classify_max_blocks(p.classifyCap),
+          reinterpret_cast<uint2*>(ctx->dScratch + p.clsFullRecsOffset),
+          reinterpret_cast<u32*>(ctx->dScratch + p.clsFullRecsOffset + (size_t)p.classifyCap * 8)};
 }
 
 InstantiateBuffers instantiate_buffers(tc_context* ctx)
@@ -314,6 +322,13 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   // run, the other runs after both.
   TC_CHECK_CUDA(cudaEventRecord(ctx->evFork, s));
   TC_CHECK_CUDA(cudaStreamWaitEvent(ctx->side, ctx->evFork, 0));
+  // The full clusters' vertices depend on classify alone and nothing later in
+  // the frame reads them: they run on a second side stream, joined at the end.
+  TC_CHECK_CUDA(cudaStreamWaitEvent(ctx->side2, ctx->evFork, 0));
+  TC_CHECK_CUDA(launch_classify_full_vertices(c, classify_buffers(ctx),
+                                              std::min(a->totalClusters, a->caps.maxVisibleClusters), ctx->numSMs,
+                                              sched.fullVertexBlocksPerSM, ctx->side2));
+  TC_CHECK_CUDA(cudaEventRecord(ctx->evJoin2, ctx->side2));
   {
     StageCtx c0 = c;
     bind_slot(ctx, c0, p.slotInstantiate0, false);
@@ -333,7 +348,6 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
     TC_CHECK_CUDA(launch_triangle_split(
         c, sb, persistent_grid(ctx, ceil_div(a->caps.maxSplitTriangles, split_items_per_tile(sb)), bpsm * (512 / sb)), s));
   }
-
   TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evJoin, 0));
   bind_slot(ctx, c, p.slotInstantiate, false);
   c.fuseSetup = TC_BUILD_SETUP_BUILD_BLAS;
@@ -348,6 +362,7 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
 
   u32* seg = reinterpret_cast<u32*>(ctx->dScratch + p.segOffset);
   TC_CHECK_CUDA(launch_blas_clusters_insert(c, seg, seg + (size_t)p.segStride * p.segRows, p.segStride, insert_grid(ctx, a), s));
+  TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evJoin2, 0));
 
   ctx->launches += kFrameFixedLaunches + passes;
   return TC_OK;
@@ -381,6 +396,20 @@ const char* tc_status_string(tc_status s)
 
 uint32_t tc_split_pass_count(uint32_t splitFactor) { return split_passes(splitFactor); }
 
+namespace {
+
+void destroy_streams(tc_context* ctx)
+{
+  for(cudaEvent_t* e : {&ctx->evFork, &ctx->evJoin, &ctx->evJoin2})
+    if(*e)
+      cudaEventDestroy(*e), *e = nullptr;
+  for(cudaStream_t* st : {&ctx->side, &ctx->side2})
+    if(*st)
+      cudaStreamDestroy(*st), *st = nullptr;
+}
+
+}  // namespace
+
 tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
 {
   if(!desc || !outCtx)
@@ -402,25 +431,22 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, desc->device);
   ctx->numSMs   = (u32)std::max(1, sms);
   if(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess
+     || cudaStreamCreateWithFlags(&ctx->side2, cudaStreamNonBlocking) != cudaSuccess
      || cudaEventCreateWithFlags(&ctx->evFork, cudaEventDisableTiming) != cudaSuccess
-     || cudaEventCreateWithFlags(&ctx->evJoin, cudaEventDisableTiming) != cudaSuccess)
+     || cudaEventCreateWithFlags(&ctx->evJoin, cudaEventDisableTiming) != cudaSuccess
+     || cudaEventCreateWithFlags(&ctx->evJoin2, cudaEventDisableTiming) != cudaSuccess)
   {
-    if(ctx->evFork)
-      cudaEventDestroy(ctx->evFork);
-    if(ctx->side)
-      cudaStreamDestroy(ctx->side);
+    destroy_streams(ctx);
     delete ctx;
     return TC_ERR_CUDA;
   }
-  ctx->schedule = {8, 256, 4, 8, 1, {0, 0, 0}};
+  ctx->schedule = {8, 256, 4, 8, 1, kDefaultFullVertexBlocksPerSM, {0, 0}};
   ctx->plan     = make_plan(*desc);
   if(cudaMalloc(&ctx->dScratch, ctx->plan.totalBytes) != cudaSuccess
      || cudaMemset(ctx->dScratch, 0, ctx->plan.totalBytes) != cudaSuccess)
   {
     cudaFree(ctx->dScratch);
-    cudaEventDestroy(ctx->evFork);
-    cudaEventDestroy(ctx->evJoin);
-    cudaStreamDestroy(ctx->side);
+    destroy_streams(ctx);
     delete ctx;
     return TC_ERR_CUDA;
   }
@@ -444,12 +470,7 @@ tc_status tc_context_destroy(tc_context* ctx)
   cudaFree(ctx->dTemplateSizes);
   cudaFree(ctx->dTable);
   cudaFree(ctx->dScratch);
-  if(ctx->evFork)
-    cudaEventDestroy(ctx->evFork);
-  if(ctx->evJoin)
-    cudaEventDestroy(ctx->evJoin);
-  if(ctx->side)
-    cudaStreamDestroy(ctx->side);
+  destroy_streams(ctx);
   delete ctx;
   return TC_OK;
 }
@@ -574,7 +595,11 @@ tc_status tc_set_schedule(tc_context* ctx, const tc_schedule* schedule)
       return TC_ERR_INVALID_ARG;
   if(q.splitBlockSize != 128 && q.splitBlockSize != 256 && q.splitBlockSize != 512)
     return TC_ERR_INVALID_ARG;
+  if(q.fullVertexBlocksPerSM > 64)
+    return TC_ERR_INVALID_ARG;
   ctx->schedule   = *schedule;
+  if(ctx->schedule.fullVertexBlocksPerSM == 0)
+    ctx->schedule.fullVertexBlocksPerSM = kDefaultFullVertexBlocksPerSM;
   ctx->graphValid = false;
   return TC_OK;
 }
@@ -716,7 +741,10 @@ tc_status tc_cluster_classify(tc_context* ctx, const tc_frame_args* a, uint32_t 
   TC_CHECK_CUDA(launch_cluster_classify(c, classify_buffers(ctx), std::min(a->totalClusters, a->caps.maxVisibleClusters),
                                         ctx->numSMs, ctx->schedule.classifyBlocksPerSM,
                                         reinterpret_cast<cudaStream_t>(stream)));
-  ctx->launches += 2;
+  TC_CHECK_CUDA(launch_classify_full_vertices(c, classify_buffers(ctx),
+                                              std::min(a->totalClusters, a->caps.maxVisibleClusters), ctx->numSMs,
+                                              4, reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += 3;
   return TC_OK;
 }
 

@@ -41,15 +41,18 @@ enum : int
   kNumCounters
 };
 
-// per-cluster counts: x = parts | splits << 7 | full << 14 | fullVertices << 15, y = CLAS bytes
-__device__ __forceinline__ uint2 pack_counts(u32 parts, u32 splits, bool full, u32 nv, u32 data)
+// per-cluster counts: x = parts | splits << 7 | full << 14 | fullVertices << 15 | fullTriangles << 22,
+// y = CLAS bytes
+__device__ __forceinline__ uint2 pack_counts(u32 parts, u32 splits, bool full, u32 nv, u32 nt, u32 data)
 {
-  return make_uint2(parts | (splits << 7) | ((full ? 1u : 0u) << 14) | ((full ? nv : 0u) << 15), full ? data : 0u);
+  return make_uint2(parts | (splits << 7) | ((full ? 1u : 0u) << 14) | ((full ? nv : 0u) << 15) | ((full ? nt : 0u) << 22),
+                    full ? data : 0u);
 }
 __device__ __forceinline__ u32 cnt_parts(uint2 r) { return r.x & 0x7F; }
 __device__ __forceinline__ u32 cnt_splits(uint2 r) { return (r.x >> 7) & 0x7F; }
 __device__ __forceinline__ u32 cnt_full(uint2 r) { return (r.x >> 14) & 1; }
 __device__ __forceinline__ u32 cnt_verts(uint2 r) { return (r.x >> 15) & 0x7F; }
+__device__ __forceinline__ u32 cnt_tris(uint2 r) { return (r.x >> 22) & 0x7F; }
 
 // tessellation.glsl:119-144 tess_getConfig, also reporting how the three
 // sub-triangle corners were rotated (0: none, 1: .yzx, 2: .zxy)
@@ -92,7 +95,11 @@ struct ClassifyScratch
   u32*            triWords;   // 64 per visible cluster
   ClusterOffsets* blockSums;  // per block of the grid
   ClusterOffsets* bases;      // the counters before the launch
+  uint2*          fullRecs;   // per full cluster (generated-cluster slot - first slot): visible index, first vertex
+  u32*            fullRange;  // [2]: the launch's generated-cluster slots [begin, end)
 };
+
+constexpr u32 kRejected = 0xFFFFFFFFu;  // fullRecs: a full cluster that did not fit the capacities
 
 // the contiguous range of visible clusters block `blk` of `nb` owns
 __device__ __forceinline__ void block_range(u32 n, u32 blk, u32 nb, u32& v0, u32& v1)
@@ -246,90 +253,112 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c
       s_wsum[warp][q] = 0;  // lane 0 accumulates the range's counts here
   }
 
-  for(u32 v = vBegin + warp; v < vEnd; v += kWarps)
+  // the warp's clusters are v = vBegin + warp + kWarps * j, j < cntW; their
+  // cluster records load one lane per cluster, 32 at a time, so that only the
+  // vertex and index loads remain on each cluster's dependent path
+  const u32  cntW   = vBegin + warp < vEnd ? (vEnd - vBegin - warp + kWarps - 1) / kWarps : 0u;
+  const u32* states = reinterpret_cast<const u32*>(b->instanceStates);
+  for(u32 j0 = 0; j0 < cntW; j0 += 32)
   {
-    const tc_ClusterInfo     ci = vis[begin + v];
-    const tc_RenderInstance* in = c.instances + ci.instanceID;
-    const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
-    u32                      nt = cl.numTriangles, nv = cl.numVertices;
-    if(nt > TC_MAX_CLUSTER_TRIANGLES || nv > TC_MAX_CLUSTER_VERTICES)
+    const u32 jn = min(32u, cntW - j0);
+    u32       hInst = 0, hMeta = 0, hFirstV = 0, hFirstT = 0, hData = 0;
+    if(lane < jn)
     {
-      if(lane == 0)
+      const tc_ClusterInfo     ci = vis[begin + vBegin + warp + kWarps * (j0 + lane)];
+      const tc_RenderInstance* in = c.instances + ci.instanceID;
+      const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
+      u32                      nt = cl.numTriangles, nv = cl.numVertices;
+      if(nt > TC_MAX_CLUSTER_TRIANGLES || nv > TC_MAX_CLUSTER_VERTICES)
+      {
         atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
-      nt = min(nt, TC_MAX_CLUSTER_TRIANGLES);
-      nv = min(nv, TC_MAX_CLUSTER_VERTICES);
+        nt = min(nt, TC_MAX_CLUSTER_TRIANGLES);
+        nv = min(nv, TC_MAX_CLUSTER_VERTICES);
+      }
+      // cluster_classify.comp.glsl:203-211: invisible instance, no tessellation
+      const bool culled = culling && (states[ci.instanceID] & TC_INSTANCE_VISIBLE_BIT) == 0;
+      hInst             = ci.instanceID;
+      hMeta             = nv | (nt << 8) | ((culled ? 1u : 0u) << 16);
+      hFirstV           = cl.firstLocalVertex;
+      hFirstT           = cl.firstLocalTriangle;
+      hData             = __ldg(reinterpret_cast<const u32*>(in->clusterTemplateInstantiatonSizes) + ci.clusterID);
     }
-    const bool culled =
-        culling && (reinterpret_cast<const u32*>(b->instanceStates)[ci.instanceID] & TC_INSTANCE_VISIBLE_BIT) == 0;
-    u32 m0 = 0, m1 = 0, w0 = 0, w1 = 0;
-    u32 simple = nt;  // cluster_classify.comp.glsl:203-211: invisible instance, no tessellation
-    if(!culled)
+    for(u32 jj = 0; jj < jn; jj++)
     {
-      // cluster_classify.comp.glsl:180-198 vertices, then 217-246 factors; each
-      // vertex is taken to world space once here (the same operations the
-      // shader applies per triangle corner, so the same bits)
-      const float* pos = reinterpret_cast<const float*>(in->positions);
-      float        m[16];
+      const u32                v      = vBegin + warp + kWarps * (j0 + jj);
+      const u32                meta   = __shfl_sync(0xFFFFFFFFu, hMeta, jj);
+      const u32                nv     = meta & 0xFF, nt = (meta >> 8) & 0xFF;
+      const bool               culled = (meta >> 16) != 0;
+      const tc_RenderInstance* in     = c.instances + __shfl_sync(0xFFFFFFFFu, hInst, jj);
+      const u32                firstV = __shfl_sync(0xFFFFFFFFu, hFirstV, jj);
+      const u32                firstT = __shfl_sync(0xFFFFFFFFu, hFirstT, jj);
+      u32                      m0 = 0, m1 = 0, w0 = 0, w1 = 0;
+      u32                      simple = nt;
+      if(!culled)
+      {
+        // indices first (their loads overlap the vertex loads); masked to the
+        // staged range: a malformed index reads a wrong vertex of the same
+        // cluster, never outside shared memory
+        const uint8_t* lt = reinterpret_cast<const uint8_t*>(in->clusterLocalTriangles) + firstT;
+        u32            ia = 0, ib = 0;
+        if(lane < nt)
+          ia = (lt[lane * 3 + 0] & 63u) | ((lt[lane * 3 + 1] & 63u) << 8) | ((lt[lane * 3 + 2] & 63u) << 16);
+        if(lane + 32 < nt)
+          ib = (lt[lane * 3 + 96] & 63u) | ((lt[lane * 3 + 97] & 63u) << 8) | ((lt[lane * 3 + 98] & 63u) << 16);
+        // cluster_classify.comp.glsl:180-198 vertices, then 217-246 factors; each
+        // vertex is taken to world space once here (the same operations the
+        // shader applies per triangle corner, so the same bits)
+        const float* pos = reinterpret_cast<const float*>(in->positions);
+        float        m[16];
 #pragma unroll
-      for(int j = 0; j < 16; j++)
-        m[j] = __ldg(in->worldMatrix.m + j);
-      for(u32 i = lane; i < nv; i += 32)
-      {
-        const f3    w = xform_point(m, ldg3(pos, cl.firstLocalVertex + i));
-        const float d = dist3(w, fp.viewPos);
-        s_vert[warp][i] = w;
-        s_dist[warp][i] = {d, __fdiv_rn(1.0f, d)};
+        for(int q = 0; q < 16; q++)
+          m[q] = __ldg(in->worldMatrix.m + q);
+        for(u32 i = lane; i < nv; i += 32)
+        {
+          const f3    w = xform_point(m, ldg3(pos, firstV + i));
+          const float d = dist3(w, fp.viewPos);
+          s_vert[warp][i] = w;
+          s_dist[warp][i] = {d, __fdiv_rn(1.0f, d)};
+        }
+        __syncwarp();
+        auto classify = [&](u32 idx, u32& mOut, u32& wOut) {
+          const u32   i0 = idx & 0xFF, i1 = (idx >> 8) & 0xFF, i2 = idx >> 16;
+          const f2    d0 = s_dist[warp][i0], d1 = s_dist[warp][i1], d2 = s_dist[warp][i2];
+          const uint3 f  = tess_factors_hoisted(s_vert[warp][i0], s_vert[warp][i1], s_vert[warp][i2], d0.x, d1.x,
+                                                d2.x, d0.y, d1.y, d2.y, rNear, fp);
+          mOut           = max(max(f.x, f.y), f.z);
+          wOut           = classify_triangle(f, sf);
+        };
+        if(lane < nt)
+          classify(ia, m0, w0);
+        if(lane + 32 < nt)
+          classify(ib, m1, w1);
+        simple = __popc(__ballot_sync(0xFFFFFFFFu, lane < nt && m0 == 1))
+                 + __popc(__ballot_sync(0xFFFFFFFFu, lane + 32 < nt && m1 == 1));
+        __syncwarp();  // s_vert is reused by the next cluster
       }
-      __syncwarp();
-      // indices are masked to the staged range: a malformed index reads a wrong
-      // vertex of the same cluster, never outside shared memory
-      const uint8_t* lt = reinterpret_cast<const uint8_t*>(in->clusterLocalTriangles) + cl.firstLocalTriangle;
-      if(lane < nt)
+      const bool full  = simple == nt;
+      u32        parts = 0, splits = 0;
+      if(!full)
       {
-        const u32   i0 = lt[lane * 3 + 0] & 63u, i1 = lt[lane * 3 + 1] & 63u, i2 = lt[lane * 3 + 2] & 63u;
-        const f2    d0 = s_dist[warp][i0], d1 = s_dist[warp][i1], d2 = s_dist[warp][i2];
-        const uint3 f  = tess_factors_hoisted(s_vert[warp][i0], s_vert[warp][i1], s_vert[warp][i2], d0.x, d1.x, d2.x,
-                                              d0.y, d1.y, d2.y, rNear, fp);
-        m0 = max(max(f.x, f.y), f.z);
-        w0 = classify_triangle(f, sf);
+        parts  = __popc(__ballot_sync(0xFFFFFFFFu, lane < nt && m0 <= TC_TESSTABLE_SIZE))
+                 + __popc(__ballot_sync(0xFFFFFFFFu, lane + 32 < nt && m1 <= TC_TESSTABLE_SIZE));
+        splits = nt - parts;
+        u32* tw = cs.triWords + (u64)v * TC_MAX_CLUSTER_TRIANGLES;
+        if(lane < nt)
+          tw[lane] = w0;
+        if(lane + 32 < nt)
+          tw[lane + 32] = w1;
       }
-      if(lane + 32 < nt)
+      const u32 data = __shfl_sync(0xFFFFFFFFu, hData, jj);
+      if(lane == 0)
       {
-        const u32   t = lane + 32;
-        const u32   i0 = lt[t * 3 + 0] & 63u, i1 = lt[t * 3 + 1] & 63u, i2 = lt[t * 3 + 2] & 63u;
-        const f2    d0 = s_dist[warp][i0], d1 = s_dist[warp][i1], d2 = s_dist[warp][i2];
-        const uint3 f  = tess_factors_hoisted(s_vert[warp][i0], s_vert[warp][i1], s_vert[warp][i2], d0.x, d1.x, d2.x,
-                                              d0.y, d1.y, d2.y, rNear, fp);
-        m1 = max(max(f.x, f.y), f.z);
-        w1 = classify_triangle(f, sf);
+        cs.counts[v] = pack_counts(parts, splits, full, nv, nt, data);
+        s_wsum[warp][kCntParts] += parts;
+        s_wsum[warp][kCntSplits] += splits;
+        s_wsum[warp][kCntGen] += full ? 1u : 0u;
+        s_wsum[warp][kCntVerts] += full ? nv : 0u;
+        s_wsum[warp][kCntData] += full ? data : 0u;
       }
-      simple = __popc(__ballot_sync(0xFFFFFFFFu, lane < nt && m0 == 1))
-               + __popc(__ballot_sync(0xFFFFFFFFu, lane + 32 < nt && m1 == 1));
-      __syncwarp();  // s_vert is reused by the next cluster
-    }
-    const bool full  = simple == nt;
-    u32        parts = 0, splits = 0;
-    if(!full)
-    {
-      parts  = __popc(__ballot_sync(0xFFFFFFFFu, lane < nt && m0 <= TC_TESSTABLE_SIZE))
-               + __popc(__ballot_sync(0xFFFFFFFFu, lane + 32 < nt && m1 <= TC_TESSTABLE_SIZE));
-      splits = nt - parts;
-      u32* tw = cs.triWords + (u64)v * TC_MAX_CLUSTER_TRIANGLES;
-      if(lane < nt)
-        tw[lane] = w0;
-      if(lane + 32 < nt)
-        tw[lane + 32] = w1;
-    }
-    if(lane == 0)
-    {
-      const u32 data =
-          full ? __ldg(reinterpret_cast<const u32*>(in->clusterTemplateInstantiatonSizes) + ci.clusterID) : 0u;
-      cs.counts[v] = pack_counts(parts, splits, full, nv, data);
-      s_wsum[warp][kCntParts] += parts;
-      s_wsum[warp][kCntSplits] += splits;
-      s_wsum[warp][kCntGen] += full ? 1u : 0u;
-      s_wsum[warp][kCntVerts] += full ? nv : 0u;
-      s_wsum[warp][kCntData] += data;
     }
   }
 
@@ -432,7 +461,6 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c
 {
   stage_prologue();
   __shared__ u32            s_range[2];
-  __shared__ FullRecord     s_full[kWarps][32];
   __shared__ u64            s_warp[33][kNumCounters];
   __shared__ ClusterOffsets s_off[kBlock];  // offsets of the chunk's clusters
   __shared__ uint2          s_cnt[kBlock];  // counts of the chunk's clusters
@@ -446,21 +474,18 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c
   tc_SceneBuilding*     b            = c.build;
   const tc_caps&        k            = c.caps;
   const tc_ClusterInfo* vis          = reinterpret_cast<const tc_ClusterInfo*>(b->visibleClusters);
-  const bool            haveTextures = c.numTextures > 0 && c.textures != nullptr;
   const u64             maxData      = (u64)k.maxGeneratedClusterMegs * 1024ull * 1024ull;
   tc_TessTriangleInfo*  splits       = reinterpret_cast<tc_TessTriangleInfo*>(b->splitTriangles);
   tc_TessTriangleInfo*  parts        = reinterpret_cast<tc_TessTriangleInfo*>(b->partTriangles);
-  float*                gv           = reinterpret_cast<float*>(b->genVertices);
   tc_BlasBuildInfo*     blas         = reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos);
   const u32             ltm          = (1u << lane) - 1u;
   u32                   statTris = 0, statTemp = 0;
 
   u64 pre[kNumCounters];  // offsets of the next chunk's first cluster
   block_prefix(cs, pre, s_warp);
-  u32 vBegin, vEnd;
+  const u32 genBase = cs.bases->gen;
+  u32       vBegin, vEnd;
   block_range(n, blockIdx.x, gridDim.x, vBegin, vEnd);
-  FullRecord* rec = s_full[warp];
-
   for(u32 c0 = vBegin; c0 < vEnd; c0 += kBlock)
   {
     // exclusive scan of the chunk's counts, in cluster order
@@ -563,17 +588,15 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c
     }
 
     // ---- phase 2: full clusters of the warp's part, 32 at a time ---------------
-    // cluster_classify.comp.glsl:271-488: instantiation arguments (one lane per
-    // cluster, so the instance / cluster loads of 32 clusters overlap), then the
-    // clusters' displaced vertices (:457-482), which are contiguous in
-    // genVertices, walked on consecutive lanes.
+    // cluster_classify.comp.glsl:271-488: instantiation arguments, one lane per
+    // cluster (the instance loads of 32 clusters overlap). The displaced
+    // vertices (:457-482) are written by k_classify_full_vertices from the
+    // records left here.
     for(u32 i0 = lo; i0 < hi; i0 += 32)
     {
-      const u32  i    = i0 + lane;
-      bool       full = false;
-      u32        nv   = 0;
-      u32        inst = 0xFFFFFFFFu;
-      FullRecord fr;
+      const u32 i    = i0 + lane;
+      bool      full = false;
+      u32       inst = 0xFFFFFFFFu;
       if(i < hi)
       {
         const uint2 r = s_cnt[i];
@@ -581,14 +604,13 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c
         {
           const ClusterOffsets off = s_off[i];
           const u32            v   = c0 + i;
-          nv                       = cnt_verts(r);
-          full = !((u64)off.vert + nv > k.maxGeneratedVertices || (u64)off.gen + 1 > k.maxGeneratedClusters
+          full = !((u64)off.vert + cnt_verts(r) > k.maxGeneratedVertices || (u64)off.gen + 1 > k.maxGeneratedClusters
                    || off.data + r.y > maxData);
+          cs.fullRecs[off.gen - genBase] = full ? make_uint2(begin + v, off.vert) : make_uint2(kRejected, 0u);
           if(full)
           {
             const tc_ClusterInfo     ci = vis[begin + v];
             const tc_RenderInstance* in = c.instances + ci.instanceID;
-            const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
             // accepted instantiations form a prefix of the serial order, so the
             // instantiation slot equals the generated-cluster slot
             const u32                  tempOffset = off.gen;
@@ -604,65 +626,22 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c
             if((c.flags & TC_FLAG_WRITE_FULLCLUSTERS) && b->fullClusters)
               reinterpret_cast<tc_ClusterInfo*>(b->fullClusters)[tempOffset] = ci;
             statTemp += 1;
-            statTris += min((u32)cl.numTriangles, TC_MAX_CLUSTER_TRIANGLES);
-            inst     = ci.instanceID;
-            fr.vo    = off.vert;
-            fr.nv    = nv;
-            fr.pos   = reinterpret_cast<const float*>(in->positions);
-            fr.nrm   = reinterpret_cast<const float*>(in->normals);
-            fr.uvs   = reinterpret_cast<const float*>(in->texcoords);
-            fr.first = cl.firstLocalVertex;
-            tc_DisplacementTexture tx = {};
-            if(haveTextures && in->displacementIndex >= 0)
-            {
-              if((u32)in->displacementIndex < c.numTextures)
-                tx = c.textures[in->displacementIndex];
-              else
-                atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
-            }
-            fr.map    = make_map_desc(tx);
-            fr.scale  = in->displacementScale * c.view->displacementScale;
-            fr.offset = in->displacementOffset + c.view->displacementOffset;
+            statTris += cnt_tris(r);
+            inst = ci.instanceID;
           }
         }
       }
       const u32 fm = __ballot_sync(0xFFFFFFFFu, full);
-      if(fm == 0)
-        continue;
-      // records packed in lane order: record r belongs to the r-th full cluster
-      if(full)
-        rec[__popc(fm & ltm)] = fr;
       // CLAS reference counts: one atomic per distinct instance of the batch
       for(u32 remaining = fm; remaining;)
       {
         const int src = __ffs(remaining) - 1;
         const u32 gk  = __shfl_sync(0xFFFFFFFFu, inst, src);
-        const u32 sum = __popc(__ballot_sync(0xFFFFFFFFu, full && inst == gk));
-        remaining &= ~__ballot_sync(0xFFFFFFFFu, full && inst == gk);
+        const u32 sel = __ballot_sync(0xFFFFFFFFu, full && inst == gk);
+        remaining &= ~sel;
         if((int)lane == src)
-          atomicAdd(&blas[gk].clusterReferencesCount, sum);
+          atomicAdd(&blas[gk].clusterReferencesCount, __popc(sel));
       }
-      __syncwarp();
-      // per record (lane r < nrec): first vertex within the batch and vertex count
-      const u32 nrec   = __popc(fm);
-      const u32 vBase  = rec[0].vo;
-      const u32 rStart = lane < nrec ? rec[lane].vo - vBase : 0u;
-      const u32 rCount = lane < nrec ? rec[lane].nv : 0u;
-      const u32 rEnd   = __shfl_sync(0xFFFFFFFFu, rStart + rCount, nrec - 1);
-      const bool owner = lane < nrec;
-      // one specialisation when the batch's clusters share a map kind
-      const u32 kind  = owner ? rec[lane].map.kind : 0u;
-      const u32 kind0 = rec[0].map.kind;
-      const u32 kw    = __all_sync(0xFFFFFFFFu, !owner || kind == kind0) ? kind0 : ~0u;
-      float*    dst   = gv + (u64)vBase * 3;
-      switch(kw)
-      {
-        case affine_kind(TC_TEXEL_F32, true): full_steps<affine_kind(TC_TEXEL_F32, true)>(rec, owner, rStart, rEnd, dst); break;
-        case affine_kind(TC_TEXEL_F16, true): full_steps<affine_kind(TC_TEXEL_F16, true)>(rec, owner, rStart, rEnd, dst); break;
-        case kAffineFlat: full_steps<kAffineFlat>(rec, owner, rStart, rEnd, dst); break;
-        default: full_steps<~0u>(rec, owner, rStart, rEnd, dst); break;
-      }
-      __syncwarp();  // records are rewritten by the next batch
     }
     __syncthreads();  // s_off / s_cnt are rewritten by the next chunk
   }
@@ -686,6 +665,8 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c
   // counters after count took their values
   if(blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
   {
+    cs.fullRange[0] = genBase;
+    cs.fullRange[1] = (u32)pre[kCntGen];
     if(n)
     {
       const ClusterOffsets b0  = *cs.bases;
@@ -702,12 +683,98 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c
   }
 }
 
+// cluster_classify.comp.glsl:457-482: the displaced vertices of the full
+// clusters the write launch accepted. A warp takes `per` <= 32 consecutive
+// generated-cluster slots (per: the slots spread over all of the grid's
+// warps): one lane per cluster sets up its record, then the clusters' vertex
+// ranges, contiguous in genVertices, are walked on consecutive lanes. Its own
+// launch so that it can overlap other work.
+__global__ void __launch_bounds__(kBlock, 4) k_classify_full_vertices(StageCtx c, ClassifyScratch cs)
+{
+  stage_prologue();
+  __shared__ FullRecord s_full[kWarps][32];
+  const u32             lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const u32             ltm  = (1u << lane) - 1u;
+  const u32             count        = cs.fullRange[1] - cs.fullRange[0];
+  const u32             totalWarps   = gridDim.x * kWarps;
+  const u32             per          = min(32u, max(1u, (count + totalWarps - 1) / totalWarps));
+  const u32             numChunks    = (count + per - 1) / per;
+  const tc_SceneBuilding* b          = c.build;
+  const tc_ClusterInfo* vis          = reinterpret_cast<const tc_ClusterInfo*>(b->visibleClusters);
+  const bool            haveTextures = c.numTextures > 0 && c.textures != nullptr;
+  float*                gv           = reinterpret_cast<float*>(b->genVertices);
+  FullRecord*           rec          = s_full[warp];
+
+  for(u32 chunk = blockIdx.x * kWarps + warp; chunk < numChunks; chunk += totalWarps)
+  {
+    const u32  slot  = chunk * per + lane;
+    bool       owner = false;
+    FullRecord fr;
+    if(lane < per && slot < count)
+    {
+      const uint2 fs = cs.fullRecs[slot];
+      if(fs.x != kRejected)
+      {
+        const tc_ClusterInfo     ci = vis[fs.x];
+        const tc_RenderInstance* in = c.instances + ci.instanceID;
+        const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
+        owner                       = true;
+        fr.vo                       = fs.y;
+        fr.nv                       = min((u32)cl.numVertices, TC_MAX_CLUSTER_VERTICES);
+        fr.pos                      = reinterpret_cast<const float*>(in->positions);
+        fr.nrm                      = reinterpret_cast<const float*>(in->normals);
+        fr.uvs                      = reinterpret_cast<const float*>(in->texcoords);
+        fr.first                    = cl.firstLocalVertex;
+        tc_DisplacementTexture tx   = {};
+        if(haveTextures && in->displacementIndex >= 0)
+        {
+          if((u32)in->displacementIndex < c.numTextures)
+            tx = c.textures[in->displacementIndex];
+          else
+            atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
+        }
+        fr.map    = make_map_desc(tx);
+        fr.scale  = in->displacementScale * c.view->displacementScale;
+        fr.offset = in->displacementOffset + c.view->displacementOffset;
+      }
+    }
+    // accepted clusters are a prefix of the slots, so the owners are the
+    // first lanes and their vertex ranges follow each other
+    const u32 fm = __ballot_sync(0xFFFFFFFFu, owner);
+    if(fm == 0)
+      continue;
+    if(owner)
+      rec[__popc(fm & ltm)] = fr;
+    __syncwarp();
+    // per record (lane r < nrec): first vertex within the batch and vertex count
+    const u32  nrec   = __popc(fm);
+    const u32  vBase  = rec[0].vo;
+    const u32  rStart = lane < nrec ? rec[lane].vo - vBase : 0u;
+    const u32  rCount = lane < nrec ? rec[lane].nv : 0u;
+    const u32  rEnd   = __shfl_sync(0xFFFFFFFFu, rStart + rCount, nrec - 1);
+    const bool own    = lane < nrec;
+    // one specialisation when the batch's clusters share a map kind
+    const u32 kind  = own ? rec[lane].map.kind : 0u;
+    const u32 kind0 = rec[0].map.kind;
+    const u32 kw    = __all_sync(0xFFFFFFFFu, !own || kind == kind0) ? kind0 : ~0u;
+    float*    dst   = gv + (u64)vBase * 3;
+    switch(kw)
+    {
+      case affine_kind(TC_TEXEL_F32, true): full_steps<affine_kind(TC_TEXEL_F32, true)>(rec, own, rStart, rEnd, dst); break;
+      case affine_kind(TC_TEXEL_F16, true): full_steps<affine_kind(TC_TEXEL_F16, true)>(rec, own, rStart, rEnd, dst); break;
+      case kAffineFlat: full_steps<kAffineFlat>(rec, own, rStart, rEnd, dst); break;
+      default: full_steps<~0u>(rec, own, rStart, rEnd, dst); break;
+    }
+    __syncwarp();  // records are rewritten by the next batch
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
                                     u32 warpBlocksPerSM, cudaStream_t s)
 {
-  ClassifyScratch cs{buf.counts, buf.triWords, buf.blockSums, buf.bases};
+  ClassifyScratch cs{buf.counts, buf.triWords, buf.blockSums, buf.bases, buf.fullRecs, buf.fullRange};
   // both launches use this grid: the blocks' cluster ranges must agree
   const u32 grid = std::max(1u, std::min(classify_max_blocks(maxClusters), numSMs * std::max(1u, warpBlocksPerSM)));
   // register budget from the requested residency: 4 or less -> 64, 5-7 -> 40, 8 and more -> 32
@@ -720,6 +787,15 @@ cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& bu
   return occ == 8   ? launch_pdl(k_classify_write<8>, grid, kBlock, s, c, cs)
          : occ == 6 ? launch_pdl(k_classify_write<6>, grid, kBlock, s, c, cs)
                     : launch_pdl(k_classify_write<4>, grid, kBlock, s, c, cs);
+}
+
+cudaError_t launch_classify_full_vertices(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
+                                          u32 blocksPerSM, cudaStream_t s)
+{
+  ClassifyScratch cs{buf.counts, buf.triWords, buf.blockSums, buf.bases, buf.fullRecs, buf.fullRange};
+  // every warp of the grid takes a share of the slots
+  const u32 grid = std::max(1u, std::min((maxClusters + kWarps - 1) / kWarps, numSMs * std::max(1u, blocksPerSM)));
+  return launch_pdl(k_classify_full_vertices, grid, kBlock, s, c, cs);
 }
 
 u32 classify_max_blocks(u32 maxClusters) { return std::max(1u, (maxClusters + kWarps - 1) / kWarps); }

@@ -27,6 +27,8 @@ struct ClassifyBuffers
   u32*            triWords;   // 64 per cluster
   ClusterOffsets* blockSums;  // per block: the sums of its clusters' counts
   ClusterOffsets* bases;      // one: the counters before the launch
+  uint2*          fullRecs;   // per full cluster of the window: visible index, first generated vertex
+  u32*            fullRange;  // [2]: the window's generated-cluster slots
 };
 
 cudaError_t launch_frame_begin(const StageCtx& c, u32 grid, cudaStream_t s);
@@ -35,6 +37,9 @@ cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStr
 cudaError_t launch_build_setup(const StageCtx& c, u32 mode, cudaStream_t s);
 cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
                                     u32 warpBlocksPerSM, cudaStream_t s);
+// the full clusters' displaced vertices of the last launch_cluster_classify
+cudaError_t launch_classify_full_vertices(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
+                                          u32 blocksPerSM, cudaStream_t s);
 u32         classify_max_blocks(u32 maxClusters);
 cudaError_t launch_triangle_split(const StageCtx& c, u32 blockSize, u32 grid, cudaStream_t s);
 // triangle_tess_template_instantiate scratch, per part triangle

@@ -192,10 +192,12 @@ class FrameArgs(ctypes.Structure):
 class Schedule(ctypes.Structure):
     _fields_ = [("classifyBlocksPerSM", ctypes.c_uint32), ("splitBlockSize", ctypes.c_uint32),
                 ("vertexBlocksPerSM", ctypes.c_uint32), ("scanBlocksPerSM", ctypes.c_uint32),
-                ("blocksPerSM", ctypes.c_uint32), ("_pad", ctypes.c_uint32 * 3)]
+                ("blocksPerSM", ctypes.c_uint32), ("fullVertexBlocksPerSM", ctypes.c_uint32),
+                ("_pad", ctypes.c_uint32 * 2)]
 
 
-SCHEDULE_FIELDS = ("classifyBlocksPerSM", "splitBlockSize", "vertexBlocksPerSM", "scanBlocksPerSM", "blocksPerSM")
+SCHEDULE_FIELDS = ("classifyBlocksPerSM", "splitBlockSize", "vertexBlocksPerSM", "scanBlocksPerSM", "blocksPerSM",
+                   "fullVertexBlocksPerSM")
 
 
 class ContextDesc(ctypes.Structure):
