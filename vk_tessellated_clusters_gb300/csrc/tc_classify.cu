@@ -689,7 +689,8 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c
 // warps): one lane per cluster sets up its record, then the clusters' vertex
 // ranges, contiguous in genVertices, are walked on consecutive lanes. Its own
 // launch so that it can overlap other work.
-__global__ void __launch_bounds__(kBlock, 4) k_classify_full_vertices(StageCtx c, ClassifyScratch cs)
+template <int MinBlocks>
+__global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_full_vertices(StageCtx c, ClassifyScratch cs)
 {
   stage_prologue();
   __shared__ FullRecord s_full[kWarps][32];
@@ -795,7 +796,10 @@ cudaError_t launch_classify_full_vertices(const StageCtx& c, const ClassifyBuffe
   ClassifyScratch cs{buf.counts, buf.triWords, buf.blockSums, buf.bases, buf.fullRecs, buf.fullRange};
   // every warp of the grid takes a share of the slots
   const u32 grid = std::max(1u, std::min((maxClusters + kWarps - 1) / kWarps, numSMs * std::max(1u, blocksPerSM)));
-  return launch_pdl(k_classify_full_vertices, grid, kBlock, s, c, cs);
+  // register budget from the requested residency: 4 or less -> 64, 5-6 -> 40, 7 and more -> 32
+  return blocksPerSM >= 7   ? launch_pdl(k_classify_full_vertices<8>, grid, kBlock, s, c, cs)
+         : blocksPerSM >= 5 ? launch_pdl(k_classify_full_vertices<6>, grid, kBlock, s, c, cs)
+                            : launch_pdl(k_classify_full_vertices<4>, grid, kBlock, s, c, cs);
 }
 
 u32 classify_max_blocks(u32 maxClusters) { return std::max(1u, (maxClusters + kWarps - 1) / kWarps); }
