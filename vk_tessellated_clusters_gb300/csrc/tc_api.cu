@@ -282,7 +282,8 @@ u32 frame_begin_grid(const tc_context* ctx, const tc_frame_args* a)
 // element are dependent loads; many resident warps hide them)
 u32 insert_grid(const tc_context* ctx, const tc_frame_args* a)
 {
-  return std::max(ctx->numSMs * 4, std::min(ceil_div(a->caps.maxGeneratedClusters, 512), 1u << 16));
+  // tiles of 1024 instantiations per block (at least four blocks per SM)
+  return std::max(ctx->numSMs * 4, std::min(ceil_div(a->caps.maxGeneratedClusters, 1024), 1u << 16));
 }
 
 u32 split_block(const tc_schedule& s)

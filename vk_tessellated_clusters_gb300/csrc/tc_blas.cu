@@ -109,8 +109,16 @@ __device__ __forceinline__ u32 run_of(const Runs& r, u32 j)
   return q;
 }
 
+// Both insert kernels walk the instantiations in tiles of kInsertTile: thread t
+// of a block takes elements t, t + 256, t + 512 and t + 768 of the tile, so each
+// load instruction stays coalesced and a thread has four independent load
+// chains in flight.
+constexpr u32 kInsertBlock = 256;
+constexpr u32 kInsertItems = 4;
+constexpr u32 kInsertTile  = kInsertBlock * kInsertItems;
+
 // segment tables: segStart/segEnd[run * stride + instance], zeroed beforehand
-__global__ void k_blas_segments(StageCtx c, u32* segStart, u32* segEnd, u32 stride)
+__global__ void __launch_bounds__(kInsertBlock) k_blas_segments(StageCtx c, u32* segStart, u32* segEnd, u32 stride)
 {
   stage_prologue();
   __shared__ Runs s_runs;
@@ -120,25 +128,42 @@ __global__ void k_blas_segments(StageCtx c, u32* segStart, u32* segEnd, u32 stri
   const tc_SceneBuilding* b     = c.build;
   const u32*              ids   = reinterpret_cast<const u32*>(b->tempInstanceIDs);
   const u32               temps = b->tempInstantiateCounter;
-  for(u32 j = blockIdx.x * blockDim.x + threadIdx.x; j < temps; j += gridDim.x * blockDim.x)
+  for(u32 t0 = blockIdx.x * kInsertTile; t0 < temps; t0 += gridDim.x * kInsertTile)
   {
-    const u32 r    = run_of(s_runs, j);
-    const u32 inst = ids[j];
-    if(inst >= c.numInstances)
+    u32 prev[kInsertItems], cur[kInsertItems], next[kInsertItems];
+#pragma unroll
+    for(u32 k = 0; k < kInsertItems; k++)
     {
-      atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
-      continue;
+      const u32 j = t0 + threadIdx.x + k * kInsertBlock;
+      cur[k]      = j < temps ? ids[j] : 0u;
+      prev[k]     = j < temps && j > 0 ? ids[j - 1] : 0u;
+      next[k]     = j + 1 < temps ? ids[j + 1] : 0u;
     }
-    const bool first = j == s_runs.bound[r] || ids[j - 1] != inst;
-    const bool last  = j + 1 == s_runs.bound[r + 1] || ids[j + 1] != inst;
-    if(first)
-      segStart[r * stride + inst] = j;
-    if(last)
-      segEnd[r * stride + inst] = j + 1;
+#pragma unroll
+    for(u32 k = 0; k < kInsertItems; k++)
+    {
+      const u32 j = t0 + threadIdx.x + k * kInsertBlock;
+      if(j >= temps)
+        continue;
+      const u32 inst = cur[k];
+      if(inst >= c.numInstances)
+      {
+        atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
+        continue;
+      }
+      const u32  r     = run_of(s_runs, j);
+      const bool first = j == s_runs.bound[r] || prev[k] != inst;
+      const bool last  = j + 1 == s_runs.bound[r + 1] || next[k] != inst;
+      if(first)
+        segStart[r * stride + inst] = j;
+      if(last)
+        segEnd[r * stride + inst] = j + 1;
+    }
   }
 }
 
-__global__ void k_blas_scatter(StageCtx c, const u32* segStart, const u32* segEnd, u32 stride)
+__global__ void __launch_bounds__(kInsertBlock) k_blas_scatter(StageCtx c, const u32* segStart, const u32* segEnd,
+                                                               u32 stride)
 {
   stage_prologue();
   __shared__ Runs s_runs;
@@ -152,22 +177,34 @@ __global__ void k_blas_scatter(StageCtx c, const u32* segStart, const u32* segEn
   const u32*              csz   = reinterpret_cast<const u32*>(b->tempClusterSizes);
   const u32               temps = b->tempInstantiateCounter;
   u64                     statData = 0;
-  const u32               gtid  = blockIdx.x * blockDim.x + threadIdx.x;
-  for(u32 j = gtid; j < temps; j += gridDim.x * blockDim.x)
+  for(u32 t0 = blockIdx.x * kInsertTile; t0 < temps; t0 += gridDim.x * kInsertTile)
   {
-    const u32 r    = run_of(s_runs, j);
-    const u32 inst = ids[j];
-    if(inst >= c.numInstances)
-      continue;
-    u32 rank = j - segStart[r * stride + inst];
-    for(u32 q = 0; q < r; q++)
-      rank += segEnd[q * stride + inst] - segStart[q * stride + inst];
-    reinterpret_cast<u64*>(infos[inst].clusterReferences)[rank] = addrs[j];
-    if(csz)
-      statData += csz[j];
+    u32 inst[kInsertItems], size[kInsertItems];
+    u64 addr[kInsertItems];
+#pragma unroll
+    for(u32 k = 0; k < kInsertItems; k++)
+    {
+      const u32 j = t0 + threadIdx.x + k * kInsertBlock;
+      inst[k]     = j < temps ? ids[j] : ~0u;
+      addr[k]     = j < temps ? addrs[j] : 0ull;
+      size[k]     = csz && j < temps ? csz[j] : 0u;
+    }
+#pragma unroll
+    for(u32 k = 0; k < kInsertItems; k++)
+    {
+      const u32 j = t0 + threadIdx.x + k * kInsertBlock;
+      if(j >= temps || inst[k] >= c.numInstances)
+        continue;
+      const u32 r    = run_of(s_runs, j);
+      u32       rank = j - segStart[r * stride + inst[k]];
+      for(u32 q = 0; q < r; q++)
+        rank += segEnd[q * stride + inst[k]] - segStart[q * stride + inst[k]];
+      reinterpret_cast<u64*>(infos[inst[k]].clusterReferences)[rank] = addr[k];
+      statData += size[k];
+    }
   }
   // final list lengths (blas_clusters_insert.comp.glsl:131 increments them one by one)
-  for(u32 i = gtid; i < c.numInstances; i += gridDim.x * blockDim.x)
+  for(u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < c.numInstances; i += gridDim.x * blockDim.x)
   {
     u32 total = 0;
     for(u32 q = 0; q < s_runs.count; q++)
@@ -190,10 +227,10 @@ cudaError_t launch_blas_setup_insertion(const StageCtx& c, u32 grid, u32 block, 
 cudaError_t launch_blas_clusters_insert(const StageCtx& c, u32* segStart, u32* segEnd, u32 stride, u32 grid,
                                         cudaStream_t s)
 {
-  cudaError_t e = launch_pdl(k_blas_segments, grid, 256, s, c, segStart, segEnd, stride);
+  cudaError_t e = launch_pdl(k_blas_segments, grid, kInsertBlock, s, c, segStart, segEnd, stride);
   if(e != cudaSuccess)
     return e;
-  return launch_pdl(k_blas_scatter, grid, 256, s, c, segStart, segEnd, stride);
+  return launch_pdl(k_blas_scatter, grid, kInsertBlock, s, c, segStart, segEnd, stride);
 }
 
 }  // namespace tc

@@ -223,9 +223,11 @@ __global__ void __launch_bounds__(kScanBlock) k_instantiate_tile_scan(StageCtx c
 // write: arguments, counts, vertices
 // ---------------------------------------------------------------------------
 
-template <u32 Kind>
+// Uniform: every part of the chunk has the map, scale and offset in `m`,
+// `scale`, `offset` (held in registers; the records' q6-q8 are not read).
+template <u32 Kind, bool Uniform>
 __device__ __forceinline__ void chunk_vertices(const StageCtx& c, const PartAffine* sp, u32 owner, u32 start,
-                                               u32 total, float* dst)
+                                               u32 total, float* dst, const MapDesc& m, float scale, float offset)
 {
   const u32 lane = threadIdx.x & 31;
   #pragma unroll 2  // two steps in flight: their loads overlap
@@ -242,7 +244,8 @@ __device__ __forceinline__ void chunk_vertices(const StageCtx& c, const PartAffi
     const PartAffine& r      = sp[pi];
     if(jj < total)
     {
-      const f3 q = affine_vertex_k<Kind>(r, __ldg(c.table.vertices + affine_first_vertex(r) + (jj - pstart)));
+      const u32 tv = __ldg(c.table.vertices + affine_first_vertex(r) + (jj - pstart));
+      const f3  q  = Uniform ? affine_vertex_u<Kind>(r, tv, m, scale, offset) : affine_vertex_k<Kind>(r, tv);
       float*   d = dst + 3 * (u64)jj;
       d[0] = q.x, d[1] = q.y, d[2] = q.z;
     }
@@ -488,7 +491,9 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_vertices(Stag
     // accepted parts form a prefix of the part order: nothing further to do
     if(!__any_sync(0xFFFFFFFFu, accepted))
       break;
-    u32 nv = 0, kind = 0;
+    u32     nv = 0, kind = 0;
+    float   scale = 0.0f, offset = 0.0f;
+    MapDesc map   = {};
     if(accepted)
     {
       const uint2*             raw = reinterpret_cast<const uint2*>(parts + p);
@@ -521,10 +526,12 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_vertices(Stag
         else
           atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
       }
-      write_part_affine(sp[lane], corner, cfg_flipped(cfg), bp, bn, bt, e.firstVertex, tx,
-                        in.displacementScale * viewScale, in.displacementOffset + viewOffset);
+      scale  = in.displacementScale * viewScale;
+      offset = in.displacementOffset + viewOffset;
+      write_part_affine(sp[lane], corner, cfg_flipped(cfg), bp, bn, bt, e.firstVertex, tx, scale, offset);
+      map  = make_map_desc(tx);
       nv   = e.numVertices;
-      kind = affine_kind_of(sp[lane]);
+      kind = map.kind;
     }
     const u32  inc   = warp_inclusive<u32>(nv, lane);
     const u32  start = inc - nv;  // first vertex of this lane's part within the chunk
@@ -534,19 +541,36 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_vertices(Stag
     // one specialisation for the whole chunk when its parts share a map kind
     const u32 kind0 = __shfl_sync(0xFFFFFFFFu, kind, 0);
     const u32 kw    = __all_sync(0xFFFFFFFFu, !owner || kind == kind0) ? kind0 : ~0u;
+    // the usual chunk: every part displaced from one map with one scale and
+    // offset (lane 0 always owns a part: accepted parts form a prefix)
+    MapDesc um;
+    um.q7 = make_float4(__shfl_sync(0xFFFFFFFFu, map.q7.x, 0), __shfl_sync(0xFFFFFFFFu, map.q7.y, 0),
+                        __shfl_sync(0xFFFFFFFFu, map.q7.z, 0), __shfl_sync(0xFFFFFFFFu, map.q7.w, 0));
+    um.q8 = make_float4(__shfl_sync(0xFFFFFFFFu, map.q8.x, 0), __shfl_sync(0xFFFFFFFFu, map.q8.y, 0),
+                        __shfl_sync(0xFFFFFFFFu, map.q8.z, 0), __shfl_sync(0xFFFFFFFFu, map.q8.w, 0));
+    um.kind            = kind0;
+    const float uScale = __shfl_sync(0xFFFFFFFFu, scale, 0), uOffset = __shfl_sync(0xFFFFFFFFu, offset, 0);
+    const bool  same   = !owner
+                      || (__float_as_uint(map.q7.x) == __float_as_uint(um.q7.x)
+                          && __float_as_uint(map.q7.y) == __float_as_uint(um.q7.y)
+                          && __float_as_uint(map.q7.z) == __float_as_uint(um.q7.z)
+                          && __float_as_uint(map.q7.w) == __float_as_uint(um.q7.w)
+                          && __float_as_uint(scale) == __float_as_uint(uScale)
+                          && __float_as_uint(offset) == __float_as_uint(uOffset) && kind == kind0);
+    const bool  uni    = __all_sync(0xFFFFFFFFu, same);
     __syncwarp();
     float* dst = gv + 3 * (u64)v0;
+#define TC_CHUNK(K)                                                                                                    \
+  (uni ? chunk_vertices<K, true>(c, sp, owner, start, total, dst, um, uScale, uOffset)                               \
+       : chunk_vertices<K, false>(c, sp, owner, start, total, dst, um, uScale, uOffset))
     switch(kw)
     {
-      case affine_kind(TC_TEXEL_F16, true):
-        chunk_vertices<affine_kind(TC_TEXEL_F16, true)>(c, sp, owner, start, total, dst);
-        break;
-      case affine_kind(TC_TEXEL_F32, true):
-        chunk_vertices<affine_kind(TC_TEXEL_F32, true)>(c, sp, owner, start, total, dst);
-        break;
-      case kAffineFlat: chunk_vertices<kAffineFlat>(c, sp, owner, start, total, dst); break;
-      default: chunk_vertices<~0u>(c, sp, owner, start, total, dst); break;
+      case affine_kind(TC_TEXEL_F16, true): TC_CHUNK(affine_kind(TC_TEXEL_F16, true)); break;
+      case affine_kind(TC_TEXEL_F32, true): TC_CHUNK(affine_kind(TC_TEXEL_F32, true)); break;
+      case kAffineFlat: chunk_vertices<kAffineFlat, false>(c, sp, owner, start, total, dst, um, uScale, uOffset); break;
+      default: chunk_vertices<~0u, false>(c, sp, owner, start, total, dst, um, uScale, uOffset); break;
     }
+#undef TC_CHUNK
     __syncwarp();  // the warp's part records are rewritten by its next chunk
   }
 }

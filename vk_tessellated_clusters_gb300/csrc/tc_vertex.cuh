@@ -233,6 +233,32 @@ __device__ __forceinline__ f3 affine_vertex_k(const PartAffine& r, u32 tableVert
   return fma3(k, N, P);
 }
 
+// affine_vertex_k for a record whose map, scale and offset (the same for
+// every part of a chunk) are passed in registers: only q0-q5 are read from `r`.
+// Same operations, so the same bits.
+template <u32 Kind>
+__device__ __forceinline__ f3 affine_vertex_u(const PartAffine& r, u32 tableVertex, const MapDesc& m, float scale,
+                                              float offset)
+{
+  const float  a  = __uint2float_rn(tableVertex & 0xFFFFu) * (1.0f / 32768.0f);
+  const float  b  = __uint2float_rn(tableVertex >> 16) * (1.0f / 32768.0f);
+  const float4 q0 = r.q[0], q1 = r.q[1], q2 = r.q[2];
+  f3           P  = {__fmaf_rn(b, q1.z, __fmaf_rn(a, q0.w, q0.x)), __fmaf_rn(b, q1.w, __fmaf_rn(a, q1.x, q0.y)),
+                     __fmaf_rn(b, q2.x, __fmaf_rn(a, q1.y, q0.z))};
+  const u32    kind = Kind == ~0u ? m.kind : Kind;
+  if(kind == kAffineFlat)
+    return P;
+  const float4 q3 = r.q[3], q4 = r.q[4], q5 = r.q[5];
+  const f3     N  = {__fmaf_rn(b, q3.w, __fmaf_rn(a, q3.x, q2.y)), __fmaf_rn(b, q4.x, __fmaf_rn(a, q3.y, q2.z)),
+                     __fmaf_rn(b, q4.y, __fmaf_rn(a, q3.z, q2.w))};
+  const float  u  = __fmaf_rn(b, q5.z, __fmaf_rn(a, q5.x, q4.z));
+  const float  v  = __fmaf_rn(b, q5.w, __fmaf_rn(a, q5.y, q4.w));
+  const float hraw   = sample_kind(kind, m.q7, m.q8, u, v);
+  const float height = __fmaf_rn(hraw, scale, offset);
+  const float k      = height * rsqrtf(__fmaf_rn(N.z, N.z, __fmaf_rn(N.y, N.y, N.x * N.x)));
+  return fma3(k, N, P);
+}
+
 __device__ __forceinline__ f3 affine_vertex(const PartAffine& r, u32 tableVertex)
 {
   return affine_vertex_k<~0u>(r, tableVertex);
