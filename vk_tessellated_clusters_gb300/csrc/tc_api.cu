@@ -441,7 +441,7 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
     delete ctx;
     return TC_ERR_CUDA;
   }
-  ctx->schedule = {8, 256, 4, 8, 1, kDefaultFullVertexBlocksPerSM, {0, 0}};
+  ctx->schedule = {4, 256, 4, 4, 1, kDefaultFullVertexBlocksPerSM, {0, 0}};  // the batched scene's tuned shape
   ctx->plan     = make_plan(*desc);
   if(cudaMalloc(&ctx->dScratch, ctx->plan.totalBytes) != cudaSuccess
      || cudaMemset(ctx->dScratch, 0, ctx->plan.totalBytes) != cudaSuccess)
