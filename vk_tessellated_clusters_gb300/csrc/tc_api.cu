@@ -89,8 +89,10 @@ struct tc_context
   cudaStream_t side    = nullptr;  // the first part run's instantiation
   cudaStream_t side2   = nullptr;  // the full clusters' vertices
   cudaEvent_t  evFork  = nullptr;
-  cudaEvent_t  evJoin  = nullptr;
-  cudaEvent_t  evJoin2 = nullptr;
+  cudaEvent_t  evJoin  = nullptr;  // first part run allocated
+  cudaEvent_t  evJoin2 = nullptr;  // full clusters' vertices written
+  cudaEvent_t  evArgs1 = nullptr;  // later part runs allocated
+  cudaEvent_t  evVerts = nullptr;  // all part vertices written
 
   // graph cache
   cudaGraphExec_t graphExec = nullptr;
@@ -319,8 +321,10 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
 
   // The parts classify produced (run 0) come first in the instantiation order
   // and their offsets depend on nothing the split passes do: they are
-  // instantiated on the side stream while the (latency-bound) split passes
-  // run, the other runs after both.
+  // allocated on the side stream while the (latency-bound) split passes run,
+  // the other runs after both. Nothing later in the frame reads generated
+  // vertices, so each run's vertex kernel stays on the side stream, beside
+  // the next allocation and the BLAS lists, and joins at the frame's end.
   TC_CHECK_CUDA(cudaEventRecord(ctx->evFork, s));
   TC_CHECK_CUDA(cudaStreamWaitEvent(ctx->side, ctx->evFork, 0));
   // The full clusters' vertices depend on classify alone and nothing later in
@@ -335,10 +339,12 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
     bind_slot(ctx, c0, p.slotInstantiate0, false);
     c0.fuseSetup = kNoSetup;
     c0.run       = 0;
-    TC_CHECK_CUDA(launch_triangle_instantiate(c0, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
-                                              sched.scanBlocksPerSM, sched.vertexBlocksPerSM, ctx->side));
+    TC_CHECK_CUDA(launch_instantiate_alloc(c0, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
+                                           sched.scanBlocksPerSM, ctx->side));
+    TC_CHECK_CUDA(cudaEventRecord(ctx->evJoin, ctx->side));
+    TC_CHECK_CUDA(launch_instantiate_vertices(c0, instantiate_buffers(ctx), a->caps.maxPartTriangles,
+                                              sched.vertexBlocksPerSM, ctx->side));
   }
-  TC_CHECK_CUDA(cudaEventRecord(ctx->evJoin, ctx->side));
 
   const u32 passes = split_passes(a->caps.splitFactor);
   const u32 sb     = split_block(sched);
@@ -353,8 +359,13 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   bind_slot(ctx, c, p.slotInstantiate, false);
   c.fuseSetup = TC_BUILD_SETUP_BUILD_BLAS;
   c.run       = kRunsAfterFirst;
-  TC_CHECK_CUDA(launch_triangle_instantiate(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
-                                            sched.scanBlocksPerSM, sched.vertexBlocksPerSM, s));
+  TC_CHECK_CUDA(launch_instantiate_alloc(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
+                                         sched.scanBlocksPerSM, s));
+  TC_CHECK_CUDA(cudaEventRecord(ctx->evArgs1, s));
+  TC_CHECK_CUDA(cudaStreamWaitEvent(ctx->side, ctx->evArgs1, 0));
+  TC_CHECK_CUDA(launch_instantiate_vertices(c, instantiate_buffers(ctx), a->caps.maxPartTriangles,
+                                            sched.vertexBlocksPerSM, ctx->side));
+  TC_CHECK_CUDA(cudaEventRecord(ctx->evVerts, ctx->side));
 
   bind_slot(ctx, c, p.slotBlas, false);
   c.fuseSetup = kNoSetup;
@@ -363,6 +374,7 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
 
   u32* seg = reinterpret_cast<u32*>(ctx->dScratch + p.segOffset);
   TC_CHECK_CUDA(launch_blas_clusters_insert(c, seg, seg + (size_t)p.segStride * p.segRows, p.segStride, insert_grid(ctx, a), s));
+  TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evVerts, 0));
   TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evJoin2, 0));
 
   ctx->launches += kFrameFixedLaunches + passes;
@@ -401,7 +413,7 @@ namespace {
 
 void destroy_streams(tc_context* ctx)
 {
-  for(cudaEvent_t* e : {&ctx->evFork, &ctx->evJoin, &ctx->evJoin2})
+  for(cudaEvent_t* e : {&ctx->evFork, &ctx->evJoin, &ctx->evJoin2, &ctx->evArgs1, &ctx->evVerts})
     if(*e)
       cudaEventDestroy(*e), *e = nullptr;
   for(cudaStream_t* st : {&ctx->side, &ctx->side2})
@@ -435,7 +447,9 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
      || cudaStreamCreateWithFlags(&ctx->side2, cudaStreamNonBlocking) != cudaSuccess
      || cudaEventCreateWithFlags(&ctx->evFork, cudaEventDisableTiming) != cudaSuccess
      || cudaEventCreateWithFlags(&ctx->evJoin, cudaEventDisableTiming) != cudaSuccess
-     || cudaEventCreateWithFlags(&ctx->evJoin2, cudaEventDisableTiming) != cudaSuccess)
+     || cudaEventCreateWithFlags(&ctx->evJoin2, cudaEventDisableTiming) != cudaSuccess
+     || cudaEventCreateWithFlags(&ctx->evArgs1, cudaEventDisableTiming) != cudaSuccess
+     || cudaEventCreateWithFlags(&ctx->evVerts, cudaEventDisableTiming) != cudaSuccess)
   {
     destroy_streams(ctx);
     delete ctx;

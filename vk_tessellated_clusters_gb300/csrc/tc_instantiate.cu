@@ -579,8 +579,8 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_vertices(Stag
 
 u32 instantiate_alloc_tiles(u32 maxParts) { return (maxParts + kTile - 1) / kTile; }
 
-cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
-                                        u32 scanBlocksPerSM, u32 vertexBlocksPerSM, cudaStream_t s)
+cudaError_t launch_instantiate_alloc(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
+                                     u32 scanBlocksPerSM, cudaStream_t s)
 {
   const u32   tiles    = std::max(1u, instantiate_alloc_tiles(maxParts));
   const u32   tileGrid = std::max(1u, std::min(tiles, numSMs * std::max(1u, scanBlocksPerSM)));
@@ -589,13 +589,25 @@ cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuff
     return e;
   if((e = launch_pdl(k_instantiate_tile_scan, 1u, kScanBlock, s, c)) != cudaSuccess)
     return e;
-  if((e = launch_pdl(k_instantiate_args, tileGrid, kBlock, s, c, buf)) != cudaSuccess)
+  return launch_pdl(k_instantiate_args, tileGrid, kBlock, s, c, buf);
+}
+
+cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
+                                        u32 scanBlocksPerSM, u32 vertexBlocksPerSM, cudaStream_t s)
+{
+  const cudaError_t e = launch_instantiate_alloc(c, buf, maxParts, numSMs, scanBlocksPerSM, s);
+  if(e != cudaSuccess)
     return e;
+  return launch_instantiate_vertices(c, buf, maxParts, vertexBlocksPerSM, s);
+}
+
+cudaError_t launch_instantiate_vertices(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts,
+                                        u32 vertexBlocksPerSM, cudaStream_t s)
+{
   const u32 chunks     = (maxParts + kPartsPerWarp - 1) / kPartsPerWarp;
   // one chunk per warp (blocks retire as they finish, so a concurrent branch's
   // blocks find room); vertexBlocksPerSM picks the register budget
   const u32 vertexGrid = std::max(1u, std::min((chunks + kWarps - 1) / kWarps, 1u << 20));
-  (void)numSMs;
   if(vertexBlocksPerSM >= 6)
     return launch_pdl(k_instantiate_vertices<6>, vertexGrid, kBlock, s, c, buf);
   if(vertexBlocksPerSM == 5)
