@@ -282,6 +282,13 @@ u32 frame_begin_grid(const tc_context* ctx, const tc_frame_args* a)
 
 // blas_clusters_insert: two instantiations per thread (the lookups per
 // element are dependent loads; many resident warps hide them)
+// kernels one batched frame launches (the BLAS set-up is fused for up to
+// kBlasSetupFusedMax instances)
+uint64_t frame_launches(const tc_frame_args* a)
+{
+  return kFrameFixedLaunches + split_passes(a->caps.splitFactor) - (a->numInstances <= kBlasSetupFusedMax ? 1 : 0);
+}
+
 u32 insert_grid(const tc_context* ctx, const tc_frame_args* a)
 {
   // tiles of 1024 instantiations per block (at least four blocks per SM)
@@ -359,8 +366,13 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   bind_slot(ctx, c, p.slotInstantiate, false);
   c.fuseSetup = TC_BUILD_SETUP_BUILD_BLAS;
   c.run       = kRunsAfterFirst;
+  // up to kBlasSetupFusedMax instances the BLAS list offsets are computed by
+  // the argument kernel's last block instead of a launch of their own
+  const bool fuseBlas = a->numInstances <= kBlasSetupFusedMax;
+  c.fuseBlasSetup     = fuseBlas ? 1u : 0u;
   TC_CHECK_CUDA(launch_instantiate_alloc(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
                                          sched.scanBlocksPerSM, s));
+  c.fuseBlasSetup = 0;
   TC_CHECK_CUDA(cudaEventRecord(ctx->evArgs1, s));
   TC_CHECK_CUDA(cudaStreamWaitEvent(ctx->side, ctx->evArgs1, 0));
   TC_CHECK_CUDA(launch_instantiate_vertices(c, instantiate_buffers(ctx), a->caps.maxPartTriangles,
@@ -370,14 +382,16 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   bind_slot(ctx, c, p.slotBlas, false);
   c.fuseSetup = kNoSetup;
   c.run       = kAllRuns;
-  TC_CHECK_CUDA(launch_blas_setup_insertion(c, std::max(1u, ceil_div(a->numInstances, kInstanceTile)), kInstanceTile, s));
+  if(!fuseBlas)
+    TC_CHECK_CUDA(
+        launch_blas_setup_insertion(c, std::max(1u, ceil_div(a->numInstances, kInstanceTile)), kInstanceTile, s));
 
   u32* seg = reinterpret_cast<u32*>(ctx->dScratch + p.segOffset);
   TC_CHECK_CUDA(launch_blas_clusters_insert(c, seg, seg + (size_t)p.segStride * p.segRows, p.segStride, insert_grid(ctx, a), s));
   TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evVerts, 0));
   TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evJoin2, 0));
 
-  ctx->launches += kFrameFixedLaunches + passes;
+  ctx->launches += frame_launches(a);
   return TC_OK;
 }
 
@@ -680,7 +694,7 @@ tc_status tc_frame_build_graph(tc_context* ctx, const tc_frame_args* args, void*
     ctx->graphValid    = true;
   }
   TC_CHECK_CUDA(cudaGraphLaunch(ctx->graphExec, s));
-  ctx->launches += kFrameFixedLaunches + split_passes(args->caps.splitFactor);
+  ctx->launches += frame_launches(args);
   return TC_OK;
 }
 

@@ -449,6 +449,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_instantiate_args(StageCtx c, Inst
   {
     if(threadIdx.x == 0 && c.fuseSetup != kNoSetup)
       build_setup_apply(c, c.fuseSetup);
+    if(c.fuseBlasSetup)
+      blas_setup_block(c);
     // done counter back to zero for a reused slot (nothing else needs clearing)
     if(threadIdx.x == 0 && c.scratch.selfClean)
       *c.scratch.done = 0;

@@ -81,6 +81,8 @@ struct StageCtx
   u32                           instEnd;
   u32                           fuseSetup;  // build_setup mode run by the last block, or kNoSetup
   u32                           run;        // instantiate: part run index or kAllRuns
+  u32                           fuseBlasSetup;  // instantiate: the last block also runs blas_setup_insertion
+  u32                           _pad1;
 };
 
 constexpr u32 kNoSetup        = 0xFFFFFFFFu;
@@ -287,6 +289,48 @@ __device__ __forceinline__ u32 block_exclusive_scan(u32 v, u32* s_warp, u32* tot
   *total = s_warp[32];
   __syncthreads();
   return r;
+}
+
+// shaders/blas_setup_insertion.comp.glsl:100-116 run by one block of 256
+// threads (fused into the last block of the launch before it): the
+// per-instance CLAS counts become list offsets, the exclusive scan in instance
+// order that the multi-block k_blas_setup_insertion computes. Each thread takes
+// up to kBlasSetupPerThread consecutive instances.
+constexpr u32 kBlasSetupPerThread = 16;
+constexpr u32 kBlasSetupFusedMax  = 256 * kBlasSetupPerThread;  // instances the fused form handles
+
+__device__ inline void blas_setup_block(const StageCtx& c)
+{
+  __shared__ u32    s_scan[33];
+  tc_SceneBuilding* b     = c.build;
+  tc_BlasBuildInfo* infos = reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos);
+  const u32*        sizes = reinterpret_cast<const u32*>(b->blasBuildSizes);
+  const u32         n     = min(b->numRenderInstances, kBlasSetupFusedMax);
+  const u32         per   = (n + blockDim.x - 1) / blockDim.x;
+  const u32         i0 = min(n, threadIdx.x * per), i1 = min(n, i0 + per);
+  const u64         base = b->blasClusterCounter;
+  u32               sum = 0, statSizes = 0;
+  for(u32 i = i0; i < i1; i++)
+    sum += __ldcg(&infos[i].clusterReferencesCount);
+  u32       total;
+  const u32 excl   = block_exclusive_scan(sum, s_scan, &total);  // its barriers also order `base` before the write below
+  u64       offset = base + excl;
+  for(u32 i = i0; i < i1; i++)
+  {
+    const u32 cnt                    = __ldcg(&infos[i].clusterReferencesCount);
+    infos[i].clusterReferencesCount  = 0;
+    infos[i].clusterReferencesStride = 8;
+    infos[i].clusterReferences       = b->blasClusterAddresses + offset * 8ull;
+    offset += cnt;
+    if(sizes)
+      statSizes += sizes[i];  // last frame's result, statistics only
+  }
+  for(int o = 16; o > 0; o >>= 1)
+    statSizes += __shfl_xor_sync(0xFFFFFFFFu, statSizes, o);
+  if((threadIdx.x & 31) == 0 && statSizes)
+    atomicAdd(&c.readback->numBlasActualSizes, statSizes);
+  if(threadIdx.x == 0 && n)
+    b->blasClusterCounter = (u32)(base + total);
 }
 
 }  // namespace tc
