@@ -29,10 +29,10 @@ struct SlotPlan
 constexpr size_t kCtrlBytes = 8 + 8 * kMaxCounters;
 
 // kernels of a batched frame besides the split passes: frame_begin,
-// instances_classify, clusters_cull, classify (3), instantiate (4, twice: the
-// first part run overlapped with the split passes, then the others), blas
-// setup, blas insert (2)
-constexpr uint64_t kFrameFixedLaunches = 17;
+// frame_begin + instances_classify (one launch), clusters_cull, classify (3),
+// instantiate (4, twice: the first part run overlapped with the split passes,
+// then the others), blas setup, blas insert (2)
+constexpr uint64_t kFrameFixedLaunches = 16;
 
 constexpr u32 kDefaultFullVertexBlocksPerSM = 4;
 
@@ -280,8 +280,6 @@ u32 frame_begin_grid(const tc_context* ctx, const tc_frame_args* a)
   return std::max(1u, std::min(ctx->numSMs * 2, ceil_div((u64)a->caps.maxSplitTriangles * 6, 256)));
 }
 
-// blas_clusters_insert: two instantiations per thread (the lookups per
-// element are dependent loads; many resident warps hide them)
 // kernels one batched frame launches (the BLAS set-up is fused for up to
 // kBlasSetupFusedMax instances)
 uint64_t frame_launches(const tc_frame_args* a)
@@ -312,10 +310,9 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   TC_CHECK_CUDA(cudaMemsetAsync(ctx->dScratch, 0, p.frameBytes, s));
 
   StageCtx c = base_ctx(ctx, a);
-  TC_CHECK_CUDA(launch_frame_begin(c, frame_begin_grid(ctx, a), s));
-
   bind_slot(ctx, c, p.slotInstances, false);
-  TC_CHECK_CUDA(launch_instances_classify(c, std::max(1u, ceil_div(a->numInstances, kInstanceTile)), kInstanceTile, s));
+  TC_CHECK_CUDA(launch_frame_begin_instances(
+      c, std::max(frame_begin_grid(ctx, a), ceil_div(a->numInstances, kInstanceTile)), s));
 
   bind_slot(ctx, c, p.slotCull, false);
   c.fuseSetup = TC_BUILD_SETUP_CLASSIFY;

@@ -89,9 +89,8 @@ __device__ inline bool intersect_hiz(const Clip&, const Clip&) { return true; }
 // per-frame reset (src/renderer_raytrace_clusters_tess.cpp:412-419)
 // ---------------------------------------------------------------------------
 
-__global__ void k_frame_begin(StageCtx c)
+__device__ inline void frame_begin_body(const StageCtx& c)
 {
-  stage_prologue();
   tc_SceneBuilding* b = c.build;
   if(blockIdx.x == 0)
   {
@@ -141,15 +140,20 @@ __global__ void k_frame_begin(StageCtx c)
   }
 }
 
+__global__ void k_frame_begin(StageCtx c)
+{
+  stage_prologue();
+  frame_begin_body(c);
+}
+
 // ---------------------------------------------------------------------------
 // instances_classify.comp.glsl:102-128, plus the exclusive prefix of
 // numClusters over instances that the batched cull uses to flatten
 // (instance, cluster) pairs.
 // ---------------------------------------------------------------------------
 
-__global__ void k_instances_classify(StageCtx c)
+__device__ inline void instances_classify_body(const StageCtx& c)
 {
-  stage_prologue();
   __shared__ u32 s_tile, s_flag, s_warp[33];
   __shared__ u64 s_excl;
   const u32      n        = c.numInstances;
@@ -200,6 +204,22 @@ __global__ void k_instances_classify(StageCtx c)
       c.instClusterStart[n] = numTiles ? (u32)c.scratch.totals[0] : 0u;
     scratch_release(c, numTiles, 1);
   }
+}
+
+__global__ void k_instances_classify(StageCtx c)
+{
+  stage_prologue();
+  instances_classify_body(c);
+}
+
+// Both in one launch (the batched frame): instances_classify reads nothing the
+// per-frame reset writes, so every block does its share of the reset and then
+// takes instance tiles.
+__global__ void k_frame_begin_instances(StageCtx c)
+{
+  stage_prologue();
+  frame_begin_body(c);
+  instances_classify_body(c);
 }
 
 // ---------------------------------------------------------------------------
@@ -313,6 +333,11 @@ cudaError_t launch_frame_begin(const StageCtx& c, u32 grid, cudaStream_t s)
 cudaError_t launch_instances_classify(const StageCtx& c, u32 grid, u32 block, cudaStream_t s)
 {
   return launch_pdl(k_instances_classify, grid, block, s, c);
+}
+
+cudaError_t launch_frame_begin_instances(const StageCtx& c, u32 grid, cudaStream_t s)
+{
+  return launch_pdl(k_frame_begin_instances, grid, kInstanceTile, s, c);
 }
 
 cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStream_t s)

@@ -33,6 +33,8 @@ struct ClassifyBuffers
 
 cudaError_t launch_frame_begin(const StageCtx& c, u32 grid, cudaStream_t s);
 cudaError_t launch_instances_classify(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
+// frame_begin and instances_classify in one launch (block = kInstanceTile)
+cudaError_t launch_frame_begin_instances(const StageCtx& c, u32 grid, cudaStream_t s);
 cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 cudaError_t launch_build_setup(const StageCtx& c, u32 mode, cudaStream_t s);
 cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
