@@ -142,7 +142,7 @@ Plan make_plan(const tc_context_desc& d)
   p.slotInstances   = add(ceil_div(d.maxInstances, kInstanceTile), 1);
   p.slotCull        = add(ceil_div(d.maxTotalClusters, kCullTile), 1);
   p.classifyCap     = (u32)std::max<u64>(1, std::min<u64>(k.maxVisibleClusters, d.maxTotalClusters));
-  p.slotClassify    = add(1, kMaxCounters);  // unused by classify's kernels (kept for the per-instance bind)
+  p.slotClassify    = add(classify_max_blocks(p.classifyCap), 3);  // the range sums (zeroed with the frame)
   p.slotSplit0      = add(ceil_div(k.maxSplitTriangles, kSplitMinItems), 2);
   for(u32 i = 1; i < passes; i++)
     add(ceil_div(k.maxSplitTriangles, kSplitMinItems), 2);
@@ -174,8 +174,8 @@ Plan make_plan(const tc_context_desc& d)
   off                 = align_up(off + (size_t)p.classifyCap * 8, 256);
   p.clsTriWordsOffset = off;
   off                 = align_up(off + (size_t)p.classifyCap * TC_MAX_CLUSTER_TRIANGLES * 4, 256);
-  p.clsBlockSumsOffset = off;  // block sums, then the counter bases
-  off = align_up(off + ((size_t)classify_max_blocks(p.classifyCap) + 1) * sizeof(ClusterOffsets), 256);
+  p.clsBlockSumsOffset = off;  // the counter bases
+  off = align_up(off + sizeof(ClusterOffsets), 256);
   p.clsFullRecsOffset = off;  // per full cluster, then the slot range
   off = align_up(off + (size_t)p.classifyCap * 8 + 8, 256);
   p.partVertexOffset  = off;
@@ -258,8 +258,8 @@ ClassifyBuffers classify_buffers(tc_context* ctx)
   const Plan& p = ctx->plan;
   return {reinterpret_cast<uint2*>(ctx->dScratch + p.clsCountsOffset),
           reinterpret_cast<u32*>(ctx->dScratch + p.clsTriWordsOffset),
+          reinterpret_cast<RangeSums*>(ctx->dScratch + p.slots[p.slotClassify].stateOffset),
           reinterpret_cast<ClusterOffsets*>(ctx->dScratch + p.clsBlockSumsOffset),
-          reinterpret_cast<ClusterOffsets*>(ctx->dScratch + p.clsBlockSumsOffset) + classify_max_blocks(p.classifyCap),
           reinterpret_cast<uint2*>(ctx->dScratch + p.clsFullRecsOffset),
           reinterpret_cast<u32*>(ctx->dScratch + p.clsFullRecsOffset + (size_t)p.classifyCap * 8)};
 }
@@ -764,6 +764,12 @@ tc_status tc_cluster_classify(tc_context* ctx, const tc_frame_args* a, uint32_t 
   c.instBegin = instanceBegin;
   c.instEnd   = instanceEnd;
   bind_slot(ctx, c, ctx->plan.slotClassify, true);
+  {
+    // the range sums the count kernel accumulates start at zero
+    const SlotPlan& sl = ctx->plan.slots[ctx->plan.slotClassify];
+    TC_CHECK_CUDA(cudaMemsetAsync(ctx->dScratch + sl.stateOffset, 0, (size_t)sl.stride * sl.counters * 8,
+                                  reinterpret_cast<cudaStream_t>(stream)));
+  }
   TC_CHECK_CUDA(launch_cluster_classify(c, classify_buffers(ctx), std::min(a->totalClusters, a->caps.maxVisibleClusters),
                                         ctx->numSMs, ctx->schedule.classifyBlocksPerSM,
                                         reinterpret_cast<cudaStream_t>(stream)));

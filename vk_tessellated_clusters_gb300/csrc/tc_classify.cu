@@ -93,8 +93,10 @@ struct ClassifyScratch
 {
   uint2*          counts;     // per visible cluster of the window
   u32*            triWords;   // 64 per visible cluster
-  ClusterOffsets* blockSums;  // per block of the grid
+  RangeSums*      rangeSums;  // per write block's range: the counts' sums, zero before count
   ClusterOffsets* bases;      // the counters before the launch
+  u32             writeBlocks;  // the write launch's grid (its blocks' ranges)
+  u32             _pad;
   uint2*          fullRecs;   // per full cluster (generated-cluster slot - first slot): visible index, first vertex
   u32*            fullRange;  // [2]: the launch's generated-cluster slots [begin, end)
 };
@@ -200,11 +202,11 @@ __device__ inline void block_prefix(const ClassifyScratch& cs, u64 (&pre)[kNumCo
   u64 x[kNumCounters] = {0, 0, 0, 0, 0};
   for(u32 i = threadIdx.x; i < blockIdx.x; i += blockDim.x)
   {
-    const ClusterOffsets o = cs.blockSums[i];
-    x[kCntParts] += o.part;
-    x[kCntSplits] += o.split;
-    x[kCntGen] += o.gen;
-    x[kCntVerts] += o.vert;
+    const RangeSums o = cs.rangeSums[i];
+    x[kCntParts] += (u32)o.partsSplits;
+    x[kCntSplits] += (u32)(o.partsSplits >> 32);
+    x[kCntGen] += (u32)o.fullVerts;
+    x[kCntVerts] += (u32)(o.fullVerts >> 32);
     x[kCntData] += o.data;
   }
   u64 tot[kNumCounters];
@@ -226,7 +228,6 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c
   stage_prologue();
   __shared__ f3  s_vert[kWarps][TC_MAX_CLUSTER_VERTICES];
   __shared__ f2  s_dist[kWarps][TC_MAX_CLUSTER_VERTICES];  // per vertex: distance to the view position, its reciprocal
-  __shared__ u64 s_wsum[kWarps][kNumCounters];
   __shared__ u32 s_range[2];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if(threadIdx.x == 0)
@@ -241,22 +242,19 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c
   const float             rNear   = __fdiv_rn(1.0f, fp.nearPlane);
   const bool              culling = (c.flags & TC_FLAG_CULLING) != 0;
   const u32               sf      = clamp_split_factor(c.caps.splitFactor);
-  u32                     vBegin, vEnd;
-  block_range(n, blockIdx.x, gridDim.x, vBegin, vEnd);
   if(blockIdx.x == 0 && threadIdx.x == 0)  // the offsets continue from the counters' current values
     *cs.bases = {b->partTriangleCounter, (u32)b->splitTriangleCounter, b->genClusterCounter, b->genVertexCounter,
                  b->genClusterDataCounter};
-  if(lane == 0)
-  {
-#pragma unroll
-    for(int q = 0; q < kNumCounters; q++)
-      s_wsum[warp][q] = 0;  // lane 0 accumulates the range's counts here
-  }
+  // the write launch's block ranges, which collect the counts' sums
+  const u32 perRange = (n + cs.writeBlocks - 1) / cs.writeBlocks;
 
-  // the warp's clusters are v = vBegin + warp + kWarps * j, j < cntW; their
-  // cluster records load one lane per cluster, 32 at a time, so that only the
-  // vertex and index loads remain on each cluster's dependent path
-  const u32  cntW   = vBegin + warp < vEnd ? (vEnd - vBegin - warp + kWarps - 1) / kWarps : 0u;
+  // the warp's clusters are v = gw + nwarps * j, j < cntW (spread over the
+  // whole list, which evens out instances of uneven cost); their cluster
+  // records load one lane per cluster, 32 at a time, so that only the vertex
+  // and index loads remain on each cluster's dependent path
+  const u32  gw     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const u32  nwarps = (gridDim.x * blockDim.x) >> 5;
+  const u32  cntW   = gw < n ? (n - gw + nwarps - 1) / nwarps : 0u;
   const u32* states = reinterpret_cast<const u32*>(b->instanceStates);
   for(u32 j0 = 0; j0 < cntW; j0 += 32)
   {
@@ -264,7 +262,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c
     u32       hInst = 0, hMeta = 0, hFirstV = 0, hFirstT = 0, hData = 0;
     if(lane < jn)
     {
-      const tc_ClusterInfo     ci = vis[begin + vBegin + warp + kWarps * (j0 + lane)];
+      const tc_ClusterInfo     ci = vis[begin + gw + nwarps * (j0 + lane)];
       const tc_RenderInstance* in = c.instances + ci.instanceID;
       const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
       u32                      nt = cl.numTriangles, nv = cl.numVertices;
@@ -284,7 +282,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c
     }
     for(u32 jj = 0; jj < jn; jj++)
     {
-      const u32                v      = vBegin + warp + kWarps * (j0 + jj);
+      const u32                v      = gw + nwarps * (j0 + jj);
       const u32                meta   = __shfl_sync(0xFFFFFFFFu, hMeta, jj);
       const u32                nv     = meta & 0xFF, nt = (meta >> 8) & 0xFF;
       const bool               culled = (meta >> 16) != 0;
@@ -353,31 +351,17 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c
       if(lane == 0)
       {
         cs.counts[v] = pack_counts(parts, splits, full, nv, nt, data);
-        s_wsum[warp][kCntParts] += parts;
-        s_wsum[warp][kCntSplits] += splits;
-        s_wsum[warp][kCntGen] += full ? 1u : 0u;
-        s_wsum[warp][kCntVerts] += full ? nv : 0u;
-        s_wsum[warp][kCntData] += full ? data : 0u;
+        RangeSums& rs = cs.rangeSums[v / perRange];
+        if(full)
+        {
+          atomicAdd(&rs.fullVerts, 1ull | ((unsigned long long)nv << 32));
+          if(data)
+            atomicAdd(&rs.data, (unsigned long long)data);
+        }
+        else
+          atomicAdd(&rs.partsSplits, (unsigned long long)parts | ((unsigned long long)splits << 32));
       }
     }
-  }
-
-  // the block's sums, for the write launch's block prefixes
-  __syncthreads();
-  if(warp == 0)
-  {
-    u64 x[kNumCounters];
-#pragma unroll
-    for(int q = 0; q < kNumCounters; q++)
-    {
-      x[q] = lane < kWarps ? s_wsum[lane][q] : 0ull;
-#pragma unroll
-      for(int o = kWarps / 2; o > 0; o >>= 1)
-        x[q] += __shfl_xor_sync(0xFFFFFFFFu, x[q], o);
-    }
-    if(lane == 0)
-      cs.blockSums[blockIdx.x] = {(u32)x[kCntParts], (u32)x[kCntSplits], (u32)x[kCntGen], (u32)x[kCntVerts],
-                                  x[kCntData]};
   }
 }
 
@@ -775,9 +759,10 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_full_vertices(St
 cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
                                     u32 warpBlocksPerSM, cudaStream_t s)
 {
-  ClassifyScratch cs{buf.counts, buf.triWords, buf.blockSums, buf.bases, buf.fullRecs, buf.fullRange};
-  // both launches use this grid: the blocks' cluster ranges must agree
+  // the write launch's blocks own contiguous ranges of clusters, whose count
+  // sums the count launch accumulates (its warps stride over the whole list)
   const u32 grid = std::max(1u, std::min(classify_max_blocks(maxClusters), numSMs * std::max(1u, warpBlocksPerSM)));
+  ClassifyScratch cs{buf.counts, buf.triWords, buf.rangeSums, buf.bases, grid, 0, buf.fullRecs, buf.fullRange};
   // register budget from the requested residency: 4 or less -> 64, 5-7 -> 40, 8 and more -> 32
   const int   occ = warpBlocksPerSM >= 8 ? 8 : (warpBlocksPerSM >= 5 ? 6 : 4);
   cudaError_t e   = occ == 8   ? launch_pdl(k_classify_count<8>, grid, kBlock, s, c, cs)
@@ -793,7 +778,7 @@ cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& bu
 cudaError_t launch_classify_full_vertices(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
                                           u32 blocksPerSM, cudaStream_t s)
 {
-  ClassifyScratch cs{buf.counts, buf.triWords, buf.blockSums, buf.bases, buf.fullRecs, buf.fullRange};
+  ClassifyScratch cs{buf.counts, buf.triWords, buf.rangeSums, buf.bases, 0, 0, buf.fullRecs, buf.fullRange};
   // every warp of the grid takes a share of the slots
   const u32 grid = std::max(1u, std::min((maxClusters + kWarps - 1) / kWarps, numSMs * std::max(1u, blocksPerSM)));
   // register budget from the requested residency: 4 or less -> 64, 5-6 -> 40, 7 and more -> 32

@@ -19,13 +19,20 @@ struct ClusterOffsets
 };
 static_assert(sizeof(ClusterOffsets) == 24, "ClusterOffsets: three 8-byte words");
 
+// per range of visible clusters: the sums of the clusters' counts, packed
+// (parts | splits << 32, full clusters | their vertices << 32, CLAS bytes)
+struct RangeSums
+{
+  unsigned long long partsSplits, fullVerts, data;
+};
+
 // cluster_classify scratch: per visible cluster of a launch's window, and per
-// block of the classify grid (each block owns a contiguous range of clusters)
+// block of the classify grid (each write block owns a contiguous range of clusters)
 struct ClassifyBuffers
 {
   uint2*          counts;
   u32*            triWords;   // 64 per cluster
-  ClusterOffsets* blockSums;  // per block: the sums of its clusters' counts
+  RangeSums*      rangeSums;  // per block: the sums of its range's counts (zero before the launch)
   ClusterOffsets* bases;      // one: the counters before the launch
   uint2*          fullRecs;   // per full cluster of the window: visible index, first generated vertex
   u32*            fullRange;  // [2]: the window's generated-cluster slots
