@@ -3,21 +3,23 @@
 //
 // shaders/cluster_classify.comp.glsl:150-666 (RT target, plain path).
 //
-// GB300 mapping, two launches per stage, neither with a cross-block wait or a
-// last-block step. Block b of the grid owns the contiguous range of visible
-// clusters [b * per, (b + 1) * per), the same range in both launches:
-//   count : the block's warps take its clusters in turn, one cluster per warp
+// GB300 mapping, three launches per stage, none with a cross-block wait. Block
+// b of the write grid owns the contiguous range of visible clusters
+// [b * per, (b + 1) * per):
+//   count : warps stride over the whole list, one cluster at a time per warp
 //           (<= 64 triangles, two per lane), vertices staged in shared
 //           memory; segment counts, configs and the cluster's counts (part /
 //           split triangles, full-cluster vertices, CLAS bytes) go to
-//           scratch, the block's sums to one record per block
-//   write : every block adds up the sums of the blocks before it (the
+//           scratch, and 64-bit atomics add them to the sums of the cluster's
+//           range
+//   write : every block adds up the sums of the ranges before its own (the
 //           counters' values before the launch included), then scans its own
 //           clusters' counts in shared memory, so every offset equals what a
-//           serial loop over the clusters gives; part / split triangles,
-//           instantiation arguments and the displaced full-cluster vertices go
-//           to those offsets, and the grid's last block writes the counters'
-//           new totals
+//           serial loop over the clusters gives; part / split triangles and
+//           instantiation arguments go to those offsets, and the grid's last
+//           block writes the counters' new totals
+//   full vertices : the displaced vertices of the accepted full clusters, from
+//           the records write leaves (a launch of its own, beside later work)
 #include <algorithm>
 
 #include "tc_kernels.h"
