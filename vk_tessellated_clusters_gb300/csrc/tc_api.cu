@@ -93,6 +93,7 @@ struct tc_context
   cudaEvent_t  evJoin2 = nullptr;  // full clusters' vertices written
   cudaEvent_t  evArgs1 = nullptr;  // later part runs allocated
   cudaEvent_t  evVerts = nullptr;  // all part vertices written
+  cudaEvent_t  evInst  = nullptr;  // instances classified
 
   // graph cache
   cudaGraphExec_t graphExec = nullptr;
@@ -314,9 +315,26 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   TC_CHECK_CUDA(launch_frame_begin_instances(
       c, std::max(frame_begin_grid(ctx, a), ceil_div(a->numInstances, kInstanceTile)), s));
 
-  bind_slot(ctx, c, p.slotCull, false);
-  c.fuseSetup = TC_BUILD_SETUP_CLASSIFY;
-  TC_CHECK_CUDA(launch_clusters_cull(c, persistent_grid(ctx, ceil_div(a->totalClusters, kCullTile), 4), kCullTile, s));
+  // With RT semantics every cluster of every instance is visible, in instance
+  // order: classify reads that list from the instances' cluster prefix and
+  // clusters_cull (which writes it out, with its counter and set-up) runs on
+  // the second side stream, joined at the frame's end.
+  const bool flat = (a->flags & TC_FLAG_RASTER_CULL) == 0;
+  {
+    StageCtx cc = c;
+    bind_slot(ctx, cc, p.slotCull, false);
+    cc.fuseSetup         = TC_BUILD_SETUP_CLASSIFY;
+    cudaStream_t cs      = s;
+    if(flat)
+    {
+      TC_CHECK_CUDA(cudaEventRecord(ctx->evInst, s));
+      TC_CHECK_CUDA(cudaStreamWaitEvent(ctx->side2, ctx->evInst, 0));
+      cs = ctx->side2;
+    }
+    TC_CHECK_CUDA(
+        launch_clusters_cull(cc, persistent_grid(ctx, ceil_div(a->totalClusters, kCullTile), 4), kCullTile, cs));
+  }
+  c.flatVisible = flat ? 1u : 0u;
 
   bind_slot(ctx, c, p.slotClassify, false);
   c.fuseSetup = TC_BUILD_SETUP_SPLIT;
@@ -424,7 +442,7 @@ namespace {
 
 void destroy_streams(tc_context* ctx)
 {
-  for(cudaEvent_t* e : {&ctx->evFork, &ctx->evJoin, &ctx->evJoin2, &ctx->evArgs1, &ctx->evVerts})
+  for(cudaEvent_t* e : {&ctx->evFork, &ctx->evJoin, &ctx->evJoin2, &ctx->evArgs1, &ctx->evVerts, &ctx->evInst})
     if(*e)
       cudaEventDestroy(*e), *e = nullptr;
   for(cudaStream_t* st : {&ctx->side, &ctx->side2})
@@ -460,7 +478,8 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
      || cudaEventCreateWithFlags(&ctx->evJoin, cudaEventDisableTiming) != cudaSuccess
      || cudaEventCreateWithFlags(&ctx->evJoin2, cudaEventDisableTiming) != cudaSuccess
      || cudaEventCreateWithFlags(&ctx->evArgs1, cudaEventDisableTiming) != cudaSuccess
-     || cudaEventCreateWithFlags(&ctx->evVerts, cudaEventDisableTiming) != cudaSuccess)
+     || cudaEventCreateWithFlags(&ctx->evVerts, cudaEventDisableTiming) != cudaSuccess
+     || cudaEventCreateWithFlags(&ctx->evInst, cudaEventDisableTiming) != cudaSuccess)
   {
     destroy_streams(ctx);
     delete ctx;

@@ -113,9 +113,61 @@ __device__ __forceinline__ void block_range(u32 n, u32 blk, u32 nb, u32& v0, u32
   v1            = min(n, v0 + per);
 }
 
+// Visible cluster v when the list is every cluster in instance order (RT
+// semantics: clusters_cull keeps them all): the instance whose first flat
+// index is the last one <= v.
+// `starts`: the instances' first flat indices (instClusterStart, or the
+// block's shared copy of it)
+__device__ __forceinline__ tc_ClusterInfo flat_cluster(const u32* starts, u32 numInstances, u32 v)
+{
+  u32 lo = 0, hi = numInstances;
+  while(hi - lo > 1)
+  {
+    const u32 mid = (lo + hi) >> 1;
+    if(starts[mid] <= v)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return {lo, v - starts[lo]};
+}
+
+// Instance counts up to kFlatShared keep the prefix in shared memory, where
+// the binary search of every cluster lookup runs.
+constexpr u32 kFlatShared = 1024;
+
+struct FlatStarts
+{
+  u32 v[kFlatShared];
+};
+
+// Called by every thread of the block (contains a barrier); returns the
+// prefix the block's lookups use.
+__device__ __forceinline__ const u32* stage_flat_starts(const StageCtx& c, FlatStarts& sh)
+{
+  if(!c.flatVisible || c.numInstances > kFlatShared)
+    return c.instClusterStart;
+  for(u32 i = threadIdx.x; i < c.numInstances; i += blockDim.x)
+    sh.v[i] = c.instClusterStart[i];
+  __syncthreads();
+  return sh.v;
+}
+
+__device__ __forceinline__ tc_ClusterInfo visible_cluster(const StageCtx& c, const u32* starts,
+                                                          const tc_ClusterInfo* vis, u32 v)
+{
+  return c.flatVisible ? flat_cluster(starts, c.numInstances, v) : vis[v];
+}
+
 // visible clusters of the instance window (visibleClusters is sorted by instance)
 __device__ inline void window_range(const StageCtx& c, u32& lo, u32& hi)
 {
+  if(c.flatVisible)  // whole window, every cluster listed (clusters_cull runs beside classify)
+  {
+    lo = 0;
+    hi = min(c.instClusterStart[c.numInstances], c.caps.maxVisibleClusters);
+    return;
+  }
   const tc_ClusterInfo* vis = reinterpret_cast<const tc_ClusterInfo*>(c.build->visibleClusters);
   lo                        = 0;
   hi                        = min(c.build->visibleClusterCounter, c.caps.maxVisibleClusters);
@@ -231,10 +283,12 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c
   __shared__ f3  s_vert[kWarps][TC_MAX_CLUSTER_VERTICES];
   __shared__ f2  s_dist[kWarps][TC_MAX_CLUSTER_VERTICES];  // per vertex: distance to the view position, its reciprocal
   __shared__ u32 s_range[2];
+  __shared__ FlatStarts s_starts;
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if(threadIdx.x == 0)
     window_range(c, s_range[0], s_range[1]);
   __syncthreads();
+  const u32* starts = stage_flat_starts(c, s_starts);
   const u32 begin = s_range[0];
   const u32 n     = min(s_range[1] - s_range[0], c.scratch.itemCapacity);
 
@@ -264,7 +318,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c
     u32       hInst = 0, hMeta = 0, hFirstV = 0, hFirstT = 0, hData = 0;
     if(lane < jn)
     {
-      const tc_ClusterInfo     ci = vis[begin + gw + nwarps * (j0 + lane)];
+      const tc_ClusterInfo     ci = visible_cluster(c, starts, vis, begin + gw + nwarps * (j0 + lane));
       const tc_RenderInstance* in = c.instances + ci.instanceID;
       const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
       u32                      nt = cl.numTriangles, nv = cl.numVertices;
@@ -450,10 +504,13 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c
   __shared__ u64            s_warp[33][kNumCounters];
   __shared__ ClusterOffsets s_off[kBlock];  // offsets of the chunk's clusters
   __shared__ uint2          s_cnt[kBlock];  // counts of the chunk's clusters
+  __shared__ tc_ClusterInfo s_ci[kBlock];   // the chunk's clusters
+  __shared__ FlatStarts     s_starts;
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if(threadIdx.x == 0)
     window_range(c, s_range[0], s_range[1]);
   __syncthreads();
+  const u32* starts = stage_flat_starts(c, s_starts);
   const u32 begin = s_range[0];
   const u32 n     = min(s_range[1] - s_range[0], c.scratch.itemCapacity);
 
@@ -478,6 +535,8 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c
     const u32 len = min(kBlock, vEnd - c0);
     {
       const uint2 r = threadIdx.x < len ? cs.counts[c0 + threadIdx.x] : make_uint2(0, 0);
+      if(threadIdx.x < len)  // looked up once per cluster, in parallel
+        s_ci[threadIdx.x] = visible_cluster(c, starts, vis, begin + c0 + threadIdx.x);
       u64 x[kNumCounters] = {cnt_parts(r), cnt_splits(r), cnt_full(r), cnt_verts(r), r.y};
       u64 tot[kNumCounters];
       block_scan5(x, tot, s_warp);
@@ -503,7 +562,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c
       if(cnt_full(cnt))
         continue;  // phase 2 (no part or split triangles)
       const u32 v = c0 + i, offPart = s_off[i].part, offSplit = s_off[i].split;
-      const tc_ClusterInfo ci = vis[begin + v];
+      const tc_ClusterInfo ci = s_ci[i];
       {
         // cluster_classify.comp.glsl:543-666: part and split triangles
         const u32  nt  = cnt_parts(cnt) + cnt_splits(cnt);
@@ -595,7 +654,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c
           cs.fullRecs[off.gen - genBase] = full ? make_uint2(begin + v, off.vert) : make_uint2(kRejected, 0u);
           if(full)
           {
-            const tc_ClusterInfo     ci = vis[begin + v];
+            const tc_ClusterInfo     ci = s_ci[i];
             const tc_RenderInstance* in = c.instances + ci.instanceID;
             // accepted instantiations form a prefix of the serial order, so the
             // instantiation slot equals the generated-cluster slot
@@ -680,6 +739,8 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_full_vertices(St
 {
   stage_prologue();
   __shared__ FullRecord s_full[kWarps][32];
+  __shared__ FlatStarts s_starts;
+  const u32*            starts = stage_flat_starts(c, s_starts);
   const u32             lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const u32             ltm  = (1u << lane) - 1u;
   const u32             count        = cs.fullRange[1] - cs.fullRange[0];
@@ -702,7 +763,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_full_vertices(St
       const uint2 fs = cs.fullRecs[slot];
       if(fs.x != kRejected)
       {
-        const tc_ClusterInfo     ci = vis[fs.x];
+        const tc_ClusterInfo     ci = visible_cluster(c, starts, vis, fs.x);
         const tc_RenderInstance* in = c.instances + ci.instanceID;
         const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
         owner                       = true;

@@ -82,7 +82,9 @@ struct StageCtx
   u32                           fuseSetup;  // build_setup mode run by the last block, or kNoSetup
   u32                           run;        // instantiate: part run index or kAllRuns
   u32                           fuseBlasSetup;  // instantiate: the last block also runs blas_setup_insertion
-  u32                           _pad1;
+  u32                           flatVisible;    // classify: the visible list is every cluster in instance order
+                                                // (RT semantics, whole window), read from instClusterStart
+                                                // instead of waiting for clusters_cull
 };
 
 constexpr u32 kNoSetup        = 0xFFFFFFFFu;
