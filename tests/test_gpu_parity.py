@@ -81,6 +81,21 @@ def test_batched_scene_culling_bit_exact(oracle, mode):
     pipe.close()
 
 
+@pytest.mark.parametrize("mode", ["batched", "plain", "graph"])
+def test_raster_cull_bit_exact(oracle, mode):
+    """Raster semantics: clusters_cull drops clusters, so classify reads the
+    compacted visible list (the RT path reads it from the instances' cluster
+    prefix instead)."""
+    sc = S.scene_batched(num_instances=24, map_size=128)
+    cam, last = S.camera_orbit(5), S.camera_orbit(4)
+    flags = FLAGS | L.FLAG_RASTER_CULL
+    pipe, out, ref, _ = run_both(oracle, sc, cam, small_caps(), flags=flags, mode=mode, cam_last=last)
+    assert int(ref["readback"]["numVisibleClusters"]) < sc.total_clusters  # something was culled
+    assert pipe.device_errors() == 0
+    assert_same(out, ref, f"raster cull {mode}", vertex_tol=vertex_tolerance(sc))
+    pipe.close()
+
+
 @pytest.mark.parametrize("which", ["parts", "splits", "vertices", "clusters", "megs", "visible"])
 def test_capacity_overflow_matches_reference_semantics(oracle, which):
     """Tiny caps: the reference drops work past each cap and lets the raw
