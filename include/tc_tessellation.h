@@ -446,7 +446,9 @@ typedef struct tc_schedule {
   uint32_t fullVertexBlocksPerSM; /* grid of the full-cluster vertex kernel = SMs x this (at most 4 resident);
                                    * it runs beside the rest of the frame (fewer blocks leave room for it);
                                    * 0: the default (4) */
-  uint32_t _pad[2];
+  uint32_t vertexGridPerSM;     /* grid of the part vertex kernel = SMs x this (grid-stride over 32-part chunks);
+                                 * 0: one resident wave (the blocks vertexBlocksPerSM allows) */
+  uint32_t _pad[1];
 } tc_schedule;
 
 typedef struct tc_context_desc {

@@ -182,12 +182,14 @@ def test_schedules_change_timing_only(oracle):
     pipe = TessellationPipeline(sc, caps, FLAGS)
     pipe.set_cameras(cam, last)
     schedules = [
-        dict(classifyBlocksPerSM=4, scanBlocksPerSM=2, splitBlockSize=128, blocksPerSM=2, vertexBlocksPerSM=2),
+        dict(classifyBlocksPerSM=4, scanBlocksPerSM=2, splitBlockSize=128, blocksPerSM=2, vertexBlocksPerSM=2,
+             vertexGridPerSM=1),
         dict(classifyBlocksPerSM=16, scanBlocksPerSM=16, splitBlockSize=512, blocksPerSM=4, vertexBlocksPerSM=5,
              fullVertexBlocksPerSM=8),
         dict(classifyBlocksPerSM=6, scanBlocksPerSM=1, splitBlockSize=256, blocksPerSM=1, vertexBlocksPerSM=1,
              fullVertexBlocksPerSM=1),
-        dict(classifyBlocksPerSM=1, scanBlocksPerSM=4, splitBlockSize=256, blocksPerSM=1, vertexBlocksPerSM=6),
+        dict(classifyBlocksPerSM=1, scanBlocksPerSM=4, splitBlockSize=256, blocksPerSM=1, vertexBlocksPerSM=6,
+             vertexGridPerSM=32),
     ]
     for sched in schedules:
         pipe.set_schedule(sched)
@@ -197,7 +199,7 @@ def test_schedules_change_timing_only(oracle):
             assert_same(pipe.outputs(), ref, f"schedule {sched} {mode}", vertex_tol=vertex_tolerance(sc))
     assert pipe.device_errors() == 0
     for bad in (dict(splitBlockSize=64), dict(vertexBlocksPerSM=0), dict(scanBlocksPerSM=65),
-                dict(fullVertexBlocksPerSM=65)):
+                dict(fullVertexBlocksPerSM=65), dict(vertexGridPerSM=65)):
         with pytest.raises(native.TcError):
             pipe.set_schedule(bad)
     pipe.close()

@@ -28,6 +28,7 @@ SPACE = {
     "blocksPerSM": (1, 2, 4),
     "vertexBlocksPerSM": (3, 4, 5, 6),
     "fullVertexBlocksPerSM": (1, 2, 3, 4),
+    "vertexGridPerSM": (0, 8, 16),
 }
 
 

@@ -364,8 +364,8 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
     TC_CHECK_CUDA(launch_instantiate_alloc(c0, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
                                            sched.scanBlocksPerSM, ctx->side));
     TC_CHECK_CUDA(cudaEventRecord(ctx->evJoin, ctx->side));
-    TC_CHECK_CUDA(launch_instantiate_vertices(c0, instantiate_buffers(ctx), a->caps.maxPartTriangles,
-                                              sched.vertexBlocksPerSM, ctx->side));
+    TC_CHECK_CUDA(launch_instantiate_vertices(c0, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
+                                              sched.vertexBlocksPerSM, sched.vertexGridPerSM, ctx->side));
   }
 
   const u32 passes = split_passes(a->caps.splitFactor);
@@ -390,8 +390,8 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   c.fuseBlasSetup = 0;
   TC_CHECK_CUDA(cudaEventRecord(ctx->evArgs1, s));
   TC_CHECK_CUDA(cudaStreamWaitEvent(ctx->side, ctx->evArgs1, 0));
-  TC_CHECK_CUDA(launch_instantiate_vertices(c, instantiate_buffers(ctx), a->caps.maxPartTriangles,
-                                            sched.vertexBlocksPerSM, ctx->side));
+  TC_CHECK_CUDA(launch_instantiate_vertices(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
+                                            sched.vertexBlocksPerSM, sched.vertexGridPerSM, ctx->side));
   TC_CHECK_CUDA(cudaEventRecord(ctx->evVerts, ctx->side));
 
   bind_slot(ctx, c, p.slotBlas, false);
@@ -485,7 +485,7 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
     delete ctx;
     return TC_ERR_CUDA;
   }
-  ctx->schedule = {4, 256, 4, 4, 1, kDefaultFullVertexBlocksPerSM, {0, 0}};  // the batched scene's tuned shape
+  ctx->schedule = {4, 256, 4, 4, 1, kDefaultFullVertexBlocksPerSM, 0, {0}};  // the batched scene's tuned shape
   ctx->plan     = make_plan(*desc);
   if(cudaMalloc(&ctx->dScratch, ctx->plan.totalBytes) != cudaSuccess
      || cudaMemset(ctx->dScratch, 0, ctx->plan.totalBytes) != cudaSuccess)
@@ -640,7 +640,7 @@ tc_status tc_set_schedule(tc_context* ctx, const tc_schedule* schedule)
       return TC_ERR_INVALID_ARG;
   if(q.splitBlockSize != 128 && q.splitBlockSize != 256 && q.splitBlockSize != 512)
     return TC_ERR_INVALID_ARG;
-  if(q.fullVertexBlocksPerSM > 64)
+  if(q.fullVertexBlocksPerSM > 64 || q.vertexGridPerSM > 64)
     return TC_ERR_INVALID_ARG;
   ctx->schedule   = *schedule;
   if(ctx->schedule.fullVertexBlocksPerSM == 0)
@@ -837,7 +837,7 @@ tc_status tc_triangle_instantiate_run(tc_context* ctx, const tc_frame_args* a, u
   bind_slot(ctx, c, ctx->plan.slotInstantiate, true);
   TC_CHECK_CUDA(launch_triangle_instantiate(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
                                             ctx->schedule.scanBlocksPerSM, ctx->schedule.vertexBlocksPerSM,
-                                            reinterpret_cast<cudaStream_t>(stream)));
+                                            ctx->schedule.vertexGridPerSM, reinterpret_cast<cudaStream_t>(stream)));
   ctx->launches += 4;
   return TC_OK;
 }

@@ -16,11 +16,12 @@
 //               capacity test, the 44 B of instantiation arguments per part,
 //               the first generated vertex of each part (scratch), CLAS
 //               reference counts and statistics.
-//   vertices  : HBM-write bound (12 B per generated vertex). One warp per 16
-//               consecutive parts (spread over the whole grid): every part's
-//               affine vertex form (tc_vertex.cuh) is set up once in shared
-//               memory, then the lanes walk the chunk's contiguous vertex
-//               range on consecutive vertices.
+//   vertices  : 12 B written per generated vertex. A warp takes chunks of 32
+//               consecutive parts (its first by index, the rest from a
+//               ticket): every part's affine vertex form (tc_vertex.cuh) is
+//               set up once in shared memory, one part per lane, then the
+//               lanes walk the chunk's contiguous vertex range on consecutive
+//               vertices.
 #include <algorithm>
 
 #include "tc_kernels.h"
@@ -454,6 +455,9 @@ __global__ void __launch_bounds__(kBlock, 4) k_instantiate_args(StageCtx c, Inst
     // done counter back to zero for a reused slot (nothing else needs clearing)
     if(threadIdx.x == 0 && c.scratch.selfClean)
       *c.scratch.done = 0;
+    // the vertex launch that follows hands out chunks from this ticket
+    if(threadIdx.x == 0)
+      *c.scratch.ticket = 0;
   }
 }
 
@@ -485,8 +489,14 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_vertices(Stag
   const u32                  numChunks    = (n + kPartsPerWarp - 1) / kPartsPerWarp;
   PartAffine*                sp           = s_part[warp];
 
-  for(u32 chunk = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; chunk < numChunks; chunk += nwarps)
+  // chunks: the first nwarps one per warp, the rest handed out by a ticket
+  // (parts differ in vertex count, so warps finish at different times); the
+  // next chunk is fetched while the current one is processed
+  for(u32 chunk = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; chunk < numChunks;)
   {
+    u32 following = 0;
+    if(lane == 0)
+      following = nwarps + atomicAdd(c.scratch.ticket, 1u);
     const u32  p        = begin + chunk * kPartsPerWarp + lane;
     const u32  vo       = (lane < kPartsPerWarp && p < begin + n) ? ib.vertexOffset[p] : ~0u;
     const bool accepted = vo != ~0u;
@@ -574,6 +584,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_vertices(Stag
     }
 #undef TC_CHUNK
     __syncwarp();  // the warp's part records are rewritten by its next chunk
+    chunk = __shfl_sync(0xFFFFFFFFu, following, 0);
   }
 }
 
@@ -595,21 +606,25 @@ cudaError_t launch_instantiate_alloc(const StageCtx& c, const InstantiateBuffers
 }
 
 cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
-                                        u32 scanBlocksPerSM, u32 vertexBlocksPerSM, cudaStream_t s)
+                                        u32 scanBlocksPerSM, u32 vertexBlocksPerSM, u32 vertexGridPerSM,
+                                        cudaStream_t s)
 {
   const cudaError_t e = launch_instantiate_alloc(c, buf, maxParts, numSMs, scanBlocksPerSM, s);
   if(e != cudaSuccess)
     return e;
-  return launch_instantiate_vertices(c, buf, maxParts, vertexBlocksPerSM, s);
+  return launch_instantiate_vertices(c, buf, maxParts, numSMs, vertexBlocksPerSM, vertexGridPerSM, s);
 }
 
-cudaError_t launch_instantiate_vertices(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts,
-                                        u32 vertexBlocksPerSM, cudaStream_t s)
+cudaError_t launch_instantiate_vertices(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
+                                        u32 vertexBlocksPerSM, u32 vertexGridPerSM, cudaStream_t s)
 {
-  const u32 chunks     = (maxParts + kPartsPerWarp - 1) / kPartsPerWarp;
-  // one chunk per warp (blocks retire as they finish, so a concurrent branch's
-  // blocks find room); vertexBlocksPerSM picks the register budget
-  const u32 vertexGrid = std::max(1u, std::min((chunks + kWarps - 1) / kWarps, 1u << 20));
+  const u32 chunks = (maxParts + kPartsPerWarp - 1) / kPartsPerWarp;
+  // warps stride over the 32-part chunks; the grid is sized to the machine,
+  // not to the capacity (blocks with no chunk would only add a tail), by
+  // default one resident wave; vertexBlocksPerSM picks the register budget
+  const u32 resident   = vertexBlocksPerSM >= 6 ? 6u : (vertexBlocksPerSM == 5 ? 5u : 4u);
+  const u32 perSM      = vertexGridPerSM ? vertexGridPerSM : resident;
+  const u32 vertexGrid = std::max(1u, std::min((chunks + kWarps - 1) / kWarps, numSMs * perSM));
   if(vertexBlocksPerSM >= 6)
     return launch_pdl(k_instantiate_vertices<6>, vertexGrid, kBlock, s, c, buf);
   if(vertexBlocksPerSM == 5)

@@ -60,14 +60,15 @@ struct InstantiateBuffers
 // four launches (tile sums, tile scan, args, vertices); the slot needs 3 state rows of
 // instantiate_alloc_tiles(maxParts)
 cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
-                                        u32 scanBlocksPerSM, u32 vertexBlocksPerSM, cudaStream_t s);
+                                        u32 scanBlocksPerSM, u32 vertexBlocksPerSM, u32 vertexGridPerSM,
+                                        cudaStream_t s);
 // the two halves of launch_triangle_instantiate: allocation and arguments
 // (tile sums, tile scan, args), then the displaced vertices, which depend on
 // the allocation alone
 cudaError_t launch_instantiate_alloc(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
                                      u32 scanBlocksPerSM, cudaStream_t s);
-cudaError_t launch_instantiate_vertices(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts,
-                                        u32 vertexBlocksPerSM, cudaStream_t s);
+cudaError_t launch_instantiate_vertices(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
+                                        u32 vertexBlocksPerSM, u32 vertexGridPerSM, cudaStream_t s);
 u32         instantiate_alloc_tiles(u32 maxParts);
 cudaError_t launch_blas_setup_insertion(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 cudaError_t launch_blas_clusters_insert(const StageCtx& c, u32* segStart, u32* segEnd, u32 stride, u32 grid,
