@@ -96,6 +96,25 @@ def test_raster_cull_bit_exact(oracle, mode):
     pipe.close()
 
 
+def test_many_instances_batched_matches_plain():
+    """More instances than the fused BLAS set-up takes (4096): the batched
+    frame launches the multi-block set-up, and its output equals the plain
+    per-instance path's byte for byte (vertices included)."""
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    sc = S.scene_batched(num_instances=4160, map_size=32, box=160.0)
+    cam = S.camera_orbit(3, radius=120.0, center=(80.0, 80.0, 80.0), height=40.0)
+    outs = {}
+    for mode in ("graph", "plain"):
+        pipe = TessellationPipeline(sc, L.default_caps(), FLAGS)
+        pipe.set_cameras(cam)
+        pipe.build(mode)
+        outs[mode] = pipe.outputs()
+        assert pipe.device_errors() == 0
+        pipe.close()
+    assert int(outs["graph"]["readback"]["numBlasClusters"]) > 0
+    assert_same(outs["graph"], outs["plain"], "4160 instances graph vs plain")
+
+
 @pytest.mark.parametrize("which", ["parts", "splits", "vertices", "clusters", "megs", "visible"])
 def test_capacity_overflow_matches_reference_semantics(oracle, which):
     """Tiny caps: the reference drops work past each cap and lets the raw
