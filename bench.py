@@ -409,6 +409,8 @@ def run_ours(args):
         torch.cuda.empty_cache()
         result["backward_forward"] = backward_forward(torch, dev, local)
         torch.cuda.empty_cache()
+        result["hit_decode"] = hit_decode(torch, local, peak)
+        torch.cuda.empty_cache()
         result["animation"] = animation_fwd_bwd(torch, dev, local, result["config"]["schedule"])
     if rank == 0:
         result["cpu_baseline"] = cpu_baseline(args)
@@ -490,6 +492,45 @@ def terrain_bandwidth(torch, dev, local, peak, tune=True):
     res["device_errors"] = pipe.device_errors()
     pipe.close()
     return res
+
+
+def hit_decode(torch, local, peak, n=1 << 20, reps=20):
+    """Hit-time decode (tc_decode_hits) of 2^20 seeded hits on a batched-scene
+    frame (orbit frame 0), hits and results resident on the device: hits/s and
+    the algorithmic GB/s (24 B hit read, 40 B result written, per part hit its
+    24 B part record, per hit the 16 B cluster header and 3 index bytes)."""
+    import numpy as np
+    from vk_tessellated_clusters_gb300 import layouts as L
+    from vk_tessellated_clusters_gb300 import scene as S
+    from vk_tessellated_clusters_gb300.hits import sample_hits
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    scene = S.scene_batched(256)
+    pipe = TessellationPipeline(scene, L.default_caps(), L.FLAG_CULLING | L.FLAG_WRITE_FULLCLUSTERS, device=local)
+    pipe.set_cameras(S.camera_orbit(0))
+    pipe.build("graph")
+    out = pipe.outputs()
+    hits = sample_hits(out, scene, pipe.entries, n, seed=3)
+    dev = f"cuda:{pipe.device}"
+    d_hits = torch.from_numpy(hits.view(np.uint8).reshape(-1).copy()).to(dev)
+    d_out = torch.empty(n * L.BaseHit.itemsize, dtype=torch.uint8, device=dev)
+    for _ in range(3):
+        pipe.decode_hits_device(d_hits, d_out)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        pipe.decode_hits_device(d_hits, d_out)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    parts = int(np.count_nonzero((hits["clusterID"] >> 30) == L.RT_CLUSTER_MODE_SINGLE_TESSELLATED))
+    alg = n * (24 + 40 + 16 + 3) + parts * 24
+    ok = int(np.count_nonzero(d_out.cpu().numpy().view(L.BaseHit)["status"] == L.HIT_OK))
+    pipe.close()
+    return {"hits": n, "part_hits": parts, "ms": ms, "hits_per_s": n / (ms / 1e3),
+            "algorithmic_gbs": alg / (ms / 1e3) / 1e9, "frac_of_peak": alg / (ms / 1e3) / 1e9 / peak,
+            "decoded_ok": ok, "l2": "hits and results (67 MB) stay in L2 across the timed launches",
+            "parity": "tests/test_gpu_parity.py::test_hit_decode_matches_oracle (field-exact vs oracle)"}
 
 
 def backward_forward(torch, dev, local, reps=10):

@@ -67,6 +67,9 @@ extern "C" {
 /* clusterID mode bits in TemplateInstantiateInfo.clusterIdOffset, shaderio.h:101-108 */
 #define TC_RT_CLUSTER_MODE_FULL_CLUSTER 0u
 #define TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED 1u
+#define TC_RT_CLUSTER_MODE_1X_SUBSET_CLUSTER 2u    /* transient builds: not produced by this library */
+#define TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED 3u
+#define TC_VISUALIZE_TRIANGLES 4u /* FrameConstants.visualize, shaderio.h:39 */
 
 /* ------------------------------------------------------------------------- */
 /* layouts (byte-identical to the reference's C++ structs)                    */
@@ -609,6 +612,44 @@ tc_status tc_generate_vertices(tc_context* ctx, const tc_frame_args* args, void*
 tc_status tc_instantiate_backward(tc_context* ctx, const tc_frame_args* args, uint64_t gradVertices,
                                   uint64_t gradTargets, uint64_t gradTexels, void* stream);
 
+/* ---- hit-time decode ------------------------------------------------------------ */
+
+/* A ray hit on the frame's cluster geometry as a cluster ray tracer reports it
+ * (render_raytrace_clusters.rchit.glsl:131-235): the instance, the hit CLAS's
+ * cluster ID with the RT_CLUSTER_MODE in its top two bits (the instantiation's
+ * clusterIdOffset), the triangle within the CLAS and the two hit barycentrics. */
+typedef struct tc_hit {
+  uint32_t instanceID;
+  uint32_t clusterID;
+  uint32_t triangleID;
+  float    barycentrics[2];
+  uint32_t _pad;
+} tc_hit;
+
+#define TC_HIT_OK 0u
+#define TC_HIT_UNSUPPORTED_MODE 1u /* transient-build modes (not produced here) */
+#define TC_HIT_OUT_OF_RANGE 2u     /* instance, part, cluster or triangle index outside the frame's data */
+
+/* The hit on the base mesh: base cluster and triangle, the triangle's vertex
+ * indices into the instance's vertex arrays, their weights, and the
+ * reference's per-hit part id (rchit.glsl:203-214; depends on
+ * FrameConstants.visualize). */
+typedef struct tc_base_hit {
+  uint32_t clusterID;
+  uint32_t triangleID;
+  uint32_t vertexIndices[3];
+  float    barycentrics[3];
+  uint32_t partID;
+  uint32_t status; /* TC_HIT_* */
+} tc_base_hit;
+
+/* Decode `count` hits (device arrays) against the frame last built in `args`
+ * (render_raytrace_clusters.rchit.glsl:131-214 without the transient-build
+ * modes): part-triangle hits go through the part's table triangle and its
+ * sub-triangle corners to base barycentrics, full-cluster hits map directly. */
+tc_status tc_decode_hits(tc_context* ctx, const tc_frame_args* args, const tc_hit* hits, uint32_t count,
+                         tc_base_hit* out, void* stream);
+
 /* ---- diagnostics ------------------------------------------------------------- */
 
 /* Synchronously read (and clear) the device error word. */
@@ -622,6 +663,8 @@ uint64_t tc_launch_count(const tc_context* ctx);
 
 #ifdef __cplusplus
 static_assert(sizeof(tc_TessTableEntry) == 8, "TessTableEntry");
+static_assert(sizeof(tc_hit) == 24, "tc_hit");
+static_assert(sizeof(tc_base_hit) == 40, "tc_base_hit");
 static_assert(sizeof(tc_TessellationTable) == 40, "TessellationTable");
 static_assert(sizeof(tc_BBox) == 32, "BBox");
 static_assert(sizeof(tc_Cluster) == 16, "Cluster");

@@ -65,6 +65,7 @@ def lib():
         l.tco_generate_vertices_f64_params.argtypes = [P(TcoTable), P(L.FrameArgs), vp, vp, vp, vp]
         l.tco_generate_vertices_f64_params.restype = ctypes.c_uint64
         l.tco_backward_f64.argtypes = [P(TcoTable), P(L.FrameArgs), vp, vp, vp, vp]
+        l.tco_decode_hits.argtypes = [P(TcoTable), P(L.FrameArgs), vp, u32, vp]
         _lib = l
     return _lib
 
@@ -105,6 +106,14 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"tco_frame_build failed ({rc})")
         return st, list(runs)
+
+    def decode_hits(self, state: FrameState, hits: np.ndarray) -> np.ndarray:
+        """tc_decode_hits restated on the CPU for the frame in `state`."""
+        hits = np.ascontiguousarray(hits, dtype=L.Hit)
+        out = np.zeros(len(hits), L.BaseHit)
+        self.lib.tco_decode_hits(ctypes.byref(self.table), ctypes.byref(state.args), hits.ctypes.data, len(hits),
+                                 out.ctypes.data)
+        return out
 
     def vertices_f64(self, state: FrameState, count: int) -> np.ndarray:
         out = np.zeros((count, 3), np.float64)

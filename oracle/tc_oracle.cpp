@@ -1052,6 +1052,95 @@ void tco_blas_clusters_insert(const tc_frame_args* a)
 }
 
 // src/renderer_raytrace_clusters_tess.cpp:410-692 (compute part)
+// render_raytrace_clusters.rchit.glsl:131-214 (RT target, no transient
+// builds): a cluster-ray-tracing hit to the base triangle, its vertices and
+// base barycentrics. The barycentric compositions are written out as separate
+// multiplies and adds in the shader's left-to-right order.
+void tco_decode_hits(const tco_table* t, const tc_frame_args* a, const tc_hit* hits, uint32_t count, tc_base_hit* out)
+{
+  Ctx                        c(a);
+  const tc_SceneBuilding*    b     = c.b;
+  const tc_TessTriangleInfo* parts = P<const tc_TessTriangleInfo>(b->partTriangles);
+  const tc_FrameConstants*   view  = reinterpret_cast<const tc_FrameConstants*>(a->view);
+  const bool                 visTriangles = view->visualize == TC_VISUALIZE_TRIANGLES;
+  auto                       compose = [](f3 p, f3 q, f3 r, f3 w) {
+    f3 o;
+    o.x = (p.x * w.x + q.x * w.y) + r.x * w.z;
+    o.y = (p.y * w.x + q.y * w.y) + r.y * w.z;
+    o.z = (p.z * w.x + q.z * w.y) + r.z * w.z;
+    return o;
+  };
+  for(uint32_t i = 0; i < count; i++)
+  {
+    const tc_hit& h    = hits[i];
+    tc_base_hit   r    = {};
+    uint32_t      mode = h.clusterID >> 30, clusterID = h.clusterID & 0x3FFFFFFFu;
+    uint32_t      triangleID = h.triangleID, subTriangleID = h.triangleID, cfg = 0;
+    uint32_t      partID     = visTriangles ? triangleID + 1 : 0u;
+    uint32_t      enc[3]     = {0, 0, 0};
+    r.status                 = TC_HIT_OK;
+    if(mode == TC_RT_CLUSTER_MODE_1X_SUBSET_CLUSTER || mode == TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED)
+      r.status = TC_HIT_UNSUPPORTED_MODE;
+    else if(h.instanceID >= a->numInstances)
+      r.status = TC_HIT_OUT_OF_RANGE;
+    else if(mode == TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED)
+    {
+      if(clusterID >= std::min(b->partTriangleCounter, a->caps.maxPartTriangles))
+        r.status = TC_HIT_OUT_OF_RANGE;
+      else
+      {
+        const tc_TessTriangleInfo& pt = parts[clusterID];
+        triangleID                    = pt.subTriangle.triangleID_config & 0xFFFF;
+        cfg                           = pt.subTriangle.triangleID_config >> 16;
+        clusterID                     = pt.cluster.clusterID;
+        for(int v = 0; v < 3; v++)
+          enc[v] = pt.subTriangle.vtxEncoded[v];
+        if(pt.cluster.instanceID != h.instanceID || subTriangleID >= t->entries[cfgIndex(cfg)].numTriangles)
+          r.status = TC_HIT_OUT_OF_RANGE;
+      }
+    }
+    const tc_RenderInstance* in = r.status == TC_HIT_OK ? &c.inst[h.instanceID] : nullptr;
+    if(in && clusterID >= in->numClusters)
+      r.status = TC_HIT_OUT_OF_RANGE;
+    tc_Cluster cl = {};
+    if(r.status == TC_HIT_OK)
+    {
+      cl = P<const tc_Cluster>(in->clusters)[clusterID];
+      if(triangleID >= cl.numTriangles)
+        r.status = TC_HIT_OUT_OF_RANGE;
+    }
+    if(r.status != TC_HIT_OK)
+    {
+      out[i] = r;
+      continue;
+    }
+    const uint8_t* lt = P<const uint8_t>(in->clusterLocalTriangles) + cl.firstLocalTriangle;
+    for(int v = 0; v < 3; v++)
+      r.vertexIndices[v] = lt[triangleID * 3 + v] + cl.firstLocalVertex;
+    const f3 w    = {(1.0f - h.barycentrics[0]) - h.barycentrics[1], h.barycentrics[0], h.barycentrics[1]};
+    f3       base = w;
+    if(mode == TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED)
+    {
+      partID = 0;
+      for(int v = 0; v < 3; v++)
+        partID ^= (enc[v] >> 20) | ((enc[v] >> 4) & 0xFFF);
+      uint32_t tri[3];
+      cfgTriangle(t, cfg, subTriangleID, tri);
+      const f3 sub = compose(cfgVertex(t, cfg, tri[0]), cfgVertex(t, cfg, tri[1]), cfgVertex(t, cfg, tri[2]), w);
+      base         = compose(decodeBary(enc[0]), decodeBary(enc[1]), decodeBary(enc[2]), sub);
+      partID       = visTriangles ? subTriangleID * 3 : partID;
+      partID       = triangleID | ((partID | 1u) << 8);
+    }
+    r.clusterID       = clusterID;
+    r.triangleID      = triangleID;
+    r.barycentrics[0] = base.x;
+    r.barycentrics[1] = base.y;
+    r.barycentrics[2] = base.z;
+    r.partID          = partID;
+    out[i]            = r;
+  }
+}
+
 int tco_frame_build(const tco_table* t, const tc_frame_args* a, int numThreads, uint32_t* partRunStarts)
 {
   tc_SceneBuilding* b = P<tc_SceneBuilding>(a->build);

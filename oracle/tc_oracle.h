@@ -69,6 +69,9 @@ void tco_triangle_split_pass(const tco_table* t, const tc_frame_args* args, int 
 void tco_triangle_instantiate(const tco_table* t, const tc_frame_args* args, int numThreads);
 void tco_blas_setup_insertion(const tc_frame_args* args);
 void tco_blas_clusters_insert(const tc_frame_args* args);
+/* hit-time decode of the frame in `args` (see tc_decode_hits) */
+void tco_decode_hits(const tco_table* t, const tc_frame_args* args, const tc_hit* hits, uint32_t count,
+                     tc_base_hit* out);
 
 /* FP64 twin of the vertex generation for the accepted instantiations of the
  * frame in `args` (after tco_frame_build or the CUDA build): writes

@@ -250,3 +250,28 @@ def test_animated_instances_replay_bit_exact(oracle):
     assert len(set(counts)) > 1  # the motion changes the work
     assert pipe.device_errors() == 0
     pipe.close()
+
+
+@pytest.mark.parametrize("visualize", [0, L.VISUALIZE_TRIANGLES])
+def test_hit_decode_matches_oracle(oracle, visualize):
+    """tc_decode_hits on the GPU equals the oracle's restatement field for
+    field (base cluster, triangle, vertices, barycentric bits, part id,
+    status) on seeded hits of a built frame, malformed hits included."""
+    from vk_tessellated_clusters_gb300.hits import sample_hits
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    sc = S.scene_batched(num_instances=24, map_size=128)
+    fc, last = S.frame_constants(S.camera_orbit(5)), S.frame_constants(S.camera_orbit(4))
+    fc["visualize"] = visualize
+    caps = small_caps()
+    ref_state, _ = oracle.frame(sc, fc, caps, FLAGS, camera_last=last)
+    pipe = TessellationPipeline(sc, caps, FLAGS)
+    pipe.set_cameras(fc, last)
+    pipe.build("graph")
+    out = pipe.outputs()
+    hits = sample_hits(out, sc, pipe.entries, 20000, seed=11, bad=200)
+    got = pipe.decode_hits(hits)
+    want = oracle.decode_hits(ref_state, hits)
+    assert pipe.device_errors() == 0
+    assert (got["status"][:20000] == L.HIT_OK).all()
+    assert got.tobytes() == want.tobytes()
+    pipe.close()

@@ -237,3 +237,56 @@ def test_fp64_adjoint_matches_finite_differences(oracle):
         fd = (lp - lm) / (2 * h)
         an = grad.reshape(-1)[i]
         assert abs(fd - an) <= 1e-4 * max(1.0, abs(fd)), (name, i, fd, an)
+
+
+def test_hit_decode_properties(oracle):
+    """Hit-time decode (render_raytrace_clusters.rchit.glsl:131-214): full-
+    cluster hits keep their barycentrics, part-triangle hits land on the base
+    triangle (weights in [0, 1] summing to 1), a hit on a table vertex maps to
+    that vertex composed with the part's corners, and malformed hits report
+    their status."""
+    from vk_tessellated_clusters_gb300.hits import sample_hits
+    sc = S.scene_batched(num_instances=8, map_size=64)
+    caps = L.default_caps(visible_bits=14, part_bits=17, split_bits=14, vertex_bits=20, megs=64)
+    st, _ = oracle.frame(sc, S.camera_orbit(7), caps, L.FLAG_CULLING | L.FLAG_WRITE_FULLCLUSTERS)
+    out = st.outputs(oracle.entries)
+    hits = sample_hits(out, sc, oracle.entries, 2000, seed=5, bad=40)
+    got = oracle.decode_hits(st, hits)
+    ok = got["status"] == L.HIT_OK
+    assert ok[:2000].all() and (got["status"][2000:] != L.HIT_OK).all()
+    assert set(np.unique(got["status"][2000:])) == {L.HIT_UNSUPPORTED_MODE, L.HIT_OUT_OF_RANGE}
+    mode = hits["clusterID"] >> 30
+    fullh = ok & (mode == 0)
+    parth = ok & (mode == 1)
+    assert fullh.any() and parth.any()
+    w = np.stack([(np.float32(1) - hits["barycentrics"][:, 0]) - hits["barycentrics"][:, 1],
+                  hits["barycentrics"][:, 0], hits["barycentrics"][:, 1]], 1).astype(np.float32)
+    assert (got["barycentrics"][fullh] == w[fullh]).all()
+    assert (got["clusterID"][fullh] == hits["clusterID"][fullh]).all()
+    b = got["barycentrics"][parth].astype(np.float64)
+    assert (b > -1e-6).all() and (b < 1 + 1e-6).all() and np.abs(b.sum(1) - 1).max() < 1e-5
+    # vertex indices are the base triangle's
+    for h in np.flatnonzero(ok)[:200]:
+        geo = sc.geometries[sc.instances[int(hits["instanceID"][h])].geometry]
+        cl = geo.clusters[got["clusterID"][h]]
+        tri = geo.local_triangles[cl["firstLocalTriangle"] + 3 * got["triangleID"][h]:][:3].astype(np.int64)
+        assert list(got["vertexIndices"][h]) == list(tri + int(cl["firstLocalVertex"]))
+    # a hit on the micro-triangle's first corner is that table vertex in the part's corners
+    p = int(np.flatnonzero(parth)[0])
+    h1 = hits[p:p + 1].copy()
+    h1["barycentrics"] = (0.0, 0.0)
+    g1 = oracle.decode_hits(st, h1)[0]
+    part = out["partTriangles"][int(h1["clusterID"][0]) & 0x3FFFFFFF]
+    cfg = int(part["triangleID_config"]) >> 16
+    e = oracle.entries[cfg & 0x7FFF]
+    tri = int(oracle.raw.triangles[int(e["firstTriangle"]) + int(h1["triangleID"][0])])
+    idx = [tri & 0xFF, (tri >> 8) & 0xFF, (tri >> 16) & 0xFF]
+    if cfg & 0x8000:
+        idx[1], idx[2] = idx[2], idx[1]
+    vtx = int(oracle.raw.vertices[int(e["firstVertex"]) + idx[0]])
+    a, bb = (vtx & 0xFFFF) / 32768.0, (vtx >> 16) / 32768.0
+    sub = np.array([1 - a - bb, a, bb]) if not cfg & 0x8000 else np.array([a, 1 - a - bb, bb])
+    corners = np.array([[1 - ((c & 0xFFFF) + (c >> 16)) / 32768.0, (c & 0xFFFF) / 32768.0, (c >> 16) / 32768.0]
+                        for c in (int(x) for x in part["vtxEncoded"])])
+    assert np.allclose(g1["barycentrics"], sub @ corners, atol=1e-6)
+

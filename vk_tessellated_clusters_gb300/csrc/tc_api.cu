@@ -954,6 +954,20 @@ tc_status tc_generate_vertices(tc_context* ctx, const tc_frame_args* a, void* st
   return TC_OK;
 }
 
+tc_status tc_decode_hits(tc_context* ctx, const tc_frame_args* a, const tc_hit* hits, uint32_t count,
+                         tc_base_hit* out, void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  if(count && (!hits || !out))
+    return TC_ERR_INVALID_ARG;
+  StageCtx c = base_ctx(ctx, a);
+  TC_CHECK_CUDA(launch_decode_hits(c, hits, count, out, reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += count ? 1 : 0;
+  return TC_OK;
+}
+
 tc_status tc_read_device_errors(tc_context* ctx, uint32_t* outBits, void* stream)
 {
   if(!ctx || !outBits)

@@ -39,6 +39,7 @@ struct ClassifyBuffers
 };
 
 cudaError_t launch_frame_begin(const StageCtx& c, u32 grid, cudaStream_t s);
+cudaError_t launch_decode_hits(const StageCtx& c, const tc_hit* hits, u32 count, tc_base_hit* out, cudaStream_t s);
 cudaError_t launch_instances_classify(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 // frame_begin and instances_classify in one launch (block = kInstanceTile)
 cudaError_t launch_frame_begin_instances(const StageCtx& c, u32 grid, cudaStream_t s);

@@ -32,6 +32,10 @@ BUILD_SETUP_BUILD_BLAS = 5
 
 RT_CLUSTER_MODE_FULL_CLUSTER = 0
 RT_CLUSTER_MODE_SINGLE_TESSELLATED = 1
+RT_CLUSTER_MODE_1X_SUBSET_CLUSTER = 2
+RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED = 3
+VISUALIZE_TRIANGLES = 4
+HIT_OK, HIT_UNSUPPORTED_MODE, HIT_OUT_OF_RANGE = 0, 1, 2
 
 TEXEL_F32 = 0
 TEXEL_F16 = 1
@@ -169,6 +173,12 @@ DisplacementTexture = _struct([("texels", "<u8"), ("width", "<u4"), ("height", "
                                ("_pad", "<u4")], 24)
 
 GradTargets = _struct([("dPositions", "<u8"), ("dNormals", "<u8")], 16)
+
+# hit-time decode (tc_hit / tc_base_hit)
+Hit = _struct([("instanceID", "<u4"), ("clusterID", "<u4"), ("triangleID", "<u4"), ("barycentrics", "<f4", 2),
+               ("_pad", "<u4")], 24)
+BaseHit = _struct([("clusterID", "<u4"), ("triangleID", "<u4"), ("vertexIndices", "<u4", 3), ("barycentrics", "<f4", 3),
+                   ("partID", "<u4"), ("status", "<u4")], 40)
 
 # ---------------------------------------------------------------------------
 # ctypes structs passed by pointer to the C ABI

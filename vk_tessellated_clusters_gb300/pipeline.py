@@ -115,6 +115,22 @@ class TessellationPipeline:
         t = self.state.gen_vertices.handle[:12 * count]
         return t.view(self.torch.float32).view(-1, 3)
 
+    def decode_hits_device(self, hits, out) -> None:
+        """tc_decode_hits on device tensors: `hits` uint8 (n x 24 B), `out` uint8 (n x 40 B)."""
+        n = hits.numel() // L.Hit.itemsize
+        native.check(self.lib.tc_decode_hits(self.ctx, ctypes.byref(self.args), hits.data_ptr(), n, out.data_ptr(),
+                                             self.stream()), "tc_decode_hits")
+
+    def decode_hits(self, hits: np.ndarray) -> np.ndarray:
+        """Decode cluster-ray-tracing hits (L.Hit records) against the last built
+        frame into base-mesh hits (L.BaseHit records)."""
+        torch = self.torch
+        hits = np.ascontiguousarray(hits, dtype=L.Hit)
+        d_hits = torch.from_numpy(hits.view(np.uint8).reshape(-1).copy()).to(f"cuda:{self.device}")
+        d_out = torch.empty(len(hits) * L.BaseHit.itemsize, dtype=torch.uint8, device=f"cuda:{self.device}")
+        self.decode_hits_device(d_hits, d_out)
+        return d_out.cpu().numpy().view(L.BaseHit)
+
     def backward(self, grad_vertices, grad_targets_addr: int, grad_texels_addr: int) -> None:
         native.check(self.lib.tc_instantiate_backward(self.ctx, ctypes.byref(self.args), int(grad_vertices),
                                                       int(grad_targets_addr), int(grad_texels_addr), self.stream()),
