@@ -411,6 +411,8 @@ def run_ours(args):
         torch.cuda.empty_cache()
         result["hit_decode"] = hit_decode(torch, local, peak)
         torch.cuda.empty_cache()
+        result["pn_ripple"] = pn_ripple(torch, local, result["config"]["schedule"])
+        torch.cuda.empty_cache()
         result["animation"] = animation_fwd_bwd(torch, dev, local, result["config"]["schedule"])
     if rank == 0:
         result["cpu_baseline"] = cpu_baseline(args)
@@ -531,6 +533,47 @@ def hit_decode(torch, local, peak, n=1 << 20, reps=20):
             "algorithmic_gbs": alg / (ms / 1e3) / 1e9, "frac_of_peak": alg / (ms / 1e3) / 1e9 / peak,
             "decoded_ok": ok, "l2": "hits and results (67 MB) stay in L2 across the timed launches",
             "parity": "tests/test_gpu_parity.py::test_hit_decode_matches_oracle (field-exact vs oracle)"}
+
+
+def pn_ripple(torch, local, schedule, frames=(3, 17, 31)):
+    """The batched scene's frame (256 instances, graph replay, L2 flushed)
+    with PN-triangle displacement and the ripple animation (amplitude 0.02,
+    frequency 8, speed 1.5) against the same frame without them: ms per frame
+    and triangles per second of each."""
+    import statistics as st
+    from vk_tessellated_clusters_gb300 import layouts as L
+    from vk_tessellated_clusters_gb300 import scene as S
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    scene = S.scene_batched(256)
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    out = {}
+    for name, extra in (("plain_flags", 0), ("pn_ripple", L.FLAG_PN | L.FLAG_RIPPLE)):
+        pipe = TessellationPipeline(scene, L.default_caps(), L.FLAG_CULLING | extra, device=local)
+        pipe.set_schedule(schedule)
+        ts, tris = [], []
+        for f in frames:
+            fc = S.frame_constants(S.camera_orbit(f))
+            fc["animationRippleAmplitude"], fc["animationRippleFrequency"] = 0.02, 8.0
+            fc["animationRippleSpeed"], fc["animationState"] = 1.5, 0.1 * f
+            pipe.set_cameras(fc, S.camera_orbit(f - 1))
+            for _ in range(3):
+                pipe.build("graph")
+            torch.cuda.synchronize()
+            flush_buf.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            pipe.build("graph")
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+            tris.append(int(pipe.outputs()["readback"]["numTotalTriangles"]))
+        assert pipe.device_errors() == 0
+        pipe.close()
+        ms = st.mean(ts)
+        out[name] = {"ms": ms, "tris_per_s": st.mean(tris) / (ms / 1e3)}
+    out["overhead"] = out["pn_ripple"]["ms"] / out["plain_flags"]["ms"]
+    out["parity"] = "tests/test_gpu_parity.py::test_pn_and_ripple_bit_exact (integers bit-exact, positions within tolerance)"
+    return out
 
 
 def backward_forward(torch, dev, local, reps=10):

@@ -406,6 +406,9 @@ typedef struct tc_caps {
 #define TC_FLAG_FREEZE_VIEWPOS 2u   /* take SceneBuilding.viewPos from viewLast */
 #define TC_FLAG_RASTER_CULL 4u      /* clusters_cull drops clusters (raster semantics) */
 #define TC_FLAG_WRITE_FULLCLUSTERS 8u /* also record accepted full clusters in SceneBuilding.fullClusters */
+#define TC_FLAG_PN 16u     /* TESS_USE_PN: part-triangle vertices on the base triangle's PN (curved point-normal) patch */
+#define TC_FLAG_RIPPLE 32u /* DO_ANIMATION: the FrameConstants ripple deformation on every generated vertex */
+/* (tc_generate_vertices and tc_instantiate_backward cover neither: they return TC_ERR_INVALID_ARG) */
 
 typedef struct tc_frame_args {
   uint64_t view;      /* const tc_FrameConstants* (device): this frame */

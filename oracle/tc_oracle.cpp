@@ -310,6 +310,81 @@ inline f3 displace(f3 pos, f3 normal, f2 uv, const tc_DisplacementTexture* tx, c
   return {pos.x + n.x * h, pos.y + n.y * h, pos.z + n.z * h};
 }
 
+// displacement.glsl:47-78 deform_setupPN: the PN triangle's ten control
+// points from the base positions and (normalised) normals, with the shader's
+// corner naming (b030 = vertex 0, b003 = vertex 1, b300 = vertex 2)
+struct BasePN
+{
+  f3 b030, b003, b300, b021, b012, b102, b201, b210, b120, b111;
+};
+
+inline f3 add3(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline f3 mul3(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+inline f3 div3(f3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+
+// displacement.glsl:40-45
+inline f3 projectToPlane(f3 p, f3 plane, f3 n) { return sub3(p, mul3(n, dot3(sub3(p, plane), n))); }
+
+inline BasePN setupPN(const f3 v[3], const f3 n[3])
+{
+  BasePN b;
+  b.b030         = v[0];
+  b.b003         = v[1];
+  b.b300         = v[2];
+  const f3 e300  = sub3(b.b003, b.b030);
+  const f3 e030  = sub3(b.b300, b.b003);
+  const f3 e003  = sub3(b.b030, b.b300);
+  b.b021         = add3(b.b030, div3(e300, 3.0f));
+  b.b012         = add3(b.b030, div3(mul3(e300, 2.0f), 3.0f));
+  b.b102         = add3(b.b003, div3(e030, 3.0f));
+  b.b201         = add3(b.b003, div3(mul3(e030, 2.0f), 3.0f));
+  b.b210         = add3(b.b300, div3(e003, 3.0f));
+  b.b120         = add3(b.b300, div3(mul3(e003, 2.0f), 3.0f));
+  b.b021         = projectToPlane(b.b021, b.b030, n[0]);
+  b.b012         = projectToPlane(b.b012, b.b003, n[1]);
+  b.b102         = projectToPlane(b.b102, b.b003, n[1]);
+  b.b201         = projectToPlane(b.b201, b.b300, n[2]);
+  b.b210         = projectToPlane(b.b210, b.b300, n[2]);
+  b.b120         = projectToPlane(b.b120, b.b030, n[0]);
+  const f3 center = div3(add3(add3(b.b003, b.b030), b.b300), 3.0f);
+  b.b111 = div3(add3(add3(add3(add3(add3(b.b021, b.b012), b.b102), b.b201), b.b210), b.b120), 6.0f);
+  b.b111 = add3(b.b111, div3(sub3(b.b111, center), 2.0f));
+  return b;
+}
+
+// displacement.glsl:80-104 deform_getPN (pow(x, 2 / 3) as products), terms
+// summed left to right, scalar factors applied left to right
+inline f3 getPN(const BasePN& b, f3 bary)
+{
+  const float u = bary.x, v = bary.y, w = bary.z;
+  const float u3 = u * u * u, v3 = v * v * v, w3 = w * w * w, u2 = u * u, v2 = v * v, w2 = w * w;
+  f3          r = mul3(b.b300, w3);
+  r             = add3(r, mul3(b.b030, u3));
+  r             = add3(r, mul3(b.b003, v3));
+  r             = add3(r, mul3(mul3(mul3(b.b210, 3.0f), w2), u));
+  r             = add3(r, mul3(mul3(mul3(b.b120, 3.0f), w), u2));
+  r             = add3(r, mul3(mul3(mul3(b.b201, 3.0f), w2), v));
+  r             = add3(r, mul3(mul3(mul3(b.b021, 3.0f), u2), v));
+  r             = add3(r, mul3(mul3(mul3(b.b102, 3.0f), w), v2));
+  r             = add3(r, mul3(mul3(mul3(b.b012, 3.0f), u), v2));
+  r             = add3(r, mul3(mul3(mul3(mul3(b.b111, 6.0f), w), u), v));
+  return r;
+}
+
+// displacement.glsl:106-120 rippleDeform(vertex, instance id, geometry size)
+inline f3 ripple(f3 p, uint32_t seed, float size, const tc_FrameConstants& view)
+{
+  const float maxCoord  = std::max(std::fabs(p.x), std::max(std::fabs(p.y), std::fabs(p.z)));
+  const float frequency = view.animationRippleFrequency / size;
+  const float phase     = view.animationState * view.animationRippleSpeed;
+  const float s         = float(seed);
+  const f3    wave      = {std::sin((maxCoord * frequency + s) + phase), std::cos((maxCoord * frequency * 3.0f + s) + phase),
+                           std::sin((maxCoord * frequency * 1.2f + s) + phase)};
+  const f3    dir       = normalize3({p.z, p.y, p.x});
+  const float amp       = view.animationRippleAmplitude * size;
+  return {p.x + dir.x * (amp * wave.x), p.y + dir.y * (amp * wave.y), p.z + dir.z * (amp * wave.z)};
+}
+
 // ---------------------------------------------------------------------------
 // threading
 // ---------------------------------------------------------------------------
@@ -820,6 +895,8 @@ void tco_cluster_classify(const tco_table* t, const tc_frame_args* a, int numThr
           const f2 uv = P<const f2>(in.texcoords)[vi];
           pos         = displace(pos, ld3(in.normals, vi), uv, tx, in, *c.view);
         }
+        if(a->flags & TC_FLAG_RIPPLE)  // cluster_classify.comp.glsl:483-485
+          pos = ripple(pos, ci.instanceID, in.geoHi.w, *c.view);
         gv[alloc[v].vertexOffset + vert] = pos;
       }
     }
@@ -1003,12 +1080,19 @@ void tco_triangle_instantiate(const tco_table* t, const tc_frame_args* a, int nu
       }
       const uint32_t nv = t->entries[cfgIndex(cfg)].numVertices;
       f3*            gv = P<f3>(b->genVertices);
+      // triangle_tess_template_instantiate.comp.glsl:333-370
+      const bool pn = (a->flags & TC_FLAG_PN) != 0, rip = (a->flags & TC_FLAG_RIPPLE) != 0;
+      BasePN     basePN;
+      if(pn)
+        basePN = setupPN(bpos, bnrm);
       for(uint32_t vert = 0; vert < nv; vert++)
       {
         f3 w   = interp3(bb, cfgVertex(t, cfg, vert));
-        f3 pos = interp3(bpos, w);
+        f3 pos = pn ? getPN(basePN, w) : interp3(bpos, w);
         if(tx)
           pos = displace(pos, interp3(bnrm, w), interp2(buv, w), tx, in, *c.view);
+        if(rip)
+          pos = ripple(pos, info.cluster.instanceID, in.geoHi.w, *c.view);
         gv[vertexOffsets[p] + vert] = pos;
       }
     }

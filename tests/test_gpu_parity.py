@@ -275,3 +275,62 @@ def test_hit_decode_matches_oracle(oracle, visualize):
     assert (got["status"][:20000] == L.HIT_OK).all()
     assert got.tobytes() == want.tobytes()
     pipe.close()
+
+
+def _ripple_constants(cam, amplitude=0.02):
+    fc = S.frame_constants(cam)
+    fc["animationRippleAmplitude"] = amplitude
+    fc["animationRippleFrequency"] = 8.0
+    fc["animationRippleSpeed"] = 1.5
+    fc["animationState"] = 0.7
+    return fc
+
+
+@pytest.mark.parametrize("mode", ["batched", "plain", "graph"])
+def test_pn_and_ripple_bit_exact(oracle, mode):
+    """PN-triangle displacement of part vertices (displacement.glsl:47-104)
+    and the ripple on every generated vertex (:106-120): integer outputs
+    bit-exact, positions within the vertex tolerance, on a curved mesh seen
+    close up (parts everywhere) and on the culled batched scene."""
+    ico = S.scene_icosphere(subdivisions=2, map_size=64)
+    near = S.Camera(eye=(0.0, 0.0, 1.3), center=(0.0, 0.0, 0.0), tess_rate_pixels=2.0)
+    sc = S.scene_batched(num_instances=24, map_size=128)
+    cases = [(ico, _ripple_constants(near), None, FLAGS | L.FLAG_PN),
+             (ico, _ripple_constants(near), None, FLAGS | L.FLAG_PN | L.FLAG_RIPPLE),
+             (sc, _ripple_constants(S.camera_orbit(5)), S.camera_orbit(4), FLAGS | L.FLAG_PN | L.FLAG_RIPPLE)]
+    for scene, fc, last, flags in cases:
+        pipe, out, ref, _ = run_both(oracle, scene, fc, small_caps(), flags=flags, mode=mode, cam_last=last)
+        assert int(ref["readback"]["numPartTriangles"]) > 1000
+        assert pipe.device_errors() == 0
+        assert_same(out, ref, f"pn/ripple flags={flags} {mode}", vertex_tol=vertex_tolerance(scene))
+        pipe.close()
+
+
+def test_pn_ripple_entry_point_matches_frame(oracle):
+    """The stages driven one by one through the C ABI with PN and ripple set
+    write the same vertices as the frame path."""
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    ico = S.scene_icosphere(subdivisions=2, map_size=64)
+    fc = _ripple_constants(S.Camera(eye=(0.0, 0.0, 1.3), center=(0.0, 0.0, 0.0), tess_rate_pixels=2.0))
+    pipe = TessellationPipeline(ico, small_caps(), FLAGS | L.FLAG_PN | L.FLAG_RIPPLE)
+    pipe.set_cameras(fc, None)
+    pipe.build("graph")
+    want = pipe.outputs()
+    pipe.stage("frame_begin")
+    pipe.stage("instances_classify")
+    pipe.stage("clusters_cull", 0, 1)
+    pipe.stage("build_setup", L.BUILD_SETUP_CLASSIFY)
+    pipe.stage("cluster_classify", 0, 1)
+    pipe.stage("build_setup", L.BUILD_SETUP_SPLIT)
+    passes = pipe.split_passes()
+    for p in range(passes):
+        pipe.stage("triangle_split", 0, 1)
+        if p + 1 < passes:
+            pipe.stage("build_setup", L.BUILD_SETUP_SPLIT_PASS)
+    pipe.stage("build_setup", L.BUILD_SETUP_INSTANTIATE_TESS)
+    pipe.stage("triangle_instantiate", 0, 0xFFFFFFFF)
+    got = pipe.outputs()
+    assert pipe.device_errors() == 0
+    assert len(want["genVertices"]) > 1000
+    assert got["genVertices"].tobytes() == want["genVertices"].tobytes()
+    pipe.close()

@@ -290,3 +290,44 @@ def test_hit_decode_properties(oracle):
                         for c in (int(x) for x in part["vtxEncoded"])])
     assert np.allclose(g1["barycentrics"], sub @ corners, atol=1e-6)
 
+
+
+def _ripple_constants(cam, amplitude=0.02):
+    fc = S.frame_constants(cam)
+    fc["animationRippleAmplitude"] = amplitude
+    fc["animationRippleFrequency"] = 8.0
+    fc["animationRippleSpeed"] = 1.5
+    fc["animationState"] = 0.7
+    return fc
+
+
+def test_pn_and_ripple_restatement(oracle):
+    """PN displacement (displacement.glsl:47-104) and the ripple
+    (:106-120) change generated vertices only: every integer output equals
+    the plain frame's; PN moves part vertices of a curved mesh by a fraction
+    of its size (flat meshes and full clusters keep theirs); a zero-amplitude
+    ripple changes nothing and a small one moves vertices by at most
+    amplitude x geometry size."""
+    caps = L.default_caps(visible_bits=14, part_bits=17, split_bits=14, vertex_bits=21, megs=64)
+    flags = L.FLAG_CULLING | L.FLAG_WRITE_FULLCLUSTERS
+    ints = ("visibleClusters", "partTriangles", "tempInstantiations", "tempInstanceIDs", "blasBuildInfos")
+    # PN on a curved mesh close up (every vertex of the frame is a part vertex)
+    ico = S.scene_icosphere(subdivisions=2, map_size=64)
+    near = S.Camera(eye=(0.0, 0.0, 1.3), center=(0.0, 0.0, 0.0), tess_rate_pixels=2.0)
+    base = oracle.frame(ico, near, caps, flags)[0].outputs(oracle.entries)
+    pn = oracle.frame(ico, near, caps, flags | L.FLAG_PN)[0].outputs(oracle.entries)
+    for f in ints:
+        assert pn[f].tobytes() == base[f].tobytes(), f
+    d = np.abs(pn["genVertices"].astype(np.float64) - base["genVertices"]).max(axis=1)
+    assert (d > 0).mean() > 0.5 and d.max() < 0.05 * float(np.linalg.norm(ico.geometries[0].hi - ico.geometries[0].lo))
+    # ripple on the batched scene (full clusters and parts)
+    sc = S.scene_batched(num_instances=8, map_size=64)
+    cam = S.camera_orbit(7)
+    base = oracle.frame(sc, cam, caps, flags)[0].outputs(oracle.entries)
+    size = max(float(np.linalg.norm(g.hi - g.lo)) for g in sc.geometries)
+    for amp in (0.0, 0.02):
+        out = oracle.frame(sc, _ripple_constants(cam, amp), caps, flags | L.FLAG_RIPPLE)[0].outputs(oracle.entries)
+        for f in ints:
+            assert out[f].tobytes() == base[f].tobytes(), (amp, f)
+        d = np.abs(out["genVertices"].astype(np.float64) - base["genVertices"]).max()
+        assert (d == 0) if amp == 0 else (0 < d <= amp * size * 1.001)

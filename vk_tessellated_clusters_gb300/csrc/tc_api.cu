@@ -930,6 +930,8 @@ tc_status tc_instantiate_backward(tc_context* ctx, const tc_frame_args* a, uint6
     return st;
   if(!gradVertices || !gradTargets || (a->numTextures && !gradTexels))
     return TC_ERR_INVALID_ARG;
+  if(a->flags & (TC_FLAG_PN | TC_FLAG_RIPPLE))  // the adjoint covers the linear, displaced path only
+    return TC_ERR_INVALID_ARG;
   if(!(a->flags & TC_FLAG_WRITE_FULLCLUSTERS))
     return TC_ERR_INVALID_ARG;
   StageCtx c = base_ctx(ctx, a);
@@ -946,7 +948,7 @@ tc_status tc_generate_vertices(tc_context* ctx, const tc_frame_args* a, void* st
   tc_status st = validate(ctx, a);
   if(st != TC_OK)
     return st;
-  if(!(a->flags & TC_FLAG_WRITE_FULLCLUSTERS))
+  if(!(a->flags & TC_FLAG_WRITE_FULLCLUSTERS) || (a->flags & (TC_FLAG_PN | TC_FLAG_RIPPLE)))
     return TC_ERR_INVALID_ARG;
   StageCtx c = base_ctx(ctx, a);
   TC_CHECK_CUDA(launch_generate_vertices(c, ctx->numSMs * 8, reinterpret_cast<cudaStream_t>(stream)));

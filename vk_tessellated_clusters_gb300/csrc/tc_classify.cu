@@ -464,12 +464,15 @@ struct FullRecord
   float        offset; // instance + view displacement offset
   u32          vo;     // first generated vertex
   u32          nv;     // vertex count
+  u32          inst;   // instance (the ripple's seed)
+  float        size;   // its geometry size (RenderInstance.geoHi.w)
 };
 
 // the vertex walk over a batch of full clusters (records in `rec`), for
 // records of map kind Kind (~0u: any)
 template <u32 Kind>
-__device__ __forceinline__ void full_steps(const FullRecord* rec, bool owner, u32 rStart, u32 rEnd, float* dst)
+__device__ __forceinline__ void full_steps(const FullRecord* rec, bool owner, u32 rStart, u32 rEnd, float* dst,
+                                           const RippleParams& rp)
 {
   const u32 lane = threadIdx.x & 31;
 #pragma unroll 2  // two steps in flight: their loads overlap
@@ -488,6 +491,8 @@ __device__ __forceinline__ void full_steps(const FullRecord* rec, bool owner, u3
       f3                p  = ldg3(fr.pos, vi);
       if(Kind != kAffineFlat)
         p = full_vertex_k<Kind>(p, ldg3(fr.nrm, vi), ldg2(fr.uvs, vi), fr.map, fr.scale, fr.offset);
+      if(rp.enabled)  // cluster_classify.comp.glsl:483-485
+        p = ripple(p, fr.inst, fr.size, rp);
       float* d = dst + (u64)jj * 3;
       d[0]     = p.x;
       d[1]     = p.y;
@@ -752,6 +757,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_full_vertices(St
   const bool            haveTextures = c.numTextures > 0 && c.textures != nullptr;
   float*                gv           = reinterpret_cast<float*>(b->genVertices);
   FullRecord*           rec          = s_full[warp];
+  const RippleParams    rp           = ripple_params(*c.view, (c.flags & TC_FLAG_RIPPLE) != 0);
 
   for(u32 chunk = blockIdx.x * kWarps + warp; chunk < numChunks; chunk += totalWarps)
   {
@@ -784,6 +790,8 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_full_vertices(St
         fr.map    = make_map_desc(tx);
         fr.scale  = in->displacementScale * c.view->displacementScale;
         fr.offset = in->displacementOffset + c.view->displacementOffset;
+        fr.inst   = ci.instanceID;
+        fr.size   = in->geoHi.w;
       }
     }
     // accepted clusters are a prefix of the slots, so the owners are the
@@ -808,10 +816,14 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_full_vertices(St
     float*    dst   = gv + (u64)vBase * 3;
     switch(kw)
     {
-      case affine_kind(TC_TEXEL_F32, true): full_steps<affine_kind(TC_TEXEL_F32, true)>(rec, own, rStart, rEnd, dst); break;
-      case affine_kind(TC_TEXEL_F16, true): full_steps<affine_kind(TC_TEXEL_F16, true)>(rec, own, rStart, rEnd, dst); break;
-      case kAffineFlat: full_steps<kAffineFlat>(rec, own, rStart, rEnd, dst); break;
-      default: full_steps<~0u>(rec, own, rStart, rEnd, dst); break;
+      case affine_kind(TC_TEXEL_F32, true):
+        full_steps<affine_kind(TC_TEXEL_F32, true)>(rec, own, rStart, rEnd, dst, rp);
+        break;
+      case affine_kind(TC_TEXEL_F16, true):
+        full_steps<affine_kind(TC_TEXEL_F16, true)>(rec, own, rStart, rEnd, dst, rp);
+        break;
+      case kAffineFlat: full_steps<kAffineFlat>(rec, own, rStart, rEnd, dst, rp); break;
+      default: full_steps<~0u>(rec, own, rStart, rEnd, dst, rp); break;
     }
     __syncwarp();  // records are rewritten by the next batch
   }

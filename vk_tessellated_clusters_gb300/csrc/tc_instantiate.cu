@@ -588,6 +588,79 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_vertices(Stag
   }
 }
 
+// triangle_tess_template_instantiate.comp.glsl:295-371 with TESS_USE_PN and /
+// or DO_ANIMATION: one warp per part triangle, lanes over its vertices; the
+// PN basis and the base attributes stay in registers. Written like the CPU
+// restatement (tess_interpolate of the base barycentrics, the reference-order
+// sampling and displacement) rather than in the affine form of the fast path.
+__global__ void __launch_bounds__(kBlock) k_instantiate_vertices_deform(StageCtx c, InstantiateBuffers ib)
+{
+  stage_prologue();
+  __shared__ u32 s_range[2];
+  const u32 lane = threadIdx.x & 31;
+  if(threadIdx.x == 0)
+    part_range(c, s_range[0], s_range[1]);
+  __syncthreads();
+  const u32                  begin = s_range[0], end = s_range[1];
+  const tc_SceneBuilding*    b     = c.build;
+  const tc_TessTriangleInfo* parts = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
+  float*                     gv    = reinterpret_cast<float*>(b->genVertices);
+  const bool                 pn    = (c.flags & TC_FLAG_PN) != 0;
+  const RippleParams         rp    = ripple_params(*c.view, (c.flags & TC_FLAG_RIPPLE) != 0);
+  const u32                  nwarps = (gridDim.x * blockDim.x) >> 5;
+  for(u32 p = begin + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); p < end; p += nwarps)
+  {
+    const u32 vo = ib.vertexOffset[p];
+    if(vo == ~0u)
+      break;  // accepted parts form a prefix of the part order
+    const tc_TessTriangleInfo pt  = parts[p];
+    const u32                 cfg = pt.subTriangle.triangleID_config >> 16;
+    const u32                 tri = pt.subTriangle.triangleID_config & 0xFFFFu;
+    const tc_TessTableEntry   e   = table_entry(c.table, cfg);
+    const tc_RenderInstance&  in  = c.instances[pt.cluster.instanceID];
+    const tc_Cluster          cl  = reinterpret_cast<const tc_Cluster*>(in.clusters)[pt.cluster.clusterID];
+    const uint8_t*            lt  = reinterpret_cast<const uint8_t*>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
+    f3                        bp[3], bn[3], bb[3];
+    f2                        bt[3];
+    for(int v = 0; v < 3; v++)
+    {
+      const u32 vi = cl.firstLocalVertex + lt[tri * 3 + v];
+      bp[v]        = ldg3(reinterpret_cast<const float*>(in.positions), vi);
+      bn[v]        = normalize3(ldg3(reinterpret_cast<const float*>(in.normals), vi));  // :329
+      bt[v]        = ldg2(reinterpret_cast<const float*>(in.texcoords), vi);
+      bb[v]        = decode_bary(pt.subTriangle.vtxEncoded[v]);
+    }
+    tc_DisplacementTexture tx    = {};
+    bool                   hasTx = false;
+    if(c.numTextures > 0 && c.textures != nullptr && in.displacementIndex >= 0)
+    {
+      if((u32)in.displacementIndex < c.numTextures)
+      {
+        tx    = c.textures[in.displacementIndex];
+        hasTx = true;
+      }
+      else if(lane == 0)
+        atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
+    }
+    BasePN basis = {};
+    if(pn)
+      basis = setup_pn(bp[0], bp[1], bp[2], bn[0], bn[1], bn[2]);
+    for(u32 vert = lane; vert < e.numVertices; vert += 32)
+    {
+      const f3 w   = interp3(bb[0], bb[1], bb[2], cfg_vertex(c.table, e, cfg, vert));
+      f3       pos = pn ? get_pn(basis, w) : interp3(bp[0], bp[1], bp[2], w);
+      if(hasTx)
+        pos = displace(pos, interp3(bn[0], bn[1], bn[2], w), sample_bilinear(tx, interp2(bt[0], bt[1], bt[2], w)),
+                       in.displacementScale, c.view->displacementScale, in.displacementOffset,
+                       c.view->displacementOffset);
+      if(rp.enabled)
+        pos = ripple(pos, pt.cluster.instanceID, in.geoHi.w, rp);
+      float* d = gv + 3 * ((u64)vo + vert);
+      d[0] = pos.x, d[1] = pos.y, d[2] = pos.z;
+    }
+  }
+}
+
 }  // namespace
 
 u32 instantiate_alloc_tiles(u32 maxParts) { return (maxParts + kTile - 1) / kTile; }
@@ -619,6 +692,9 @@ cudaError_t launch_instantiate_vertices(const StageCtx& c, const InstantiateBuff
                                         u32 vertexBlocksPerSM, u32 vertexGridPerSM, cudaStream_t s)
 {
   const u32 chunks = (maxParts + kPartsPerWarp - 1) / kPartsPerWarp;
+  if(c.flags & (TC_FLAG_PN | TC_FLAG_RIPPLE))  // the deformation path: one warp per part
+    return launch_pdl(k_instantiate_vertices_deform, std::max(1u, std::min((maxParts + kWarps - 1) / kWarps, numSMs * 8)),
+                      kBlock, s, c, buf);
   // warps stride over the 32-part chunks; the grid is sized to the machine,
   // not to the capacity (blocks with no chunk would only add a tail), by
   // default one resident wave; vertexBlocksPerSM picks the register budget

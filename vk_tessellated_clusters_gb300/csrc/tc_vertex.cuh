@@ -267,3 +267,94 @@ __device__ __forceinline__ f3 affine_vertex(const PartAffine& r, u32 tableVertex
 __device__ __forceinline__ u32 affine_first_vertex(const PartAffine& r) { return __float_as_uint(r.q[6].z); }
 
 }  // namespace tc
+
+namespace tc {
+
+// ---------------------------------------------------------------------------
+// PN-triangle displacement and the ripple deformation (displacement.glsl),
+// written like the CPU restatement: separate IEEE multiplies, adds and
+// divisions in the shader's order.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ f3 add3(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 mul3(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ f3 div3(f3 a, float s) { return {__fdiv_rn(a.x, s), __fdiv_rn(a.y, s), __fdiv_rn(a.z, s)}; }
+
+// displacement.glsl:40-45
+__device__ __forceinline__ f3 project_to_plane(f3 p, f3 plane, f3 n) { return sub3(p, mul3(n, dot3(sub3(p, plane), n))); }
+
+// displacement.glsl:27-38 (b030 = base vertex 0, b003 = vertex 1, b300 = vertex 2)
+struct BasePN
+{
+  f3 b030, b003, b300, b021, b012, b102, b201, b210, b120, b111;
+};
+
+// displacement.glsl:47-78 deform_setupPN; n: normalised base normals
+__device__ __forceinline__ BasePN setup_pn(f3 v0, f3 v1, f3 v2, f3 n0, f3 n1, f3 n2)
+{
+  BasePN   b;
+  b.b030         = v0;
+  b.b003         = v1;
+  b.b300         = v2;
+  const f3 e300  = sub3(b.b003, b.b030);
+  const f3 e030  = sub3(b.b300, b.b003);
+  const f3 e003  = sub3(b.b030, b.b300);
+  b.b021         = project_to_plane(add3(b.b030, div3(e300, 3.0f)), b.b030, n0);
+  b.b012         = project_to_plane(add3(b.b030, div3(mul3(e300, 2.0f), 3.0f)), b.b003, n1);
+  b.b102         = project_to_plane(add3(b.b003, div3(e030, 3.0f)), b.b003, n1);
+  b.b201         = project_to_plane(add3(b.b003, div3(mul3(e030, 2.0f), 3.0f)), b.b300, n2);
+  b.b210         = project_to_plane(add3(b.b300, div3(e003, 3.0f)), b.b300, n2);
+  b.b120         = project_to_plane(add3(b.b300, div3(mul3(e003, 2.0f), 3.0f)), b.b030, n0);
+  const f3 center = div3(add3(add3(b.b003, b.b030), b.b300), 3.0f);
+  b.b111 = div3(add3(add3(add3(add3(add3(b.b021, b.b012), b.b102), b.b201), b.b210), b.b120), 6.0f);
+  b.b111 = add3(b.b111, div3(sub3(b.b111, center), 2.0f));
+  return b;
+}
+
+// displacement.glsl:80-104 deform_getPN (the powers as products)
+__device__ __forceinline__ f3 get_pn(const BasePN& b, f3 bary)
+{
+  const float u = bary.x, v = bary.y, w = bary.z;
+  const float u3 = u * u * u, v3 = v * v * v, w3 = w * w * w, u2 = u * u, v2 = v * v, w2 = w * w;
+  f3          r = mul3(b.b300, w3);
+  r             = add3(r, mul3(b.b030, u3));
+  r             = add3(r, mul3(b.b003, v3));
+  r             = add3(r, mul3(mul3(mul3(b.b210, 3.0f), w2), u));
+  r             = add3(r, mul3(mul3(mul3(b.b120, 3.0f), w), u2));
+  r             = add3(r, mul3(mul3(mul3(b.b201, 3.0f), w2), v));
+  r             = add3(r, mul3(mul3(mul3(b.b021, 3.0f), u2), v));
+  r             = add3(r, mul3(mul3(mul3(b.b102, 3.0f), w), v2));
+  r             = add3(r, mul3(mul3(mul3(b.b012, 3.0f), u), v2));
+  r             = add3(r, mul3(mul3(mul3(mul3(b.b111, 6.0f), w), u), v));
+  return r;
+}
+
+// the FrameConstants terms of displacement.glsl:106-120
+struct RippleParams
+{
+  float frequency;  // animationRippleFrequency
+  float phase;      // animationState * animationRippleSpeed
+  float amplitude;  // animationRippleAmplitude
+  u32   enabled;
+};
+
+__device__ __forceinline__ RippleParams ripple_params(const tc_FrameConstants& view, bool enabled)
+{
+  return {view.animationRippleFrequency, view.animationState * view.animationRippleSpeed,
+          view.animationRippleAmplitude, enabled ? 1u : 0u};
+}
+
+// displacement.glsl:106-120 rippleDeform(vertex, instance id, geometry size)
+__device__ __forceinline__ f3 ripple(f3 p, u32 seed, float size, const RippleParams& rp)
+{
+  const float maxCoord  = fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z)));
+  const float frequency = __fdiv_rn(rp.frequency, size);
+  const float s         = __uint2float_rn(seed);
+  const f3    wave      = {sinf((maxCoord * frequency + s) + rp.phase), cosf((maxCoord * frequency * 3.0f + s) + rp.phase),
+                           sinf((maxCoord * frequency * 1.2f + s) + rp.phase)};
+  const f3    dir       = normalize3({p.z, p.y, p.x});
+  const float amp       = rp.amplitude * size;
+  return {p.x + dir.x * (amp * wave.x), p.y + dir.y * (amp * wave.y), p.z + dir.z * (amp * wave.z)};
+}
+
+}  // namespace tc

@@ -45,6 +45,8 @@ FLAG_CULLING = 1
 FLAG_FREEZE_VIEWPOS = 2
 FLAG_RASTER_CULL = 4
 FLAG_WRITE_FULLCLUSTERS = 8
+FLAG_PN = 16
+FLAG_RIPPLE = 32
 
 DEVERR_LOOKBACK_TIMEOUT = 1
 DEVERR_BAD_CLUSTER = 2
