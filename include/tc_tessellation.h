@@ -67,7 +67,7 @@ extern "C" {
 /* clusterID mode bits in TemplateInstantiateInfo.clusterIdOffset, shaderio.h:101-108 */
 #define TC_RT_CLUSTER_MODE_FULL_CLUSTER 0u
 #define TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED 1u
-#define TC_RT_CLUSTER_MODE_1X_SUBSET_CLUSTER 2u    /* transient builds: not produced by this library */
+#define TC_RT_CLUSTER_MODE_1X_SUBSET_CLUSTER 2u    /* transient build of a cluster's untessellated triangles */
 #define TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED 3u
 #define TC_VISUALIZE_TRIANGLES 4u /* FrameConstants.visualize, shaderio.h:39 */
 
@@ -408,7 +408,21 @@ typedef struct tc_caps {
 #define TC_FLAG_WRITE_FULLCLUSTERS 8u /* also record accepted full clusters in SceneBuilding.fullClusters */
 #define TC_FLAG_PN 16u     /* TESS_USE_PN: part-triangle vertices on the base triangle's PN (curved point-normal) patch */
 #define TC_FLAG_RIPPLE 32u /* DO_ANIMATION: the FrameConstants ripple deformation on every generated vertex */
-/* (tc_generate_vertices and tc_instantiate_backward cover neither: they return TC_ERR_INVALID_ARG) */
+/* TESS_USE_1X_TRANSIENTBUILDS (cluster_classify.comp.glsl:254-343, 394-437, 489-535): a cluster with more
+ * than one untessellated triangle (but not all) gets a transient CLAS build of those triangles over its own
+ * vertices (ClasBuildInfo in SceneBuilding.transBuilds, u8 indices after the vertices, u8 triangle map
+ * after a ClusterInfo header at the back of partTriangles) */
+#define TC_FLAG_TRANSIENT_1X 64u
+/* TESS_USE_2X_TRANSIENTBUILDS (cluster_classify.comp.glsl:675-905): triangles with edge factors <= 2 are
+ * tessellated in place and packed, TC_2X_MINI_BATCHSIZE at a time, into transient builds (u16 map) */
+#define TC_FLAG_TRANSIENT_2X 128u
+/* The transient flags need SceneBuilding.basicClusterSizes (TC_MAX_CLUSTER_TRIANGLES + 1 entries) and the
+ * trans* arrays; they are ray-tracing semantics (TC_ERR_INVALID_ARG with TC_FLAG_RASTER_CULL).
+ * tc_generate_vertices and tc_instantiate_backward cover none of PN, ripple or transient builds: they
+ * return TC_ERR_INVALID_ARG. */
+#define TC_2X_MINI_BATCHSIZE 8u /* shaderio.h:149-158 */
+#define TC_2X_MINI_TRIANGLES 4u
+#define TC_2X_MINI_VERTICES 6u
 
 typedef struct tc_frame_args {
   uint64_t view;      /* const tc_FrameConstants* (device): this frame */
@@ -630,7 +644,7 @@ typedef struct tc_hit {
 } tc_hit;
 
 #define TC_HIT_OK 0u
-#define TC_HIT_UNSUPPORTED_MODE 1u /* transient-build modes (not produced here) */
+#define TC_HIT_UNSUPPORTED_MODE 1u /* a transient-build mode the frame was not built with */
 #define TC_HIT_OUT_OF_RANGE 2u     /* instance, part, cluster or triangle index outside the frame's data */
 
 /* The hit on the base mesh: base cluster and triangle, the triangle's vertex
@@ -647,9 +661,11 @@ typedef struct tc_base_hit {
 } tc_base_hit;
 
 /* Decode `count` hits (device arrays) against the frame last built in `args`
- * (render_raytrace_clusters.rchit.glsl:131-214 without the transient-build
- * modes): part-triangle hits go through the part's table triangle and its
- * sub-triangle corners to base barycentrics, full-cluster hits map directly. */
+ * (render_raytrace_clusters.rchit.glsl:131-214): part-triangle and 2X batch
+ * hits go through the table triangle and the sub-triangle corners to base
+ * barycentrics, 1X subset hits through the triangle map, full-cluster hits map
+ * directly. The transient modes decode when args->flags has the matching
+ * TC_FLAG_TRANSIENT_* bit, else they report TC_HIT_UNSUPPORTED_MODE. */
 tc_status tc_decode_hits(tc_context* ctx, const tc_frame_args* args, const tc_hit* hits, uint32_t count,
                          tc_base_hit* out, void* stream);
 

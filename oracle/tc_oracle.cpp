@@ -684,10 +684,13 @@ void tco_clusters_cull(const tc_frame_args* a)
   }
 }
 
-// shaders/build_setup.comp.glsl:102-265 (RT target, no transient builds, multipass split)
+// shaders/build_setup.comp.glsl:102-265 (RT target, multipass split; with
+// transient builds :193-265 read the two-sided part counter and the transient
+// build count)
 void tco_build_setup(const tc_frame_args* a, uint32_t mode)
 {
   Ctx               c(a);
+  const bool        trans = (a->flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X)) != 0;
   tc_SceneBuilding* b  = c.b;
   tc_Readback*      rb = c.rb;
   const tc_caps&    k  = a->caps;
@@ -739,7 +742,9 @@ void tco_build_setup(const tc_frame_args* a, uint32_t mode)
     case TC_BUILD_SETUP_BUILD_BLAS:
     {
       uint32_t temp               = b->tempInstantiateCounter;
-      rb->numBlasClusters         = temp;
+      uint32_t tr                 = trans ? b->transBuildCounter : 0u;
+      rb->numBlasClusters         = temp + tr;
+      rb->numTransBuilds          = tr;
       rb->numTempInstantiations   = temp;
       rb->numGenDatas             = b->genClusterDataCounter;
       rb->numGenVertices          = b->genVertexCounter;
@@ -748,13 +753,28 @@ void tco_build_setup(const tc_frame_args* a, uint32_t mode)
       b->tempInstantiateCounter   = temp;
       rb->numActualTempInstantiations = temp;
       b->dispatchBlasTempInsert   = {(temp + 63) / 64, 1, 1};
+      if(trans)
+      {
+        tr                          = std::min(k.maxGeneratedClusters, temp + tr) - temp;
+        b->transBuildCounter        = tr;
+        rb->numActualTransBuilds    = tr;
+        b->dispatchBlasTransInsert  = {(tr + 63) / 64, 1, 1};
+      }
       break;
     }
     case TC_BUILD_SETUP_INSTANTIATE_TESS:
     {
       uint32_t part           = b->partTriangleCounter;
-      rb->numPartTriangles    = part;
       rb->numSplitTriangles   = b->splitWriteCounter;
+      if(trans)
+      {
+        // requests from both ends; partTriangleCounter is the written front's end
+        const uint32_t lo = (uint32_t)b->dualPartTriangleCounter, hi = (uint32_t)(b->dualPartTriangleCounter >> 32);
+        rb->numPartTriangles      = lo + hi;
+        rb->numTransPartTriangles = hi;
+      }
+      else
+        rb->numPartTriangles = part;
       part                    = std::min(part, k.maxPartTriangles);
       b->partTriangleCounter  = part;
       b->dispatchTriangleInstantiate = {(part + 31) / 32, 1, 1};
@@ -764,6 +784,24 @@ void tco_build_setup(const tc_frame_args* a, uint32_t mode)
       break;
   }
 }
+
+}  // extern "C"
+
+namespace {
+
+// per visible cluster: its triangles' edge factors and how many need no tessellation
+struct ClassifyRec
+{
+  uint32_t simple;
+  uint32_t numTriangles;
+  uint32_t factors[64][3];
+};
+
+void classifyTransient(const tco_table* t, const tc_frame_args* a, std::vector<ClassifyRec>& recs, int numThreads);
+
+}  // namespace
+
+extern "C" {
 
 // shaders/cluster_classify.comp.glsl:150-666 (RT target, plain path)
 void tco_cluster_classify(const tco_table* t, const tc_frame_args* a, int numThreads)
@@ -775,12 +813,7 @@ void tco_cluster_classify(const tco_table* t, const tc_frame_args* a, int numThr
   const uint32_t*      states = P<const uint32_t>(b->instanceStates);
   const bool           culling = (a->flags & TC_FLAG_CULLING) != 0;
 
-  struct Rec
-  {
-    uint32_t simple;
-    uint32_t numTriangles;
-    uint32_t factors[64][3];
-  };
+  using Rec = ClassifyRec;
   std::vector<Rec> recs(nvis);
 
   // phase 1: factors (parallel)
@@ -810,6 +843,12 @@ void tco_cluster_classify(const tco_table* t, const tc_frame_args* a, int numThr
       }
     }
   });
+
+  if(a->flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X))
+  {
+    classifyTransient(t, a, recs, numThreads);
+    return;
+  }
 
   // phase 2: serial allocation in canonical order
   struct Alloc
@@ -999,6 +1038,7 @@ void tco_triangle_split_pass(const tco_table* t, const tc_frame_args* a, int num
     }
   });
 
+  const bool trans = (a->flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X)) != 0;
   for(uint32_t i = 0; i < n; i++)
     for(const Child& ch : children[i])
     {
@@ -1007,6 +1047,19 @@ void tco_triangle_split_pass(const tco_table* t, const tc_frame_args* a, int num
         uint32_t off = b->splitWriteCounter++;
         if(off < a->caps.maxSplitTriangles)
           items[off] = ch.info;
+      }
+      else if(trans)
+      {
+        // build.glsl:68-82 through the two-sided counter, one child at a time;
+        // partTriangleCounter keeps the end of the written front
+        // (triangle_split.comp.glsl:321-328)
+        const uint32_t x = (uint32_t)b->dualPartTriangleCounter, y = (uint32_t)(b->dualPartTriangleCounter >> 32);
+        b->dualPartTriangleCounter += 1;
+        if((uint64_t)x + y + 2 <= a->caps.maxPartTriangles)
+        {
+          P<tc_TessTriangleInfo>(b->partTriangles)[x] = ch.info;
+          b->partTriangleCounter                      = std::max(b->partTriangleCounter, x + 1);
+        }
       }
       else
       {
@@ -1118,7 +1171,8 @@ void tco_blas_setup_insertion(const tc_frame_args* a)
   }
 }
 
-// shaders/blas_clusters_insert.comp.glsl:97-136 (template instantiations, in order)
+// shaders/blas_clusters_insert.comp.glsl:97-136 (template instantiations in
+// order, then transient builds in order)
 void tco_blas_clusters_insert(const tc_frame_args* a)
 {
   Ctx               c(a);
@@ -1133,11 +1187,23 @@ void tco_blas_clusters_insert(const tc_frame_args* a)
     P<uint64_t>(infos[inst].clusterReferences)[idx] = addr;
     c.rb->numGenActualDatas += size;
   }
+  // the second dispatch (push.instanceID 1): transient builds, after every
+  // template instantiation of the frame
+  if(a->flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X))
+    for(uint32_t j = 0; j < b->transBuildCounter; j++)
+    {
+      uint32_t inst = P<const uint32_t>(b->transInstanceIDs)[j];
+      uint64_t addr = P<const uint64_t>(b->transClusterAddresses)[j];
+      uint32_t size = b->transClusterSizes ? P<const uint32_t>(b->transClusterSizes)[j] : 0;
+      uint32_t idx  = infos[inst].clusterReferencesCount++;
+      P<uint64_t>(infos[inst].clusterReferences)[idx] = addr;
+      c.rb->numGenActualDatas += size;
+    }
 }
 
 // src/renderer_raytrace_clusters_tess.cpp:410-692 (compute part)
-// render_raytrace_clusters.rchit.glsl:131-214 (RT target, no transient
-// builds): a cluster-ray-tracing hit to the base triangle, its vertices and
+// render_raytrace_clusters.rchit.glsl:131-214 (RT target; the transient-build
+// modes when the frame's flags have them): a cluster-ray-tracing hit to the base triangle, its vertices and
 // base barycentrics. The barycentric compositions are written out as separate
 // multiplies and adds in the shader's left-to-right order.
 void tco_decode_hits(const tco_table* t, const tc_frame_args* a, const tc_hit* hits, uint32_t count, tc_base_hit* out)
@@ -1162,11 +1228,46 @@ void tco_decode_hits(const tco_table* t, const tc_frame_args* a, const tc_hit* h
     uint32_t      triangleID = h.triangleID, subTriangleID = h.triangleID, cfg = 0;
     uint32_t      partID     = visTriangles ? triangleID + 1 : 0u;
     uint32_t      enc[3]     = {0, 0, 0};
+    bool          tess       = mode == TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED;
     r.status                 = TC_HIT_OK;
-    if(mode == TC_RT_CLUSTER_MODE_1X_SUBSET_CLUSTER || mode == TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED)
+    if((mode == TC_RT_CLUSTER_MODE_1X_SUBSET_CLUSTER && !(a->flags & TC_FLAG_TRANSIENT_1X))
+       || (mode == TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED && !(a->flags & TC_FLAG_TRANSIENT_2X)))
       r.status = TC_HIT_UNSUPPORTED_MODE;
     else if(h.instanceID >= a->numInstances)
       r.status = TC_HIT_OUT_OF_RANGE;
+    else if(mode == TC_RT_CLUSTER_MODE_1X_SUBSET_CLUSTER || mode == TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED)
+    {
+      // rchit.glsl:150-180: the ClusterInfo header and the triangle map of a
+      // transient build at the back of partTriangles
+      const bool     mini = mode == TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED;
+      const uint64_t need = mini ? 10ull + 2ull * triangleID : 9ull + triangleID;  // header + map entry, in bytes
+      if(clusterID >= a->caps.maxPartTriangles || need > uint64_t(a->caps.maxPartTriangles - clusterID) * 24
+         || triangleID >= (mini ? 32u : 64u))
+        r.status = TC_HIT_OUT_OF_RANGE;
+      else
+      {
+        const uint8_t*       rec = P<const uint8_t>(b->partTriangles) + uint64_t(clusterID) * 24;
+        const tc_ClusterInfo hdr = *reinterpret_cast<const tc_ClusterInfo*>(rec);
+        if(mini)
+        {
+          uint16_t packed;
+          std::memcpy(&packed, rec + 8 + 2 * triangleID, 2);
+          triangleID    = packed & 0xFF;
+          subTriangleID = (packed >> 8) & 4;  // the shader's mask (rchit.glsl:161), kept as written
+          enc[0]        = 0;
+          enc[1]        = TC_TESSTABLE_COORD_MAX;
+          enc[2]        = TC_TESSTABLE_COORD_MAX << 16;
+          uint32_t f[3] = {1u + ((packed >> 12) & 1u), 1u + ((packed >> 13) & 1u), 1u + (uint32_t)(packed >> 14)};
+          cfg           = getConfig(f, enc);
+          tess          = true;
+        }
+        else
+          triangleID = rec[8 + triangleID];
+        clusterID = hdr.clusterID;
+        if(hdr.instanceID != h.instanceID || (tess && subTriangleID >= t->entries[cfgIndex(cfg)].numTriangles))
+          r.status = TC_HIT_OUT_OF_RANGE;
+      }
+    }
     else if(mode == TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED)
     {
       if(clusterID >= std::min(b->partTriangleCounter, a->caps.maxPartTriangles))
@@ -1203,7 +1304,7 @@ void tco_decode_hits(const tco_table* t, const tc_frame_args* a, const tc_hit* h
       r.vertexIndices[v] = lt[triangleID * 3 + v] + cl.firstLocalVertex;
     const f3 w    = {(1.0f - h.barycentrics[0]) - h.barycentrics[1], h.barycentrics[0], h.barycentrics[1]};
     f3       base = w;
-    if(mode == TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED)
+    if(tess)
     {
       partID = 0;
       for(int v = 0; v < 3; v++)
@@ -1257,6 +1358,382 @@ int tco_frame_build(const tco_table* t, const tc_frame_args* a, int numThreads, 
 }
 
 }  // extern "C"
+
+namespace {
+
+constexpr uint32_t kClusterInfoBytes = 8, kTessInfoBytes = 24;
+constexpr uint32_t kMiniBatchTris    = TC_2X_MINI_BATCHSIZE * TC_2X_MINI_TRIANGLES;
+constexpr uint32_t kMiniBatchVerts   = TC_2X_MINI_BATCHSIZE * TC_2X_MINI_VERTICES;
+
+// build.glsl:52-82: the two-sided part counter. The low half counts part
+// triangles from the front of partTriangles, the high half the slots taken
+// from its back by transient builds; an allocation that would make them meet
+// gets the out-of-range offset maxPartTriangles (the counter still advances).
+struct DualCounter
+{
+  uint64_t& v;
+  uint32_t  max;
+  uint32_t front(uint32_t n)
+  {
+    const uint32_t x = (uint32_t)v, y = (uint32_t)(v >> 32);
+    v += n;
+    return (uint64_t)x + y + n + 1 > max ? max : x;
+  }
+  uint32_t back(uint32_t m)
+  {
+    const uint32_t x = (uint32_t)v, y = (uint32_t)(v >> 32);
+    v += (uint64_t)m << 32;
+    return (uint64_t)x + y + m + 1 > max ? max : max - y - m;
+  }
+};
+
+// cluster_classify.comp.glsl:401-431 / 751-786
+tc_ClasBuildInfo clasBuildInfo(uint32_t mode, uint32_t partOffset, uint32_t numTriangles, uint32_t numVertices,
+                               uint32_t truncateBits, uint64_t vertexBuffer)
+{
+  tc_ClasBuildInfo bi                  = {};
+  bi.clusterID                         = (mode << 30) | partOffset;
+  bi.clusterFlags                      = 0;
+  bi.packed                            = numTriangles | (numVertices << 9) | (truncateBits << 18) | (1u << 24);
+  bi.baseGeometryIndexAndFlags         = 4u << 29;
+  bi.indexBufferStride                 = 1;
+  bi.vertexBufferStride                = 12;
+  bi.geometryIndexAndFlagsBufferStride = 0;
+  bi.opacityMicromapIndexBufferStride  = 0;
+  bi.vertexBuffer                      = vertexBuffer;
+  bi.indexBuffer                       = vertexBuffer + uint64_t(numVertices) * 12;
+  return bi;
+}
+
+inline uint32_t maxFactor(const uint32_t f[3]) { return std::max(std::max(f[0], f[1]), f[2]); }
+
+// cluster_classify.comp.glsl:254-905 with TESS_USE_1X_TRANSIENTBUILDS and / or
+// TESS_USE_2X_TRANSIENTBUILDS, in the canonical order: clusters in visible
+// order; within a cluster the full-cluster / 1X allocation, then per 32-triangle
+// chunk (the reference's subgroup) its part and split allocations followed by
+// its 2X batches in triangle order. The bytes the reference leaves unwritten
+// inside an allocation (index and map padding, unused batch vertex slots) are
+// written as zeros.
+void classifyTransient(const tco_table* t, const tc_frame_args* a, std::vector<ClassifyRec>& recs, int numThreads)
+{
+  Ctx                   c(a);
+  tc_SceneBuilding*     b    = c.b;
+  const tc_caps&        k    = a->caps;
+  const uint32_t        nvis = b->visibleClusterCounter;
+  const tc_ClusterInfo* vis  = P<const tc_ClusterInfo>(b->visibleClusters);
+  const bool            t1   = (a->flags & TC_FLAG_TRANSIENT_1X) != 0;
+  const bool            t2   = (a->flags & TC_FLAG_TRANSIENT_2X) != 0;
+  const uint32_t*       basic = P<const uint32_t>(b->basicClusterSizes);
+  DualCounter           dual{b->dualPartTriangleCounter, k.maxPartTriangles};
+  tc_BlasBuildInfo*     blas = P<tc_BlasBuildInfo>(b->blasBuildInfos);
+
+  // vertex jobs: full clusters and 1X subsets (the cluster's vertices), 2X batches
+  struct ClusterJob
+  {
+    uint32_t v, vertexOffset, partOffset, partSlots;  // partSlots 0: full cluster
+  };
+  struct MiniJob
+  {
+    uint32_t v, vertexOffset, partOffset, count;
+    uint32_t tris[TC_2X_MINI_BATCHSIZE];
+  };
+  struct TriOut
+  {
+    uint32_t cluster, tri, offset;
+    bool     split;
+  };
+  std::vector<ClusterJob> clusterJobs;
+  std::vector<MiniJob>    miniJobs;
+  std::vector<TriOut>     triOut;
+  auto accepts = [&](uint64_t vertexOffset, uint32_t vertexSize, uint32_t genOffset, uint64_t dataOffset,
+                     uint64_t dataSize, uint64_t partOffset, uint32_t partSize) {
+    return !((vertexOffset + vertexSize > k.maxGeneratedVertices) || (genOffset + 1ull > k.maxGeneratedClusters)
+             || (dataOffset + dataSize > c.maxDataBytes) || (partOffset + partSize > k.maxPartTriangles));
+  };
+
+  for(uint32_t v = 0; v < nvis; v++)
+  {
+    const tc_ClusterInfo&    ci     = vis[v];
+    const tc_RenderInstance& in     = c.inst[ci.instanceID];
+    const tc_Cluster&        cl     = P<const tc_Cluster>(in.clusters)[ci.clusterID];
+    const ClassifyRec&       r      = recs[v];
+    const uint32_t           nt     = r.numTriangles, simple = r.simple, nv = cl.numVertices;
+    const bool               isFull = simple == nt;
+    const bool               oneX   = t1 && !isFull && simple > 1;
+    // :254-437 full cluster or 1X subset
+    if(isFull || oneX)
+    {
+      if(isFull)
+        c.rb->numFullClusters += 1;
+      const uint32_t genOffset  = b->genClusterCounter++;
+      const uint64_t dataSize   = isFull ? P<const uint32_t>(in.clusterTemplateInstantiatonSizes)[ci.clusterID] : basic[simple];
+      const uint32_t vertexSize = nv + (isFull ? 0u : (simple * 3 + 11) / 12);
+      const uint32_t partSize   = isFull ? 0u : (kClusterInfoBytes + simple + kTessInfoBytes - 1) / kTessInfoBytes;
+      const uint32_t partOffset = isFull ? 0u : dual.back(partSize);
+      const uint64_t dataOffset = b->genClusterDataCounter;
+      b->genClusterDataCounter += dataSize;
+      const uint32_t vertexOffset = b->genVertexCounter;
+      b->genVertexCounter += vertexSize;
+      if(accepts(vertexOffset, vertexSize, genOffset, dataOffset, dataSize, partOffset, partSize))
+      {
+        if(isFull)
+        {
+          const uint32_t             tempOffset = b->tempInstantiateCounter++;
+          tc_TemplateInstantiateInfo ti;
+          ti.clusterIdOffset        = 0;
+          ti.geometryIndexOffset    = 0;
+          ti.clusterTemplateAddress = P<const uint64_t>(in.clusterTemplateAdresses)[ci.clusterID];
+          ti.vertexBufferAddress    = b->genVertices + uint64_t(vertexOffset) * 12;
+          ti.vertexBufferStride     = 12;
+          P<tc_TemplateInstantiateInfo>(b->tempInstantiations)[tempOffset] = ti;
+          P<uint32_t>(b->tempInstanceIDs)[tempOffset]                      = ci.instanceID;
+          P<uint64_t>(b->tempClusterAddresses)[tempOffset]                 = b->genClusterData + dataOffset;
+          if((a->flags & TC_FLAG_WRITE_FULLCLUSTERS) && b->fullClusters)
+            P<tc_ClusterInfo>(b->fullClusters)[tempOffset] = ci;
+        }
+        else
+        {
+          const uint32_t transOffset = b->transBuildCounter++;
+          P<tc_ClasBuildInfo>(b->transBuilds)[transOffset] =
+              clasBuildInfo(TC_RT_CLUSTER_MODE_1X_SUBSET_CLUSTER, partOffset, simple, nv, b->positionTruncateBitCount,
+                            b->genVertices + uint64_t(vertexOffset) * 12);
+          P<uint32_t>(b->transInstanceIDs)[transOffset]      = ci.instanceID;
+          P<uint64_t>(b->transClusterAddresses)[transOffset] = b->genClusterData + dataOffset;
+        }
+        clusterJobs.push_back({v, vertexOffset, partOffset, partSize});
+        blas[ci.instanceID].clusterReferencesCount += 1;
+        c.rb->numTotalTriangles += simple;
+      }
+    }
+    if(isFull)
+      continue;
+    // :543-905 the remaining triangles, one 32-triangle chunk at a time
+    for(uint32_t t0 = 0; t0 < nt; t0 += 32)
+    {
+      const uint32_t t1e = std::min(nt, t0 + 32);
+      uint32_t       nPart = 0, nSplit = 0;
+      uint32_t       mini[32], nMini = 0;
+      uint8_t        kind[32];  // 0 handled by the 1X subset, 1 split, 2 part, 3 mini
+      for(uint32_t tri = t0; tri < t1e; tri++)
+      {
+        const uint32_t m = maxFactor(r.factors[tri]);
+        uint8_t        kd;
+        if(oneX && m == 1)
+          kd = 0;
+        else if(m > TC_TESSTABLE_SIZE)
+          kd = 1;
+        else if(t2 && m <= 2)
+          kd = 3;
+        else
+          kd = 2;
+        kind[tri - t0] = kd;
+        nSplit += kd == 1;
+        nPart += kd == 2;
+        if(kd == 3)
+          mini[nMini++] = tri;
+      }
+      const uint32_t splitBase = (uint32_t)b->splitTriangleCounter;
+      b->splitTriangleCounter += (int32_t)nSplit;
+      const uint32_t partBase = dual.front(nPart);
+      if(nPart && partBase < k.maxPartTriangles)  // written: the front's written end
+        b->partTriangleCounter = std::max(b->partTriangleCounter, partBase + nPart);
+      uint32_t is = 0, ip = 0;
+      for(uint32_t tri = t0; tri < t1e; tri++)
+      {
+        if(kind[tri - t0] == 1)
+          triOut.push_back({v, tri, splitBase + is++, true});
+        else if(kind[tri - t0] == 2)
+          triOut.push_back({v, tri, partBase + ip++, false});
+      }
+      // :675-790 the chunk's 2X batches
+      for(uint32_t m0 = 0; m0 < nMini; m0 += TC_2X_MINI_BATCHSIZE)
+      {
+        MiniJob job = {};
+        job.v       = v;
+        job.count   = std::min(TC_2X_MINI_BATCHSIZE, nMini - m0);
+        uint32_t numBatchTris = 0;
+        for(uint32_t j = 0; j < job.count; j++)
+        {
+          job.tris[j]     = mini[m0 + j];
+          uint32_t f[3]   = {r.factors[job.tris[j]][0], r.factors[job.tris[j]][1], r.factors[job.tris[j]][2]};
+          uint32_t tv[3]  = {0, TC_TESSTABLE_COORD_MAX, TC_TESSTABLE_COORD_MAX << 16};
+          numBatchTris += t->entries[cfgIndex(getConfig(f, tv))].numTriangles;
+        }
+        const uint64_t dataSize   = basic[kMiniBatchTris];
+        const uint32_t vertexSize = kMiniBatchVerts + (kMiniBatchTris * 3 + 11) / 12;
+        const uint32_t partSize   = (kClusterInfoBytes + kMiniBatchTris * 2 + kTessInfoBytes - 1) / kTessInfoBytes;
+        const uint32_t genOffset  = b->genClusterCounter++;
+        const uint32_t partOffset = dual.back(partSize);
+        const uint64_t dataOffset = b->genClusterDataCounter;
+        b->genClusterDataCounter += dataSize;
+        const uint32_t vertexOffset = b->genVertexCounter;
+        b->genVertexCounter += vertexSize;
+        if(!accepts(vertexOffset, vertexSize, genOffset, dataOffset, dataSize, partOffset, partSize))
+          continue;
+        const uint32_t transOffset = b->transBuildCounter++;
+        P<tc_ClasBuildInfo>(b->transBuilds)[transOffset] =
+            clasBuildInfo(TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED, partOffset, numBatchTris, kMiniBatchVerts,
+                          b->positionTruncateBitCount, b->genVertices + uint64_t(vertexOffset) * 12);
+        P<uint32_t>(b->transInstanceIDs)[transOffset]      = ci.instanceID;
+        P<uint64_t>(b->transClusterAddresses)[transOffset] = b->genClusterData + dataOffset;
+        blas[ci.instanceID].clusterReferencesCount += 1;
+        c.rb->numTotalTriangles += numBatchTris;
+        job.vertexOffset = vertexOffset;
+        job.partOffset   = partOffset;
+        miniJobs.push_back(job);
+      }
+    }
+  }
+
+  uint8_t* gvb = P<uint8_t>(b->genVertices);
+  uint8_t* ptb = P<uint8_t>(b->partTriangles);
+  f3*      gv  = P<f3>(b->genVertices);
+  const bool pn = (a->flags & TC_FLAG_PN) != 0, rip = (a->flags & TC_FLAG_RIPPLE) != 0;
+
+  // full clusters and 1X subsets: the cluster's displaced vertices (:457-487),
+  // then for a subset its indices after the vertices and its triangle map
+  // after the ClusterInfo header (:489-535)
+  parallelFor(clusterJobs.size(), numThreads, [&](size_t lo, size_t hi) {
+    for(size_t j = lo; j < hi; j++)
+    {
+      const ClusterJob&             job = clusterJobs[j];
+      const tc_ClusterInfo&         ci  = vis[job.v];
+      const tc_RenderInstance&      in  = c.inst[ci.instanceID];
+      const tc_Cluster&             cl  = P<const tc_Cluster>(in.clusters)[ci.clusterID];
+      const tc_DisplacementTexture* tx  = instanceTexture(a, in);
+      for(uint32_t vert = 0; vert < cl.numVertices; vert++)
+      {
+        uint32_t vi  = cl.firstLocalVertex + vert;
+        f3       pos = ld3(in.positions, vi);
+        if(tx)
+          pos = displace(pos, ld3(in.normals, vi), P<const f2>(in.texcoords)[vi], tx, in, *c.view);
+        if(rip)
+          pos = ripple(pos, ci.instanceID, in.geoHi.w, *c.view);
+        gv[job.vertexOffset + vert] = pos;
+      }
+      if(job.partSlots == 0)
+        continue;
+      const ClassifyRec& r      = recs[job.v];
+      const uint8_t*     lt     = P<const uint8_t>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
+      uint8_t*           idx    = gvb + (uint64_t(job.vertexOffset) + cl.numVertices) * 12;
+      uint8_t*           map    = ptb + uint64_t(job.partOffset) * kTessInfoBytes;
+      std::memset(idx, 0, (size_t)((r.simple * 3 + 11) / 12) * 12);
+      std::memset(map, 0, (size_t)job.partSlots * kTessInfoBytes);
+      std::memcpy(map, &ci, kClusterInfoBytes);
+      uint32_t out = 0;
+      for(uint32_t tri = 0; tri < r.numTriangles; tri++)
+        if(maxFactor(r.factors[tri]) == 1)
+        {
+          map[kClusterInfoBytes + out] = (uint8_t)tri;
+          for(int q = 0; q < 3; q++)
+            idx[out * 3 + q] = lt[tri * 3 + q];
+          out++;
+        }
+    }
+  });
+
+  // 2X batches (:792-904): per base triangle its 3 to 6 vertices at its batch
+  // slot, its table triangles' u16 map entries and u8 indices
+  parallelFor(miniJobs.size(), numThreads, [&](size_t lo, size_t hi) {
+    for(size_t j = lo; j < hi; j++)
+    {
+      const MiniJob&                job = miniJobs[j];
+      const tc_ClusterInfo&         ci  = vis[job.v];
+      const tc_RenderInstance&      in  = c.inst[ci.instanceID];
+      const tc_Cluster&             cl  = P<const tc_Cluster>(in.clusters)[ci.clusterID];
+      const uint8_t*                lt  = P<const uint8_t>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
+      const tc_DisplacementTexture* tx  = instanceTexture(a, in);
+      const ClassifyRec&            r   = recs[job.v];
+      uint8_t*                      idx = gvb + (uint64_t(job.vertexOffset) + kMiniBatchVerts) * 12;
+      uint8_t*                      map = ptb + uint64_t(job.partOffset) * kTessInfoBytes;
+      std::memset(gvb + uint64_t(job.vertexOffset) * 12, 0,
+                  (size_t)(kMiniBatchVerts + (kMiniBatchTris * 3 + 11) / 12) * 12);
+      std::memset(map, 0, (size_t)((kClusterInfoBytes + kMiniBatchTris * 2 + kTessInfoBytes - 1) / kTessInfoBytes) * kTessInfoBytes);
+      std::memcpy(map, &ci, kClusterInfoBytes);
+      uint32_t baseTris = 0;
+      for(uint32_t rel = 0; rel < job.count; rel++)
+      {
+        const uint32_t tri  = job.tris[rel];
+        uint32_t       f[3] = {r.factors[tri][0], r.factors[tri][1], r.factors[tri][2]};
+        uint32_t       tv[3] = {0, TC_TESSTABLE_COORD_MAX, TC_TESSTABLE_COORD_MAX << 16};
+        const uint32_t cfg   = getConfig(f, tv);
+        const tc_TessTableEntry& e = t->entries[cfgIndex(cfg)];
+        f3 bb[3], bpos[3], bnrm[3];
+        f2 buv[3];
+        for(int q = 0; q < 3; q++)
+        {
+          uint32_t vi = cl.firstLocalVertex + lt[tri * 3 + q];
+          bb[q]       = decodeBary(tv[q]);
+          bpos[q]     = ld3(in.positions, vi);
+          bnrm[q]     = normalize3(ld3(in.normals, vi));
+          buv[q]      = P<const f2>(in.texcoords)[vi];
+        }
+        BasePN basePN;
+        if(pn)
+          basePN = setupPN(bpos, bnrm);
+        for(uint32_t vert = 0; vert < e.numVertices; vert++)
+        {
+          f3 w   = interp3(bb, cfgVertex(t, cfg, vert));
+          f3 pos = pn ? getPN(basePN, w) : interp3(bpos, w);
+          if(tx)
+            pos = displace(pos, interp3(bnrm, w), interp2(buv, w), tx, in, *c.view);
+          if(rip)
+            pos = ripple(pos, ci.instanceID, in.geoHi.w, *c.view);
+          gv[job.vertexOffset + rel * TC_2X_MINI_VERTICES + vert] = pos;
+        }
+        // the edge factors as computed (tess_getConfig takes them by value)
+        const uint32_t* f0            = r.factors[tri];
+        const uint32_t  packedFactors = (f0[0] - 1) | ((f0[1] - 1) << 1) | ((f0[2] - 1) << 2);
+        for(uint32_t i = 0; i < e.numTriangles; i++)
+        {
+          const uint32_t triOffset = baseTris + i;
+          const uint16_t m16       = (uint16_t)(tri | (i << 8) | (packedFactors << 12));
+          std::memcpy(map + kClusterInfoBytes + 2 * triOffset, &m16, 2);
+          uint32_t ct[3];
+          cfgTriangle(t, cfg, i, ct);
+          for(int q = 0; q < 3; q++)
+            idx[triOffset * 3 + q] = (uint8_t)(ct[q] + rel * TC_2X_MINI_VERTICES);
+        }
+        baseTris += e.numTriangles;
+      }
+    }
+  });
+
+  // part and split triangles (:608-666)
+  const uint32_t sf = clampSplitFactor(k.splitFactor);
+  parallelFor(triOut.size(), numThreads, [&](size_t lo, size_t hi) {
+    for(size_t i = lo; i < hi; i++)
+    {
+      const TriOut& o    = triOut[i];
+      ClassifyRec&  r    = recs[o.cluster];
+      uint32_t      f[3] = {r.factors[o.tri][0], r.factors[o.tri][1], r.factors[o.tri][2]};
+      tc_TessTriangleInfo info;
+      info.cluster                       = vis[o.cluster];
+      info.subTriangle.vtxEncoded[0]     = 0;
+      info.subTriangle.vtxEncoded[1]     = TC_TESSTABLE_COORD_MAX;
+      info.subTriangle.vtxEncoded[2]     = TC_TESSTABLE_COORD_MAX << 16;
+      info.subTriangle.triangleID_config = o.tri;
+      if(o.split)
+      {
+        if(o.offset >= k.maxSplitTriangles)
+          continue;
+        for(int j = 0; j < 3; j++)
+          f[j] = splitFactor1(f[j], sf);
+        info.subTriangle.triangleID_config |= getConfig(f, info.subTriangle.vtxEncoded) << 16;
+        P<tc_TessTriangleInfo>(b->splitTriangles)[o.offset] = info;
+      }
+      else
+      {
+        if(o.offset >= k.maxPartTriangles)
+          continue;
+        info.subTriangle.triangleID_config |= getConfig(f, info.subTriangle.vtxEncoded) << 16;
+        P<tc_TessTriangleInfo>(b->partTriangles)[o.offset] = info;
+      }
+    }
+  });
+}
+
+}  // namespace
 
 // ===========================================================================
 // FP64 twin and adjoint of the vertex generation

@@ -22,7 +22,8 @@ COUNTER_FIELDS = ("numRenderInstances", "visibleClusterCounter", "fullClusterCou
                   "viewPos")
 
 ARRAY_FIELDS = ("instanceStates", "visibleClusters", "splitTriangles", "partTriangles", "tempInstantiations",
-                "tempInstanceIDs", "tempClusterAddresses", "blasBuildInfos", "blasClusterAddresses", "fullClusters")
+                "tempInstanceIDs", "tempClusterAddresses", "blasBuildInfos", "blasClusterAddresses", "fullClusters",
+                "transBuilds", "transInstanceIDs", "transClusterAddresses", "transParts", "transIndices")
 
 
 def _first_diff(a: np.ndarray, b: np.ndarray):

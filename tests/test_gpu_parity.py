@@ -334,3 +334,69 @@ def test_pn_ripple_entry_point_matches_frame(oracle):
     assert len(want["genVertices"]) > 1000
     assert got["genVertices"].tobytes() == want["genVertices"].tobytes()
     pipe.close()
+
+
+TRANSIENT = L.FLAG_TRANSIENT_1X | L.FLAG_TRANSIENT_2X
+
+
+@pytest.mark.parametrize("mode", ["batched", "plain", "graph"])
+def test_transient_builds_bit_exact(oracle, mode):
+    """1X subset and 2X batch transient builds (cluster_classify.comp.glsl:
+    254-905): ClasBuildInfos, instance IDs, CLAS addresses, the back slots of
+    partTriangles, the index bytes, the two-sided counter and every other
+    output bit-exact; positions within the vertex tolerance. Each flag alone
+    and both, on the icosphere and the culled batched scene, and with PN and
+    the ripple."""
+    ico = S.scene_icosphere()
+    sc = S.scene_batched(num_instances=24, map_size=128)
+    cases = [(ico, S.camera_icosphere(), None, FLAGS | L.FLAG_TRANSIENT_1X),
+             (ico, S.camera_icosphere(), None, FLAGS | L.FLAG_TRANSIENT_2X),
+             (ico, S.camera_icosphere(), None, FLAGS | TRANSIENT),
+             (sc, S.camera_orbit(0), S.camera_orbit(59), FLAGS | TRANSIENT),
+             (sc, _ripple_constants(S.camera_orbit(5)), S.camera_orbit(4), FLAGS | TRANSIENT | L.FLAG_PN | L.FLAG_RIPPLE)]
+    for scene, cam, last, flags in cases:
+        pipe, out, ref, _ = run_both(oracle, scene, cam, small_caps(), flags=flags, mode=mode, cam_last=last)
+        assert len(ref["transBuilds"]) > 10
+        assert pipe.device_errors() == 0
+        assert_same(out, ref, f"transient flags={flags} {mode}", vertex_tol=vertex_tolerance(scene))
+        pipe.close()
+
+
+@pytest.mark.parametrize("which", ["parts", "clusters", "vertices"])
+def test_transient_builds_capacity_overflow(oracle, which):
+    """Capacity overflow with transient builds: the two-sided part counter
+    running out (front chunks and back slots rejected as wholes), generated
+    clusters and vertices running out; outputs equal the oracle's."""
+    sc = S.scene_batched(num_instances=24, map_size=128)
+    kw = {"parts": {"maxPartTriangles": 3000}, "clusters": {"maxGeneratedClusters": 4000},
+          "vertices": {"maxGeneratedVertices": 150000}}[which]
+    pipe, out, ref, _ = run_both(oracle, sc, S.camera_orbit(0), small_caps(**kw), flags=FLAGS | TRANSIENT,
+                                 cam_last=S.camera_orbit(59))
+    assert pipe.device_errors() == 0
+    assert_same(out, ref, f"transient overflow {which}", vertex_tol=vertex_tolerance(sc))
+    pipe.close()
+
+
+def test_transient_hit_decode_matches_oracle(oracle):
+    """tc_decode_hits with 1X subset and 2X batch hits (rchit.glsl:150-180)
+    equals the oracle's restatement field for field."""
+    from vk_tessellated_clusters_gb300.hits import sample_hits
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    sc = S.scene_batched(num_instances=24, map_size=128)
+    flags = FLAGS | TRANSIENT
+    for visualize in (0, L.VISUALIZE_TRIANGLES):
+        fc, last = S.frame_constants(S.camera_orbit(0)), S.frame_constants(S.camera_orbit(59))
+        fc["visualize"] = visualize
+        ref_state, _ = oracle.frame(sc, fc, small_caps(), flags, camera_last=last)
+        pipe = TessellationPipeline(sc, small_caps(), flags)
+        pipe.set_cameras(fc, last)
+        pipe.build("graph")
+        out = pipe.outputs()
+        hits = sample_hits(out, sc, pipe.entries, 20000, seed=5, bad=200)
+        assert ((hits["clusterID"][:20000] >> 30) >= 2).sum() > 1000
+        got = pipe.decode_hits(hits)
+        want = oracle.decode_hits(ref_state, hits)
+        assert pipe.device_errors() == 0
+        assert (got["status"][:20000] == L.HIT_OK).all()
+        assert got.tobytes() == want.tobytes()
+        pipe.close()

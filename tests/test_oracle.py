@@ -331,3 +331,85 @@ def test_pn_and_ripple_restatement(oracle):
             assert out[f].tobytes() == base[f].tobytes(), (amp, f)
         d = np.abs(out["genVertices"].astype(np.float64) - base["genVertices"]).max()
         assert (d == 0) if amp == 0 else (0 < d <= amp * size * 1.001)
+
+
+@pytest.mark.parametrize("which", ["icosphere", "batched"])
+def test_transient_builds_restatement(oracle, which):
+    """cluster_classify with 1X and 2X transient builds
+    (cluster_classify.comp.glsl:254-905) against the same frame without them:
+    the tessellated triangle total is unchanged; every 2X batch's vertices
+    equal the part instantiation's vertices of the same base triangle; a 1X
+    subset lists the cluster's untessellated triangles with their local
+    indices; ClasBuildInfo fields follow the shader; BLAS lists hold every
+    template instantiation, then the transient builds."""
+    if which == "icosphere":
+        sc, cam, last = S.scene_icosphere(), S.camera_icosphere(), None
+    else:
+        sc, cam, last = S.scene_batched(num_instances=24, map_size=64), S.camera_orbit(0), S.camera_orbit(59)
+    caps = L.default_caps(visible_bits=16, part_bits=18, split_bits=14, vertex_bits=21, megs=256)
+    flags = L.FLAG_CULLING | L.FLAG_WRITE_FULLCLUSTERS
+    base = oracle.frame(sc, cam, caps, flags, camera_last=last)[0].outputs(oracle.entries)
+    st, _ = oracle.frame(sc, cam, caps, flags | L.FLAG_TRANSIENT_1X | L.FLAG_TRANSIENT_2X, camera_last=last)
+    out = st.outputs(oracle.entries)
+    rb, b = out["readback"], out["build"]
+    assert int(rb["numTotalTriangles"]) == int(base["readback"]["numTotalTriangles"])
+    tb = out["transBuilds"]
+    modes = tb["clusterID"] >> 30
+    assert (modes == L.RT_CLUSTER_MODE_1X_SUBSET_CLUSTER).any() and (modes == L.RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED).any()
+    assert int(rb["numTransBuilds"]) == len(tb) == int(b["transBuildCounter"])
+    assert int(rb["numBlasClusters"]) == len(tb) + len(out["tempInstantiations"])
+    assert int(b["dualPartTriangleCounter"]) & 0xFFFFFFFF == int(b["partTriangleCounter"])
+    assert int(rb["numTransPartTriangles"]) == int(b["dualPartTriangleCounter"]) >> 32
+    assert (tb["baseGeometryIndexAndFlags"] == 4 << 29).all() and (tb["indexBufferStride"] == 1).all()
+    assert (tb["vertexBufferStride"] == 12).all() and ((tb["packed"] >> 24) == 1).all()
+    nv = (tb["packed"] >> 9) & 0x1FF
+    assert (tb["indexBuffer"] == tb["vertexBuffer"] + nv * 12).all()
+    # the base frame's part instantiations by (instance, cluster, triangle)
+    ti, parts, gvb = base["tempInstantiations"], base["partTriangles"], base["genVertices"]
+    part_verts = {}
+    for j in np.flatnonzero((ti["clusterIdOffset"] >> 30) == L.RT_CLUSTER_MODE_SINGLE_TESSELLATED):
+        p = parts[int(ti[j]["clusterIdOffset"]) & 0x3FFFFFFF]
+        cfg = (int(p["triangleID_config"]) >> 16) & 0x7FFF
+        key = (int(p["instanceID"]), int(p["clusterID"]), int(p["triangleID_config"]) & 0xFFFF)
+        v0 = int(ti[j]["vertexBufferAddress"]) // 12
+        part_verts[key] = gvb[v0:v0 + int(oracle.entries[cfg]["numVertices"])]
+    gv, raw, idx = out["genVertices"], out["transParts"], out["transIndices"]
+    ppos = ipos = 0
+    checked = 0
+    for r, inst in zip(tb, out["transInstanceIDs"]):
+        mode, ntri = int(r["clusterID"]) >> 30, int(r["packed"]) & 0x1FF
+        slots = 3 if mode == L.RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED else (8 + ntri + 23) // 24
+        rec = raw[ppos:ppos + 24 * slots]
+        ppos += 24 * slots
+        nidx = 96 if mode == L.RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED else (ntri * 3 + 11) // 12 * 12
+        ib = idx[ipos:ipos + nidx]
+        ipos += nidx
+        hdr = rec[:8].view(np.uint32)
+        assert int(hdr[0]) == int(inst)
+        geo = sc.geometries[sc.instances[int(inst)].geometry]
+        cl = geo.clusters[int(hdr[1])]
+        lt = geo.local_triangles[int(cl["firstLocalTriangle"]):]
+        v0 = int(r["vertexBuffer"]) // 12
+        if mode == L.RT_CLUSTER_MODE_1X_SUBSET_CLUSTER:
+            tris = rec[8:8 + ntri]
+            assert (np.diff(tris.astype(int)) > 0).all() and ntri > 1
+            assert (ib[:3 * ntri].reshape(-1, 3) == lt.reshape(-1, 3)[tris]).all() and not ib[3 * ntri:].any()
+            continue
+        m16 = rec[8:8 + 2 * 32].view(np.uint16)[:ntri]
+        assert not rec[8 + 2 * ntri:].any() and not ib[3 * ntri:].any()
+        rels = {}
+        for e in m16:
+            rels.setdefault(int(e) & 0xFF, len(rels))
+        for tri, rel in rels.items():
+            want = part_verts[(int(inst), int(hdr[1]), tri)]
+            got = gv[v0 + 6 * rel:v0 + 6 * rel + len(want)]
+            assert got.tobytes() == want.tobytes()
+            checked += 1
+    assert checked > 100 and ppos == len(raw) and ipos == len(idx)
+    # BLAS lists: the transient builds follow the instance's template instantiations
+    bi, lists = out["blasBuildInfos"], out["blasClusterAddresses"]
+    for i in np.unique(out["transInstanceIDs"])[:8]:
+        start = int(bi[i]["clusterReferences"]) // 8
+        n = int(bi[i]["clusterReferencesCount"])
+        mine = out["transClusterAddresses"][out["transInstanceIDs"] == i]
+        assert (lists[start + n - len(mine):start + n] == mine).all()

@@ -143,7 +143,7 @@ Plan make_plan(const tc_context_desc& d)
   p.slotInstances   = add(ceil_div(d.maxInstances, kInstanceTile), 1);
   p.slotCull        = add(ceil_div(d.maxTotalClusters, kCullTile), 1);
   p.classifyCap     = (u32)std::max<u64>(1, std::min<u64>(k.maxVisibleClusters, d.maxTotalClusters));
-  p.slotClassify    = add(classify_max_blocks(p.classifyCap), 3);  // the range sums (zeroed with the frame)
+  p.slotClassify    = add(classify_max_blocks(p.classifyCap), 4);  // the range sums (zeroed with the frame)
   p.slotSplit0      = add(ceil_div(k.maxSplitTriangles, kSplitMinItems), 2);
   for(u32 i = 1; i < passes; i++)
     add(ceil_div(k.maxSplitTriangles, kSplitMinItems), 2);
@@ -160,23 +160,23 @@ Plan make_plan(const tc_context_desc& d)
     off           = align_up(off + kCtrlBytes, 256);
   }
   p.segStride = std::max(1u, d.maxInstances);
-  p.segRows   = kMaxRuns + 1;
+  p.segRows   = kMaxRuns + 2;  // the instantiation runs, then the transient builds
   p.segOffset = off;
   off         = align_up(off + (size_t)p.segStride * p.segRows * 4 * 2, 256);
   p.frameBytes = off;
   p.runOffset  = off;
-  off          = align_up(off + 4 * (kMaxRuns + 2), 256);
+  off          = align_up(off + 4 * kRunStartsSize, 256);
   p.instOffset = off;
   off          = align_up(off + 4 * ((size_t)d.maxInstances + 1), 256);
   p.errOffset  = off;
   off          = align_up(off + 4, 256);
   // per-item scratch (written before it is read every launch; never zeroed)
   p.clsCountsOffset   = off;
-  off                 = align_up(off + (size_t)p.classifyCap * 8, 256);
+  off                 = align_up(off + (size_t)p.classifyCap * 16, 256);  // uint2, or uint4 with transient builds
   p.clsTriWordsOffset = off;
   off                 = align_up(off + (size_t)p.classifyCap * TC_MAX_CLUSTER_TRIANGLES * 4, 256);
   p.clsBlockSumsOffset = off;  // the counter bases
-  off = align_up(off + sizeof(ClusterOffsets), 256);
+  off = align_up(off + sizeof(ClusterOffsets) + sizeof(TransBases), 256);
   p.clsFullRecsOffset = off;  // per full cluster, then the slot range
   off = align_up(off + (size_t)p.classifyCap * 8 + 8, 256);
   p.partVertexOffset  = off;
@@ -208,6 +208,9 @@ tc_status validate(const tc_context* ctx, const tc_frame_args* a)
   if(!caps_fit(a->caps, ctx->desc.caps))
     return TC_ERR_CAPACITY;
   if(a->caps.splitFactor < 2 || a->caps.splitFactor > TC_TESSTABLE_SIZE)
+    return TC_ERR_INVALID_ARG;
+  // transient builds are ray-tracing semantics (shaderio.h:140-141)
+  if((a->flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X)) && (a->flags & TC_FLAG_RASTER_CULL))
     return TC_ERR_INVALID_ARG;
   return TC_OK;
 }
@@ -930,7 +933,8 @@ tc_status tc_instantiate_backward(tc_context* ctx, const tc_frame_args* a, uint6
     return st;
   if(!gradVertices || !gradTargets || (a->numTextures && !gradTexels))
     return TC_ERR_INVALID_ARG;
-  if(a->flags & (TC_FLAG_PN | TC_FLAG_RIPPLE))  // the adjoint covers the linear, displaced path only
+  // the adjoint covers the linear, displaced path of template instantiations only
+  if(a->flags & (TC_FLAG_PN | TC_FLAG_RIPPLE | TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X))
     return TC_ERR_INVALID_ARG;
   if(!(a->flags & TC_FLAG_WRITE_FULLCLUSTERS))
     return TC_ERR_INVALID_ARG;
@@ -948,7 +952,8 @@ tc_status tc_generate_vertices(tc_context* ctx, const tc_frame_args* a, void* st
   tc_status st = validate(ctx, a);
   if(st != TC_OK)
     return st;
-  if(!(a->flags & TC_FLAG_WRITE_FULLCLUSTERS) || (a->flags & (TC_FLAG_PN | TC_FLAG_RIPPLE)))
+  if(!(a->flags & TC_FLAG_WRITE_FULLCLUSTERS)
+     || (a->flags & (TC_FLAG_PN | TC_FLAG_RIPPLE | TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X)))
     return TC_ERR_INVALID_ARG;
   StageCtx c = base_ctx(ctx, a);
   TC_CHECK_CUDA(launch_generate_vertices(c, ctx->numSMs * 8, reinterpret_cast<cudaStream_t>(stream)));

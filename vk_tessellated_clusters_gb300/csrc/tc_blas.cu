@@ -6,7 +6,8 @@
 // in instance order (block scan + look-back), as a serial loop would assign.
 //
 // blas_clusters_insert (shaders/blas_clusters_insert.comp.glsl:97-136): every
-// template instantiation appends its CLAS address to its instance's list. The
+// template instantiation (then every transient build) appends its CLAS
+// address to its instance's list. The
 // reference's atomicAdd per insertion gives an arbitrary order within a list;
 // here the order is the instantiation order (a stable scatter). The
 // instantiation list is a concatenation of runs (full clusters, then the part
@@ -79,11 +80,17 @@ __global__ void k_blas_setup_insertion(StageCtx c)
   }
 }
 
-// Temp-instantiation run boundaries: [0, F) full clusters, then part runs.
+// Run boundaries over the insertion list: template instantiations [0, F)
+// full clusters, then part runs; with transient builds one more run, the
+// transient builds (list positions temps + j), inserted after every template
+// instantiation like the reference's second dispatch
+// (blas_clusters_insert.comp.glsl:99-121).
 struct Runs
 {
-  u32 bound[kMaxRuns + 3];
+  u32 bound[kMaxRuns + 4];
   u32 count;
+  u32 temps;  // list positions below hold template instantiations
+  u32 total;
 };
 
 __device__ inline void load_runs(const StageCtx& c, Runs& r)
@@ -99,6 +106,21 @@ __device__ inline void load_runs(const StageCtx& c, Runs& r)
   r.count = nparts + 1;
   // the last run always ends at the instantiation count
   r.bound[r.count] = temps;
+  r.temps          = temps;
+  r.total          = temps;
+  if(c.flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X))
+  {
+    r.total = temps + b->transBuildCounter;
+    r.count += 1;
+    r.bound[r.count] = r.total;
+  }
+}
+
+// list position j: its instance, CLAS address and size
+__device__ __forceinline__ u32 entry_instance(const tc_SceneBuilding* b, const Runs& r, u32 j)
+{
+  return j < r.temps ? reinterpret_cast<const u32*>(b->tempInstanceIDs)[j]
+                     : reinterpret_cast<const u32*>(b->transInstanceIDs)[j - r.temps];
 }
 
 __device__ __forceinline__ u32 run_of(const Runs& r, u32 j)
@@ -126,8 +148,7 @@ __global__ void __launch_bounds__(kInsertBlock) k_blas_segments(StageCtx c, u32*
     load_runs(c, s_runs);
   __syncthreads();
   const tc_SceneBuilding* b     = c.build;
-  const u32*              ids   = reinterpret_cast<const u32*>(b->tempInstanceIDs);
-  const u32               temps = b->tempInstantiateCounter;
+  const u32               temps = s_runs.total;
   for(u32 t0 = blockIdx.x * kInsertTile; t0 < temps; t0 += gridDim.x * kInsertTile)
   {
     u32 prev[kInsertItems], cur[kInsertItems], next[kInsertItems];
@@ -135,9 +156,9 @@ __global__ void __launch_bounds__(kInsertBlock) k_blas_segments(StageCtx c, u32*
     for(u32 k = 0; k < kInsertItems; k++)
     {
       const u32 j = t0 + threadIdx.x + k * kInsertBlock;
-      cur[k]      = j < temps ? ids[j] : 0u;
-      prev[k]     = j < temps && j > 0 ? ids[j - 1] : 0u;
-      next[k]     = j + 1 < temps ? ids[j + 1] : 0u;
+      cur[k]      = j < temps ? entry_instance(b, s_runs, j) : 0u;
+      prev[k]     = j < temps && j > 0 ? entry_instance(b, s_runs, j - 1) : 0u;
+      next[k]     = j + 1 < temps ? entry_instance(b, s_runs, j + 1) : 0u;
     }
 #pragma unroll
     for(u32 k = 0; k < kInsertItems; k++)
@@ -172,10 +193,9 @@ __global__ void __launch_bounds__(kInsertBlock) k_blas_scatter(StageCtx c, const
   __syncthreads();
   const tc_SceneBuilding* b     = c.build;
   tc_BlasBuildInfo*       infos = reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos);
-  const u32*              ids   = reinterpret_cast<const u32*>(b->tempInstanceIDs);
-  const u64*              addrs = reinterpret_cast<const u64*>(b->tempClusterAddresses);
-  const u32*              csz   = reinterpret_cast<const u32*>(b->tempClusterSizes);
-  const u32               temps = b->tempInstantiateCounter;
+  const u32*              tcsz  = reinterpret_cast<const u32*>(b->tempClusterSizes);
+  const u32*              rcsz  = reinterpret_cast<const u32*>(b->transClusterSizes);
+  const u32               temps = s_runs.total;
   u64                     statData = 0;
   for(u32 t0 = blockIdx.x * kInsertTile; t0 < temps; t0 += gridDim.x * kInsertTile)
   {
@@ -184,10 +204,14 @@ __global__ void __launch_bounds__(kInsertBlock) k_blas_scatter(StageCtx c, const
 #pragma unroll
     for(u32 k = 0; k < kInsertItems; k++)
     {
-      const u32 j = t0 + threadIdx.x + k * kInsertBlock;
-      inst[k]     = j < temps ? ids[j] : ~0u;
-      addr[k]     = j < temps ? addrs[j] : 0ull;
-      size[k]     = csz && j < temps ? csz[j] : 0u;
+      const u32  j     = t0 + threadIdx.x + k * kInsertBlock;
+      const bool tmp   = j < s_runs.temps;
+      const u32  jj    = tmp ? j : j - s_runs.temps;
+      const u64* addrs = reinterpret_cast<const u64*>(tmp ? b->tempClusterAddresses : b->transClusterAddresses);
+      const u32* csz   = tmp ? tcsz : rcsz;
+      inst[k]          = j < temps ? entry_instance(b, s_runs, j) : ~0u;
+      addr[k]          = j < temps ? addrs[jj] : 0ull;
+      size[k]          = csz && j < temps ? csz[jj] : 0u;
     }
 #pragma unroll
     for(u32 k = 0; k < kInsertItems; k++)

@@ -1,7 +1,10 @@
 // tc_classify.cu — cluster_classify: per-triangle edge segment counts and the
 // full / part / split classification of every visible cluster.
 //
-// shaders/cluster_classify.comp.glsl:150-666 (RT target, plain path).
+// shaders/cluster_classify.comp.glsl:150-666 (RT target, plain path), and with
+// TC_FLAG_TRANSIENT_1X / _2X :254-905 (transient CLAS builds of untessellated
+// triangles and of 2X batches) through a count variant and a write kernel of
+// their own.
 //
 // GB300 mapping, three launches per stage, none with a cross-block wait. Block
 // b of the write grid owns the contiguous range of visible clusters
@@ -244,6 +247,44 @@ __device__ inline void block_scan5(u64 (&v)[kNumCounters], u64 (&tot)[kNumCounte
   __syncthreads();
 }
 
+// block-wide exclusive scan of N values per thread (totals in tot)
+template <int N>
+__device__ inline void block_scan_n(u64 (&v)[N], u64 (&tot)[N], u64 (*s_warp)[N])
+{
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  u64       inc[N];
+#pragma unroll
+  for(int q = 0; q < N; q++)
+  {
+    inc[q] = warp_inclusive<u64>(v[q], lane);
+    if(lane == 31)
+      s_warp[warp][q] = inc[q];
+  }
+  __syncthreads();
+  if(warp == 0)
+  {
+#pragma unroll
+    for(int q = 0; q < N; q++)
+    {
+      u64 w = lane < nw ? s_warp[lane][q] : 0;
+      u64 s = warp_inclusive<u64>(w, lane);
+      __syncwarp();
+      if(lane < nw)
+        s_warp[lane][q] = s - w;
+      if(lane == 31)
+        s_warp[32][q] = s;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for(int q = 0; q < N; q++)
+  {
+    tot[q] = s_warp[32][q];
+    v[q]   = s_warp[warp][q] + inc[q] - v[q];
+  }
+  __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // count
 // ---------------------------------------------------------------------------
@@ -273,10 +314,111 @@ __device__ inline void block_prefix(const ClassifyScratch& cs, u64 (&pre)[kNumCo
   pre[kCntData]           = b0.data + tot[kCntData];
 }
 
+// ---------------------------------------------------------------------------
+// transient builds (TC_FLAG_TRANSIENT_1X / _2X)
+// ---------------------------------------------------------------------------
+
+// per-triangle word bits beyond config | rotation << 16 | split << 18
+constexpr u32 kWordMini        = 1u << 19;  // packed into a 2X batch
+constexpr u32 kWordSubset      = 1u << 20;  // in the cluster's 1X subset
+constexpr u32 kWordFactorShift = 21;        // edge factors - 1 (3 bits) of a triangle with factors <= 2
+
+constexpr u32 kClusterInfoBytes = 8, kTessInfoBytes = 24;
+constexpr u32 kMiniBatch        = TC_2X_MINI_BATCHSIZE;
+constexpr u32 kMiniBatchTris    = TC_2X_MINI_BATCHSIZE * TC_2X_MINI_TRIANGLES;
+constexpr u32 kMiniBatchVerts   = TC_2X_MINI_BATCHSIZE * TC_2X_MINI_VERTICES;
+constexpr u32 kMiniVertexSize   = kMiniBatchVerts + (kMiniBatchTris * 3 + 11) / 12;  // vertices, then index bytes
+constexpr u32 kMiniPartSlots    = (kClusterInfoBytes + kMiniBatchTris * 2 + kTessInfoBytes - 1) / kTessInfoBytes;
+__device__ __forceinline__ u32 subset_vertex_size(u32 nv, u32 simple) { return nv + (simple * 3 + 11) / 12; }
+__device__ __forceinline__ u32 subset_part_slots(u32 simple)
+{
+  return (kClusterInfoBytes + simple + kTessInfoBytes - 1) / kTessInfoBytes;
+}
+
+// per-cluster counts with transient builds (16 bytes):
+// x = parts | splits << 7 | generated clusters << 14 | transient builds << 19 | back slots << 23 | full << 28 | 1X << 29
+// y = vertices | simple triangles << 10 | numVertices << 17 | numTriangles << 24, z = CLAS bytes
+__device__ __forceinline__ u32 t_parts(uint4 r) { return r.x & 0x7F; }
+__device__ __forceinline__ u32 t_splits(uint4 r) { return (r.x >> 7) & 0x7F; }
+__device__ __forceinline__ u32 t_gen(uint4 r) { return (r.x >> 14) & 0x1F; }
+__device__ __forceinline__ u32 t_trans(uint4 r) { return (r.x >> 19) & 0xF; }
+__device__ __forceinline__ u32 t_back(uint4 r) { return (r.x >> 23) & 0x1F; }
+__device__ __forceinline__ bool t_full(uint4 r) { return (r.x >> 28) & 1; }
+__device__ __forceinline__ bool t_subset(uint4 r) { return (r.x >> 29) & 1; }
+__device__ __forceinline__ u32 t_verts(uint4 r) { return r.y & 0x3FF; }
+__device__ __forceinline__ u32 t_simple(uint4 r) { return (r.y >> 10) & 0x7F; }
+__device__ __forceinline__ u32 t_nv(uint4 r) { return (r.y >> 17) & 0x7F; }
+__device__ __forceinline__ u32 t_nt(uint4 r) { return (r.y >> 24) & 0x7F; }
+
+// cluster_classify.comp.glsl:254-343 and 543-790, counting only: which
+// triangles go to the 1X subset, to parts, to splits and to 2X batches, and
+// what the cluster takes from every counter (each allocation counts whether or
+// not it will fit, like the reference's atomics). m0/m1, w0/w1: the max factor
+// and word of triangles lane and lane + 32.
+__device__ __forceinline__ void count_transient(const StageCtx& c, const ClassifyScratch& cs, u32 v, u32 perRange, u32 nv,
+                                             u32 nt, u32 simple, u32 m0, u32 m1, u32 w0, u32 w1, u32 templateSize)
+{
+  const u32  lane   = threadIdx.x & 31;
+  const bool full   = simple == nt;
+  const bool subset = (c.flags & TC_FLAG_TRANSIENT_1X) && !full && simple > 1;
+  const bool mini2x = (c.flags & TC_FLAG_TRANSIENT_2X) != 0;
+  const u32* basic  = reinterpret_cast<const u32*>(c.build->basicClusterSizes);
+  u32        parts = 0, splits = 0, batches = 0;
+  if(!full)
+  {
+    auto mark = [&](u32 m, u32& w) {  // :573-590
+      if(subset && m == 1)
+        w |= kWordSubset;
+      else if(m <= TC_TESSTABLE_SIZE && mini2x && m <= 2)
+        w |= kWordMini;
+    };
+    if(lane < nt)
+      mark(m0, w0);
+    if(lane + 32 < nt)
+      mark(m1, w1);
+    const bool v0 = lane < nt, v1 = lane + 32 < nt;
+    parts  = __popc(__ballot_sync(0xFFFFFFFFu, v0 && (w0 & (kWordMini | kWordSubset | (1u << 18))) == 0))
+             + __popc(__ballot_sync(0xFFFFFFFFu, v1 && (w1 & (kWordMini | kWordSubset | (1u << 18))) == 0));
+    splits = __popc(__ballot_sync(0xFFFFFFFFu, v0 && (w0 & (1u << 18)))) + __popc(__ballot_sync(0xFFFFFFFFu, v1 && (w1 & (1u << 18))));
+    const u32 mini0 = __popc(__ballot_sync(0xFFFFFFFFu, v0 && (w0 & kWordMini)));
+    const u32 mini1 = __popc(__ballot_sync(0xFFFFFFFFu, v1 && (w1 & kWordMini)));
+    batches         = (mini0 + kMiniBatch - 1) / kMiniBatch + (mini1 + kMiniBatch - 1) / kMiniBatch;
+    u32* tw         = cs.triWords + (u64)v * TC_MAX_CLUSTER_TRIANGLES;
+    if(v0)
+      tw[lane] = w0;
+    if(v1)
+      tw[lane + 32] = w1;
+  }
+  if(lane != 0)
+    return;
+  const u32 one   = (full || subset) ? 1u : 0u;
+  const u32 gen   = one + batches, trans = (subset ? 1u : 0u) + batches;
+  const u32 verts = (full ? nv : (subset ? subset_vertex_size(nv, simple) : 0u)) + kMiniVertexSize * batches;
+  const u32 back  = (subset ? subset_part_slots(simple) : 0u) + kMiniPartSlots * batches;
+  u64       data  = full ? (u64)templateSize : (subset ? (u64)basic[simple] : 0ull);
+  if(batches)
+    data += (u64)basic[kMiniBatchTris] * batches;
+  reinterpret_cast<uint4*>(cs.counts)[v] =
+      make_uint4(parts | (splits << 7) | (gen << 14) | (trans << 19) | (back << 23) | ((full ? 1u : 0u) << 28)
+                     | ((subset ? 1u : 0u) << 29),
+                 verts | (simple << 10) | (nv << 17) | (nt << 24), (u32)data, 0u);
+  RangeSums& rs = cs.rangeSums[v / perRange];
+  if(parts | splits)
+    atomicAdd(&rs.partsSplits, (unsigned long long)parts | ((unsigned long long)splits << 32));
+  if(gen)
+  {
+    atomicAdd(&rs.fullVerts, (unsigned long long)gen | ((unsigned long long)verts << 32));
+    if(data)
+      atomicAdd(&rs.data, (unsigned long long)data);
+  }
+  if(trans)
+    atomicAdd(&rs.backTrans, (unsigned long long)back | ((unsigned long long)trans << 32));
+}
+
 // MinBlocks: resident 256-thread blocks per SM the registers are sized for
 // (4: 64 registers, 6: 40, 8: 32); more resident warps hide more of the
 // dependent-load latency per cluster at the cost of some spills.
-template <int MinBlocks>
+template <int MinBlocks, bool Trans = false>
 __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c, ClassifyScratch cs)
 {
   stage_prologue();
@@ -299,8 +441,19 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c
   const bool              culling = (c.flags & TC_FLAG_CULLING) != 0;
   const u32               sf      = clamp_split_factor(c.caps.splitFactor);
   if(blockIdx.x == 0 && threadIdx.x == 0)  // the offsets continue from the counters' current values
-    *cs.bases = {b->partTriangleCounter, (u32)b->splitTriangleCounter, b->genClusterCounter, b->genVertexCounter,
-                 b->genClusterDataCounter};
+  {
+    if constexpr(Trans)
+    {
+      // parts from the front of the two-sided counter (build.glsl:52-82)
+      *cs.bases = {(u32)b->dualPartTriangleCounter, (u32)b->splitTriangleCounter, b->genClusterCounter,
+                   b->genVertexCounter, b->genClusterDataCounter};
+      *reinterpret_cast<TransBases*>(cs.bases + 1) = {(u32)(b->dualPartTriangleCounter >> 32), b->transBuildCounter,
+                                                      b->tempInstantiateCounter, 0u};
+    }
+    else
+      *cs.bases = {b->partTriangleCounter, (u32)b->splitTriangleCounter, b->genClusterCounter, b->genVertexCounter,
+                   b->genClusterDataCounter};
+  }
   // the write launch's block ranges, which collect the counts' sums
   const u32 perRange = (n + cs.writeBlocks - 1) / cs.writeBlocks;
 
@@ -381,6 +534,9 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c
                                                 d2.x, d0.y, d1.y, d2.y, rNear, fp);
           mOut           = max(max(f.x, f.y), f.z);
           wOut           = classify_triangle(f, sf);
+          if constexpr(Trans)  // factors of a 2X candidate, for its triangle map (cluster_classify.comp.glsl:817)
+            if(mOut <= 2)
+              wOut |= ((f.x - 1) | ((f.y - 1) << 1) | ((f.z - 1) << 2)) << kWordFactorShift;
         };
         if(lane < nt)
           classify(ia, m0, w0);
@@ -391,6 +547,11 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c
         __syncwarp();  // s_vert is reused by the next cluster
       }
       const bool full  = simple == nt;
+      if constexpr(Trans)
+      {
+        count_transient(c, cs, v, perRange, nv, nt, simple, m0, m1, w0, w1, __shfl_sync(0xFFFFFFFFu, hData, jj));
+        continue;
+      }
       u32        parts = 0, splits = 0;
       if(!full)
       {
@@ -484,10 +645,11 @@ __device__ __forceinline__ void full_steps(const FullRecord* rec, bool owner, u3
     const u32 ri     = before - 1 + __popc(inside & ((2u << lane) - 2u));
     const u32 rs     = __shfl_sync(0xFFFFFFFFu, rStart, ri & 31);
     const u32 jj     = base + lane;
-    if(jj < rEnd)
+    const FullRecord& fr = rec[ri];
+    // (transient builds leave index bytes and 2X batches between the ranges)
+    if(jj < rEnd && jj - rs < fr.nv)
     {
-      const FullRecord& fr = rec[ri];
-      const u32         vi = fr.first + (jj - rs);
+      const u32 vi = fr.first + (jj - rs);
       f3                p  = ldg3(fr.pos, vi);
       if(Kind != kAffineFlat)
         p = full_vertex_k<Kind>(p, ldg3(fr.nrm, vi), ldg2(fr.uvs, vi), fr.map, fr.scale, fr.offset);
@@ -733,6 +895,446 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c
   }
 }
 
+// ---------------------------------------------------------------------------
+// write, with transient builds
+// ---------------------------------------------------------------------------
+
+enum : int
+{
+  kTFront = 0,
+  kTSplit,
+  kTGen,
+  kTVert,
+  kTData,
+  kTBack,
+  kTTrans,
+  kTNum
+};
+
+// a cluster's offsets into every counter (exclusive, in the canonical order)
+struct TransOffsets
+{
+  u32 front, split, gen, vert, back, trans;
+  u64 data;
+};
+
+// build.glsl:52-66: slots from the back of partTriangles; maxPartTriangles
+// when the two ends would meet (the counter advances either way)
+__device__ __forceinline__ u32 back_alloc(u32 x, u32& y, u32 m, u32 maxParts)
+{
+  const u32 off = ((u64)x + y + m + 1 > maxParts) ? maxParts : maxParts - y - m;
+  y += m;
+  return off;
+}
+
+// cluster_classify.comp.glsl:401-431 / 751-786
+__device__ __forceinline__ void store_clas_build(tc_ClasBuildInfo* dst, u32 mode, u32 partOffset, u32 numTriangles,
+                                                 u32 numVertices, u32 truncateBits, u64 vertexBuffer)
+{
+  uint4* d = reinterpret_cast<uint4*>(dst);
+  d[0]     = make_uint4((mode << 30) | partOffset, 0u, numTriangles | (numVertices << 9) | (truncateBits << 18) | (1u << 24),
+                        4u << 29);
+  d[1]     = make_uint4(1u | (12u << 16), 0u, (u32)(vertexBuffer + (u64)numVertices * 12), (u32)((vertexBuffer + (u64)numVertices * 12) >> 32));
+  d[2]     = make_uint4((u32)vertexBuffer, (u32)(vertexBuffer >> 32), 0u, 0u);
+  d[3]     = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// cluster_classify.comp.glsl:810-903: one base triangle of a 2X batch (its
+// word's config and corner rotation): its 3 to 6 vertices at its batch slot,
+// then per table triangle the u16 map entry and three u8 indices
+__device__ inline void mini_triangle(const StageCtx& c, const tc_RenderInstance* in, const tc_Cluster& cl, u32 inst,
+                                     u32 tri, u32 word, u32 rel, u32 baseTris, u32 vertexOffset, u32 partOffset,
+                                     const RippleParams& rp)
+{
+  tc_SceneBuilding* b   = c.build;
+  const u32         cfg = word & 0xFFFFu;
+  const tc_TessTableEntry e = table_entry(c.table, cfg);
+  u32               enc[3] = {0u, TC_TESSTABLE_COORD_MAX, TC_TESSTABLE_COORD_MAX << 16};
+  const u32         rot    = (word >> 16) & 3;
+  if(rot == 1)
+  {
+    const u32 t0 = enc[0];
+    enc[0] = enc[1], enc[1] = enc[2], enc[2] = t0;
+  }
+  else if(rot == 2)
+  {
+    const u32 t2 = enc[2];
+    enc[2] = enc[1], enc[1] = enc[0], enc[0] = t2;
+  }
+  const uint8_t* lt = reinterpret_cast<const uint8_t*>(in->clusterLocalTriangles) + cl.firstLocalTriangle;
+  f3             bp[3], bn[3], bb[3];
+  f2             bt[3];
+  for(int q = 0; q < 3; q++)
+  {
+    const u32 vi = cl.firstLocalVertex + lt[tri * 3 + q];
+    bp[q]        = ldg3(reinterpret_cast<const float*>(in->positions), vi);
+    bn[q]        = normalize3(ldg3(reinterpret_cast<const float*>(in->normals), vi));
+    bt[q]        = ldg2(reinterpret_cast<const float*>(in->texcoords), vi);
+    bb[q]        = decode_bary(enc[q]);
+  }
+  tc_DisplacementTexture tx    = {};
+  bool                   hasTx = false;
+  if(c.numTextures > 0 && c.textures != nullptr && in->displacementIndex >= 0)
+  {
+    if((u32)in->displacementIndex < c.numTextures)
+    {
+      tx    = c.textures[in->displacementIndex];
+      hasTx = true;
+    }
+    else
+      atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
+  }
+  const bool pn    = (c.flags & TC_FLAG_PN) != 0;
+  BasePN     basis = {};
+  if(pn)
+    basis = setup_pn(bp[0], bp[1], bp[2], bn[0], bn[1], bn[2]);
+  float* gv = reinterpret_cast<float*>(b->genVertices);
+  for(u32 vert = 0; vert < e.numVertices; vert++)
+  {
+    const f3 w   = interp3(bb[0], bb[1], bb[2], cfg_vertex(c.table, e, cfg, vert));
+    f3       pos = pn ? get_pn(basis, w) : interp3(bp[0], bp[1], bp[2], w);
+    if(hasTx)
+      pos = displace(pos, interp3(bn[0], bn[1], bn[2], w), sample_bilinear(tx, interp2(bt[0], bt[1], bt[2], w)),
+                     in->displacementScale, c.view->displacementScale, in->displacementOffset, c.view->displacementOffset);
+    if(rp.enabled)
+      pos = ripple(pos, inst, in->geoHi.w, rp);
+    float* d = gv + 3 * ((u64)vertexOffset + rel * TC_2X_MINI_VERTICES + vert);
+    d[0] = pos.x, d[1] = pos.y, d[2] = pos.z;
+  }
+  const u32 pf  = (word >> kWordFactorShift) & 7;
+  uint8_t*  idx = reinterpret_cast<uint8_t*>(b->genVertices) + ((u64)vertexOffset + kMiniBatchVerts) * 12;
+  uint16_t* map = reinterpret_cast<uint16_t*>(reinterpret_cast<uint8_t*>(b->partTriangles) + (u64)partOffset * kTessInfoBytes
+                                              + kClusterInfoBytes);
+  for(u32 i = 0; i < e.numTriangles; i++)
+  {
+    const uint3 ct        = cfg_triangle(c.table, e, cfg, i);
+    const u32   triOffset = baseTris + i;
+    map[triOffset]        = (uint16_t)(tri | (i << 8) | (pf << 12));
+    idx[triOffset * 3 + 0] = (uint8_t)(ct.x + rel * TC_2X_MINI_VERTICES);
+    idx[triOffset * 3 + 1] = (uint8_t)(ct.y + rel * TC_2X_MINI_VERTICES);
+    idx[triOffset * 3 + 2] = (uint8_t)(ct.z + rel * TC_2X_MINI_VERTICES);
+  }
+}
+
+// the warp zeroes `words` 32-bit words at p (4-byte aligned)
+__device__ __forceinline__ void warp_zero(void* p, u32 words)
+{
+  u32* w = reinterpret_cast<u32*>(p);
+  for(u32 i = threadIdx.x & 31; i < words; i += 32)
+    w[i] = 0u;
+}
+
+// cluster_classify.comp.glsl:254-905 with transient builds, for one cluster,
+// by one warp, in the canonical order: the full-cluster or 1X allocation, then
+// per 32-triangle chunk its parts and splits followed by its 2X batches.
+// Offsets come from the block scan; every allocation is tested like the
+// reference's (the counters advance whether or not it fits). Bytes the
+// reference leaves unwritten inside an allocation are written as zeros.
+__device__ inline void write_cluster_transient(const StageCtx& c, const ClassifyScratch& cs, u32 visIndex, u32 v,
+                                               const tc_ClusterInfo& ci, uint4 r, TransOffsets o, u32 genBase,
+                                               const TransBases& tb, u32& statTemp, u32& statTrans, u32& statTris)
+{
+  const u32         lane = threadIdx.x & 31, ltm = (1u << lane) - 1u;
+  tc_SceneBuilding* b    = c.build;
+  const tc_caps&    k    = c.caps;
+  const u64         maxData = (u64)k.maxGeneratedClusterMegs * 1024ull * 1024ull;
+  const u32*        basic   = reinterpret_cast<const u32*>(b->basicClusterSizes);
+  tc_BlasBuildInfo* blas    = reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos);
+  const u32         nt = t_nt(r), nv = t_nv(r), simple = t_simple(r);
+  const bool        full = t_full(r), subset = t_subset(r);
+  const tc_RenderInstance* in = c.instances + ci.instanceID;
+  const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
+  u32 x = o.front, y = o.back, s = o.split, g = o.gen, vo = o.vert, tr = o.trans;
+  u64 d = o.data;
+  auto fits = [&](u32 vertexSize, u64 dataSize, u32 partOffset, u32 partSize) {
+    return !((u64)vo + vertexSize > k.maxGeneratedVertices || (u64)g + 1 > k.maxGeneratedClusters
+             || d + dataSize > maxData || (u64)partOffset + partSize > k.maxPartTriangles);
+  };
+  uint8_t* gvb = reinterpret_cast<uint8_t*>(b->genVertices);
+  uint8_t* ptb = reinterpret_cast<uint8_t*>(b->partTriangles);
+
+  // ---- :254-437 full cluster or 1X subset ----------------------------------------
+  if(full || subset)
+  {
+    const u32 vertexSize = full ? nv : subset_vertex_size(nv, simple);
+    const u64 dataSize   = full ? (u64)__ldg(reinterpret_cast<const u32*>(in->clusterTemplateInstantiatonSizes) + ci.clusterID)
+                                : (u64)basic[simple];
+    const u32 partSize   = full ? 0u : subset_part_slots(simple);
+    const u32 partOffset = full ? 0u : back_alloc(x, y, partSize, k.maxPartTriangles);
+    const bool ok        = fits(vertexSize, dataSize, partOffset, partSize);
+    if(lane == 0)  // the vertex walk's record, per visible cluster with transient builds
+      cs.fullRecs[v] = ok ? make_uint2(visIndex, vo) : make_uint2(kRejected, 0u);
+    if(ok)
+    {
+      if(lane == 0)
+      {
+        if(full)
+        {
+          const u32                  tempOffset = tb.temp + (g - genBase) - (tr - tb.trans);
+          tc_TemplateInstantiateInfo ti;
+          ti.clusterIdOffset        = 0;
+          ti.geometryIndexOffset    = 0;
+          ti.clusterTemplateAddress = __ldg(reinterpret_cast<const u64*>(in->clusterTemplateAdresses) + ci.clusterID);
+          ti.vertexBufferAddress    = b->genVertices + (u64)vo * 12ull;
+          ti.vertexBufferStride     = 12;
+          reinterpret_cast<tc_TemplateInstantiateInfo*>(b->tempInstantiations)[tempOffset] = ti;
+          reinterpret_cast<u32*>(b->tempInstanceIDs)[tempOffset]                          = ci.instanceID;
+          reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset]                     = b->genClusterData + d;
+          if((c.flags & TC_FLAG_WRITE_FULLCLUSTERS) && b->fullClusters)
+            reinterpret_cast<tc_ClusterInfo*>(b->fullClusters)[tempOffset] = ci;
+          statTemp += 1;
+        }
+        else
+        {
+          store_clas_build(reinterpret_cast<tc_ClasBuildInfo*>(b->transBuilds) + tr, TC_RT_CLUSTER_MODE_1X_SUBSET_CLUSTER,
+                           partOffset, simple, nv, b->positionTruncateBitCount, b->genVertices + (u64)vo * 12ull);
+          reinterpret_cast<u32*>(b->transInstanceIDs)[tr]      = ci.instanceID;
+          reinterpret_cast<u64*>(b->transClusterAddresses)[tr] = b->genClusterData + d;
+          statTrans += 1;
+        }
+        statTris += simple;
+        atomicAdd(&blas[ci.instanceID].clusterReferencesCount, 1u);
+      }
+      if(subset)
+      {
+        // :489-535 indices after the vertices, triangle map after the header
+        uint8_t* idx = gvb + ((u64)vo + nv) * 12;
+        uint8_t* map = ptb + (u64)partOffset * kTessInfoBytes;
+        warp_zero(idx, (simple * 3 + 11) / 12 * 3);
+        warp_zero(map, partSize * kTessInfoBytes / 4);
+        __syncwarp();
+        if(lane == 0)
+          *reinterpret_cast<uint2*>(map) = make_uint2(ci.instanceID, ci.clusterID);
+        const u32* tw = cs.triWords + (u64)v * TC_MAX_CLUSTER_TRIANGLES;
+        const uint8_t* lt = reinterpret_cast<const uint8_t*>(in->clusterLocalTriangles) + cl.firstLocalTriangle;
+        u32 out = 0;
+        for(u32 t0 = 0; t0 < nt; t0 += 32)
+        {
+          const u32  tri = t0 + lane;
+          const bool sub = tri < nt && (tw[tri] & kWordSubset);
+          const u32  bm  = __ballot_sync(0xFFFFFFFFu, sub);
+          if(sub)
+          {
+            const u32 q = out + __popc(bm & ltm);
+            map[kClusterInfoBytes + q] = (uint8_t)tri;
+            idx[q * 3 + 0]            = lt[tri * 3 + 0];
+            idx[q * 3 + 1]            = lt[tri * 3 + 1];
+            idx[q * 3 + 2]            = lt[tri * 3 + 2];
+          }
+          out += __popc(bm);
+        }
+      }
+    }
+    g += 1, vo += vertexSize, d += dataSize;
+    if(subset)
+      tr += 1;
+  }
+  else if(lane == 0)
+    cs.fullRecs[v] = make_uint2(kRejected, 0u);
+  if(full)
+    return;
+
+  // ---- :543-905 the other triangles, one 32-triangle chunk at a time -------------
+  const u32*   tw  = cs.triWords + (u64)v * TC_MAX_CLUSTER_TRIANGLES;
+  tc_TessTriangleInfo* splits = reinterpret_cast<tc_TessTriangleInfo*>(b->splitTriangles);
+  tc_TessTriangleInfo* parts  = reinterpret_cast<tc_TessTriangleInfo*>(b->partTriangles);
+  const RippleParams rp = ripple_params(*c.view, (c.flags & TC_FLAG_RIPPLE) != 0);
+  for(u32 t0 = 0; t0 < nt; t0 += 32)
+  {
+    const u32  tri   = t0 + lane;
+    const bool valid = tri < nt;
+    const u32  word  = valid ? tw[tri] : 0u;
+    const bool split = valid && (word & (1u << 18));
+    const bool mini  = valid && (word & kWordMini);
+    const bool part  = valid && !split && !mini && !(word & kWordSubset);
+    const u32  bp = __ballot_sync(0xFFFFFFFFu, part), bs = __ballot_sync(0xFFFFFFFFu, split);
+    const u32  bm = __ballot_sync(0xFFFFFFFFu, mini);
+    // parts from the front of the two-sided counter: the chunk fits as a whole or not at all
+    const u32  nPart   = __popc(bp);
+    const bool frontOk = nPart != 0 && (u64)x + y + nPart + 1 <= k.maxPartTriangles;
+    if(part && frontOk)
+      emit_triangle(parts + x + __popc(bp & ltm), ci, tri, word);
+    if(frontOk && lane == 0)  // the written front's end
+      atomicMax(&b->partTriangleCounter, x + nPart);
+    x += nPart;
+    if(split)
+    {
+      const u64 so = (u64)s + __popc(bs & ltm);
+      if(so < k.maxSplitTriangles)
+      {
+        emit_triangle(splits + so, ci, tri, word);
+        if(c.splitBase)
+        {
+          const uint8_t* lt  = reinterpret_cast<const uint8_t*>(in->clusterLocalTriangles) + cl.firstLocalTriangle;
+          const float*   pos = reinterpret_cast<const float*>(in->positions);
+          float          m[16];
+#pragma unroll
+          for(int j = 0; j < 16; j++)
+            m[j] = __ldg(in->worldMatrix.m + j);
+          float* dd = c.splitBase + 9 * so;
+#pragma unroll
+          for(int vv = 0; vv < 3; vv++)
+          {
+            const f3 wp = xform_point(m, ldg3(pos, cl.firstLocalVertex + lt[tri * 3 + vv]));
+            dd[3 * vv + 0] = wp.x, dd[3 * vv + 1] = wp.y, dd[3 * vv + 2] = wp.z;
+          }
+        }
+      }
+    }
+    s += __popc(bs);
+    // :675-790 the chunk's 2X batches, kMiniBatch triangles each, in triangle order
+    const u32 nMini = __popc(bm), rank = __popc(bm & ltm);
+    for(u32 m0 = 0; m0 < nMini; m0 += kMiniBatch)
+    {
+      const bool member = mini && rank >= m0 && rank < m0 + kMiniBatch;
+      const u32  ntris  = member ? (u32)table_entry(c.table, word & 0xFFFFu).numTriangles : 0u;
+      const u32  incl   = warp_inclusive<u32>(ntris, lane);
+      const u32  numBatchTris = __shfl_sync(0xFFFFFFFFu, incl, 31);
+      const u64  dataSize     = (u64)basic[kMiniBatchTris];
+      const u32  partOffset   = back_alloc(x, y, kMiniPartSlots, k.maxPartTriangles);
+      const bool ok           = fits(kMiniVertexSize, dataSize, partOffset, kMiniPartSlots);
+      if(ok)  // (its vertices are written here, not by the vertex walk)
+      {
+        if(lane == 0)
+        {
+          store_clas_build(reinterpret_cast<tc_ClasBuildInfo*>(b->transBuilds) + tr,
+                           TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED, partOffset, numBatchTris, kMiniBatchVerts,
+                           b->positionTruncateBitCount, b->genVertices + (u64)vo * 12ull);
+          reinterpret_cast<u32*>(b->transInstanceIDs)[tr]      = ci.instanceID;
+          reinterpret_cast<u64*>(b->transClusterAddresses)[tr] = b->genClusterData + d;
+          atomicAdd(&blas[ci.instanceID].clusterReferencesCount, 1u);
+          statTrans += 1;
+          statTris += numBatchTris;
+        }
+        warp_zero(gvb + (u64)vo * 12, kMiniVertexSize * 3);
+        warp_zero(ptb + (u64)partOffset * kTessInfoBytes, kMiniPartSlots * kTessInfoBytes / 4);
+        __syncwarp();
+        if(lane == 0)
+          *reinterpret_cast<uint2*>(ptb + (u64)partOffset * kTessInfoBytes) = make_uint2(ci.instanceID, ci.clusterID);
+        if(member)
+          mini_triangle(c, in, cl, ci.instanceID, tri, word, rank - m0, incl - ntris, vo, partOffset, rp);
+        __syncwarp();
+      }
+      g += 1, vo += kMiniVertexSize, d += dataSize, tr += 1;
+    }
+  }
+}
+
+// The offsets at which block `blockIdx.x` of the write launch starts, with
+// transient builds (the seven counters of TransOffsets).
+__device__ inline void block_prefix_transient(const ClassifyScratch& cs, u64 (&pre)[kTNum], u64 (*s_warp)[kTNum])
+{
+  u64 x[kTNum] = {0, 0, 0, 0, 0, 0, 0};
+  for(u32 i = threadIdx.x; i < blockIdx.x; i += blockDim.x)
+  {
+    const RangeSums o = cs.rangeSums[i];
+    x[kTFront] += (u32)o.partsSplits;
+    x[kTSplit] += (u32)(o.partsSplits >> 32);
+    x[kTGen] += (u32)o.fullVerts;
+    x[kTVert] += (u32)(o.fullVerts >> 32);
+    x[kTData] += o.data;
+    x[kTBack] += (u32)o.backTrans;
+    x[kTTrans] += (u32)(o.backTrans >> 32);
+  }
+  u64 tot[kTNum];
+  block_scan_n<kTNum>(x, tot, s_warp);
+  const ClusterOffsets b0 = *cs.bases;
+  const TransBases     t0 = *reinterpret_cast<const TransBases*>(cs.bases + 1);
+  pre[kTFront] = b0.part + tot[kTFront];
+  pre[kTSplit] = b0.split + tot[kTSplit];
+  pre[kTGen]   = b0.gen + tot[kTGen];
+  pre[kTVert]  = b0.vert + tot[kTVert];
+  pre[kTData]  = b0.data + tot[kTData];
+  pre[kTBack]  = t0.back + tot[kTBack];
+  pre[kTTrans] = t0.trans + tot[kTTrans];
+}
+
+__global__ void __launch_bounds__(kBlock, 4) k_classify_write_transient(StageCtx c, ClassifyScratch cs)
+{
+  stage_prologue();
+  __shared__ u32            s_range[2];
+  __shared__ u64            s_warp[33][kTNum];
+  __shared__ TransOffsets   s_off[kBlock];
+  __shared__ uint4          s_cnt[kBlock];
+  __shared__ tc_ClusterInfo s_ci[kBlock];
+  __shared__ FlatStarts     s_starts;
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if(threadIdx.x == 0)
+    window_range(c, s_range[0], s_range[1]);
+  __syncthreads();
+  const u32* starts = stage_flat_starts(c, s_starts);
+  const u32  begin  = s_range[0];
+  const u32  n      = min(s_range[1] - s_range[0], c.scratch.itemCapacity);
+  tc_SceneBuilding*     b   = c.build;
+  const tc_ClusterInfo* vis = reinterpret_cast<const tc_ClusterInfo*>(b->visibleClusters);
+  const uint4*          counts = reinterpret_cast<const uint4*>(cs.counts);
+  u32                   statTemp = 0, statTrans = 0, statTris = 0;
+
+  u64 pre[kTNum];
+  block_prefix_transient(cs, pre, s_warp);
+  const u32        genBase = cs.bases->gen;
+  const TransBases tb      = *reinterpret_cast<const TransBases*>(cs.bases + 1);
+  u32              vBegin, vEnd;
+  block_range(n, blockIdx.x, gridDim.x, vBegin, vEnd);
+  for(u32 c0 = vBegin; c0 < vEnd; c0 += kBlock)
+  {
+    const u32 len = min(kBlock, vEnd - c0);
+    {
+      const uint4 r = threadIdx.x < len ? counts[c0 + threadIdx.x] : make_uint4(0, 0, 0, 0);
+      if(threadIdx.x < len)
+        s_ci[threadIdx.x] = visible_cluster(c, starts, vis, begin + c0 + threadIdx.x);
+      u64 x[kTNum] = {t_parts(r), t_splits(r), t_gen(r), t_verts(r), r.z, t_back(r), t_trans(r)};
+      u64 tot[kTNum];
+      block_scan_n<kTNum>(x, tot, s_warp);
+      s_cnt[threadIdx.x] = r;
+      s_off[threadIdx.x] = {(u32)(pre[kTFront] + x[kTFront]), (u32)(pre[kTSplit] + x[kTSplit]),
+                            (u32)(pre[kTGen] + x[kTGen]),     (u32)(pre[kTVert] + x[kTVert]),
+                            (u32)(pre[kTBack] + x[kTBack]),   (u32)(pre[kTTrans] + x[kTTrans]),
+                            pre[kTData] + x[kTData]};
+#pragma unroll
+      for(int q = 0; q < kTNum; q++)
+        pre[q] += tot[q];
+    }
+    __syncthreads();
+    const u32 perW = (len + kWarps - 1) / kWarps;
+    const u32 lo = min(len, warp * perW), hi = min(len, lo + perW);
+    for(u32 i = lo; i < hi; i++)
+      write_cluster_transient(c, cs, begin + c0 + i, c0 + i, s_ci[i], s_cnt[i], s_off[i], genBase, tb, statTemp,
+                              statTrans, statTris);
+    __syncthreads();
+  }
+  if(lane == 0)
+  {
+    if(statTemp)
+      atomicAdd(&b->tempInstantiateCounter, statTemp);
+    if(statTrans)
+      atomicAdd(&b->transBuildCounter, statTrans);
+    if(statTris)
+      atomicAdd(&c.readback->numTotalTriangles, statTris);
+  }
+  if(blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
+  {
+    cs.fullRange[0] = 0;  // the walk's records are per visible cluster here
+    cs.fullRange[1] = n;
+    if(n)
+    {
+      const ClusterOffsets b0 = *cs.bases;
+      b->dualPartTriangleCounter = (u64)(u32)pre[kTFront] | ((u64)(u32)pre[kTBack] << 32);
+      b->splitTriangleCounter    = (int32_t)(u32)pre[kTSplit];
+      b->genClusterCounter       = (u32)pre[kTGen];
+      b->genVertexCounter        = (u32)pre[kTVert];
+      b->genClusterDataCounter   = pre[kTData];
+      // :299 counts every full-cluster attempt; the full attempts also bound
+      // the full clusters' run of the instantiation list
+      const u32 fullAttempts = ((u32)pre[kTGen] - b0.gen) - ((u32)pre[kTTrans] - tb.trans);
+      c.readback->numFullClusters += fullAttempts;
+      c.runStarts[kFullAttemptsSlot] += fullAttempts;
+    }
+    if(c.fuseSetup != kNoSetup)
+      build_setup_apply(c, c.fuseSetup);
+  }
+}
+
 // cluster_classify.comp.glsl:457-482: the displaced vertices of the full
 // clusters the write launch accepted. A warp takes `per` <= 32 consecutive
 // generated-cluster slots (per: the slots spread over all of the grid's
@@ -794,8 +1396,8 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_full_vertices(St
         fr.size   = in->geoHi.w;
       }
     }
-    // accepted clusters are a prefix of the slots, so the owners are the
-    // first lanes and their vertex ranges follow each other
+    // the owners' records in slot order (their vertex ranges follow each
+    // other, with gaps only where transient builds placed other data)
     const u32 fm = __ballot_sync(0xFFFFFFFFu, owner);
     if(fm == 0)
       continue;
@@ -839,6 +1441,13 @@ cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& bu
   const u32 grid = std::max(1u, std::min(classify_max_blocks(maxClusters), numSMs * std::max(1u, warpBlocksPerSM)));
   ClassifyScratch cs{buf.counts, buf.triWords, buf.rangeSums, buf.bases, grid, 0, buf.fullRecs, buf.fullRange};
   // register budget from the requested residency: 4 or less -> 64, 5-7 -> 40, 8 and more -> 32
+  if(c.flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X))
+  {
+    cudaError_t e = launch_pdl(k_classify_count<4, true>, grid, kBlock, s, c, cs);
+    if(e != cudaSuccess)
+      return e;
+    return launch_pdl(k_classify_write_transient, grid, kBlock, s, c, cs);
+  }
   const int   occ = warpBlocksPerSM >= 8 ? 8 : (warpBlocksPerSM >= 5 ? 6 : 4);
   cudaError_t e   = occ == 8   ? launch_pdl(k_classify_count<8>, grid, kBlock, s, c, cs)
                     : occ == 6 ? launch_pdl(k_classify_count<6>, grid, kBlock, s, c, cs)

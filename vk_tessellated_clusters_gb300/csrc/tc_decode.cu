@@ -1,6 +1,7 @@
 // tc_decode.cu — hit-time decode of cluster ray-tracing hits into base-mesh
-// hits: render_raytrace_clusters.rchit.glsl:131-214 (RT target, no transient
-// builds), as a kernel any CUDA ray tracer can run over its hit records.
+// hits: render_raytrace_clusters.rchit.glsl:131-214 (RT target; 1X subset and
+// 2X batch hits when the frame was built with those transient builds), as a
+// kernel any CUDA ray tracer can run over its hit records.
 //
 // One thread per hit; every index is checked against the frame's data (a hit
 // from another frame reports TC_HIT_OUT_OF_RANGE instead of reading past a
@@ -39,11 +40,44 @@ __global__ void k_decode_hits(StageCtx c, const tc_hit* hits, u32 count, tc_base
   const bool   visTriangles = c.view->visualize == TC_VISUALIZE_TRIANGLES;
   u32          partID       = visTriangles ? triangleID + 1 : 0u;
   uint4        enc          = {0, 0, 0, 0};
+  bool         tess         = mode == TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED;
   r.status                  = TC_HIT_OK;
-  if(mode == TC_RT_CLUSTER_MODE_1X_SUBSET_CLUSTER || mode == TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED)
+  if((mode == TC_RT_CLUSTER_MODE_1X_SUBSET_CLUSTER && !(c.flags & TC_FLAG_TRANSIENT_1X))
+     || (mode == TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED && !(c.flags & TC_FLAG_TRANSIENT_2X)))
     r.status = TC_HIT_UNSUPPORTED_MODE;
   else if(h.instanceID >= c.numInstances)
     r.status = TC_HIT_OUT_OF_RANGE;
+  else if(mode == TC_RT_CLUSTER_MODE_1X_SUBSET_CLUSTER || mode == TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED)
+  {
+    // rchit.glsl:150-180: a transient build's ClusterInfo header and triangle
+    // map at the back of partTriangles
+    const bool mini = mode == TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED;
+    const u64  need = mini ? 10ull + 2ull * triangleID : 9ull + triangleID;  // header + map entry, in bytes
+    if(clusterID >= c.caps.maxPartTriangles || need > (u64)(c.caps.maxPartTriangles - clusterID) * 24
+       || triangleID >= (mini ? 32u : 64u))
+      r.status = TC_HIT_OUT_OF_RANGE;
+    else
+    {
+      const uint8_t* rec = reinterpret_cast<const uint8_t*>(c.build->partTriangles) + (u64)clusterID * 24;
+      const uint2    hdr = *reinterpret_cast<const uint2*>(rec);
+      if(mini)
+      {
+        const u32 packed = reinterpret_cast<const uint16_t*>(rec + 8)[triangleID];
+        triangleID       = packed & 0xFFu;
+        subTriangleID    = (packed >> 8) & 4u;  // the shader's mask (rchit.glsl:161), kept as written
+        u32 e3[3]        = {0u, TC_TESSTABLE_COORD_MAX, TC_TESSTABLE_COORD_MAX << 16};
+        const uint3 f    = make_uint3(1u + ((packed >> 12) & 1u), 1u + ((packed >> 13) & 1u), 1u + (packed >> 14));
+        cfg              = get_config(f, e3[0], e3[1], e3[2]);
+        enc              = {e3[0], e3[1], e3[2], 0};
+        tess             = true;
+      }
+      else
+        triangleID = rec[8 + triangleID];
+      clusterID = hdr.y;
+      if(hdr.x != h.instanceID || (tess && subTriangleID >= table_entry(c.table, cfg).numTriangles))
+        r.status = TC_HIT_OUT_OF_RANGE;
+    }
+  }
   else if(mode == TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED)
   {
     // rchit.glsl:146, 183-186: the part triangle names its base cluster and triangle
@@ -83,7 +117,7 @@ __global__ void k_decode_hits(StageCtx c, const tc_hit* hits, u32 count, tc_base
   const f3 w = {__fsub_rn(__fsub_rn(1.0f, h.barycentrics[0]), h.barycentrics[1]), h.barycentrics[0],
                 h.barycentrics[1]};
   f3       base = w;
-  if(mode == TC_RT_CLUSTER_MODE_SINGLE_TESSELLATED)
+  if(tess)
   {
     // rchit.glsl:207-235: micro-triangle -> sub-triangle -> base triangle
     const u32 e[3] = {enc.x, enc.y, enc.z};

@@ -127,7 +127,7 @@ __device__ inline void frame_begin_body(const StageCtx& c)
       b->tempInstantiateCounter      = 0;
       b->transBuildCounter           = 0;
     }
-    for(u32 i = threadIdx.x; i < kMaxRuns + 2; i += blockDim.x)
+    for(u32 i = threadIdx.x; i < kRunStartsSize; i += blockDim.x)
       c.runStarts[i] = 0;
   }
   // the split queue is filled with ~0 every frame

@@ -66,6 +66,12 @@ __device__ inline void part_range(const StageCtx& c, u32& lo, u32& hi)
     const u32 rs = c.runStarts[c.run], re = c.runStarts[c.run + 1];
     lo           = min(rs, cap);
     hi           = min(max(re, rs), cap);
+    if(c.flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X))
+    {
+      // classify's run ends at its part requests; only the written front holds parts
+      hi = min(hi, c.build->partTriangleCounter);
+      lo = min(lo, hi);
+    }
   }
   if(!whole_window(c))
   {
@@ -210,6 +216,9 @@ __global__ void __launch_bounds__(kScanBlock) k_instantiate_tile_scan(StageCtx c
   if(threadIdx.x == 0)
   {
     c.scratch.totals[0] = genBase;
+    // instantiation slots continue after the accepted ones (transient builds
+    // take generated-cluster slots but no instantiation slot)
+    c.scratch.totals[1] = b->tempInstantiateCounter;
     if(numTiles)
     {
       // the reference's counters count every attempt, accepted or not
@@ -268,6 +277,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_instantiate_args(StageCtx c, Inst
   const u32 numTiles = clamp_tiles(c, (n + kTile - 1) / kTile);
   const u32 stride   = c.scratch.lbStride;
   const u64 genBase  = c.scratch.totals[0];
+  const u64 tempBase = c.scratch.totals[1];
 
   const tc_caps&             k            = c.caps;
   const tc_TessTriangleInfo* parts        = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
@@ -327,8 +337,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_instantiate_args(StageCtx c, Inst
       ib.vertexOffset[p] = accept ? (u32)vertexOffset : ~0u;
       if(!accept)
         continue;
-      // accepted instantiations form a prefix of the serial order: slot == generated cluster index
-      const u32                   tempOffset = (u32)genOffset;
+      // accepted instantiations form a prefix of the serial order: consecutive slots
+      const u32                   tempOffset = (u32)(tempBase + q);
       tc_TemplateInstantiateInfo* dst = reinterpret_cast<tc_TemplateInstantiateInfo*>(b->tempInstantiations) + tempOffset;
       const u64   tmpl  = __ldg(c.table.templateAddresses + cfg_index(cfg[i]));
       const u64   vaddr = b->genVertices + vertexOffset * 12ull;

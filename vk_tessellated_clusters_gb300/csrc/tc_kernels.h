@@ -19,21 +19,31 @@ struct ClusterOffsets
 };
 static_assert(sizeof(ClusterOffsets) == 24, "ClusterOffsets: three 8-byte words");
 
+// with transient builds, the bases of the counters only they use (stored
+// right after the ClusterOffsets bases): the back of the two-sided part
+// counter, the transient builds and the template instantiations so far
+struct TransBases
+{
+  u32 back, trans, temp, _pad;
+};
+
 // per range of visible clusters: the sums of the clusters' counts, packed
-// (parts | splits << 32, full clusters | their vertices << 32, CLAS bytes)
+// (parts | splits << 32, full clusters | their vertices << 32, CLAS bytes;
+// with transient builds: generated clusters | vertices << 32, and back slots |
+// transient builds << 32 in backTrans)
 struct RangeSums
 {
-  unsigned long long partsSplits, fullVerts, data;
+  unsigned long long partsSplits, fullVerts, data, backTrans;
 };
 
 // cluster_classify scratch: per visible cluster of a launch's window, and per
 // block of the classify grid (each write block owns a contiguous range of clusters)
 struct ClassifyBuffers
 {
-  uint2*          counts;
+  uint2*          counts;     // 8 bytes per cluster (16 with transient builds)
   u32*            triWords;   // 64 per cluster
   RangeSums*      rangeSums;  // per block: the sums of its range's counts (zero before the launch)
-  ClusterOffsets* bases;      // one: the counters before the launch
+  ClusterOffsets* bases;      // one: the counters before the launch (then one TransBases)
   uint2*          fullRecs;   // per full cluster of the window: visible index, first generated vertex
   u32*            fullRange;  // [2]: the window's generated-cluster slots
 };

@@ -94,6 +94,22 @@ __device__ __forceinline__ Child make_child(const Table& table, const SplitItem&
   return ch;
 }
 
+// the part counter a split pass continues from: the front of the two-sided
+// counter with transient builds
+__device__ __forceinline__ u32 part_base(const StageCtx& c)
+{
+  return (c.flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X)) ? (u32)c.build->dualPartTriangleCounter
+                                                                    : c.build->partTriangleCounter;
+}
+__device__ __forceinline__ u32 part_cap(const StageCtx& c)
+{
+  const u32 m = c.caps.maxPartTriangles;
+  if(!(c.flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X)))
+    return m;
+  const u32 y = (u32)(c.build->dualPartTriangleCounter >> 32);
+  return (u64)y + 1 < m ? m - y - 1 : 0u;
+}
+
 template <int T, int B>
 __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
 {
@@ -120,6 +136,9 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
   const u32         warp = threadIdx.x >> 5;
   tc_SceneBuilding* b    = c.build;
   const tc_caps&    k    = c.caps;
+  // with transient builds a child part fits when it leaves the back's slots
+  // and one more free (build.glsl:68-82, one child at a time)
+  const u32 partCap = part_cap(c);
   tc_TessTriangleInfo* queue = reinterpret_cast<tc_TessTriangleInfo*>(b->splitTriangles);
 
   if(threadIdx.x == 0)
@@ -291,7 +310,7 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
       const u32 agg = __shfl_sync(0xFFFFFFFFu, incl, 31);
       u64       base = 0;
       if(tile == 0)
-        base = q == kCntSplit ? b->splitWriteCounter : b->partTriangleCounter;
+        base = q == kCntSplit ? b->splitWriteCounter : part_base(c);
       const u64 ex = warp_lookback_exclusive(c.scratch.lbState + (u64)q * c.scratch.lbStride, tile, agg, base, c.errorWord);
       if(lane == 0)
       {
@@ -345,7 +364,7 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
       else if(part)
       {
         const u64 o = s_excl[kCntPart] + s_cnt[kCntPart][ch * kW + warp] + __popc(bp & ltm);
-        if(o < k.maxPartTriangles)
+        if(o < partCap)
         {
           uint2* dst = reinterpret_cast<uint2*>(reinterpret_cast<tc_TessTriangleInfo*>(b->partTriangles) + o);
           dst[0]     = make_uint2(s_item[item].ci.instanceID, s_item[item].ci.clusterID);
@@ -363,8 +382,19 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
     {
       if(numTiles)
       {
-        b->splitWriteCounter   = (u32)c.scratch.totals[kCntSplit];
-        b->partTriangleCounter = (u32)c.scratch.totals[kCntPart];
+        b->splitWriteCounter = (u32)c.scratch.totals[kCntSplit];
+        const u32 total      = (u32)c.scratch.totals[kCntPart];
+        if(c.flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X))
+        {
+          // requests to the counter's front half; partTriangleCounter is the
+          // end of the written front (triangle_split.comp.glsl:321-328)
+          const u32 start = (u32)b->dualPartTriangleCounter, written = min(total, partCap);
+          b->dualPartTriangleCounter = (b->dualPartTriangleCounter & 0xFFFFFFFF00000000ull) | total;
+          if(written > start)
+            b->partTriangleCounter = max(b->partTriangleCounter, written);
+        }
+        else
+          b->partTriangleCounter = total;
       }
       if(c.fuseSetup != kNoSetup)
         build_setup_apply(c, c.fuseSetup);

@@ -73,7 +73,7 @@ struct StageCtx
   Table                         table;
   tc_caps                       caps;
   u32*                          errorWord;
-  u32*                          runStarts;         // [kMaxRuns + 2]: part counter at each run start, then full-cluster count
+  u32*                          runStarts;         // [kRunStartsSize]: part counter at each run start, the full-cluster count, full attempts
   u32*                          instClusterStart;  // [numInstances + 1] exclusive prefix of numClusters
   float*                        splitBase;         // [maxSplitTriangles][9]: world positions of each split item's base triangle
   LaunchScratch                 scratch;
@@ -91,13 +91,17 @@ constexpr u32 kNoSetup        = 0xFFFFFFFFu;
 constexpr u32 kAllRuns        = 0xFFFFFFFFu;
 constexpr u32 kRunsAfterFirst = 0xFFFFFFFEu;  // instantiate: every run but the first (the split passes' parts)
 constexpr u32 kMaxRuns  = 16;
+// runStarts[kFullAttemptsSlot]: full-cluster attempts of the frame's classify
+// launches (with transient builds, generated clusters are not all full ones)
+constexpr u32 kFullAttemptsSlot = kMaxRuns + 2;
+constexpr u32 kRunStartsSize    = kMaxRuns + 3;
 
 __device__ __forceinline__ u32 clamp_split_factor(u32 sf) { return max(2u, min(sf, TC_TESSTABLE_SIZE)); }
 
 __device__ __forceinline__ bool whole_window(const StageCtx& c) { return c.instBegin == 0 && c.instEnd >= c.numInstances; }
 
-// shaders/build_setup.comp.glsl:102-265 (RT target, no transient builds,
-// non-persistent split), plus bookkeeping of the part-run boundaries that the
+// shaders/build_setup.comp.glsl:102-265 (RT target, non-persistent split; the
+// transient-build branches with TC_FLAG_TRANSIENT_*), plus bookkeeping of the part-run boundaries that the
 // per-instance launch path and the backward pass use.
 __device__ inline void build_setup_apply(const StageCtx& c, u32 mode)
 {
@@ -138,9 +142,20 @@ __device__ inline void build_setup_apply(const StageCtx& c, u32 mode)
       b->splitPassStart        = 0;
       b->splitPassEnd          = count;
       b->dispatchTriangleSplit = {(count + 63) / 64, 1, 1};
-      c.runStarts[0]           = 0;
-      c.runStarts[1]           = b->partTriangleCounter;
-      c.runStarts[kMaxRuns + 1] = b->genClusterCounter;  // full-cluster instantiation attempts
+      c.runStarts[0] = 0;
+      if(c.flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X))
+      {
+        // classify's part requests from the front (its blocks may still be
+        // raising the written end, partTriangleCounter, which the
+        // instantiation clamps this run to)
+        c.runStarts[1]            = (u32)b->dualPartTriangleCounter;
+        c.runStarts[kMaxRuns + 1] = c.runStarts[kFullAttemptsSlot];
+      }
+      else
+      {
+        c.runStarts[1]            = b->partTriangleCounter;
+        c.runStarts[kMaxRuns + 1] = b->genClusterCounter;  // full-cluster instantiation attempts
+      }
       break;
     }
     case TC_BUILD_SETUP_SPLIT_PASS:
@@ -158,8 +173,11 @@ __device__ inline void build_setup_apply(const StageCtx& c, u32 mode)
     }
     case TC_BUILD_SETUP_BUILD_BLAS:
     {
-      u32 temp                        = b->tempInstantiateCounter;
-      rb->numBlasClusters             = temp;
+      const bool trans                = (c.flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X)) != 0;
+      u32        temp                 = b->tempInstantiateCounter;
+      u32        tr                   = trans ? b->transBuildCounter : 0u;
+      rb->numBlasClusters             = temp + tr;
+      rb->numTransBuilds              = tr;
       rb->numTempInstantiations       = temp;
       rb->numGenDatas                 = b->genClusterDataCounter;
       rb->numGenVertices              = b->genVertexCounter;
@@ -168,13 +186,30 @@ __device__ inline void build_setup_apply(const StageCtx& c, u32 mode)
       b->tempInstantiateCounter       = temp;
       rb->numActualTempInstantiations = temp;
       b->dispatchBlasTempInsert       = {(temp + 63) / 64, 1, 1};
+      if(trans)  // :211-233
+      {
+        tr                          = min(k.maxGeneratedClusters, temp + tr) - temp;
+        b->transBuildCounter        = tr;
+        rb->numActualTransBuilds    = tr;
+        b->dispatchBlasTransInsert  = {(tr + 63) / 64, 1, 1};
+      }
       break;
     }
     case TC_BUILD_SETUP_INSTANTIATE_TESS:
     {
       u32 part              = b->partTriangleCounter;
-      rb->numPartTriangles  = part;
       rb->numSplitTriangles = b->splitWriteCounter;
+      if(c.flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X))
+      {
+        // :242-265: requests from both ends; partTriangleCounter is the end
+        // of the written front
+        const u32 lo              = (u32)b->dualPartTriangleCounter;
+        const u32 hi              = (u32)(b->dualPartTriangleCounter >> 32);
+        rb->numPartTriangles      = lo + hi;
+        rb->numTransPartTriangles = hi;
+      }
+      else
+        rb->numPartTriangles = part;
       if(b->splitPass + 2 <= kMaxRuns)
         c.runStarts[b->splitPass + 2] = part;
       part                           = min(part, k.maxPartTriangles);

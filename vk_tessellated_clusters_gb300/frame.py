@@ -158,6 +158,23 @@ class FrameState:
         sb["blasBuildInfos"] = self.blas_build_infos.addr
         sb["blasBuildSizes"] = self.blas_build_sizes.addr
         sb["blasClusterAddresses"] = self.blas_cluster_addresses.addr
+        self.transient = bool(self.flags & (L.FLAG_TRANSIENT_1X | L.FLAG_TRANSIENT_2X))
+        if self.transient:
+            from .scene import basic_cluster_sizes
+            g = k["maxGeneratedClusters"]
+            self.trans_instance_ids = mem.alloc(4 * g)
+            self.trans_builds = mem.alloc(L.ClasBuildInfo.itemsize * g)
+            self.trans_cluster_addresses = mem.alloc(8 * g)
+            self.trans_cluster_sizes = mem.alloc(4 * g)
+            self.basic_cluster_sizes = mem.upload(basic_cluster_sizes())
+            sb["transInstanceIDs"] = self.trans_instance_ids.addr
+            sb["transBuilds"] = self.trans_builds.addr
+            sb["transClusterAddresses"] = self.trans_cluster_addresses.addr
+            sb["transClusterSizes"] = self.trans_cluster_sizes.addr
+            sb["basicClusterSizes"] = self.basic_cluster_sizes.addr
+            # the index and map bytes alias the vertex and part arrays (shaderio_building.h:240-246)
+            sb["transTriMappings"] = self.part_triangles.addr
+            sb["transTriIndices"] = self.gen_vertices.addr
         self.scene_building_host = sb
         self.build = mem.upload(sb)
         self.args = L.FrameArgs()
@@ -222,7 +239,51 @@ class FrameState:
                     entries = lookup_entries(load_raw_table())
                 part = out["partTriangles"][int(last["clusterIdOffset"]) & 0x3FFFFFFF]
                 nverts = base + int(entries[(int(part["triangleID_config"]) >> 16) & 0x7FFF]["numVertices"])
-        out["genVertices"] = self.gen_vertices.read(np.float32, 3 * nverts).reshape(-1, 3)
+        if not self.transient:
+            out["genVertices"] = self.gen_vertices.read(np.float32, 3 * nverts).reshape(-1, 3)
+            return out
+        # transient builds: their records, the back slots of partTriangles and
+        # the index bytes after their vertices (in build order); genVertices
+        # keeps only vertex slots (a batch's unused slots are zeros), every
+        # other byte (index bytes, rejected allocations) reads as zero
+        ntr = min(int(sb["transBuildCounter"]), k["maxGeneratedClusters"])
+        tb = self.trans_builds.read(L.ClasBuildInfo, ntr).copy()
+        tb["vertexBuffer"] -= np.uint64(self.gen_vertices.addr)
+        tb["indexBuffer"] -= np.uint64(self.gen_vertices.addr)
+        out["transBuilds"] = tb
+        out["transInstanceIDs"] = self.trans_instance_ids.read(np.uint32, ntr)
+        out["transClusterAddresses"] = self.trans_cluster_addresses.read(np.uint64, ntr)
+        ranges = []  # (first vertex, vertex count)
+        for j in range(ntemp):
+            base = int(ti[j]["vertexBufferAddress"]) // 12
+            if (int(ti[j]["clusterIdOffset"]) >> 30) == 0:
+                ranges.append((base, self._full_cluster_vertices(out, j)))
+            else:
+                if entries is None:
+                    from .table import load_raw_table, lookup_entries
+                    entries = lookup_entries(load_raw_table())
+                part = out["partTriangles"][int(ti[j]["clusterIdOffset"]) & 0x3FFFFFFF]
+                ranges.append((base, int(entries[(int(part["triangleID_config"]) >> 16) & 0x7FFF]["numVertices"])))
+        parts_raw = self.part_triangles.read(np.uint8, L.TessTriangleInfo.itemsize * k["maxPartTriangles"])
+        tparts, tidx = [], []
+        for r in tb:
+            mode, poff = int(r["clusterID"]) >> 30, int(r["clusterID"]) & 0x3FFFFFFF
+            ntri, nv = int(r["packed"]) & 0x1FF, (int(r["packed"]) >> 9) & 0x1FF
+            slots = 3 if mode == L.RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED else (8 + ntri + 23) // 24
+            tparts.append(parts_raw[24 * poff:24 * (poff + slots)])
+            ibytes = 96 if mode == L.RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED else (ntri * 3 + 11) // 12 * 12
+            tidx.append((int(r["indexBuffer"]), ibytes))
+            ranges.append((int(r["vertexBuffer"]) // 12, nv))
+        out["transParts"] = np.concatenate(tparts) if tparts else np.zeros(0, np.uint8)
+        end = max([a + n for a, n in ranges] + [(o + n + 11) // 12 for o, n in tidx] + [0])
+        raw = self.gen_vertices.read(np.uint8, 12 * end)
+        out["transIndices"] = (np.concatenate([raw[o:o + n] for o, n in tidx]) if tidx else np.zeros(0, np.uint8))
+        keep = np.zeros(end, bool)
+        for a, n in ranges:
+            keep[a:a + n] = True
+        gv = raw.view(np.float32).reshape(-1, 3).copy()
+        gv[~keep] = 0
+        out["genVertices"] = gv
         return out
 
     def _full_cluster_vertices(self, out, j) -> int:

@@ -1,6 +1,7 @@
 """Seeded ray-tracing hits on a built frame (hit-decode tests and bench): hits on
-accepted instantiations (full clusters and part triangles, as a cluster ray
-tracer reports them) plus malformed ones."""
+accepted instantiations (full clusters and part triangles) and transient
+builds (1X subsets, 2X batches), as a cluster ray tracer reports them, plus
+malformed ones."""
 import numpy as np
 
 from . import layouts as L
@@ -12,9 +13,19 @@ def sample_hits(out: dict, scene, entries: np.ndarray, n: int, seed: int = 0, ba
     full = out["fullClusters"]
     mode = ti["clusterIdOffset"] >> 30
     full_slot = np.cumsum(mode == 0) - 1  # rank of each full instantiation among the full ones
+    tb = out.get("transBuilds")
+    ntrans = 0 if tb is None else len(tb)
     hits = np.zeros(n + bad, L.Hit)
-    slots = rng.integers(0, len(ti), n)
+    slots = rng.integers(0, len(ti) + ntrans, n)
     for k, s in enumerate(slots):
+        if s >= len(ti):  # a transient build: its clusterID and triangle count
+            r = tb[s - len(ti)]
+            u, v = rng.random(2, dtype=np.float32)
+            if u + v > 1:
+                u, v = np.float32(1) - u, np.float32(1) - v
+            hits[k] = (int(out["transInstanceIDs"][s - len(ti)]), int(r["clusterID"]),
+                       int(rng.integers(0, int(r["packed"]) & 0x1FF)), (u, v), 0)
+            continue
         inst = int(ids[s])
         if mode[s] == L.RT_CLUSTER_MODE_FULL_CLUSTER:
             cid = int(full[full_slot[s]]["clusterID"])

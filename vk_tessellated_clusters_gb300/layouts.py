@@ -47,6 +47,9 @@ FLAG_RASTER_CULL = 4
 FLAG_WRITE_FULLCLUSTERS = 8
 FLAG_PN = 16
 FLAG_RIPPLE = 32
+FLAG_TRANSIENT_1X = 64
+FLAG_TRANSIENT_2X = 128
+MINI_BATCHSIZE, MINI_TRIANGLES, MINI_VERTICES = 8, 4, 6
 
 DEVERR_LOOKBACK_TIMEOUT = 1
 DEVERR_BAD_CLUSTER = 2
@@ -100,6 +103,13 @@ TessTriangleInfo = _struct([("instanceID", "<u4"), ("clusterID", "<u4"), ("vtxEn
 TemplateInstantiateInfo = _struct([("clusterIdOffset", "<u4"), ("geometryIndexOffset", "<u4"),
                                    ("clusterTemplateAddress", "<u8"), ("vertexBufferAddress", "<u8"),
                                    ("vertexBufferStride", "<u8")], 32)
+
+ClasBuildInfo = _struct([("clusterID", "<u4"), ("clusterFlags", "<u4"), ("packed", "<u4"),
+                         ("baseGeometryIndexAndFlags", "<u4"), ("indexBufferStride", "<u2"),
+                         ("vertexBufferStride", "<u2"), ("geometryIndexAndFlagsBufferStride", "<u2"),
+                         ("opacityMicromapIndexBufferStride", "<u2"), ("indexBuffer", "<u8"), ("vertexBuffer", "<u8"),
+                         ("geometryIndexAndFlagsBuffer", "<u8"), ("opacityMicromapArray", "<u8"),
+                         ("opacityMicromapIndexBuffer", "<u8")], 64)
 
 BlasBuildInfo = _struct([("clusterReferencesCount", "<u4"), ("clusterReferencesStride", "<u4"),
                          ("clusterReferences", "<u8")], 16)

@@ -537,6 +537,14 @@ def instance_records(scene: Scene, addresses: list[dict]) -> np.ndarray:
     return recs
 
 
+def basic_cluster_sizes() -> np.ndarray:
+    """Worst-case CLAS sizes by triangle count (0..64) for transient builds, a
+    synthetic stand-in for the driver's size query the reference uploads
+    (raytracing_cluster_data.cpp:363-386); above the template sizes (128 + 48
+    per triangle) because they cannot use the cluster's topology."""
+    return (192 + 64 * np.arange(65, dtype=np.uint32)).astype(np.uint32)
+
+
 def scene_icosphere(subdivisions: int = 5, map_size: int = 1024, octaves: int = 4, seed: int = 0,
                     displacement_scale: float = 0.05) -> Scene:
     """One icosphere (radius 1) with a value-noise displacement map (plain small config)."""
