@@ -53,7 +53,7 @@ def parse_args():
     p.add_argument("--no-extras", action="store_true", help="skip the plain-path and terrain measurements")
     p.add_argument("--no-tune", action="store_true", help="keep the default launch schedule (no autotuning)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
-    p.add_argument("--profile-case", choices=["batched", "terrain"], default=None,
+    p.add_argument("--profile-case", choices=["batched", "terrain", "transient"], default=None,
                    help="run only `warmup` + `steps` graph frames of one case (for ncu captures) and exit")
     return p.parse_args()
 
@@ -411,7 +411,7 @@ def run_ours(args):
         torch.cuda.empty_cache()
         result["hit_decode"] = hit_decode(torch, local, peak)
         torch.cuda.empty_cache()
-        result["pn_ripple"] = pn_ripple(torch, local, result["config"]["schedule"])
+        result["frame_variants"] = frame_variants(torch, local, result["config"]["schedule"])
         torch.cuda.empty_cache()
         result["animation"] = animation_fwd_bwd(torch, dev, local, result["config"]["schedule"])
     if rank == 0:
@@ -535,22 +535,26 @@ def hit_decode(torch, local, peak, n=1 << 20, reps=20):
             "parity": "tests/test_gpu_parity.py::test_hit_decode_matches_oracle (field-exact vs oracle)"}
 
 
-def pn_ripple(torch, local, schedule, frames=(3, 17, 31)):
+def frame_variants(torch, local, schedule, frames=(3, 17, 31)):
     """The batched scene's frame (256 instances, graph replay, L2 flushed)
-    with PN-triangle displacement and the ripple animation (amplitude 0.02,
-    frequency 8, speed 1.5) against the same frame without them: ms per frame
-    and triangles per second of each."""
+    with the reference's optional shader paths on: PN-triangle displacement
+    with the ripple animation (amplitude 0.02, frequency 8, speed 1.5), 1X and
+    2X transient builds, and all of them (the reference's ray-tracing
+    defaults), against the same frames without: ms per frame and triangles per
+    second of each."""
     import statistics as st
     from vk_tessellated_clusters_gb300 import layouts as L
     from vk_tessellated_clusters_gb300 import scene as S
     from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
     scene = S.scene_batched(256)
     flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    trans = L.FLAG_TRANSIENT_1X | L.FLAG_TRANSIENT_2X
     out = {}
-    for name, extra in (("plain_flags", 0), ("pn_ripple", L.FLAG_PN | L.FLAG_RIPPLE)):
+    for name, extra in (("plain_flags", 0), ("pn_ripple", L.FLAG_PN | L.FLAG_RIPPLE), ("transient", trans),
+                        ("pn_ripple_transient", L.FLAG_PN | L.FLAG_RIPPLE | trans)):
         pipe = TessellationPipeline(scene, L.default_caps(), L.FLAG_CULLING | extra, device=local)
         pipe.set_schedule(schedule)
-        ts, tris = [], []
+        ts, tris, builds = [], [], []
         for f in frames:
             fc = S.frame_constants(S.camera_orbit(f))
             fc["animationRippleAmplitude"], fc["animationRippleFrequency"] = 0.02, 8.0
@@ -566,13 +570,17 @@ def pn_ripple(torch, local, schedule, frames=(3, 17, 31)):
             e1.record()
             torch.cuda.synchronize()
             ts.append(e0.elapsed_time(e1))
-            tris.append(int(pipe.outputs()["readback"]["numTotalTriangles"]))
+            rb = pipe.outputs()["readback"]
+            tris.append(int(rb["numTotalTriangles"]))
+            builds.append(int(rb["numTransBuilds"]))
         assert pipe.device_errors() == 0
         pipe.close()
         ms = st.mean(ts)
-        out[name] = {"ms": ms, "tris_per_s": st.mean(tris) / (ms / 1e3)}
-    out["overhead"] = out["pn_ripple"]["ms"] / out["plain_flags"]["ms"]
-    out["parity"] = "tests/test_gpu_parity.py::test_pn_and_ripple_bit_exact (integers bit-exact, positions within tolerance)"
+        out[name] = {"ms": ms, "tris_per_s": st.mean(tris) / (ms / 1e3), "transient_builds": st.mean(builds)}
+    for name in ("pn_ripple", "transient", "pn_ripple_transient"):
+        out[name]["over_plain_flags"] = out[name]["ms"] / out["plain_flags"]["ms"]
+    out["parity"] = ("tests/test_gpu_parity.py::test_pn_and_ripple_bit_exact, ::test_transient_builds_bit_exact "
+                     "(integers bit-exact, positions within tolerance)")
     return out
 
 
@@ -774,13 +782,16 @@ def run_profile_case(args):
     from vk_tessellated_clusters_gb300 import layouts as L
     from vk_tessellated_clusters_gb300 import scene as S
     from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
-    if args.profile_case == "batched":
+    flags = L.FLAG_CULLING
+    if args.profile_case in ("batched", "transient"):
         scene, caps = S.scene_batched(256), L.default_caps()
         cams = [S.camera_orbit(f) for f in range(args.warmup + args.steps)]
+        if args.profile_case == "transient":
+            flags |= L.FLAG_TRANSIENT_1X | L.FLAG_TRANSIENT_2X
     else:
         scene, caps = S.scene_terrain(), terrain_caps()
         cams = [S.camera_terrain()] * (args.warmup + args.steps)
-    pipe = TessellationPipeline(scene, caps, L.FLAG_CULLING)
+    pipe = TessellationPipeline(scene, caps, flags)
     for i, cam in enumerate(cams):
         pipe.set_cameras(cam, cams[i - 1] if i else cam)
         pipe.build("graph")

@@ -1182,40 +1182,60 @@ __device__ inline void write_cluster_transient(const StageCtx& c, const Classify
       }
     }
     s += __popc(bs);
-    // :675-790 the chunk's 2X batches, kMiniBatch triangles each, in triangle order
-    const u32 nMini = __popc(bm), rank = __popc(bm & ltm);
-    for(u32 m0 = 0; m0 < nMini; m0 += kMiniBatch)
+    // :675-790 the chunk's 2X batches, kMiniBatch triangles each, in triangle
+    // order. Batch q's offsets follow from the chunk's (every batch takes the
+    // same amounts), so all of them are set up and written at once: lane by
+    // lane for the base triangles, the batch's first triangle for the build.
+    const u32 nMini = __popc(bm);
+    if(nMini)
     {
-      const bool member = mini && rank >= m0 && rank < m0 + kMiniBatch;
-      const u32  ntris  = member ? (u32)table_entry(c.table, word & 0xFFFFu).numTriangles : 0u;
-      const u32  incl   = warp_inclusive<u32>(ntris, lane);
-      const u32  numBatchTris = __shfl_sync(0xFFFFFFFFu, incl, 31);
-      const u64  dataSize     = (u64)basic[kMiniBatchTris];
-      const u32  partOffset   = back_alloc(x, y, kMiniPartSlots, k.maxPartTriangles);
-      const bool ok           = fits(kMiniVertexSize, dataSize, partOffset, kMiniPartSlots);
-      if(ok)  // (its vertices are written here, not by the vertex walk)
-      {
-        if(lane == 0)
+      const u32  nb       = (nMini + kMiniBatch - 1) / kMiniBatch;
+      const u64  dataSize = (u64)basic[kMiniBatchTris];
+      const u32  rank = __popc(bm & ltm), q = rank / kMiniBatch, rel = rank % kMiniBatch;
+      // the lanes of this lane's batch, the sum of their table triangles and this one's start
+      const u32  group   = __match_any_sync(0xFFFFFFFFu, mini ? q : 0xFFFFFFFFu);
+      const u32  ntris   = mini ? (u32)table_entry(c.table, word & 0xFFFFu).numTriangles : 0u;
+      const u32  incl    = warp_inclusive<u32>(ntris, lane);
+      const u32  first   = __shfl_sync(0xFFFFFFFFu, incl - ntris, __ffs(group) - 1);
+      const u32  last    = __shfl_sync(0xFFFFFFFFu, incl, 31 - __clz(group));
+      auto       back_of = [&](u32 qq) {  // build.glsl:52-66 for batch qq of the chunk
+        const u32 yq = y + kMiniPartSlots * qq;
+        return ((u64)x + yq + kMiniPartSlots + 1 > k.maxPartTriangles) ? k.maxPartTriangles
+                                                                        : k.maxPartTriangles - yq - kMiniPartSlots;
+      };
+      auto fits_q = [&](u32 qq) {
+        const u32 po = back_of(qq);
+        return !((u64)vo + kMiniVertexSize * (qq + 1) > k.maxGeneratedVertices
+                 || (u64)g + qq + 1 > k.maxGeneratedClusters || d + dataSize * (qq + 1) > maxData
+                 || (u64)po + kMiniPartSlots > k.maxPartTriangles);
+      };
+      for(u32 qq = 0; qq < nb; qq++)  // zero the accepted batches' regions
+        if(fits_q(qq))
         {
-          store_clas_build(reinterpret_cast<tc_ClasBuildInfo*>(b->transBuilds) + tr,
-                           TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED, partOffset, numBatchTris, kMiniBatchVerts,
-                           b->positionTruncateBitCount, b->genVertices + (u64)vo * 12ull);
-          reinterpret_cast<u32*>(b->transInstanceIDs)[tr]      = ci.instanceID;
-          reinterpret_cast<u64*>(b->transClusterAddresses)[tr] = b->genClusterData + d;
+          warp_zero(gvb + ((u64)vo + kMiniVertexSize * qq) * 12, kMiniVertexSize * 3);
+          warp_zero(ptb + (u64)back_of(qq) * kTessInfoBytes, kMiniPartSlots * kTessInfoBytes / 4);
+        }
+      __syncwarp();
+      if(mini && fits_q(q))
+      {
+        const u32 vq = vo + kMiniVertexSize * q, po = back_of(q);
+        if(rel == 0)
+        {
+          const u32 trq = tr + q;
+          store_clas_build(reinterpret_cast<tc_ClasBuildInfo*>(b->transBuilds) + trq,
+                           TC_RT_CLUSTER_MODE_2X_BATCHED_TESSELLATED, po, last - first, kMiniBatchVerts,
+                           b->positionTruncateBitCount, b->genVertices + (u64)vq * 12ull);
+          reinterpret_cast<u32*>(b->transInstanceIDs)[trq]      = ci.instanceID;
+          reinterpret_cast<u64*>(b->transClusterAddresses)[trq] = b->genClusterData + d + dataSize * q;
+          *reinterpret_cast<uint2*>(ptb + (u64)po * kTessInfoBytes) = make_uint2(ci.instanceID, ci.clusterID);
           atomicAdd(&blas[ci.instanceID].clusterReferencesCount, 1u);
           statTrans += 1;
-          statTris += numBatchTris;
+          statTris += last - first;
         }
-        warp_zero(gvb + (u64)vo * 12, kMiniVertexSize * 3);
-        warp_zero(ptb + (u64)partOffset * kTessInfoBytes, kMiniPartSlots * kTessInfoBytes / 4);
-        __syncwarp();
-        if(lane == 0)
-          *reinterpret_cast<uint2*>(ptb + (u64)partOffset * kTessInfoBytes) = make_uint2(ci.instanceID, ci.clusterID);
-        if(member)
-          mini_triangle(c, in, cl, ci.instanceID, tri, word, rank - m0, incl - ntris, vo, partOffset, rp);
-        __syncwarp();
+        mini_triangle(c, in, cl, ci.instanceID, tri, word, rel, incl - ntris - first, vq, po, rp);
       }
-      g += 1, vo += kMiniVertexSize, d += dataSize, tr += 1;
+      __syncwarp();
+      g += nb, vo += kMiniVertexSize * nb, d += dataSize * nb, tr += nb, y += kMiniPartSlots * nb;
     }
   }
 }
@@ -1303,6 +1323,9 @@ __global__ void __launch_bounds__(kBlock, 4) k_classify_write_transient(StageCtx
                               statTrans, statTris);
     __syncthreads();
   }
+  statTemp  = __reduce_add_sync(0xFFFFFFFFu, statTemp);
+  statTrans = __reduce_add_sync(0xFFFFFFFFu, statTrans);
+  statTris  = __reduce_add_sync(0xFFFFFFFFu, statTris);
   if(lane == 0)
   {
     if(statTemp)
