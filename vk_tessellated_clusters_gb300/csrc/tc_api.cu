@@ -288,7 +288,8 @@ u32 frame_begin_grid(const tc_context* ctx, const tc_frame_args* a)
 // kBlasSetupFusedMax instances)
 uint64_t frame_launches(const tc_frame_args* a)
 {
-  return kFrameFixedLaunches + split_passes(a->caps.splitFactor) - (a->numInstances <= kBlasSetupFusedMax ? 1 : 0);
+  return kFrameFixedLaunches + split_passes(a->caps.splitFactor) - (a->numInstances <= kBlasSetupFusedMax ? 1 : 0)
+         + ((a->flags & TC_FLAG_TRANSIENT_2X) ? 1 : 0);  // the 2X batches' vertices
 }
 
 u32 insert_grid(const tc_context* ctx, const tc_frame_args* a)
@@ -798,7 +799,7 @@ tc_status tc_cluster_classify(tc_context* ctx, const tc_frame_args* a, uint32_t 
   TC_CHECK_CUDA(launch_classify_full_vertices(c, classify_buffers(ctx),
                                               std::min(a->totalClusters, a->caps.maxVisibleClusters), ctx->numSMs,
                                               4, reinterpret_cast<cudaStream_t>(stream)));
-  ctx->launches += 3;
+  ctx->launches += (a->flags & TC_FLAG_TRANSIENT_2X) ? 4 : 3;
   return TC_OK;
 }
 

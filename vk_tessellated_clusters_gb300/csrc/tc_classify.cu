@@ -939,12 +939,10 @@ __device__ __forceinline__ void store_clas_build(tc_ClasBuildInfo* dst, u32 mode
   d[3]     = make_uint4(0u, 0u, 0u, 0u);
 }
 
-// cluster_classify.comp.glsl:810-903: one base triangle of a 2X batch (its
-// word's config and corner rotation): its 3 to 6 vertices at its batch slot,
-// then per table triangle the u16 map entry and three u8 indices
-__device__ inline void mini_triangle(const StageCtx& c, const tc_RenderInstance* in, const tc_Cluster& cl, u32 inst,
-                                     u32 tri, u32 word, u32 rel, u32 baseTris, u32 vertexOffset, u32 partOffset,
-                                     const RippleParams& rp)
+// cluster_classify.comp.glsl:810-878: one base triangle of a 2X batch (its
+// word's config and corner rotation): its 3 to 6 vertices at its batch slot
+__device__ inline void mini_vertices(const StageCtx& c, const tc_RenderInstance* in, const tc_Cluster& cl, u32 inst,
+                                     u32 tri, u32 word, u32 rel, u32 vertexOffset, const RippleParams& rp)
 {
   tc_SceneBuilding* b   = c.build;
   const u32         cfg = word & 0xFFFFu;
@@ -1001,6 +999,15 @@ __device__ inline void mini_triangle(const StageCtx& c, const tc_RenderInstance*
     float* d = gv + 3 * ((u64)vertexOffset + rel * TC_2X_MINI_VERTICES + vert);
     d[0] = pos.x, d[1] = pos.y, d[2] = pos.z;
   }
+}
+
+// the same base triangle's u16 map entries and u8 indices (:880-903)
+__device__ inline void mini_indices(const StageCtx& c, u32 tri, u32 word, u32 rel, u32 baseTris, u32 vertexOffset,
+                                    u32 partOffset)
+{
+  tc_SceneBuilding*       b   = c.build;
+  const u32               cfg = word & 0xFFFFu;
+  const tc_TessTableEntry e   = table_entry(c.table, cfg);
   const u32 pf  = (word >> kWordFactorShift) & 7;
   uint8_t*  idx = reinterpret_cast<uint8_t*>(b->genVertices) + ((u64)vertexOffset + kMiniBatchVerts) * 12;
   uint16_t* map = reinterpret_cast<uint16_t*>(reinterpret_cast<uint8_t*>(b->partTriangles) + (u64)partOffset * kTessInfoBytes
@@ -1131,14 +1138,18 @@ __device__ inline void write_cluster_transient(const StageCtx& c, const Classify
   }
   else if(lane == 0)
     cs.fullRecs[v] = make_uint2(kRejected, 0u);
+  u32 miniChunk[4] = {0u, 0u, 0u, 0u};  // per chunk: first batch vertex, accepted batches
   if(full)
+  {
+    if(lane == 0)
+      reinterpret_cast<uint4*>(cs.counts)[v] = make_uint4(0u, 0u, 0u, 0u);
     return;
+  }
 
   // ---- :543-905 the other triangles, one 32-triangle chunk at a time -------------
   const u32*   tw  = cs.triWords + (u64)v * TC_MAX_CLUSTER_TRIANGLES;
   tc_TessTriangleInfo* splits = reinterpret_cast<tc_TessTriangleInfo*>(b->splitTriangles);
   tc_TessTriangleInfo* parts  = reinterpret_cast<tc_TessTriangleInfo*>(b->partTriangles);
-  const RippleParams rp = ripple_params(*c.view, (c.flags & TC_FLAG_RIPPLE) != 0);
   for(u32 t0 = 0; t0 < nt; t0 += 32)
   {
     const u32  tri   = t0 + lane;
@@ -1232,12 +1243,23 @@ __device__ inline void write_cluster_transient(const StageCtx& c, const Classify
           statTrans += 1;
           statTris += last - first;
         }
-        mini_triangle(c, in, cl, ci.instanceID, tri, word, rel, incl - ntris - first, vq, po, rp);
+        mini_indices(c, tri, word, rel, incl - ntris - first, vq, po);
+      }
+      // for k_classify_mini_vertices: the chunk's first batch vertex and its accepted batches
+      u32 okMask = 0;
+      for(u32 qq = 0; qq < nb; qq++)
+        okMask |= fits_q(qq) ? 1u << qq : 0u;
+      if(lane == 0)
+      {
+        miniChunk[2 * (t0 >> 5)]     = vo;
+        miniChunk[2 * (t0 >> 5) + 1] = okMask;
       }
       __syncwarp();
       g += nb, vo += kMiniVertexSize * nb, d += dataSize * nb, tr += nb, y += kMiniPartSlots * nb;
     }
   }
+  if(lane == 0)  // (counts of this cluster were read into shared memory before)
+    reinterpret_cast<uint4*>(cs.counts)[v] = make_uint4(miniChunk[0], miniChunk[1], miniChunk[2], miniChunk[3]);
 }
 
 // The offsets at which block `blockIdx.x` of the write launch starts, with
@@ -1355,6 +1377,51 @@ __global__ void __launch_bounds__(kBlock, 4) k_classify_write_transient(StageCtx
     }
     if(c.fuseSetup != kNoSetup)
       build_setup_apply(c, c.fuseSetup);
+  }
+}
+
+// cluster_classify.comp.glsl:810-878: the vertices of the accepted 2X
+// batches, from what k_classify_write_transient left per cluster (each
+// chunk's first batch vertex and accepted batches, in place of its counts).
+// One warp per cluster, one lane per base triangle.
+__global__ void __launch_bounds__(kBlock, 4) k_classify_mini_vertices(StageCtx c, ClassifyScratch cs)
+{
+  stage_prologue();
+  __shared__ u32        s_range[2];
+  __shared__ FlatStarts s_starts;
+  if(threadIdx.x == 0)
+    window_range(c, s_range[0], s_range[1]);
+  __syncthreads();
+  const u32*            starts = stage_flat_starts(c, s_starts);
+  const u32             lane = threadIdx.x & 31, ltm = (1u << lane) - 1u;
+  const u32             begin = s_range[0];
+  const u32             n     = min(s_range[1] - s_range[0], c.scratch.itemCapacity);
+  const tc_ClusterInfo* vis   = reinterpret_cast<const tc_ClusterInfo*>(c.build->visibleClusters);
+  const RippleParams    rp    = ripple_params(*c.view, (c.flags & TC_FLAG_RIPPLE) != 0);
+  const u32             nwarps = (gridDim.x * blockDim.x) >> 5;
+  for(u32 v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nwarps)
+  {
+    const uint4 m = reinterpret_cast<const uint4*>(cs.counts)[v];
+    if((m.y | m.w) == 0)
+      continue;
+    const tc_ClusterInfo     ci = visible_cluster(c, starts, vis, begin + v);
+    const tc_RenderInstance* in = c.instances + ci.instanceID;
+    const tc_Cluster         cl = reinterpret_cast<const tc_Cluster*>(in->clusters)[ci.clusterID];
+    const u32                nt = min((u32)cl.numTriangles, TC_MAX_CLUSTER_TRIANGLES);
+    const u32*               tw = cs.triWords + (u64)v * TC_MAX_CLUSTER_TRIANGLES;
+    for(u32 q = 0; q < 2; q++)
+    {
+      const u32 ok = q ? m.w : m.y, vo = q ? m.z : m.x;
+      if(ok == 0)
+        continue;
+      const u32  tri  = 32 * q + lane;
+      const u32  word = tri < nt ? tw[tri] : 0u;
+      const bool mini = tri < nt && (word & kWordMini);
+      const u32  rank = __popc(__ballot_sync(0xFFFFFFFFu, mini) & ltm);
+      const u32  qb   = rank / kMiniBatch;
+      if(mini && ((ok >> qb) & 1u))
+        mini_vertices(c, in, cl, ci.instanceID, tri, word, rank % kMiniBatch, vo + kMiniVertexSize * qb, rp);
+    }
   }
 }
 
@@ -1489,9 +1556,14 @@ cudaError_t launch_classify_full_vertices(const StageCtx& c, const ClassifyBuffe
   // every warp of the grid takes a share of the slots
   const u32 grid = std::max(1u, std::min((maxClusters + kWarps - 1) / kWarps, numSMs * std::max(1u, blocksPerSM)));
   // register budget from the requested residency: 4 or less -> 64, 5-6 -> 40, 7 and more -> 32
-  return blocksPerSM >= 7   ? launch_pdl(k_classify_full_vertices<8>, grid, kBlock, s, c, cs)
-         : blocksPerSM >= 5 ? launch_pdl(k_classify_full_vertices<6>, grid, kBlock, s, c, cs)
-                            : launch_pdl(k_classify_full_vertices<4>, grid, kBlock, s, c, cs);
+  cudaError_t e = blocksPerSM >= 7   ? launch_pdl(k_classify_full_vertices<8>, grid, kBlock, s, c, cs)
+                  : blocksPerSM >= 5 ? launch_pdl(k_classify_full_vertices<6>, grid, kBlock, s, c, cs)
+                                     : launch_pdl(k_classify_full_vertices<4>, grid, kBlock, s, c, cs);
+  if(e != cudaSuccess || !(c.flags & TC_FLAG_TRANSIENT_2X))
+    return e;
+  // the 2X batches' vertices (one warp per visible cluster of the window)
+  const u32 miniGrid = std::max(1u, std::min((maxClusters + kWarps - 1) / kWarps, numSMs * 8));
+  return launch_pdl(k_classify_mini_vertices, miniGrid, kBlock, s, c, cs);
 }
 
 u32 classify_max_blocks(u32 maxClusters) { return std::max(1u, (maxClusters + kWarps - 1) / kWarps); }
