@@ -669,6 +669,47 @@ typedef struct tc_base_hit {
 tc_status tc_decode_hits(tc_context* ctx, const tc_frame_args* args, const tc_hit* hits, uint32_t count,
                          tc_base_hit* out, void* stream);
 
+/* ---- raster batching --------------------------------------------------------- */
+
+/* render_raster_clusters_batched.task.glsl:115-215 and .mesh.glsl:141-435 as
+ * compute: the frame's part triangles, 32 at a time (one task workgroup), are
+ * packed into batches of consecutive parts of at most TC_RASTER_BATCH_VERTICES
+ * vertices and TC_RASTER_BATCH_TRIANGLES triangles (the task shader's linear
+ * fill); every part's tessellated vertices are displaced, taken to world and
+ * clip space and written with its triangles' batch-local indices and
+ * primitive IDs, like the mesh shader's outputs. Vertex and triangle arrays are
+ * in part order (a batch's are contiguous). */
+#define TC_RASTER_BATCH_VERTICES 96u  /* shaderio_scene.h:57-58 */
+#define TC_RASTER_BATCH_TRIANGLES 121u
+
+typedef struct tc_raster_batch {
+  uint32_t firstPart;     /* index into SceneBuilding.partTriangles */
+  uint32_t partCount;
+  uint32_t firstVertex;   /* into clipPositions / worldPositions */
+  uint32_t numVertices;
+  uint32_t firstTriangle; /* into indices / primitiveIDs */
+  uint32_t numTriangles;
+} tc_raster_batch;
+
+typedef struct tc_raster_outputs {
+  uint64_t batches;        /* tc_raster_batch[maxBatches] (device) */
+  uint64_t counts;         /* uint32_t[3] (device): batches, vertices, triangles written */
+  uint64_t clipPositions;  /* float[4 * maxVertices]: viewProjMatrix * world position (gl_Position) */
+  uint64_t worldPositions; /* float[3 * maxVertices] (the mesh shader's wPos) */
+  uint64_t indices;        /* uint8_t[3 * maxTriangles]: vertex indices local to the batch */
+  uint64_t primitiveIDs;   /* uint32_t[maxTriangles]: gl_PrimitiveID ((triangleID & 0xFF) | (partID | 1) << 8) */
+  uint32_t maxBatches;
+  uint32_t maxVertices;
+  uint32_t maxTriangles;
+  uint32_t _pad;
+} tc_raster_outputs;
+
+/* Batches of the parts of the frame last built in `args` (ray-tracing or
+ * raster frames alike). Totals beyond the output capacities are counted but
+ * not written (TC_DEVERR_CAPACITY in the device error word). The readback is
+ * not touched (the raster path's statistics would count the frame twice). */
+tc_status tc_raster_batches(tc_context* ctx, const tc_frame_args* args, const tc_raster_outputs* out, void* stream);
+
 /* ---- diagnostics ------------------------------------------------------------- */
 
 /* Synchronously read (and clear) the device error word. */
@@ -691,6 +732,8 @@ static_assert(sizeof(tc_RenderInstance) == 192, "RenderInstance");
 static_assert(sizeof(tc_ClusterInfo) == 8, "ClusterInfo_size (shaderio_building.h:68)");
 static_assert(sizeof(tc_TessTriangleInfo) == 24, "TessTriangleInfo_size (shaderio_building.h:92)");
 static_assert(sizeof(tc_ClasBuildInfo) == 64, "ClasBuildInfo");
+static_assert(sizeof(tc_raster_batch) == 24, "raster batch");
+static_assert(sizeof(tc_raster_outputs) == 64, "raster outputs");
 static_assert(sizeof(tc_TemplateInstantiateInfo) == 32, "TemplateInstantiateInfo");
 static_assert(sizeof(tc_BlasBuildInfo) == 16, "BlasBuildInfo");
 static_assert(sizeof(tc_SceneBuilding) == 368, "SceneBuilding");

@@ -66,6 +66,7 @@ def lib():
         l.tco_generate_vertices_f64_params.restype = ctypes.c_uint64
         l.tco_backward_f64.argtypes = [P(TcoTable), P(L.FrameArgs), vp, vp, vp, vp]
         l.tco_decode_hits.argtypes = [P(TcoTable), P(L.FrameArgs), vp, u32, vp]
+        l.tco_raster_batches.argtypes = [P(TcoTable), P(L.FrameArgs), P(L.RasterOutputs)]
         _lib = l
     return _lib
 
@@ -114,6 +115,12 @@ class Oracle:
         self.lib.tco_decode_hits(ctypes.byref(self.table), ctypes.byref(state.args), hits.ctypes.data, len(hits),
                                  out.ctypes.data)
         return out
+
+    def raster_batches(self, state: FrameState) -> dict:
+        """tc_raster_batches restated on the CPU for the frame in `state`."""
+        ro, _ = state.raster_outputs()
+        self.lib.tco_raster_batches(ctypes.byref(self.table), ctypes.byref(state.args), ctypes.byref(ro))
+        return state.raster_results()
 
     def vertices_f64(self, state: FrameState, count: int) -> np.ndarray:
         out = np.zeros((count, 3), np.float64)

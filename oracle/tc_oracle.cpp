@@ -1326,6 +1326,148 @@ void tco_decode_hits(const tco_table* t, const tc_frame_args* a, const tc_hit* h
   }
 }
 
+// render_raster_clusters_batched.task.glsl:115-215: per group of 32 parts the
+// linear fill into batches (a batch ends at the last part whose running
+// vertex and triangle sums both stay within the limits), then
+// render_raster_clusters_batched.mesh.glsl:141-435: every part's vertices
+// (the instantiation's displaced position, then world and clip space) and its
+// table triangles with the batch-local indices and primitive IDs.
+void tco_raster_batches(const tco_table* t, const tc_frame_args* a, const tc_raster_outputs* out)
+{
+  Ctx                        c(a);
+  const tc_SceneBuilding*    b      = c.b;
+  const uint32_t             nparts = std::min(b->partTriangleCounter, a->caps.maxPartTriangles);
+  const tc_TessTriangleInfo* parts  = P<const tc_TessTriangleInfo>(b->partTriangles);
+  tc_raster_batch*           batches = P<tc_raster_batch>(out->batches);
+  float*                     clip   = P<float>(out->clipPositions);
+  float*                     world  = P<float>(out->worldPositions);
+  uint8_t*                   idx    = P<uint8_t>(out->indices);
+  uint32_t*                  prim   = P<uint32_t>(out->primitiveIDs);
+  const bool                 visTriangles = c.view->visualize == TC_VISUALIZE_TRIANGLES;
+  const bool                 pn = (a->flags & TC_FLAG_PN) != 0, rip = (a->flags & TC_FLAG_RIPPLE) != 0;
+  uint32_t                   nb = 0, nv = 0, ntr = 0;
+  for(uint32_t g0 = 0; g0 < nparts; g0 += 32)
+  {
+    const uint32_t local = std::min(32u, nparts - g0);
+    uint32_t       sumV[32], sumT[32];
+    uint32_t       accV = 0, accT = 0;
+    for(uint32_t i = 0; i < 32; i++)
+    {
+      uint32_t v = TC_RASTER_BATCH_VERTICES, tr = TC_RASTER_BATCH_TRIANGLES;
+      if(i < local)
+      {
+        const tc_TessTableEntry& e = t->entries[cfgIndex(parts[g0 + i].subTriangle.triangleID_config >> 16)];
+        v = e.numVertices, tr = e.numTriangles;
+      }
+      accV += v, accT += tr;
+      sumV[i] = accV, sumT[i] = accT;
+    }
+    uint32_t start = 0, lastV = 0, lastT = 0, left = local, batchIndex = 0;
+    while(left != 0 && batchIndex < 32)
+    {
+      int end = -1;
+      for(uint32_t i = 0; i < 32; i++)  // unsigned differences: parts before the batch do not fit
+        if(sumV[i] - lastV <= TC_RASTER_BATCH_VERTICES && sumT[i] - lastT <= TC_RASTER_BATCH_TRIANGLES)
+          end = (int)i;
+      const uint32_t count = 1 + (uint32_t)end - start;
+      if(nb < out->maxBatches)
+      {
+        tc_raster_batch& r = batches[nb];
+        r.firstPart        = g0 + start;
+        r.partCount        = std::min(count, left);
+        r.firstVertex      = nv + (start ? sumV[start - 1] : 0);
+        r.firstTriangle    = ntr + (start ? sumT[start - 1] : 0);
+        r.numVertices      = sumV[end] - (start ? sumV[start - 1] : 0);
+        r.numTriangles     = sumT[end] - (start ? sumT[start - 1] : 0);
+      }
+      nb++;
+      lastV = sumV[end], lastT = sumT[end];
+      start = (uint32_t)end + 1;
+      left -= std::min(count, left);
+      batchIndex++;
+    }
+    // the parts' vertices and triangles (group-local prefix sums, then the
+    // running totals of the groups before)
+    for(uint32_t i = 0; i < local; i++)
+    {
+      const tc_TessTriangleInfo& info  = parts[g0 + i];
+      const uint32_t             cfg   = info.subTriangle.triangleID_config >> 16;
+      const uint32_t             triID = info.subTriangle.triangleID_config & 0xFFFF;
+      const tc_TessTableEntry&   e     = t->entries[cfgIndex(cfg)];
+      const uint32_t             v0    = nv + sumV[i] - e.numVertices;
+      const uint32_t             t0    = ntr + sumT[i] - e.numTriangles;
+      // the batch-local first vertex of this part: vertices since its batch's first part
+      uint32_t batchFirstV = 0;
+      for(uint32_t q = 0, s0 = 0, lv = 0, lt = 0; q < 32 && s0 <= i; q++)
+      {
+        int end = -1;
+        for(uint32_t j = 0; j < 32; j++)
+          if(sumV[j] - lv <= TC_RASTER_BATCH_VERTICES && sumT[j] - lt <= TC_RASTER_BATCH_TRIANGLES)
+            end = (int)j;
+        if(i <= (uint32_t)end)
+        {
+          batchFirstV = s0 ? sumV[s0 - 1] : 0;
+          break;
+        }
+        lv = sumV[end], lt = sumT[end], s0 = (uint32_t)end + 1;
+      }
+      const tc_RenderInstance&      in = c.inst[info.cluster.instanceID];
+      const tc_Cluster&             cl = P<const tc_Cluster>(in.clusters)[info.cluster.clusterID];
+      const uint8_t*                lt = P<const uint8_t>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
+      const tc_DisplacementTexture* tx = instanceTexture(a, in);
+      f3                            bb[3], bpos[3], bnrm[3];
+      f2                            buv[3];
+      uint32_t                      partID = 0;
+      for(int j = 0; j < 3; j++)
+      {
+        uint32_t vi = cl.firstLocalVertex + lt[triID * 3 + j];
+        bb[j]       = decodeBary(info.subTriangle.vtxEncoded[j]);
+        bpos[j]     = ld3(in.positions, vi);
+        bnrm[j]     = normalize3(ld3(in.normals, vi));
+        buv[j]      = P<const f2>(in.texcoords)[vi];
+        partID ^= (info.subTriangle.vtxEncoded[j] >> 20) | ((info.subTriangle.vtxEncoded[j] >> 4) & 0xFFF);
+      }
+      BasePN basePN;
+      if(pn)
+        basePN = setupPN(bpos, bnrm);
+      const float* vp = c.view->viewProjMatrix.m;
+      for(uint32_t vert = 0; vert < e.numVertices; vert++)
+      {
+        if(v0 + vert >= out->maxVertices)
+          break;
+        f3 w   = interp3(bb, cfgVertex(t, cfg, vert));
+        f3 pos = pn ? getPN(basePN, w) : interp3(bpos, w);
+        if(tx)
+          pos = displace(pos, interp3(bnrm, w), interp2(buv, w), tx, in, *c.view);
+        if(rip)
+          pos = ripple(pos, info.cluster.instanceID, in.geoHi.w, *c.view);
+        const f3 wp = xform_point(in.worldMatrix.m, pos);
+        const f3 cp = xform_point(vp, wp);
+        float*   wo = world + 3 * uint64_t(v0 + vert);
+        float*   co = clip + 4 * uint64_t(v0 + vert);
+        wo[0] = wp.x, wo[1] = wp.y, wo[2] = wp.z;
+        co[0] = cp.x, co[1] = cp.y, co[2] = cp.z;
+        co[3] = ((vp[3] * wp.x + vp[7] * wp.y) + vp[11] * wp.z) + vp[15];
+      }
+      for(uint32_t tri = 0; tri < e.numTriangles; tri++)
+      {
+        if(t0 + tri >= out->maxTriangles)
+          break;
+        uint32_t ct[3];
+        cfgTriangle(t, cfg, tri, ct);
+        const uint32_t vs = v0 - nv - batchFirstV;  // the part's first vertex within its batch
+        for(int j = 0; j < 3; j++)
+          idx[3 * uint64_t(t0 + tri) + j] = (uint8_t)(ct[j] + vs);
+        const uint32_t pid   = visTriangles ? tri * 3 : partID;
+        prim[t0 + tri]       = (triID & 0xFF) | ((pid | 1u) << 8);
+      }
+    }
+    nv += sumV[local - 1], ntr += sumT[local - 1];
+  }
+  uint32_t* counts = P<uint32_t>(out->counts);
+  counts[0] = nb, counts[1] = nv, counts[2] = ntr;
+}
+
 int tco_frame_build(const tco_table* t, const tc_frame_args* a, int numThreads, uint32_t* partRunStarts)
 {
   tc_SceneBuilding* b = P<tc_SceneBuilding>(a->build);

@@ -70,6 +70,8 @@ void tco_triangle_instantiate(const tco_table* t, const tc_frame_args* args, int
 void tco_blas_setup_insertion(const tc_frame_args* args);
 void tco_blas_clusters_insert(const tc_frame_args* args);
 /* hit-time decode of the frame in `args` (see tc_decode_hits) */
+/* render_raster_clusters_batched.task.glsl:115-215 + .mesh.glsl:141-435 (tc_raster_batches) */
+void tco_raster_batches(const tco_table* t, const tc_frame_args* args, const tc_raster_outputs* out);
 void tco_decode_hits(const tco_table* t, const tc_frame_args* args, const tc_hit* hits, uint32_t count,
                      tc_base_hit* out);
 

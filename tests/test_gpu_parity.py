@@ -400,3 +400,43 @@ def test_transient_hit_decode_matches_oracle(oracle):
         assert (got["status"][:20000] == L.HIT_OK).all()
         assert got.tobytes() == want.tobytes()
         pipe.close()
+
+
+@pytest.mark.parametrize("case", ["icosphere", "batched_pn_ripple", "close_splits", "transient"])
+def test_raster_batches_match_oracle(oracle, case):
+    """tc_raster_batches (render_raster_clusters_batched task + mesh shaders as
+    compute): batch records, counts, batch-local indices and primitive IDs
+    bit-exact; world and clip positions within the vertex tolerance (scaled
+    by the instances' transforms)."""
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    flags, last = FLAGS, None
+    if case == "icosphere":
+        sc, cam = S.scene_icosphere(), S.frame_constants(S.camera_icosphere())
+    elif case == "batched_pn_ripple":
+        sc, cam, last = S.scene_batched(num_instances=24, map_size=128), _ripple_constants(S.camera_orbit(5)), S.camera_orbit(4)
+        cam["visualize"] = L.VISUALIZE_TRIANGLES
+        flags |= L.FLAG_PN | L.FLAG_RIPPLE
+    elif case == "close_splits":
+        sc = S.scene_icosphere(subdivisions=3, map_size=256)
+        cam = S.frame_constants(S.Camera(eye=(0.0, 0.0, 1.08), center=(0.0, 0.0, 0.0), tess_rate_pixels=1.0,
+                                         near=0.01, far=10.0))
+    else:
+        sc, cam, last = S.scene_batched(num_instances=24, map_size=128), S.frame_constants(S.camera_orbit(0)), S.camera_orbit(59)
+        flags |= TRANSIENT
+    caps = small_caps(maxSplitTriangles=1 << 17, maxPartTriangles=1 << 19, maxGeneratedVertices=1 << 23)
+    ref_state, _ = oracle.frame(sc, cam, caps, flags, camera_last=last)
+    want = oracle.raster_batches(ref_state)
+    pipe = TessellationPipeline(sc, caps, flags)
+    pipe.set_cameras(cam, last)
+    pipe.build("graph")
+    got = pipe.raster_batches()
+    assert pipe.device_errors() == 0
+    assert got["counts"] == want["counts"] and want["counts"][0] > 100
+    for f in ("batches", "indices", "primitiveIDs"):
+        assert got[f].tobytes() == want[f].tobytes(), f
+    scale = max(float(np.abs(np.asarray(i.world)[:3, :3]).sum(axis=1).max()) for i in sc.instances)
+    tol = vertex_tolerance(sc) * max(1.0, scale)
+    assert np.abs(got["worldPositions"].astype(np.float64) - want["worldPositions"]).max() <= tol
+    cm = float(np.abs(want["clipPositions"]).max())
+    assert np.abs(got["clipPositions"].astype(np.float64) - want["clipPositions"]).max() <= 1e-5 * cm + 1e-4
+    pipe.close()

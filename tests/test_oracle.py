@@ -413,3 +413,57 @@ def test_transient_builds_restatement(oracle, which):
         n = int(bi[i]["clusterReferencesCount"])
         mine = out["transClusterAddresses"][out["transInstanceIDs"] == i]
         assert (lists[start + n - len(mine):start + n] == mine).all()
+
+
+def test_raster_batches_restatement(oracle):
+    """Raster batching (render_raster_clusters_batched.task.glsl:115-215,
+    .mesh.glsl:141-435): per group of 32 parts the batches are consecutive,
+    within 96 vertices and 121 triangles, and maximal (the next part would not
+    fit); vertex and triangle arrays follow part order; indices stay inside
+    their batch; world positions are the instantiation's vertices taken to
+    world space and clip positions those taken through viewProjMatrix."""
+    sc = S.scene_batched(num_instances=8, map_size=64)
+    cam = S.camera_orbit(7)
+    caps = L.default_caps(visible_bits=14, part_bits=15, split_bits=12, vertex_bits=20, megs=64)
+    st, _ = oracle.frame(sc, cam, caps, L.FLAG_CULLING | L.FLAG_WRITE_FULLCLUSTERS)
+    out = st.outputs(oracle.entries)
+    r = oracle.raster_batches(st)
+    parts = out["partTriangles"]
+    n = len(parts)
+    assert n > 100
+    cfg = (parts["triangleID_config"] >> 16) & 0x7FFF
+    nv = oracle.entries[cfg]["numVertices"].astype(np.int64)
+    nt = oracle.entries[cfg]["numTriangles"].astype(np.int64)
+    nb, tv, tt = r["counts"]
+    assert tv == nv.sum() and tt == nt.sum() and nb == len(r["batches"])
+    b = r["batches"]
+    assert (b["numVertices"] <= 96).all() and (b["numTriangles"] <= 121).all()
+    assert b["firstPart"][0] == 0 and (np.diff(b["firstPart"].astype(np.int64)) == b["partCount"][:-1]).all()
+    assert int(b["firstPart"][-1]) + int(b["partCount"][-1]) == n
+    cv, ct = np.concatenate([[0], np.cumsum(nv)]), np.concatenate([[0], np.cumsum(nt)])
+    for rec in b:
+        p0, pc = int(rec["firstPart"]), int(rec["partCount"])
+        assert p0 // 32 == (p0 + pc - 1) // 32  # within one group of 32
+        assert rec["firstVertex"] == cv[p0] and rec["numVertices"] == cv[p0 + pc] - cv[p0]
+        assert rec["firstTriangle"] == ct[p0] and rec["numTriangles"] == ct[p0 + pc] - ct[p0]
+        nxt = p0 + pc
+        if nxt < n and nxt % 32:  # maximal: the next part of the group does not fit
+            assert cv[nxt + 1] - cv[p0] > 96 or ct[nxt + 1] - ct[p0] > 121
+        tri = r["indices"][int(rec["firstTriangle"]):int(rec["firstTriangle"]) + int(rec["numTriangles"])]
+        assert (tri < rec["numVertices"]).all()
+    # positions: the part instantiations' vertices (object space) taken to world and clip space
+    ti = out["tempInstantiations"]
+    sel = np.flatnonzero((ti["clusterIdOffset"] >> 30) == L.RT_CLUSTER_MODE_SINGLE_TESSELLATED)[:50]
+    for j in sel:
+        p = int(ti[j]["clusterIdOffset"]) & 0x3FFFFFFF
+        v0 = int(ti[j]["vertexBufferAddress"]) // 12
+        obj = out["genVertices"][v0:v0 + nv[p]].astype(np.float64)
+        inst = sc.instances[int(out["tempInstanceIDs"][j])]
+        m = np.asarray(inst.world, np.float64)  # row-major: p' = m @ (p, 1)
+        w = r["worldPositions"][cv[p]:cv[p + 1]].astype(np.float64)
+        np.testing.assert_allclose(w, obj @ m[:3, :3].T + m[:3, 3], rtol=0, atol=1e-4)
+        fc = S.frame_constants(cam)
+        vp = np.asarray(fc["viewProjMatrix"]["m"] if fc["viewProjMatrix"].dtype.names else fc["viewProjMatrix"],
+                        np.float64).reshape(4, 4).T
+        c = r["clipPositions"][cv[p]:cv[p + 1]].astype(np.float64)
+        np.testing.assert_allclose(c, np.c_[w, np.ones(len(w))] @ vp.T, rtol=1e-5, atol=1e-4)

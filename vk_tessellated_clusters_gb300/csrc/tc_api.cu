@@ -49,6 +49,7 @@ struct Plan
   size_t runOffset;   // run starts (u32 x kMaxRuns+2)
   u32    classifyCap; // clusters the classify scratch holds
   size_t clsCountsOffset, clsTriWordsOffset, clsBlockSumsOffset, clsFullRecsOffset;
+  size_t rasterOffset;
   size_t partVertexOffset;  // u32 per part triangle
   size_t splitBaseOffset;   // 9 floats per split item: its base triangle's world positions
   size_t instOffset;  // instance cluster prefix (u32 x maxInstances+1)
@@ -183,6 +184,8 @@ Plan make_plan(const tc_context_desc& d)
   off                 = align_up(off + (size_t)std::max(1u, k.maxPartTriangles) * 4, 256);
   p.splitBaseOffset   = off;
   off                 = align_up(off + (size_t)std::max(1u, k.maxSplitTriangles) * 36, 256);
+  p.rasterOffset      = off;  // raster batching: per group of 32 parts its counts, then offsets
+  off                 = align_up(off + (size_t)ceil_div(std::max(1u, k.maxPartTriangles), 32) * 16, 256);
   p.totalBytes        = off;
   return p;
 }
@@ -973,6 +976,21 @@ tc_status tc_decode_hits(tc_context* ctx, const tc_frame_args* a, const tc_hit* 
   StageCtx c = base_ctx(ctx, a);
   TC_CHECK_CUDA(launch_decode_hits(c, hits, count, out, reinterpret_cast<cudaStream_t>(stream)));
   ctx->launches += count ? 1 : 0;
+  return TC_OK;
+}
+
+tc_status tc_raster_batches(tc_context* ctx, const tc_frame_args* a, const tc_raster_outputs* out, void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  if(!out || !out->batches || !out->counts || !out->clipPositions || !out->worldPositions || !out->indices
+     || !out->primitiveIDs)
+    return TC_ERR_INVALID_ARG;
+  StageCtx c = base_ctx(ctx, a);
+  TC_CHECK_CUDA(launch_raster_batches(c, reinterpret_cast<uint4*>(ctx->dScratch + ctx->plan.rasterOffset), *out,
+                                      a->caps.maxPartTriangles, ctx->numSMs, reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += 3;
   return TC_OK;
 }
 

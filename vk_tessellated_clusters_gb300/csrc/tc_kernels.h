@@ -84,6 +84,9 @@ u32         instantiate_alloc_tiles(u32 maxParts);
 cudaError_t launch_blas_setup_insertion(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 cudaError_t launch_blas_clusters_insert(const StageCtx& c, u32* segStart, u32* segEnd, u32 stride, u32 grid,
                                         cudaStream_t s);
+// raster batching of the frame's parts; `groups`: one uint4 per 32 parts
+cudaError_t launch_raster_batches(const StageCtx& c, uint4* groups, const tc_raster_outputs& o, u32 maxParts,
+                                  u32 numSMs, cudaStream_t s);
 cudaError_t launch_generate_vertices(const StageCtx& c, u32 grid, cudaStream_t s);
 cudaError_t launch_instantiate_backward(const StageCtx& c, const float* gradVertices, const tc_GradTargets* targets,
                                         float* const* gradTexels, u32 grid, cudaStream_t s);

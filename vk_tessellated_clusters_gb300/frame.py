@@ -190,6 +190,36 @@ class FrameState:
         self.args.flags = self.flags
         self.args.caps = L.caps_from(self.caps)
 
+    def raster_outputs(self, parts: int | None = None):
+        """Output buffers for tc_raster_batches, sized for `parts` part
+        triangles (default: the built frame's; at most one batch per part, 78
+        vertices and 121 triangles each)."""
+        if parts is None:
+            parts = min(int(self.scene_building()["partTriangleCounter"]), self.caps["maxPartTriangles"])
+        n = max(1, int(parts))
+        if getattr(self, "_raster", None) is None or self._raster_parts < n:
+            self._raster_parts = n
+            mv, mt = 78 * n, L.RASTER_BATCH_TRIANGLES * n
+            bufs = {"batches": self.mem.alloc(L.RasterBatch.itemsize * n), "counts": self.mem.alloc(16),
+                    "clipPositions": self.mem.alloc(16 * mv), "worldPositions": self.mem.alloc(12 * mv),
+                    "indices": self.mem.alloc(3 * mt), "primitiveIDs": self.mem.alloc(4 * mt)}
+            ro = L.RasterOutputs()
+            for k, b in bufs.items():
+                setattr(ro, k, b.addr)
+            ro.maxBatches, ro.maxVertices, ro.maxTriangles = n, mv, mt
+            self._raster = (ro, bufs)
+        return self._raster
+
+    def raster_results(self) -> dict:
+        """The last tc_raster_batches results, cut to the written counts."""
+        _, bufs = self._raster
+        nb, nv, nt = (int(x) for x in bufs["counts"].read(np.uint32, 3))
+        return {"counts": (nb, nv, nt), "batches": bufs["batches"].read(L.RasterBatch, nb),
+                "clipPositions": bufs["clipPositions"].read(np.float32, 4 * nv).reshape(-1, 4),
+                "worldPositions": bufs["worldPositions"].read(np.float32, 3 * nv).reshape(-1, 3),
+                "indices": bufs["indices"].read(np.uint8, 3 * nt).reshape(-1, 3),
+                "primitiveIDs": bufs["primitiveIDs"].read(np.uint32, nt)}
+
     def set_cameras(self, fc_now: np.ndarray, fc_last: np.ndarray | None = None) -> None:
         self.view.write(fc_now)
         self.view_last.write(fc_now if fc_last is None else fc_last)

@@ -222,6 +222,18 @@ SCHEDULE_FIELDS = ("classifyBlocksPerSM", "splitBlockSize", "vertexBlocksPerSM",
                    "fullVertexBlocksPerSM", "vertexGridPerSM")
 
 
+RASTER_BATCH_VERTICES, RASTER_BATCH_TRIANGLES = 96, 121
+RasterBatch = _struct([("firstPart", "<u4"), ("partCount", "<u4"), ("firstVertex", "<u4"), ("numVertices", "<u4"),
+                       ("firstTriangle", "<u4"), ("numTriangles", "<u4")], 24)
+
+
+class RasterOutputs(ctypes.Structure):
+    _fields_ = [("batches", ctypes.c_uint64), ("counts", ctypes.c_uint64), ("clipPositions", ctypes.c_uint64),
+                ("worldPositions", ctypes.c_uint64), ("indices", ctypes.c_uint64), ("primitiveIDs", ctypes.c_uint64),
+                ("maxBatches", ctypes.c_uint32), ("maxVertices", ctypes.c_uint32), ("maxTriangles", ctypes.c_uint32),
+                ("_pad", ctypes.c_uint32)]
+
+
 class ContextDesc(ctypes.Structure):
     _fields_ = [("maxInstances", ctypes.c_uint32), ("maxTotalClusters", ctypes.c_uint32), ("caps", Caps),
                 ("device", ctypes.c_int32), ("_pad", ctypes.c_uint32)]

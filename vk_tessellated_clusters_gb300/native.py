@@ -54,6 +54,7 @@ def _bind(lib):
         "tc_instantiate_backward": (st, [vp, ctypes.POINTER(L.FrameArgs), u64, u64, u64, vp]),
         "tc_generate_vertices": (st, [vp, ctypes.POINTER(L.FrameArgs), vp]),
         "tc_decode_hits": (st, [vp, ctypes.POINTER(L.FrameArgs), vp, u32, vp, vp]),
+        "tc_raster_batches": (st, [vp, ctypes.POINTER(L.FrameArgs), ctypes.POINTER(L.RasterOutputs), vp]),
         "tc_read_device_errors": (st, [vp, ctypes.POINTER(u32), vp]),
         "tc_launch_count": (u64, [vp]),
     }
@@ -73,7 +74,7 @@ def exported_symbols() -> list[str]:
         "tc_cluster_classify", "tc_triangle_split", "tc_triangle_instantiate", "tc_triangle_instantiate_run",
         "tc_blas_setup_insertion", "tc_blas_clusters_insert", "tc_blas_setup_insertion_noalloc",
         "tc_split_pass_count", "tc_instantiate_backward",
-        "tc_generate_vertices", "tc_decode_hits",
+        "tc_generate_vertices", "tc_decode_hits", "tc_raster_batches",
         "tc_read_device_errors", "tc_launch_count",
     ]
 

@@ -131,6 +131,15 @@ class TessellationPipeline:
         self.decode_hits_device(d_hits, d_out)
         return d_out.cpu().numpy().view(L.BaseHit)
 
+    def raster_batches(self) -> dict:
+        """tc_raster_batches on the last built frame: batch records, vertices in
+        world and clip space, batch-local indices and primitive IDs."""
+        ro, _ = self.state.raster_outputs()
+        native.check(self.lib.tc_raster_batches(self.ctx, ctypes.byref(self.args), ctypes.byref(ro), self.stream()),
+                     "tc_raster_batches")
+        self.torch.cuda.synchronize(self.device)
+        return self.state.raster_results()
+
     def backward(self, grad_vertices, grad_targets_addr: int, grad_texels_addr: int) -> None:
         native.check(self.lib.tc_instantiate_backward(self.ctx, ctypes.byref(self.args), int(grad_vertices),
                                                       int(grad_targets_addr), int(grad_texels_addr), self.stream()),
