@@ -413,6 +413,8 @@ def run_ours(args):
         torch.cuda.empty_cache()
         result["frame_variants"] = frame_variants(torch, local, result["config"]["schedule"])
         torch.cuda.empty_cache()
+        result["raster_batches"] = raster_batches(torch, local, peak)
+        torch.cuda.empty_cache()
         result["animation"] = animation_fwd_bwd(torch, dev, local, result["config"]["schedule"])
     if rank == 0:
         result["cpu_baseline"] = cpu_baseline(args)
@@ -533,6 +535,47 @@ def hit_decode(torch, local, peak, n=1 << 20, reps=20):
             "algorithmic_gbs": alg / (ms / 1e3) / 1e9, "frac_of_peak": alg / (ms / 1e3) / 1e9 / peak,
             "decoded_ok": ok, "l2": "hits and results (67 MB) stay in L2 across the timed launches",
             "parity": "tests/test_gpu_parity.py::test_hit_decode_matches_oracle (field-exact vs oracle)"}
+
+
+def raster_batches(torch, local, peak, reps=20):
+    """tc_raster_batches on a batched-scene frame (256 instances, orbit frame
+    0): parts batched per second and the algorithmic GB/s (per part its 24 B
+    record, base attributes (3 x 32 B) and per vertex 28 B written (world +
+    clip), per triangle 7 B written), outputs resident on the device."""
+    import ctypes
+    from vk_tessellated_clusters_gb300 import layouts as L
+    from vk_tessellated_clusters_gb300 import native
+    from vk_tessellated_clusters_gb300 import scene as S
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    pipe = TessellationPipeline(S.scene_batched(256), L.default_caps(), L.FLAG_CULLING, device=local)
+    pipe.set_cameras(S.camera_orbit(0))
+    pipe.build("graph")
+    res = pipe.raster_batches()
+    ro, _ = pipe.state.raster_outputs()
+
+    def launch():
+        native.check(pipe.lib.tc_raster_batches(pipe.ctx, ctypes.byref(pipe.args), ctypes.byref(ro), pipe.stream()),
+                     "tc_raster_batches")
+
+    for _ in range(3):
+        launch()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(torch.cuda.current_stream())
+    for _ in range(reps):
+        launch()
+    e1.record(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    nb, nv, nt = res["counts"]
+    parts = int(res["batches"]["partCount"].sum()) if nb else 0
+    alg = parts * (24 + 96) + nv * 28 + nt * 7
+    errs = pipe.device_errors()
+    pipe.close()
+    return {"parts": parts, "batches": nb, "vertices": nv, "triangles": nt, "ms": ms,
+            "parts_per_s": parts / (ms / 1e3), "algorithmic_gbs": alg / (ms / 1e3) / 1e9,
+            "frac_of_peak": alg / (ms / 1e3) / 1e9 / peak, "device_errors": errs,
+            "parity": "tests/test_gpu_parity.py::test_raster_batches_match_oracle"}
 
 
 def frame_variants(torch, local, schedule, frames=(3, 17, 31)):

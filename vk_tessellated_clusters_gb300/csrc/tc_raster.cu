@@ -7,8 +7,8 @@
 //
 // Three launches: per group of 32 parts (one warp) its batch, vertex and
 // triangle counts; one block scans the groups' counts into offsets; per group
-// again the batch records, then part by part the vertices (lanes over the
-// part's vertices) and triangles.
+// again (four warps, a quarter of the parts each) the batch records, then part
+// by part the vertices (lanes over the part's vertices) and triangles.
 #include "tc_kernels.h"
 #include "tc_stage.cuh"
 #include "tc_vertex.cuh"
@@ -17,7 +17,8 @@ namespace tc {
 
 namespace {
 
-constexpr u32 kRasterBlock = 256;
+constexpr u32 kRasterBlock   = 256;
+constexpr u32 kWarpsPerGroup = 4;  // k_raster_write: warps per group of 32 parts
 
 // the group's parts: per lane (part g0 + lane) its inclusive vertex and
 // triangle sums; lanes past the parts count as a full batch (they never fit)
@@ -165,8 +166,12 @@ __global__ void __launch_bounds__(kRasterBlock) k_raster_write(StageCtx c, const
   for(int q = 0; q < 16; q++)
     vp[q] = c.view->viewProjMatrix.m[q];
   bool overflow = false;
-  for(u32 g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ngroups; g += (gridDim.x * blockDim.x) >> 5)
+  // kWarpsPerGroup warps share a group, each taking a quarter of its parts
+  // (the batch layout is recomputed by each, the first writes the records)
+  for(u32 gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gw < ngroups * kWarpsPerGroup;
+      gw += (gridDim.x * blockDim.x) >> 5)
   {
+    const u32       g = gw / kWarpsPerGroup, sub = gw % kWarpsPerGroup;
     const u32       g0 = g * 32, local = min(32u, n - g0);
     const uint4     off = groups[g];  // batches, vertices, triangles before this group
     const GroupSums s   = group_sums(c, g0, local);
@@ -176,7 +181,7 @@ __global__ void __launch_bounds__(kRasterBlock) k_raster_write(StageCtx c, const
       const u32 ev = __shfl_sync(0xFFFFFFFFu, s.sumV, end), et = __shfl_sync(0xFFFFFFFFu, s.sumT, end);
       if(lane >= start && lane <= end)
         batchStartV = lastV;
-      if(lane == 0)
+      if(lane == 0 && sub == 0)
       {
         const u32 slot = off.x + q;
         if(slot < o.maxBatches)
@@ -195,7 +200,7 @@ __global__ void __launch_bounds__(kRasterBlock) k_raster_write(StageCtx c, const
       }
     });
     // mesh.glsl:190-435 part by part: lanes over its vertices, then its triangles
-    for(u32 i = 0; i < local; i++)
+    for(u32 i = sub * (32 / kWarpsPerGroup); i < min(local, (sub + 1) * (32 / kWarpsPerGroup)); i++)
     {
       const tc_TessTriangleInfo pt    = parts[g0 + i];
       const u32                 cfg   = pt.subTriangle.triangleID_config >> 16;
@@ -282,13 +287,14 @@ cudaError_t launch_raster_batches(const StageCtx& c, uint4* groups, const tc_ras
 {
   const u32   ngroups = std::max(1u, (maxParts + 31) / 32);
   const u32   grid    = std::max(1u, std::min((ngroups + 7) / 8, numSMs * 8));
+  const u32   wgrid   = std::max(1u, std::min((ngroups * kWarpsPerGroup + 7) / 8, numSMs * 8));
   cudaError_t e       = launch_pdl(k_raster_counts, grid, kRasterBlock, s, c, groups);
   if(e != cudaSuccess)
     return e;
   e = launch_pdl(k_raster_scan, 1u, 1024u, s, c, groups, reinterpret_cast<u32*>(o.counts));
   if(e != cudaSuccess)
     return e;
-  return launch_pdl(k_raster_write, grid, kRasterBlock, s, c, const_cast<const uint4*>(groups), o);
+  return launch_pdl(k_raster_write, wgrid, kRasterBlock, s, c, const_cast<const uint4*>(groups), o);
 }
 
 }  // namespace tc
