@@ -53,7 +53,7 @@ def parse_args():
     p.add_argument("--no-extras", action="store_true", help="skip the plain-path and terrain measurements")
     p.add_argument("--no-tune", action="store_true", help="keep the default launch schedule (no autotuning)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
-    p.add_argument("--profile-case", choices=["batched", "terrain", "transient"], default=None,
+    p.add_argument("--profile-case", choices=["batched", "terrain", "transient", "raster"], default=None,
                    help="run only `warmup` + `steps` graph frames of one case (for ncu captures) and exit")
     return p.parse_args()
 
@@ -826,7 +826,7 @@ def run_profile_case(args):
     from vk_tessellated_clusters_gb300 import scene as S
     from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
     flags = L.FLAG_CULLING
-    if args.profile_case in ("batched", "transient"):
+    if args.profile_case in ("batched", "transient", "raster"):
         scene, caps = S.scene_batched(256), L.default_caps()
         cams = [S.camera_orbit(f) for f in range(args.warmup + args.steps)]
         if args.profile_case == "transient":
@@ -838,6 +838,8 @@ def run_profile_case(args):
     for i, cam in enumerate(cams):
         pipe.set_cameras(cam, cams[i - 1] if i else cam)
         pipe.build("graph")
+        if args.profile_case == "raster":
+            pipe.raster_batches()
     torch.cuda.synchronize()
     print(json.dumps({"profile_case": args.profile_case, "frames": len(cams), "device_errors": pipe.device_errors(),
                       "readback_tris": int(pipe.state.readback.read(L.Readback, 1)[0]["numTotalTriangles"])}))

@@ -19,6 +19,19 @@ namespace {
 
 constexpr u32 kRasterBlock   = 256;
 constexpr u32 kWarpsPerGroup = 4;  // k_raster_write: warps per group of 32 parts
+constexpr u32 kPartsPerWarp  = 32 / kWarpsPerGroup;
+
+// what the vertex and triangle loops of one part need
+struct RasterPart
+{
+  f3                     bp[3], bn[3], bb[3];
+  f2                     bt[3];
+  tc_DisplacementTexture tx;
+  const float*           world;
+  float                  scale, offset, size;
+  u32                    cfg, triID, inst, partID, v0, t0, vs;
+  bool                   hasTx;
+};
 
 // the group's parts: per lane (part g0 + lane) its inclusive vertex and
 // triangle sums; lanes past the parts count as a full batch (they never fit)
@@ -151,6 +164,7 @@ __global__ void __launch_bounds__(1024) k_raster_scan(StageCtx c, uint4* groups,
 __global__ void __launch_bounds__(kRasterBlock) k_raster_write(StageCtx c, const uint4* groups, tc_raster_outputs o)
 {
   stage_prologue();
+  __shared__ RasterPart      s_parts[kRasterBlock / 32][kPartsPerWarp];
   const u32                  lane = threadIdx.x & 31, n = num_parts(c), ngroups = (n + 31) / 32;
   const tc_TessTriangleInfo* parts = reinterpret_cast<const tc_TessTriangleInfo*>(c.build->partTriangles);
   tc_raster_batch*           batches = reinterpret_cast<tc_raster_batch*>(o.batches);
@@ -199,82 +213,106 @@ __global__ void __launch_bounds__(kRasterBlock) k_raster_write(StageCtx c, const
           overflow = true;
       }
     });
-    // mesh.glsl:190-435 part by part: lanes over its vertices, then its triangles
-    for(u32 i = sub * (32 / kWarpsPerGroup); i < min(local, (sub + 1) * (32 / kWarpsPerGroup)); i++)
+    // mesh.glsl:190-435: lanes 0..7 set up the warp's parts at once (their
+    // dependent loads overlap), then part by part lanes take its vertices
+    // and triangles
+    const u32 pBegin = sub * kPartsPerWarp, pEnd = min(local, pBegin + kPartsPerWarp);
+    RasterPart* rec = s_parts[threadIdx.x >> 5];
+    // lane l < kPartsPerWarp sets up part pBegin + l: its exclusive sums and
+    // its first vertex within its batch, from that part's lane
+    const u32 src = pBegin + (lane & (kPartsPerWarp - 1));
+    const u32 exV = __shfl_sync(0xFFFFFFFFu, s.sumV - s.v, src), exT = __shfl_sync(0xFFFFFFFFu, s.sumT - s.t, src);
+    const u32 vsP = __shfl_sync(0xFFFFFFFFu, s.sumV - s.v - batchStartV, src);
+    if(pBegin + lane < pEnd && lane < kPartsPerWarp)
     {
-      const tc_TessTriangleInfo pt    = parts[g0 + i];
-      const u32                 cfg   = pt.subTriangle.triangleID_config >> 16;
-      const u32                 triID = pt.subTriangle.triangleID_config & 0xFFFFu;
-      const tc_TessTableEntry   e     = table_entry(c.table, cfg);
-      const u32                 v0    = off.y + __shfl_sync(0xFFFFFFFFu, s.sumV - s.v, i);
-      const u32                 t0    = off.z + __shfl_sync(0xFFFFFFFFu, s.sumT - s.t, i);
-      const u32                 vs    = __shfl_sync(0xFFFFFFFFu, s.sumV - s.v - batchStartV, i);
-      const tc_RenderInstance&  in    = c.instances[pt.cluster.instanceID];
-      const tc_Cluster          cl    = reinterpret_cast<const tc_Cluster*>(in.clusters)[pt.cluster.clusterID];
+      const u32                 i   = pBegin + lane;
+      const tc_TessTriangleInfo pt  = parts[g0 + i];
+      RasterPart&               r   = rec[lane];
+      r.cfg                         = pt.subTriangle.triangleID_config >> 16;
+      r.triID                       = pt.subTriangle.triangleID_config & 0xFFFFu;
+      r.inst                        = pt.cluster.instanceID;
+      r.v0                          = off.y + exV;
+      r.t0                          = off.z + exT;
+      r.vs                          = vsP;
+      const tc_RenderInstance& in   = c.instances[pt.cluster.instanceID];
+      const tc_Cluster         cl   = reinterpret_cast<const tc_Cluster*>(in.clusters)[pt.cluster.clusterID];
       const uint8_t* lt = reinterpret_cast<const uint8_t*>(in.clusterLocalTriangles) + cl.firstLocalTriangle;
-      f3             bp[3], bn[3], bb[3];
-      f2             bt[3];
       u32            partID = 0;
       for(int v = 0; v < 3; v++)
       {
-        const u32 vi = cl.firstLocalVertex + lt[triID * 3 + v];
-        bp[v]        = ldg3(reinterpret_cast<const float*>(in.positions), vi);
-        bn[v]        = normalize3(ldg3(reinterpret_cast<const float*>(in.normals), vi));
-        bt[v]        = ldg2(reinterpret_cast<const float*>(in.texcoords), vi);
-        bb[v]        = decode_bary(pt.subTriangle.vtxEncoded[v]);
+        const u32 vi = cl.firstLocalVertex + lt[r.triID * 3 + v];
+        r.bp[v]      = ldg3(reinterpret_cast<const float*>(in.positions), vi);
+        r.bn[v]      = normalize3(ldg3(reinterpret_cast<const float*>(in.normals), vi));
+        r.bt[v]      = ldg2(reinterpret_cast<const float*>(in.texcoords), vi);
+        r.bb[v]      = decode_bary(pt.subTriangle.vtxEncoded[v]);
         partID ^= (pt.subTriangle.vtxEncoded[v] >> 20) | ((pt.subTriangle.vtxEncoded[v] >> 4) & 0xFFFu);
       }
-      tc_DisplacementTexture tx    = {};
-      bool                   hasTx = false;
+      r.partID = partID;
+      r.hasTx  = false;
       if(c.numTextures > 0 && c.textures != nullptr && in.displacementIndex >= 0)
       {
         if((u32)in.displacementIndex < c.numTextures)
         {
-          tx    = c.textures[in.displacementIndex];
-          hasTx = true;
+          r.tx    = c.textures[in.displacementIndex];
+          r.hasTx = true;
         }
-        else if(lane == 0)
+        else
           atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
       }
-      BasePN basis = {};
+      r.scale  = in.displacementScale;
+      r.offset = in.displacementOffset;
+      r.size   = in.geoHi.w;
+      r.world  = in.worldMatrix.m;
+    }
+    __syncwarp();
+    for(u32 i = pBegin; i < pEnd; i++)
+    {
+      const RasterPart&       r = rec[i - pBegin];
+      const tc_TessTableEntry e = table_entry(c.table, r.cfg);
+      BasePN                  basis = {};
       if(pn)
-        basis = setup_pn(bp[0], bp[1], bp[2], bn[0], bn[1], bn[2]);
+        basis = setup_pn(r.bp[0], r.bp[1], r.bp[2], r.bn[0], r.bn[1], r.bn[2]);
       for(u32 vert = lane; vert < e.numVertices; vert += 32)
       {
-        if(v0 + vert >= o.maxVertices)
+        if(r.v0 + vert >= o.maxVertices)
         {
           overflow = true;
           break;
         }
-        const f3 w   = interp3(bb[0], bb[1], bb[2], cfg_vertex(c.table, e, cfg, vert));
-        f3       pos = pn ? get_pn(basis, w) : interp3(bp[0], bp[1], bp[2], w);
-        if(hasTx)
-          pos = displace(pos, interp3(bn[0], bn[1], bn[2], w), sample_bilinear(tx, interp2(bt[0], bt[1], bt[2], w)),
-                         in.displacementScale, c.view->displacementScale, in.displacementOffset,
-                         c.view->displacementOffset);
+        const f3 w   = interp3(r.bb[0], r.bb[1], r.bb[2], cfg_vertex(c.table, e, r.cfg, vert));
+        f3       pos = pn ? get_pn(basis, w) : interp3(r.bp[0], r.bp[1], r.bp[2], w);
+        if(r.hasTx)
+          pos = displace(pos, interp3(r.bn[0], r.bn[1], r.bn[2], w),
+                         sample_bilinear(r.tx, interp2(r.bt[0], r.bt[1], r.bt[2], w)), r.scale,
+                         c.view->displacementScale, r.offset, c.view->displacementOffset);
         if(rp.enabled)
-          pos = ripple(pos, pt.cluster.instanceID, in.geoHi.w, rp);
-        const f3 wp = xform_point(in.worldMatrix.m, pos);
+          pos = ripple(pos, r.inst, r.size, rp);
+        float m[16];
+#pragma unroll
+        for(int q = 0; q < 16; q++)
+          m[q] = __ldg(r.world + q);
+        const f3 wp = xform_point(m, pos);
         const f3 cp = xform_point(vp, wp);
-        float*   wo = world + 3 * (u64)(v0 + vert);
-        float*   co = clip + 4 * (u64)(v0 + vert);
+        float*   wo = world + 3 * (u64)(r.v0 + vert);
+        float*   co = clip + 4 * (u64)(r.v0 + vert);
         wo[0] = wp.x, wo[1] = wp.y, wo[2] = wp.z;
         co[0] = cp.x, co[1] = cp.y, co[2] = cp.z;
         co[3] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(vp[3], wp.x), __fmul_rn(vp[7], wp.y)), __fmul_rn(vp[11], wp.z)), vp[15]);
       }
       for(u32 tri = lane; tri < e.numTriangles; tri += 32)
       {
-        if(t0 + tri >= o.maxTriangles)
+        if(r.t0 + tri >= o.maxTriangles)
         {
           overflow = true;
           break;
         }
-        const uint3 ct = cfg_triangle(c.table, e, cfg, tri);
-        uint8_t*    d  = idx + 3 * (u64)(t0 + tri);
-        d[0] = (uint8_t)(ct.x + vs), d[1] = (uint8_t)(ct.y + vs), d[2] = (uint8_t)(ct.z + vs);
-        prim[t0 + tri] = (triID & 0xFFu) | (((visTriangles ? tri * 3 : partID) | 1u) << 8);
+        const uint3 ct = cfg_triangle(c.table, e, r.cfg, tri);
+        uint8_t*    d  = idx + 3 * (u64)(r.t0 + tri);
+        d[0] = (uint8_t)(ct.x + r.vs), d[1] = (uint8_t)(ct.y + r.vs), d[2] = (uint8_t)(ct.z + r.vs);
+        prim[r.t0 + tri] = (r.triID & 0xFFu) | (((visTriangles ? tri * 3 : r.partID) | 1u) << 8);
       }
     }
+    __syncwarp();  // the records are rewritten by the warp's next group
   }
   if(overflow)
     atomicOr(c.errorWord, TC_DEVERR_CAPACITY);
