@@ -3,8 +3,9 @@
 tess_table.json : digest and sizes of the committed table blob, which
                   data/make_tess_table.py produces by compiling the reference's
                   src/tessellation_table_nv_raw.hpp unchanged (oracle/Makefile `ref`).
-oracle_frames.json : digests of the oracle's outputs for small seeded frames,
-                  pinning the CPU restatement against accidental drift.
+oracle_frames.json : digests of the oracle's outputs for small seeded frames
+                  (plain, and with PN + ripple, transient builds and raster
+                  batching), pinning the CPU restatement against accidental drift.
 
 Usage: python tests/golden/make_golden.py
 """
@@ -28,8 +29,10 @@ def table_digest():
 
 
 def frame_digests():
-    from tests.golden.cases import CASES, run_case_digest
-    return {name: run_case_digest(name) for name in CASES}
+    from tests.golden.cases import CASES, VARIANTS, run_case_digest, run_variant_digest
+    d = {name: run_case_digest(name) for name in CASES}
+    d.update({name: run_variant_digest(name) for name in VARIANTS})
+    return d
 
 
 if __name__ == "__main__":

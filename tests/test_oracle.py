@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-from tests.golden.cases import CASES, run_case, outputs_digest
+from tests.golden.cases import CASES, VARIANTS, outputs_digest, run_case, run_variant_digest
 from vk_tessellated_clusters_gb300 import layouts as L
 from vk_tessellated_clusters_gb300 import scene as S
 
@@ -119,6 +119,14 @@ def test_golden_frame_digests(name, oracle):
     with open(os.path.join(ROOT, "tests", "golden", "oracle_frames.json")) as f:
         want = json.load(f)[name]
     assert run_case(name, oracle) and outputs_digest(run_case(name, oracle)[2]) == want
+
+
+@pytest.mark.parametrize("name", sorted(VARIANTS))
+def test_golden_variant_digests(name, oracle):
+    """PN + ripple, transient builds and raster batching outputs pinned by digest."""
+    with open(os.path.join(ROOT, "tests", "golden", "oracle_frames.json")) as f:
+        want = json.load(f)[name]
+    assert run_variant_digest(name, oracle) == want
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
