@@ -1384,7 +1384,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_classify_write_transient(StageCtx
 // batches, from what k_classify_write_transient left per cluster (each
 // chunk's first batch vertex and accepted batches, in place of its counts).
 // One warp per cluster, one lane per base triangle.
-__global__ void __launch_bounds__(kBlock, 4) k_classify_mini_vertices(StageCtx c, ClassifyScratch cs)
+__global__ void __launch_bounds__(kBlock, 2) k_classify_mini_vertices(StageCtx c, ClassifyScratch cs)
 {
   stage_prologue();
   __shared__ u32        s_range[2];
