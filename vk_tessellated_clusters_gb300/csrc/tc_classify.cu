@@ -1291,7 +1291,7 @@ __device__ inline void block_prefix_transient(const ClassifyScratch& cs, u64 (&p
   pre[kTTrans] = t0.trans + tot[kTTrans];
 }
 
-__global__ void __launch_bounds__(kBlock, 4) k_classify_write_transient(StageCtx c, ClassifyScratch cs)
+__global__ void __launch_bounds__(kBlock, 6) k_classify_write_transient(StageCtx c, ClassifyScratch cs)
 {
   stage_prologue();
   __shared__ u32            s_range[2];
@@ -1533,10 +1533,15 @@ cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& bu
   // register budget from the requested residency: 4 or less -> 64, 5-7 -> 40, 8 and more -> 32
   if(c.flags & (TC_FLAG_TRANSIENT_1X | TC_FLAG_TRANSIENT_2X))
   {
-    cudaError_t e = launch_pdl(k_classify_count<4, true>, grid, kBlock, s, c, cs);
+    // the transient write is latency-bound per cluster: a full wave of its
+    // six resident blocks per SM (the count uses the same ranges)
+    const u32 tgrid = std::max(1u, std::min(classify_max_blocks(maxClusters), numSMs * std::max(6u, warpBlocksPerSM)));
+    ClassifyScratch ts = cs;
+    ts.writeBlocks     = tgrid;
+    cudaError_t e      = launch_pdl(k_classify_count<4, true>, tgrid, kBlock, s, c, ts);
     if(e != cudaSuccess)
       return e;
-    return launch_pdl(k_classify_write_transient, grid, kBlock, s, c, cs);
+    return launch_pdl(k_classify_write_transient, tgrid, kBlock, s, c, ts);
   }
   const int   occ = warpBlocksPerSM >= 8 ? 8 : (warpBlocksPerSM >= 5 ? 6 : 4);
   cudaError_t e   = occ == 8   ? launch_pdl(k_classify_count<8>, grid, kBlock, s, c, cs)
