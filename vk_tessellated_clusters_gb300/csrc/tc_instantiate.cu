@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_vertices(Stag
 }
 
 // triangle_tess_template_instantiate.comp.glsl:295-371 with TESS_USE_PN and /
-// or DO_ANIMATION: one warp per part triangle, lanes over its vertices; the
+// or DO_ANIMATION: eight lanes per part triangle over its vertices; the
 // PN basis and the base attributes stay in registers. Written like the CPU
 // restatement (tess_interpolate of the base barycentrics, the reference-order
 // sampling and displacement) rather than in the affine form of the fast path.
@@ -617,8 +617,10 @@ __global__ void __launch_bounds__(kBlock) k_instantiate_vertices_deform(StageCtx
   float*                     gv    = reinterpret_cast<float*>(b->genVertices);
   const bool                 pn    = (c.flags & TC_FLAG_PN) != 0;
   const RippleParams         rp    = ripple_params(*c.view, (c.flags & TC_FLAG_RIPPLE) != 0);
-  const u32                  nwarps = (gridDim.x * blockDim.x) >> 5;
-  for(u32 p = begin + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); p < end; p += nwarps)
+  // eight lanes per part (parts average a handful of vertices), four parts per warp
+  const u32                  subLane = lane & 7;
+  const u32                  nsubs  = (gridDim.x * blockDim.x) >> 3;
+  for(u32 p = begin + ((blockIdx.x * blockDim.x + threadIdx.x) >> 3); p < end; p += nsubs)
   {
     const u32 vo = ib.vertexOffset[p];
     if(vo == ~0u)
@@ -649,13 +651,13 @@ __global__ void __launch_bounds__(kBlock) k_instantiate_vertices_deform(StageCtx
         tx    = c.textures[in.displacementIndex];
         hasTx = true;
       }
-      else if(lane == 0)
+      else if(subLane == 0)
         atomicOr(c.errorWord, TC_DEVERR_BAD_CLUSTER);
     }
     BasePN basis = {};
     if(pn)
       basis = setup_pn(bp[0], bp[1], bp[2], bn[0], bn[1], bn[2]);
-    for(u32 vert = lane; vert < e.numVertices; vert += 32)
+    for(u32 vert = subLane; vert < e.numVertices; vert += 8)
     {
       const f3 w   = interp3(bb[0], bb[1], bb[2], cfg_vertex(c.table, e, cfg, vert));
       f3       pos = pn ? get_pn(basis, w) : interp3(bp[0], bp[1], bp[2], w);
@@ -703,7 +705,7 @@ cudaError_t launch_instantiate_vertices(const StageCtx& c, const InstantiateBuff
 {
   const u32 chunks = (maxParts + kPartsPerWarp - 1) / kPartsPerWarp;
   if(c.flags & (TC_FLAG_PN | TC_FLAG_RIPPLE))  // the deformation path: one warp per part
-    return launch_pdl(k_instantiate_vertices_deform, std::max(1u, std::min((maxParts + kWarps - 1) / kWarps, numSMs * 8)),
+    return launch_pdl(k_instantiate_vertices_deform, std::max(1u, std::min((maxParts + 4 * kWarps - 1) / (4 * kWarps), numSMs * 8)),
                       kBlock, s, c, buf);
   // warps stride over the 32-part chunks; the grid is sized to the machine,
   // not to the capacity (blocks with no chunk would only add a tail), by
