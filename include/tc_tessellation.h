@@ -468,7 +468,9 @@ typedef struct tc_schedule {
                                    * 0: the default (4) */
   uint32_t vertexGridPerSM;     /* grid of the part vertex kernel = SMs x this (grid-stride over 32-part chunks);
                                  * 0: one resident wave (the blocks vertexBlocksPerSM allows) */
-  uint32_t _pad[1];
+  uint32_t lookbackSpinLimit;   /* polls a bounded look-back wait makes before it gives up, sets
+                                 * TC_DEVERR_LOOKBACK_TIMEOUT and goes on with what it has (the frame's offsets are
+                                 * then unreliable); 0: the default, 2^22 polls (seconds, with back-off) */
 } tc_schedule;
 
 typedef struct tc_context_desc {
@@ -592,12 +594,19 @@ tc_status tc_blas_clusters_insert(tc_context* ctx, const tc_frame_args* args, vo
  * process exits.
  *   - args->numInstances (which must equal SceneBuilding.numRenderInstances)
  *     above TC_NOALLOC_MAX_INSTANCES: TC_ERR_CAPACITY, nothing launched.
- *   - The first call on a device (the current device) resolves the array's
- *     address with cudaGetSymbolAddress; make it before any stream capture.
+ *     The kernel sizes its work from SceneBuilding.numRenderInstances on the
+ *     device; if that count exceeds TC_NOALLOC_MAX_INSTANCES the instances
+ *     beyond it get no list offsets, and only deviceErrors
+ *     (TC_DEVERR_CAPACITY) tells: pass a deviceErrors word to see it.
+ *   - Every call looks the array's address up (cudaGetSymbolAddress) in the
+ *     current context, so it follows cudaDeviceReset and caller-owned
+ *     contexts; the first call in a context may load the library's device
+ *     code: make it before any stream capture.
  *   - Every call shares the array and clears it (cudaMemsetAsync on `stream`)
  *     before its launch; calls that overlap on the GPU race on it.
  *   - deviceErrors: optional device word that receives TC_DEVERR_* bits
- *     (atomic OR; 0 = not reported). */
+ *     (atomic OR; 0 = not reported: the bits then land in the shared array
+ *     and the next call clears them). */
 tc_status tc_blas_setup_insertion_noalloc(const tc_frame_args* args, uint32_t* deviceErrors, void* stream);
 
 /* Number of split passes the host issues for a split factor
@@ -716,6 +725,17 @@ tc_status tc_raster_batches(tc_context* ctx, const tc_frame_args* args, const tc
 tc_status tc_read_device_errors(tc_context* ctx, uint32_t* outBits, void* stream);
 /* Number of kernel launches issued by this context since creation. */
 uint64_t tc_launch_count(const tc_context* ctx);
+
+/* No counterpart in the reference (whose look-back-free atomics never wait):
+ * a check of the bounded device-side wait every look-back of this library
+ * uses. One warp waits, as tile 1, for tile 0's state word in the context's
+ * frame scratch. With predecessorPublished != 0 tile 0 holds an inclusive
+ * prefix of 7 and *outPrefix = 7. With 0 nothing ever publishes it: the wait
+ * gives up after the schedule's lookbackSpinLimit polls, sets
+ * TC_DEVERR_LOOKBACK_TIMEOUT in the error word (tc_read_device_errors) and
+ * returns, *outPrefix = 0. Synchronises `stream`; must not overlap a frame of
+ * the same context (it reuses the frame scratch). */
+tc_status tc_lookback_probe(tc_context* ctx, uint32_t predecessorPublished, uint64_t* outPrefix, void* stream);
 
 #ifdef __cplusplus
 }

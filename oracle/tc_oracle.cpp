@@ -580,6 +580,56 @@ uint32_t tco_get_config(const uint32_t* factors3, uint32_t* triangleVertices3)
 
 uint32_t tco_split_factor(uint32_t factor, uint32_t splitFactor) { return splitFactor1(factor, clampSplitFactor(splitFactor)); }
 
+void tco_config_triangle(const tco_table* t, uint32_t cfg, uint32_t tri, uint32_t* out3) { cfgTriangle(t, cfg, tri, out3); }
+
+void tco_config_vertex(const tco_table* t, uint32_t cfg, uint32_t vert, float* out3)
+{
+  const f3 w = cfgVertex(t, cfg, vert);
+  out3[0] = w.x, out3[1] = w.y, out3[2] = w.z;
+}
+
+void tco_interpolate3(const float* base9, const float* wuv, float* out3)
+{
+  const f3 b[3] = {{base9[0], base9[1], base9[2]}, {base9[3], base9[4], base9[5]}, {base9[6], base9[7], base9[8]}};
+  const f3 r    = interp3(b, {wuv[0], wuv[1], wuv[2]});
+  out3[0] = r.x, out3[1] = r.y, out3[2] = r.z;
+}
+
+void tco_pn_position(const float* verts9, const float* normals9, const float* bary3, float* out3)
+{
+  const f3 v[3] = {{verts9[0], verts9[1], verts9[2]}, {verts9[3], verts9[4], verts9[5]}, {verts9[6], verts9[7], verts9[8]}};
+  const f3 n[3] = {{normals9[0], normals9[1], normals9[2]},
+                   {normals9[3], normals9[4], normals9[5]},
+                   {normals9[6], normals9[7], normals9[8]}};
+  const f3 r    = getPN(setupPN(v, n), {bary3[0], bary3[1], bary3[2]});
+  out3[0] = r.x, out3[1] = r.y, out3[2] = r.z;
+}
+
+void tco_ripple(const float* p3, uint32_t seed, float geometrySize, const tc_FrameConstants* view, float* out3)
+{
+  const f3 r = ripple({p3[0], p3[1], p3[2]}, seed, geometrySize, *view);
+  out3[0] = r.x, out3[1] = r.y, out3[2] = r.z;
+}
+
+int tco_intersect_frustum(const float* lo3, const float* hi3, const float* world16, const tc_FrameConstants* viewLast,
+                          float* clipMin4, float* clipMax4, int* clipValid)
+{
+  Clip       cmin, cmax;
+  bool       valid = false;
+  const bool in    = intersectFrustum({lo3[0], lo3[1], lo3[2]}, {hi3[0], hi3[1], hi3[2]}, world16, *viewLast, cmin, cmax, valid);
+  clipMin4[0] = cmin.x, clipMin4[1] = cmin.y, clipMin4[2] = cmin.z, clipMin4[3] = cmin.w;
+  clipMax4[0] = cmax.x, clipMax4[1] = cmax.y, clipMax4[2] = cmax.z, clipMax4[3] = cmax.w;
+  *clipValid  = valid ? 1 : 0;
+  return in ? 1 : 0;
+}
+
+int tco_intersect_size(const float* clipMin4, const float* clipMax4, const tc_FrameConstants* viewLast)
+{
+  const Clip cmin = {clipMin4[0], clipMin4[1], clipMin4[2], clipMin4[3]};
+  const Clip cmax = {clipMax4[0], clipMax4[1], clipMax4[2], clipMax4[3]};
+  return intersectSize(cmin, cmax, *viewLast) ? 1 : 0;
+}
+
 // src/renderer_raytrace_clusters_tess.cpp:516-519
 uint32_t tco_split_pass_count(uint32_t splitFactor)
 {

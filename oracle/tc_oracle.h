@@ -7,12 +7,14 @@
  * and by bench.py's CPU-baseline leg, always as the checker. The shipped
  * library (libtc_gb300.so) never links or calls it.
  *
- * Parity pinning: the tessellation table is pinned to the reference's own
- * generated header compiled here (oracle/Makefile target `ref`); struct layouts
- * are pinned by static_asserts against the reference's declared sizes. The
- * shader arithmetic itself is NOT pinned against the reference: the reference
- * only runs as Vulkan GLSL and no graphics stack exists here ("parity unpinned"
- * for the shader math; the restatement follows the cited lines).
+ * Parity pinning (oracle/Makefile target `ref`, checked by tests/test_ref_pin.py):
+ * the tessellation table is pinned to the reference's own generated header
+ * compiled here; the struct layouts of include/tc_tessellation.h to the
+ * reference's shaderio headers compiled as C++ (every field's offset and size);
+ * the shader functions of tessellation.glsl:28-201, culling.glsl:27-92 and
+ * displacement.glsl:27-120 to the reference's own GLSL text compiled as C++
+ * through a mechanical rewrite and a GLSL built-in shim (oracle/ref_shim/),
+ * function by function, on exhaustive and seeded samples.
  *
  * Every "address" inside the tc_* structs handed to the oracle is a HOST
  * pointer. Output order is the canonical serial order (instance, cluster,
@@ -52,6 +54,17 @@ void     tco_tess_factors(const float* a, const float* b, const float* c, const 
 uint32_t tco_get_config(const uint32_t* factors3, uint32_t* triangleVertices3);
 uint32_t tco_split_factor(uint32_t factor, uint32_t splitFactor);
 uint32_t tco_split_pass_count(uint32_t splitFactor);
+/* tessellation.glsl:165-189 (flip-aware config triangle / vertex), :191-195 */
+void     tco_config_triangle(const tco_table* t, uint32_t cfg, uint32_t tri, uint32_t* out3);
+void     tco_config_vertex(const tco_table* t, uint32_t cfg, uint32_t vert, float* out3);
+void     tco_interpolate3(const float* base9, const float* wuv, float* out3);
+/* displacement.glsl:47-104 (deform_setupPN + deform_getPN), :106-120 rippleDeform */
+void     tco_pn_position(const float* verts9, const float* normals9, const float* bary3, float* out3);
+void     tco_ripple(const float* p3, uint32_t seed, float geometrySize, const tc_FrameConstants* view, float* out3);
+/* culling.glsl:50-90 intersectFrustum, :30-35 intersectSize */
+int      tco_intersect_frustum(const float* lo3, const float* hi3, const float* world16, const tc_FrameConstants* viewLast,
+                               float* clipMin4, float* clipMax4, int* clipValid);
+int      tco_intersect_size(const float* clipMin4, const float* clipMax4, const tc_FrameConstants* viewLast);
 
 /* One frame of the chain (frame_begin .. blas_clusters_insert).
  * args: host addresses everywhere. partRunStarts (may be NULL) receives the raw

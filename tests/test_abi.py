@@ -95,3 +95,15 @@ def test_context_create_reports_cuda_error_without_gpu(lib):
     ctx = ctypes.c_void_p()
     assert lib.tc_context_create(ctypes.byref(desc), ctypes.byref(ctx)) == L.TC_ERR_CUDA
     assert not ctx.value
+
+
+def test_noalloc_source_names_no_allocation_call():
+    """tc_blas_setup_insertion_noalloc's translation unit calls no device
+    allocator: its scratch is a file-scope __device__ array."""
+    src = open(os.path.join(ROOT, "vk_tessellated_clusters_gb300", "csrc", "tc_noalloc.cu")).read()
+    code = "\n".join(line.split("//")[0] for line in src.splitlines())
+    for name in ("cudaMalloc", "cudaFree", "cudaMallocAsync", "cudaFreeAsync", "cudaMallocManaged", "cudaMallocHost",
+                 "cuMemAlloc", "cuMemCreate", "malloc(", "new "):
+        assert name not in code, name
+    assert "static __device__ __align__(256)" in code
+    assert "cudaGetSymbolAddress" in code

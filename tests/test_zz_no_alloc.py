@@ -7,6 +7,10 @@ the per-instance counts. Collected last on purpose: it must pass both alone in
 a fresh process (its first call sets the scratch address up) and after the
 other GPU tests."""
 import ctypes
+import os
+import subprocess
+import sys
+import textwrap
 
 import numpy as np
 import pytest
@@ -141,3 +145,49 @@ def test_rejects_sizes_beyond_the_maximum_and_missing_buffers():
     args.build = 0
     assert _noalloc(args, None, stream) == L.TC_ERR_INVALID_ARG
     assert native.lib().tc_blas_setup_insertion_noalloc(None, None, stream) == L.TC_ERR_INVALID_ARG
+
+
+_FRESH = textwrap.dedent("""
+    import sys
+    sys.path.insert(0, {root!r})
+    import numpy as np
+    import torch
+    from tests.test_zz_no_alloc import _noalloc, _standalone_buffers
+    from vk_tessellated_clusters_gb300 import layouts as L
+    rng = np.random.default_rng(11)
+    stream = torch.cuda.current_stream().cuda_stream
+    errors = torch.zeros(1, dtype=torch.int32, device="cuda")
+    n, base = 70000, 5
+    counts, sizes, d_infos, d_sb, d_rb, args = _standalone_buffers(torch, n, rng, base)
+    snap = d_infos.clone()
+    torch.cuda.synchronize()
+    want = base + np.concatenate([[0], np.cumsum(counts.astype(np.uint64))[:-1]])
+    # the first call in this process's context: it looks the scratch array up
+    assert _noalloc(args, errors.data_ptr(), stream) == L.TC_OK
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for call in range(2):
+        d_infos.copy_(snap)
+        sb = d_sb.cpu().numpy().view(L.SceneBuilding)
+        sb["blasClusterCounter"] = base
+        d_sb.copy_(torch.from_numpy(sb.view(np.uint8).copy()))
+        assert _noalloc(args, errors.data_ptr(), stream) == L.TC_OK
+        torch.cuda.synchronize()
+        infos = d_infos.cpu().numpy().view(L.BlasBuildInfo)
+        assert np.array_equal(infos["clusterReferences"], 0x500000000000 + want.astype(np.uint64) * 8), call
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0, (free0, free1)
+    assert int(errors.item()) == 0
+    print("fresh-process no-alloc ok")
+""")
+
+
+def test_first_call_in_a_fresh_process_and_no_device_allocation():
+    """The set-up path (the first call in a new CUDA context) runs in a child
+    process of its own, and the calls after it leave the device's free memory
+    unchanged: nothing is allocated."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, "-c", _FRESH.format(root=root)], capture_output=True, text=True,
+                         timeout=600, cwd=root)
+    assert out.returncode == 0, out.stdout[-2000:] + out.stderr[-4000:]
+    assert "fresh-process no-alloc ok" in out.stdout

@@ -245,6 +245,7 @@ StageCtx base_ctx(tc_context* ctx, const tc_frame_args* a)
   c.instEnd                 = a->numInstances;
   c.fuseSetup               = kNoSetup;
   c.run                     = kAllRuns;
+  c.spinLimit               = ctx->schedule.lookbackSpinLimit ? ctx->schedule.lookbackSpinLimit : kSpinLimit;
   return c;
 }
 
@@ -492,7 +493,7 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
     delete ctx;
     return TC_ERR_CUDA;
   }
-  ctx->schedule = {4, 256, 4, 4, 1, kDefaultFullVertexBlocksPerSM, 0, {0}};  // the batched scene's tuned shape
+  ctx->schedule = {4, 256, 4, 4, 1, kDefaultFullVertexBlocksPerSM, 0, 0};  // the batched scene's tuned shape
   ctx->plan     = make_plan(*desc);
   if(cudaMalloc(&ctx->dScratch, ctx->plan.totalBytes) != cudaSuccess
      || cudaMemset(ctx->dScratch, 0, ctx->plan.totalBytes) != cudaSuccess)
@@ -1002,6 +1003,22 @@ tc_status tc_read_device_errors(tc_context* ctx, uint32_t* outBits, void* stream
   u32*         err = reinterpret_cast<u32*>(ctx->dScratch + ctx->plan.errOffset);
   TC_CHECK_CUDA(cudaMemcpyAsync(outBits, err, 4, cudaMemcpyDeviceToHost, s));
   TC_CHECK_CUDA(cudaMemsetAsync(err, 0, 4, s));
+  TC_CHECK_CUDA(cudaStreamSynchronize(s));
+  return TC_OK;
+}
+
+tc_status tc_lookback_probe(tc_context* ctx, uint32_t predecessorPublished, uint64_t* outPrefix, void* stream)
+{
+  if(!ctx || !outPrefix)
+    return TC_ERR_INVALID_ARG;
+  cudaStream_t s     = reinterpret_cast<cudaStream_t>(stream);
+  u64*         state = reinterpret_cast<u64*>(ctx->dScratch + ctx->plan.segOffset);  // frame scratch, >= 3 words
+  u32*         err   = reinterpret_cast<u32*>(ctx->dScratch + ctx->plan.errOffset);
+  const u32    limit = ctx->schedule.lookbackSpinLimit ? ctx->schedule.lookbackSpinLimit : kSpinLimit;
+  TC_CHECK_CUDA(launch_lookback_probe(reinterpret_cast<unsigned long long*>(state), predecessorPublished ? 1u : 0u,
+                                      err, limit, s));
+  ctx->launches += 1;
+  TC_CHECK_CUDA(cudaMemcpyAsync(outPrefix, state + 2, sizeof(u64), cudaMemcpyDeviceToHost, s));
   TC_CHECK_CUDA(cudaStreamSynchronize(s));
   return TC_OK;
 }

@@ -48,7 +48,8 @@ __global__ void k_blas_setup_insertion(StageCtx c)
     if(threadIdx.x < 32)
     {
       const u64 ex =
-          warp_lookback_exclusive(c.scratch.lbState, tile, total, tile == 0 ? b->blasClusterCounter : 0, c.errorWord);
+          warp_lookback_exclusive(c.scratch.lbState, tile, total, tile == 0 ? b->blasClusterCounter : 0, c.errorWord,
+                                  c.spinLimit);
       if(threadIdx.x == 0)
       {
         s_excl = ex;

@@ -393,7 +393,8 @@ __device__ __forceinline__ void stage_prologue()
 // ordered exactly like a serial loop. Each state word holds a 62-bit value and
 // a 2-bit flag (1 = tile aggregate, 2 = inclusive prefix). Tiles are handed out
 // through a ticket counter so a tile's predecessors are always owned by running
-// blocks. Waits are bounded: after kSpinLimit polls the tile records
+// blocks. Waits are bounded: after `spinLimit` polls (the schedule's
+// lookbackSpinLimit, by default kSpinLimit) the tile records
 // TC_DEVERR_LOOKBACK_TIMEOUT, uses what it accumulated and moves on.
 // ---------------------------------------------------------------------------
 
@@ -423,7 +424,8 @@ constexpr int kLbSlots      = 4;
 constexpr int kLbWindow     = 32 * kLbSlots;
 constexpr u32 kLbEagerPolls = 64;
 
-__device__ __forceinline__ u64 warp_lookback_exclusive(u64* state, u32 tile, u64 aggregate, u64 base, u32* errorWord)
+__device__ __forceinline__ u64 warp_lookback_exclusive(u64* state, u32 tile, u64 aggregate, u64 base, u32* errorWord,
+                                                        u32 spinLimit)
 {
   const u32 lane = threadIdx.x & 31;
   if(tile == 0)
@@ -455,7 +457,7 @@ __device__ __forceinline__ u64 warp_lookback_exclusive(u64* state, u32 tile, u64
         pending |= (s[k] & ~kLbValueMask) == 0;
       if(!__any_sync(0xFFFFFFFFu, pending))
         break;
-      if(++spins > kSpinLimit)
+      if(++spins > spinLimit)
       {
         if(lane == 0)
           atomicOr(errorWord, TC_DEVERR_LOOKBACK_TIMEOUT);

@@ -185,7 +185,8 @@ __device__ inline void instances_classify_body(const StageCtx& c)
     u32 excl = block_exclusive_scan(nc, s_warp, &total);
     if(threadIdx.x < 32)
     {
-      const u64 ex = warp_lookback_exclusive(c.scratch.lbState, tile, total, 0, c.errorWord);
+      const u64 ex = warp_lookback_exclusive(c.scratch.lbState, tile, total, 0, c.errorWord,
+                                  c.spinLimit);
       if(threadIdx.x == 0)
       {
         s_excl = ex;
@@ -287,7 +288,8 @@ __global__ void k_clusters_cull(StageCtx c)
     if(threadIdx.x < 32)
     {
       const u64 ex =
-          warp_lookback_exclusive(c.scratch.lbState, tile, total, tile == 0 ? b->visibleClusterCounter : 0, c.errorWord);
+          warp_lookback_exclusive(c.scratch.lbState, tile, total, tile == 0 ? b->visibleClusterCounter : 0, c.errorWord,
+                                  c.spinLimit);
       if(threadIdx.x == 0)
       {
         s_excl = ex;
@@ -321,9 +323,33 @@ __global__ void k_build_setup(StageCtx c, u32 mode)
     build_setup_apply(c, mode);
 }
 
+// One warp runs the look-back wait of tile 1 against tile 0's state word,
+// which holds an inclusive prefix of 7 when `published`, and otherwise stays
+// at zero (pending): nothing ever publishes it, so the wait has to run out,
+// set TC_DEVERR_LOOKBACK_TIMEOUT and return. out[0] = the prefix tile 1 got.
+__global__ void k_lookback_probe(u64* state, u32 published, u32* errorWord, u32 spinLimit, u64* out)
+{
+  if(threadIdx.x == 0 && published)
+    st_relaxed_u64(state, kLbPrefix | 7ull);
+  __syncwarp();
+  const u64 ex = warp_lookback_exclusive(state, 1, 5, 0, errorWord, spinLimit);
+  if(threadIdx.x == 0)
+    out[0] = ex;
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+
+cudaError_t launch_lookback_probe(u64* state, u32 published, u32* errorWord, u32 spinLimit, cudaStream_t s)
+{
+  // state[0..1]: tile states, state[2]: the result
+  const cudaError_t e = cudaMemsetAsync(state, 0, 3 * sizeof(u64), s);
+  if(e != cudaSuccess)
+    return e;
+  k_lookback_probe<<<1, 32, 0, s>>>(state, published, errorWord, spinLimit, state + 2);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_frame_begin(const StageCtx& c, u32 grid, cudaStream_t s)
 {

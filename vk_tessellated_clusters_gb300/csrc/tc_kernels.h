@@ -55,6 +55,9 @@ cudaError_t launch_instances_classify(const StageCtx& c, u32 grid, u32 block, cu
 cudaError_t launch_frame_begin_instances(const StageCtx& c, u32 grid, cudaStream_t s);
 cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 cudaError_t launch_build_setup(const StageCtx& c, u32 mode, cudaStream_t s);
+// the bounded look-back wait on its own (state: 3 words, zeroed here)
+cudaError_t launch_lookback_probe(unsigned long long* state, u32 published, u32* errorWord, u32 spinLimit,
+                                  cudaStream_t s);
 cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,
                                     u32 warpBlocksPerSM, cudaStream_t s);
 // the full clusters' displaced vertices of the last launch_cluster_classify

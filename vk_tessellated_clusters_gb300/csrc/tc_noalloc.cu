@@ -19,15 +19,16 @@
 // on the caller's stream) before its launch. Calls that overlap on the GPU (two
 // streams, or two host threads with unordered streams) race on it.
 //
-// Set-up: the first call on a device (the current device at the time of the
-// call) resolves the array's device address with cudaGetSymbolAddress and
-// caches it; that first call should come before any stream capture. In host
-// code the name g_blasSetupScratch is only a host-side stand-in for the
-// symbol, never a device address: kernels get the resolved pointer.
+// Set-up: every call looks the array's device address up with
+// cudaGetSymbolAddress in the caller's current context (the device that is
+// current at the call) and passes that pointer to the kernel; nothing is
+// cached, so a context created after cudaDeviceReset, or a caller that makes
+// its own context current, gets the address in that context. The first call
+// in a context may load the library's device code (lazy module loading):
+// make it before any stream capture. In host code the name g_blasSetupScratch
+// is only a host-side stand-in for the symbol, never a device address.
 #include <algorithm>
-#include <atomic>
 #include <cstring>
-#include <mutex>
 
 #include "tc_kernels.h"
 #include "tc_stage.cuh"
@@ -43,42 +44,12 @@ static_assert(TC_NOALLOC_MAX_INSTANCES % kInstanceTile == 0, "whole tiles");
 
 static __device__ __align__(256) unsigned char g_blasSetupScratch[kNoAllocBytes];
 
-constexpr int               kCachedDevices = 64;
-std::atomic<unsigned char*> g_scratchAddress[kCachedDevices];
-std::mutex                  g_setupMutex;
-
-// Device address of g_blasSetupScratch on the current device (set-up on the
-// first call per device).
+// Device address of g_blasSetupScratch in the current context.
 tc_status scratch_address(unsigned char** out)
 {
-  int device = 0;
-  if(cudaGetDevice(&device) != cudaSuccess)
-    return TC_ERR_CUDA;
-  const bool cached = device >= 0 && device < kCachedDevices;
-  if(cached)
-  {
-    unsigned char* p = g_scratchAddress[device].load(std::memory_order_acquire);
-    if(p)
-    {
-      *out = p;
-      return TC_OK;
-    }
-  }
-  std::lock_guard<std::mutex> lock(g_setupMutex);
-  if(cached)
-  {
-    unsigned char* p = g_scratchAddress[device].load(std::memory_order_acquire);
-    if(p)
-    {
-      *out = p;
-      return TC_OK;
-    }
-  }
   void* address = nullptr;
   if(cudaGetSymbolAddress(&address, g_blasSetupScratch) != cudaSuccess || address == nullptr)
     return TC_ERR_CUDA;
-  if(cached)
-    g_scratchAddress[device].store(static_cast<unsigned char*>(address), std::memory_order_release);
   *out = static_cast<unsigned char*>(address);
   return TC_OK;
 }
@@ -122,6 +93,7 @@ extern "C" tc_status tc_blas_setup_insertion_noalloc(const tc_frame_args* a, uin
   c.scratch.lbStride     = kNoAllocTiles;
   c.scratch.selfClean    = 0;  // cleared by the memset above
   c.scratch.itemCapacity = TC_NOALLOC_MAX_INSTANCES;
+  c.spinLimit            = kSpinLimit;
   if(launch_blas_setup_insertion(c, tiles, kInstanceTile, s) != cudaSuccess)
     return TC_ERR_CUDA;
   return TC_OK;

@@ -311,7 +311,8 @@ __global__ void __launch_bounds__(B) k_triangle_split(StageCtx c)
       u64       base = 0;
       if(tile == 0)
         base = q == kCntSplit ? b->splitWriteCounter : part_base(c);
-      const u64 ex = warp_lookback_exclusive(c.scratch.lbState + (u64)q * c.scratch.lbStride, tile, agg, base, c.errorWord);
+      const u64 ex = warp_lookback_exclusive(c.scratch.lbState + (u64)q * c.scratch.lbStride, tile, agg, base, c.errorWord,
+                                  c.spinLimit);
       if(lane == 0)
       {
         s_excl[q] = ex;

@@ -69,7 +69,7 @@ struct StageCtx
   u32                           numInstances;
   u32                           numTextures;
   u32                           flags;
-  u32                           _pad0;
+  u32                           spinLimit;  // polls before a look-back wait gives up
   Table                         table;
   tc_caps                       caps;
   u32*                          errorWord;

@@ -22,8 +22,9 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 
 
 def main() -> int:
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    subprocess.check_call(["make", "-C", os.path.join(REPO, "oracle"), "ref", f"REF_ROOT={ref_root}"])
+    # the checkout: argv[1], else TC_REFERENCE_ROOT, else the oracle recipe's default
+    extra = [f"REF_ROOT={sys.argv[1]}"] if len(sys.argv) > 1 else []
+    subprocess.check_call(["make", "-C", os.path.join(REPO, "oracle"), "ref"] + extra)
     dumper = os.path.join(REPO, "oracle", "_ref", "ref_table_dump")
     tmp = os.path.join(REPO, "oracle", "_ref", "tess_table_nv.bin")
     subprocess.check_call([dumper, tmp])

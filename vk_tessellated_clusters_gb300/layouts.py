@@ -215,11 +215,11 @@ class Schedule(ctypes.Structure):
     _fields_ = [("classifyBlocksPerSM", ctypes.c_uint32), ("splitBlockSize", ctypes.c_uint32),
                 ("vertexBlocksPerSM", ctypes.c_uint32), ("scanBlocksPerSM", ctypes.c_uint32),
                 ("blocksPerSM", ctypes.c_uint32), ("fullVertexBlocksPerSM", ctypes.c_uint32),
-                ("vertexGridPerSM", ctypes.c_uint32), ("_pad", ctypes.c_uint32)]
+                ("vertexGridPerSM", ctypes.c_uint32), ("lookbackSpinLimit", ctypes.c_uint32)]
 
 
 SCHEDULE_FIELDS = ("classifyBlocksPerSM", "splitBlockSize", "vertexBlocksPerSM", "scanBlocksPerSM", "blocksPerSM",
-                   "fullVertexBlocksPerSM", "vertexGridPerSM")
+                   "fullVertexBlocksPerSM", "vertexGridPerSM", "lookbackSpinLimit")
 
 
 RASTER_BATCH_VERTICES, RASTER_BATCH_TRIANGLES = 96, 121

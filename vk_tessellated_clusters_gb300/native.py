@@ -57,6 +57,7 @@ def _bind(lib):
         "tc_raster_batches": (st, [vp, ctypes.POINTER(L.FrameArgs), ctypes.POINTER(L.RasterOutputs), vp]),
         "tc_read_device_errors": (st, [vp, ctypes.POINTER(u32), vp]),
         "tc_launch_count": (u64, [vp]),
+        "tc_lookback_probe": (st, [vp, u32, ctypes.POINTER(u64), vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -75,7 +76,7 @@ def exported_symbols() -> list[str]:
         "tc_blas_setup_insertion", "tc_blas_clusters_insert", "tc_blas_setup_insertion_noalloc",
         "tc_split_pass_count", "tc_instantiate_backward",
         "tc_generate_vertices", "tc_decode_hits", "tc_raster_batches",
-        "tc_read_device_errors", "tc_launch_count",
+        "tc_read_device_errors", "tc_launch_count", "tc_lookback_probe",
     ]
 
 

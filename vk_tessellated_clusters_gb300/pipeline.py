@@ -33,6 +33,7 @@ class TessellationPipeline:
         self.device = device
         self.scene = scene
         self.caps = dict(caps or L.default_caps())
+        self.flags = flags
         self.mem = DeviceMemory(device)
         self.state = FrameState(scene, self.mem, self.caps, flags)
         desc = L.ContextDesc()
@@ -105,6 +106,15 @@ class TessellationPipeline:
         bits = ctypes.c_uint32()
         native.check(self.lib.tc_read_device_errors(self.ctx, ctypes.byref(bits), self.stream()), "tc_read_device_errors")
         return bits.value
+
+    def lookback_probe(self, published: bool) -> int:
+        """tc_lookback_probe: one bounded look-back wait for a predecessor that
+        is published (returns its prefix, 7) or never is (the wait runs out
+        after the schedule's lookbackSpinLimit polls and returns 0)."""
+        out = ctypes.c_uint64()
+        native.check(self.lib.tc_lookback_probe(self.ctx, 1 if published else 0, ctypes.byref(out), self.stream()),
+                     "tc_lookback_probe")
+        return out.value
 
     def outputs(self) -> dict:
         self.torch.cuda.synchronize(self.device)
