@@ -19,14 +19,27 @@ def caps():
     return L.default_caps(visible_bits=14, part_bits=17, split_bits=14, vertex_bits=21, megs=256)
 
 
-@pytest.fixture(scope="module")
-def setup(oracle):
+# reduced: subdivision 4, 256² map, a far camera mixing 59 full clusters and
+# 1344 part triangles; config3: the plain small config at full size (icosphere
+# of 20,480 triangles, 1024² fp32 map of 4 octaves, camera at distance 3,
+# 8 px per segment), the frame the backward is specified on
+CASES = {
+    "reduced": dict(subdivisions=4, map_size=256,
+                    cam=S.Camera(eye=(0.0, 0.0, 8.0), center=(0.0, 0.0, 0.0), tess_rate_pixels=8.0)),
+    "config3": dict(subdivisions=5, map_size=1024, cam=S.camera_icosphere()),
+}
+
+
+@pytest.fixture(scope="module", params=sorted(CASES))
+def setup(oracle, request):
     import torch
     from vk_tessellated_clusters_gb300.autograd import FrozenFrame, tessellate
     from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
-    sc = S.scene_icosphere(subdivisions=4, map_size=256)
-    # at this distance the frame mixes 59 full clusters and 1344 part triangles
-    cam = S.Camera(eye=(0.0, 0.0, 8.0), center=(0.0, 0.0, 0.0), tess_rate_pixels=8.0)
+    case = CASES[request.param]
+    sc = S.scene_icosphere(subdivisions=case["subdivisions"], map_size=case["map_size"])
+    if request.param == "config3":
+        assert sc.total_triangles == 20480 and sc.textures[0].texels.shape == (1024, 1024)
+    cam = case["cam"]
     pipe = TessellationPipeline(sc, caps(), FLAGS)
     pipe.set_cameras(cam)
     pipe.build("batched")
@@ -36,7 +49,7 @@ def setup(oracle):
     tex = frozen.texels[0]
     orig = tex.detach().clone()
     with torch.no_grad():
-        tex.copy_(torch.from_numpy(S.value_noise(256, 4, seed=11)).to(tex.device))
+        tex.copy_(torch.from_numpy(S.value_noise(case["map_size"], 4, seed=11)).to(tex.device))
     target = frozen.generate()
     with torch.no_grad():
         tex.copy_(orig)

@@ -42,6 +42,9 @@ def test_icosphere_batched_bit_exact(oracle, icosphere):
     # spec bar and the error against the FP64 twin
     ref64 = oracle.vertices_f64(ref_state, len(ref["genVertices"]))
     err = max_position_error(out["genVertices"], ref64)
+    d = np.abs(out["genVertices"].astype(np.float64) - ref64)
+    print(f"icosphere (config 0): |GPU - FP64| max {err:.3e} rms {np.sqrt((d ** 2).mean()):.3e} "
+          f"(scene diagonal {scene_diagonal(icosphere):.3f})")
     assert err <= 1e-5 * scene_diagonal(icosphere), err
     pipe.close()
 

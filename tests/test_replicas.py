@@ -48,3 +48,35 @@ def test_replica_totals_with_two_gloo_ranks():
 def test_replica_totals_single_process_is_identity():
     import bench
     assert bench.replica_totals(0.25, 7.0, "cpu") == (0.25, 7.0)
+
+
+_RANK_SCRIPT = """
+import json, os, sys
+sys.path.insert(0, {root!r})
+import torch.distributed as dist
+import bench
+rank, world, local = bench.dist_env()
+dist.init_process_group("gloo")
+seconds, tris = bench.replica_totals(0.5 + rank, 1000.0 * (rank + 1), "cpu")
+dist.barrier()
+if rank == 0:
+    print(json.dumps({{"n_gpus": world, "local_rank": local, "seconds": seconds, "tris": tris}}))
+dist.destroy_process_group()
+"""
+
+
+def test_spawn_path_runs_two_gloo_replicas(tmp_path, capfd):
+    """bench.py --gpus N without torchrun spawns N ranks with torchrun's
+    environment; here two gloo ranks on the CPU run the replica reduction and
+    rank 0 alone prints."""
+    import json
+
+    import bench
+    script = tmp_path / "rank.py"
+    script.write_text(_RANK_SCRIPT.format(root=os.path.dirname(os.path.dirname(os.path.abspath(__file__)))))
+    import sys
+    assert bench.spawn_replicas([sys.executable, str(script)], 2) == 0
+    out = [line for line in capfd.readouterr().out.splitlines() if line.startswith("{")]
+    assert len(out) == 1
+    got = json.loads(out[0])
+    assert got == {"n_gpus": 2, "local_rank": 0, "seconds": 1.5, "tris": 3000.0}
