@@ -302,6 +302,39 @@ def profile_stages(pipe, torch, frames, set_frame, flush, reps=1):
     return acc, outs
 
 
+def split_timings(pipe, torch, frames, set_frame, flush):
+    """The split stage both ways on the same frames (CUDA events on the
+    launching stream): every pass its own launch with the SPLIT_PASS set-up
+    between (the reference's multipass dispatches) against all passes in one
+    launch (tc_triangle_split_all, what the frame graph uses)."""
+    from vk_tessellated_clusters_gb300 import layouts as L
+    n = pipe.args.numInstances
+    passes = pipe.split_passes()
+    res = {"passes": passes, "per_pass_launches_ms": [], "one_launch_ms": []}
+    for f in frames:
+        for form in ("per_pass_launches_ms", "one_launch_ms"):
+            set_frame(f)
+            for name, extra in stage_sequence(pipe, n)[:6]:  # frame_begin .. BUILD_SETUP_SPLIT
+                pipe.stage(name, *extra)
+            flush()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            if form == "one_launch_ms":
+                pipe.stage("triangle_split_all")
+            else:
+                for p in range(passes):
+                    pipe.stage("triangle_split", 0, n)
+                    if p + 1 < passes:
+                        pipe.stage("build_setup", L.BUILD_SETUP_SPLIT_PASS)
+            e1.record()
+            torch.cuda.synchronize()
+            res[form].append(e0.elapsed_time(e1))
+    res["per_pass_launches_ms"] = statistics.median(res["per_pass_launches_ms"])
+    res["one_launch_ms"] = statistics.median(res["one_launch_ms"])
+    res["split_items"] = int(pipe.outputs()["readback"]["numSplitTriangles"])
+    return res
+
+
 def run_ours(args):
     import torch
     from vk_tessellated_clusters_gb300 import build_lib, native
@@ -556,6 +589,7 @@ def terrain_bandwidth(torch, dev, local, peak, tune=True):
         frame_ms.append(e0.elapsed_time(e1))
     res["frame_ms_graph"] = statistics.median(frame_ms)
     res["tris_per_s"] = res["tessellated_tris"] / (res["frame_ms_graph"] / 1e3)
+    res["split"] = split_timings(pipe, torch, [0, 0, 0], lambda f: None, lambda: flush_buf.fill_(1))
     res["device_errors"] = pipe.device_errors()
     pipe.close()
     return res

@@ -471,6 +471,11 @@ typedef struct tc_schedule {
   uint32_t lookbackSpinLimit;   /* polls a bounded look-back wait makes before it gives up, sets
                                  * TC_DEVERR_LOOKBACK_TIMEOUT and goes on with what it has (the frame's offsets are
                                  * then unreliable); 0: the default, 2^22 polls (seconds, with back-off) */
+  uint32_t frameShape;          /* the batched frame's graph: 0 allocates the first part run (classify's parts) on a
+                                 * side stream while the split passes run, the later runs after them; 1 allocates
+                                 * every run once after the split passes (fewer launches when splits are rare).
+                                 * Outputs are identical. */
+  uint32_t _pad[1];
 } tc_schedule;
 
 typedef struct tc_context_desc {
@@ -573,6 +578,13 @@ tc_status tc_triangle_instantiate(tc_context* ctx, const tc_frame_args* args, ui
  * output exactly. */
 tc_status tc_triangle_instantiate_run(tc_context* ctx, const tc_frame_args* args, uint32_t run, uint32_t instanceBegin,
                                       uint32_t instanceEnd, void* stream);
+/* Every pass of triangle_split in one launch (triangle_split.comp.glsl:146-331,
+ * whose main_persistent :476-594 is the reference's single-dispatch form): the
+ * same output as tc_triangle_split for each pass with
+ * tc_build_setup(TC_BUILD_SETUP_SPLIT_PASS) between passes, for the whole
+ * instance range; call it after tc_build_setup(TC_BUILD_SETUP_SPLIT) and follow
+ * it with tc_build_setup(TC_BUILD_SETUP_INSTANTIATE_TESS). */
+tc_status tc_triangle_split_all(tc_context* ctx, const tc_frame_args* args, void* stream);
 /* shaders/blas_setup_insertion.comp.glsl:100-116 */
 tc_status tc_blas_setup_insertion(tc_context* ctx, const tc_frame_args* args, void* stream);
 /* shaders/blas_clusters_insert.comp.glsl:97-136 (template instantiations) */
@@ -769,6 +781,7 @@ static_assert(sizeof(tc_FrameConstants) == 784, "FrameConstants prefix");
 static_assert(sizeof(tc_Readback) == 880, "Readback");
 static_assert(sizeof(tc_DisplacementTexture) == 24, "DisplacementTexture");
 static_assert(sizeof(tc_frame_args) == 96, "frame args");
+static_assert(sizeof(tc_schedule) == 40, "schedule");
 #endif
 
 #endif /* TC_TESSELLATION_H_ */

@@ -144,15 +144,26 @@ def test_split_factor_variants(oracle):
         pipe.close()
 
 
-def test_per_stage_entry_points_match_frame(oracle, icosphere):
-    """Driving the stages one by one through the C ABI equals the fused frame."""
+@pytest.mark.parametrize("split", ["per_pass", "all_passes"])
+@pytest.mark.parametrize("camera", ["far", "close"])
+def test_per_stage_entry_points_match_frame(oracle, icosphere, split, camera):
+    """Driving the stages one by one through the C ABI equals the fused frame,
+    with the split passes one call each (and the SPLIT_PASS set-ups between
+    them) or all in one tc_triangle_split_all call; the close camera makes
+    the split passes fire."""
     from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
     caps = small_caps()
+    sc = icosphere
     cam = S.camera_icosphere()
-    pipe = TessellationPipeline(icosphere, caps, FLAGS)
+    if camera == "close":
+        sc = S.scene_icosphere(subdivisions=3, map_size=256)
+        cam = S.Camera(eye=(0.0, 0.0, 1.08), center=(0.0, 0.0, 0.0), tess_rate_pixels=1.0, near=0.01, far=10.0)
+    pipe = TessellationPipeline(sc, caps, FLAGS)
     pipe.set_cameras(cam)
     pipe.build("batched")
     want = pipe.outputs()
+    if camera == "close":
+        assert int(want["readback"]["numSplitTriangles"]) > 0
     pipe.stage("frame_begin")
     pipe.stage("instances_classify")
     pipe.stage("clusters_cull", 0, 1)
@@ -160,10 +171,13 @@ def test_per_stage_entry_points_match_frame(oracle, icosphere):
     pipe.stage("cluster_classify", 0, 1)
     pipe.stage("build_setup", L.BUILD_SETUP_SPLIT)
     passes = pipe.split_passes()
-    for p in range(passes):
-        pipe.stage("triangle_split", 0, 1)
-        if p + 1 < passes:
-            pipe.stage("build_setup", L.BUILD_SETUP_SPLIT_PASS)
+    if split == "all_passes":
+        pipe.stage("triangle_split_all")
+    else:
+        for p in range(passes):
+            pipe.stage("triangle_split", 0, 1)
+            if p + 1 < passes:
+                pipe.stage("build_setup", L.BUILD_SETUP_SPLIT_PASS)
     pipe.stage("build_setup", L.BUILD_SETUP_INSTANTIATE_TESS)
     pipe.stage("triangle_instantiate", 0, 0xFFFFFFFF)
     pipe.stage("build_setup", L.BUILD_SETUP_BUILD_BLAS)
@@ -207,11 +221,11 @@ def test_schedules_change_timing_only(oracle):
         dict(classifyBlocksPerSM=4, scanBlocksPerSM=2, splitBlockSize=128, blocksPerSM=2, vertexBlocksPerSM=2,
              vertexGridPerSM=1),
         dict(classifyBlocksPerSM=16, scanBlocksPerSM=16, splitBlockSize=512, blocksPerSM=4, vertexBlocksPerSM=5,
-             fullVertexBlocksPerSM=8),
+             fullVertexBlocksPerSM=8, frameShape=1),
         dict(classifyBlocksPerSM=6, scanBlocksPerSM=1, splitBlockSize=256, blocksPerSM=1, vertexBlocksPerSM=1,
              fullVertexBlocksPerSM=1),
         dict(classifyBlocksPerSM=1, scanBlocksPerSM=4, splitBlockSize=256, blocksPerSM=1, vertexBlocksPerSM=6,
-             vertexGridPerSM=32),
+             vertexGridPerSM=32, frameShape=0),
     ]
     for sched in schedules:
         pipe.set_schedule(sched)
@@ -221,9 +235,36 @@ def test_schedules_change_timing_only(oracle):
             assert_same(pipe.outputs(), ref, f"schedule {sched} {mode}", vertex_tol=vertex_tolerance(sc))
     assert pipe.device_errors() == 0
     for bad in (dict(splitBlockSize=64), dict(vertexBlocksPerSM=0), dict(scanBlocksPerSM=65),
-                dict(fullVertexBlocksPerSM=65), dict(vertexGridPerSM=65)):
+                dict(fullVertexBlocksPerSM=65), dict(vertexGridPerSM=65), dict(frameShape=2)):
         with pytest.raises(native.TcError):
             pipe.set_schedule(bad)
+    pipe.close()
+
+
+@pytest.mark.parametrize("case", ["splits", "transient"])
+def test_frame_shapes_identical(oracle, case):
+    """Both frame-graph shapes (the first part run allocated beside the split
+    passes, or every run after them) give the oracle's output, on a
+    split-heavy frame and on one with 1X + 2X transient builds."""
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    sc = S.scene_icosphere(subdivisions=3, map_size=256)
+    cam = S.Camera(eye=(0.0, 0.0, 1.08), center=(0.0, 0.0, 0.0), tess_rate_pixels=1.0, near=0.01, far=10.0)
+    flags = FLAGS | ((L.FLAG_TRANSIENT_1X | L.FLAG_TRANSIENT_2X) if case == "transient" else 0)
+    if case == "transient":
+        sc, cam = S.scene_icosphere(), S.camera_icosphere()
+    caps = small_caps()
+    ref_state, _ = oracle.frame(sc, cam, caps, flags)
+    ref = ref_state.outputs(oracle.entries)
+    if case == "splits":
+        assert int(ref["readback"]["numSplitTriangles"]) > 0
+    pipe = TessellationPipeline(sc, caps, flags)
+    pipe.set_cameras(cam)
+    for shape in (1, 0):
+        pipe.set_schedule({"frameShape": shape})
+        for mode in ("batched", "graph"):
+            pipe.build(mode)
+            assert_same(pipe.outputs(), ref, f"{case} shape {shape} {mode}", vertex_tol=vertex_tolerance(sc))
+    assert pipe.device_errors() == 0
     pipe.close()
 
 

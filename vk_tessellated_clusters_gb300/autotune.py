@@ -5,7 +5,9 @@ grid multipliers of the classify warp kernels and of the instantiate
 allocation, the vertex kernel's register budget, the grid of the
 full-cluster vertex kernel (which runs beside the rest of the frame), the
 split tile size
-(128 threads x 16 items, 256 or 512 threads x 32 items) and the split grid.
+(128 threads x 16 items, 256 or 512 threads x 32 items), the split grid, and
+the frame graph's shape (the first part run allocated beside the split passes,
+or every run after them).
 Outputs do not depend on it (every allocation is a prefix sum in a fixed
 order), so tuning is a pure timing search.
 
@@ -29,6 +31,7 @@ SPACE = {
     "vertexBlocksPerSM": (3, 4, 5, 6),
     "fullVertexBlocksPerSM": (1, 2, 3, 4),
     "vertexGridPerSM": (0, 8, 16),
+    "frameShape": (0, 1),
 }
 
 

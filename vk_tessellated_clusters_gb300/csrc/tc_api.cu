@@ -26,9 +26,10 @@ struct SlotPlan
   size_t ctrlOffset;  // ticket, done (u32 x2) + totals (u64 x kMaxCounters)
 };
 
-constexpr size_t kCtrlBytes = 8 + 8 * kMaxCounters;
+constexpr size_t kCtrlBytes = 64;  // ticket, done, totals (u64 x kMaxCounters), then the split levels' words
+static_assert(8 + 8 * kMaxCounters <= 48, "the split levels' control words start at byte 48");
 
-// kernels of a batched frame besides the split passes: frame_begin,
+// kernels of a batched frame besides the split launch (every pass in one): frame_begin,
 // frame_begin + instances_classify (one launch), clusters_cull, classify (3),
 // instantiate (4, twice: the first part run overlapped with the split passes,
 // then the others), blas setup, blas insert (2)
@@ -51,6 +52,7 @@ struct Plan
   size_t clsCountsOffset, clsTriWordsOffset, clsBlockSumsOffset, clsFullRecsOffset;
   size_t rasterOffset;
   size_t partVertexOffset;  // u32 per part triangle
+  size_t chunkSumsOffset;   // u64 per 32 part triangles
   size_t splitBaseOffset;   // 9 floats per split item: its base triangle's world positions
   size_t instOffset;  // instance cluster prefix (u32 x maxInstances+1)
   size_t errOffset;   // device error word
@@ -182,6 +184,8 @@ Plan make_plan(const tc_context_desc& d)
   off = align_up(off + (size_t)p.classifyCap * 8 + 8, 256);
   p.partVertexOffset  = off;
   off                 = align_up(off + (size_t)std::max(1u, k.maxPartTriangles) * 4, 256);
+  p.chunkSumsOffset   = off;
+  off                 = align_up(off + (size_t)ceil_div(std::max(1u, k.maxPartTriangles), 1024) * 32 * 8, 256);
   p.splitBaseOffset   = off;
   off                 = align_up(off + (size_t)std::max(1u, k.maxSplitTriangles) * 36, 256);
   p.rasterOffset      = off;  // raster batching: per group of 32 parts its counts, then offsets
@@ -274,7 +278,8 @@ ClassifyBuffers classify_buffers(tc_context* ctx)
 
 InstantiateBuffers instantiate_buffers(tc_context* ctx)
 {
-  return {reinterpret_cast<u32*>(ctx->dScratch + ctx->plan.partVertexOffset)};
+  return {reinterpret_cast<u32*>(ctx->dScratch + ctx->plan.partVertexOffset),
+          reinterpret_cast<unsigned long long*>(ctx->dScratch + ctx->plan.chunkSumsOffset)};
 }
 
 u32 persistent_grid(const tc_context* ctx, u32 maxTiles, u32 blocksPerSM)
@@ -290,9 +295,10 @@ u32 frame_begin_grid(const tc_context* ctx, const tc_frame_args* a)
 
 // kernels one batched frame launches (the BLAS set-up is fused for up to
 // kBlasSetupFusedMax instances)
-uint64_t frame_launches(const tc_frame_args* a)
+uint64_t frame_launches(const tc_context* ctx, const tc_frame_args* a)
 {
-  return kFrameFixedLaunches + split_passes(a->caps.splitFactor) - (a->numInstances <= kBlasSetupFusedMax ? 1 : 0)
+  return kFrameFixedLaunches + 1 - (a->numInstances <= kBlasSetupFusedMax ? 1 : 0)
+         - (ctx->schedule.frameShape == 1 ? 4 : 0)  // one allocation + vertex launch instead of two
          + ((a->flags & TC_FLAG_TRANSIENT_2X) ? 1 : 0);  // the 2X batches' vertices
 }
 
@@ -300,6 +306,21 @@ u32 insert_grid(const tc_context* ctx, const tc_frame_args* a)
 {
   // tiles of 1024 instantiations per block (at least four blocks per SM)
   return std::max(ctx->numSMs * 4, std::min(ceil_div(a->caps.maxGeneratedClusters, 1024), 1u << 16));
+}
+
+SplitLevels split_levels(const tc_context* ctx, u32 passes)
+{
+  SplitLevels lv = {};
+  const Plan& p  = ctx->plan;
+  lv.levels      = std::min(passes, kMaxSplitLevels);
+  lv.stride      = p.slots[p.slotSplit0].stride;
+  for(u32 L = 0; L < lv.levels; L++)
+  {
+    const SlotPlan& s = p.slots[p.slotSplit0 + L];
+    lv.lbState[L]     = reinterpret_cast<unsigned long long*>(ctx->dScratch + s.stateOffset);
+    lv.ctrl[L]        = reinterpret_cast<u32*>(ctx->dScratch + s.ctrlOffset);
+  }
+  return lv;
 }
 
 u32 split_block(const tc_schedule& s)
@@ -364,6 +385,8 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
                                               std::min(a->totalClusters, a->caps.maxVisibleClusters), ctx->numSMs,
                                               sched.fullVertexBlocksPerSM, ctx->side2));
   TC_CHECK_CUDA(cudaEventRecord(ctx->evJoin2, ctx->side2));
+  const bool earlyRun0 = sched.frameShape == 0;
+  if(earlyRun0)
   {
     StageCtx c0 = c;
     bind_slot(ctx, c0, p.slotInstantiate0, false);
@@ -376,19 +399,21 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
                                               sched.vertexBlocksPerSM, sched.vertexGridPerSM, ctx->side));
   }
 
-  const u32 passes = split_passes(a->caps.splitFactor);
-  const u32 sb     = split_block(sched);
-  for(u32 q = 0; q < passes; q++)
+  // every split pass in one persistent launch (level by level inside)
   {
-    bind_slot(ctx, c, p.slotSplit0 + q, false);
-    c.fuseSetup = (q + 1 < passes) ? TC_BUILD_SETUP_SPLIT_PASS : TC_BUILD_SETUP_INSTANTIATE_TESS;
-    TC_CHECK_CUDA(launch_triangle_split(
-        c, sb, persistent_grid(ctx, ceil_div(a->caps.maxSplitTriangles, split_items_per_tile(sb)), bpsm * (512 / sb)), s));
+    const u32   sb = split_block(sched);
+    SplitLevels lv = split_levels(ctx, split_passes(a->caps.splitFactor));
+    bind_slot(ctx, c, p.slotSplit0, false);
+    c.fuseSetup = TC_BUILD_SETUP_INSTANTIATE_TESS;
+    TC_CHECK_CUDA(launch_triangle_split_levels(
+        c, lv, sb, persistent_grid(ctx, ceil_div(a->caps.maxSplitTriangles, split_items_per_tile(sb)), bpsm * (512 / sb)),
+        s));
   }
-  TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evJoin, 0));
+  if(earlyRun0)
+    TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evJoin, 0));
   bind_slot(ctx, c, p.slotInstantiate, false);
   c.fuseSetup = TC_BUILD_SETUP_BUILD_BLAS;
-  c.run       = kRunsAfterFirst;
+  c.run       = earlyRun0 ? kRunsAfterFirst : kAllRuns;
   // up to kBlasSetupFusedMax instances the BLAS list offsets are computed by
   // the argument kernel's last block instead of a launch of their own
   const bool fuseBlas = a->numInstances <= kBlasSetupFusedMax;
@@ -414,7 +439,7 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evVerts, 0));
   TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evJoin2, 0));
 
-  ctx->launches += frame_launches(a);
+  ctx->launches += frame_launches(ctx, a);
   return TC_OK;
 }
 
@@ -493,7 +518,7 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
     delete ctx;
     return TC_ERR_CUDA;
   }
-  ctx->schedule = {4, 256, 4, 4, 1, kDefaultFullVertexBlocksPerSM, 0, 0};  // the batched scene's tuned shape
+  ctx->schedule = {4, 256, 4, 4, 1, kDefaultFullVertexBlocksPerSM, 0, 0, 0, {0}};  // the batched scene's tuned shape
   ctx->plan     = make_plan(*desc);
   if(cudaMalloc(&ctx->dScratch, ctx->plan.totalBytes) != cudaSuccess
      || cudaMemset(ctx->dScratch, 0, ctx->plan.totalBytes) != cudaSuccess)
@@ -648,7 +673,7 @@ tc_status tc_set_schedule(tc_context* ctx, const tc_schedule* schedule)
       return TC_ERR_INVALID_ARG;
   if(q.splitBlockSize != 128 && q.splitBlockSize != 256 && q.splitBlockSize != 512)
     return TC_ERR_INVALID_ARG;
-  if(q.fullVertexBlocksPerSM > 64 || q.vertexGridPerSM > 64)
+  if(q.fullVertexBlocksPerSM > 64 || q.vertexGridPerSM > 64 || q.frameShape > 1)
     return TC_ERR_INVALID_ARG;
   ctx->schedule   = *schedule;
   if(ctx->schedule.fullVertexBlocksPerSM == 0)
@@ -718,7 +743,7 @@ tc_status tc_frame_build_graph(tc_context* ctx, const tc_frame_args* args, void*
     ctx->graphValid    = true;
   }
   TC_CHECK_CUDA(cudaGraphLaunch(ctx->graphExec, s));
-  ctx->launches += frame_launches(args);
+  ctx->launches += frame_launches(ctx, args);
   return TC_OK;
 }
 
@@ -828,6 +853,32 @@ tc_status tc_triangle_split(tc_context* ctx, const tc_frame_args* a, uint32_t in
   return TC_OK;
 }
 
+tc_status tc_triangle_split_all(tc_context* ctx, const tc_frame_args* a, void* stream)
+{
+  tc_status st = validate(ctx, a);
+  if(st != TC_OK)
+    return st;
+  cudaStream_t s      = reinterpret_cast<cudaStream_t>(stream);
+  const Plan&  p      = ctx->plan;
+  const u32    passes = split_passes(a->caps.splitFactor);
+  // the levels' look-back rows and control words start at zero
+  const SlotPlan& first = p.slots[p.slotSplit0];
+  const SlotPlan& last  = p.slots[p.slotSplit0 + passes - 1];
+  TC_CHECK_CUDA(cudaMemsetAsync(ctx->dScratch + first.stateOffset, 0, last.ctrlOffset + kCtrlBytes - first.stateOffset, s));
+  StageCtx c = base_ctx(ctx, a);
+  bind_slot(ctx, c, p.slotSplit0, false);
+  c.fuseSetup          = kNoSetup;  // the caller's BUILD_SETUP_INSTANTIATE_TESS follows, as after the last pass
+  const u32 sb         = split_block(ctx->schedule);
+  const SplitLevels lv = split_levels(ctx, passes);
+  TC_CHECK_CUDA(launch_triangle_split_levels(
+      c, lv, sb,
+      persistent_grid(ctx, ceil_div(a->caps.maxSplitTriangles, split_items_per_tile(sb)),
+                      std::max(1u, ctx->schedule.blocksPerSM) * (512 / sb)),
+      s));
+  ctx->launches += 1;
+  return TC_OK;
+}
+
 tc_status tc_triangle_instantiate_run(tc_context* ctx, const tc_frame_args* a, uint32_t run, uint32_t instanceBegin,
                                       uint32_t instanceEnd, void* stream)
 {
@@ -843,10 +894,12 @@ tc_status tc_triangle_instantiate_run(tc_context* ctx, const tc_frame_args* a, u
   c.instEnd   = instanceEnd;
   c.run       = run;
   bind_slot(ctx, c, ctx->plan.slotInstantiate, true);
-  TC_CHECK_CUDA(launch_triangle_instantiate(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
-                                            ctx->schedule.scanBlocksPerSM, ctx->schedule.vertexBlocksPerSM,
-                                            ctx->schedule.vertexGridPerSM, reinterpret_cast<cudaStream_t>(stream)));
-  ctx->launches += 4;
+  // one kernel for arguments and vertices (the frame graph keeps them apart:
+  // its BLAS lists need the arguments only)
+  TC_CHECK_CUDA(launch_instantiate_fused(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
+                                         ctx->schedule.scanBlocksPerSM, ctx->schedule.vertexBlocksPerSM,
+                                         ctx->schedule.vertexGridPerSM, reinterpret_cast<cudaStream_t>(stream)));
+  ctx->launches += (a->flags & (TC_FLAG_PN | TC_FLAG_RIPPLE)) ? 4 : 3;
   return TC_OK;
 }
 

@@ -261,18 +261,10 @@ __global__ void __launch_bounds__(256) k_generate_vertices(StageCtx c)
         tc_DisplacementTexture tx = {};
         if(haveTextures && in.displacementIndex >= 0 && (u32)in.displacementIndex < c.numTextures)
           tx = c.textures[in.displacementIndex];
-        f3 bp[3], bn[3];
-        f2 bt[3];
-#pragma unroll
-        for(int k = 0; k < 3; k++)
-        {
-          const u32 vi = cl.firstLocalVertex + lt[tri * 3 + k];
-          bp[k]        = ldg3(reinterpret_cast<const float*>(in.positions), vi);
-          bn[k]        = ldg3(reinterpret_cast<const float*>(in.normals), vi);
-          bt[k]        = ldg2(reinterpret_cast<const float*>(in.texcoords), vi);
-        }
-        write_part_affine(r, pi.subTriangle.vtxEncoded, cfg_flipped(cfg), bp, bn, bt, e.firstVertex, tx,
-                          in.displacementScale * vscale, in.displacementOffset + voffset);
+        part_affine(r, pi.subTriangle.vtxEncoded, cfg_flipped(cfg), reinterpret_cast<const float*>(in.positions),
+                    reinterpret_cast<const float*>(in.normals), reinterpret_cast<const float*>(in.texcoords),
+                    cl.firstLocalVertex, lt + tri * 3, e.firstVertex, tx, in.displacementScale * vscale,
+                    in.displacementOffset + voffset);
       }
       __syncwarp();
       for(u32 v = lane; v < e.numVertices; v += 32)

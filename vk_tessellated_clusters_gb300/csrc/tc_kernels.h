@@ -65,10 +65,23 @@ cudaError_t launch_classify_full_vertices(const StageCtx& c, const ClassifyBuffe
                                           u32 blocksPerSM, cudaStream_t s);
 u32         classify_max_blocks(u32 maxClusters);
 cudaError_t launch_triangle_split(const StageCtx& c, u32 blockSize, u32 grid, cudaStream_t s);
+// every split pass in one launch: per level its look-back rows and control
+// words (a scratch slot each; the ticket of level 0's slot is the launch's)
+constexpr u32 kMaxSplitLevels = 16;
+struct SplitLevels
+{
+  unsigned long long* lbState[kMaxSplitLevels];  // [2][stride] per level
+  u32*                ctrl[kMaxSplitLevels];     // 16 words per level (see tc_split.cu)
+  u32                 stride;                    // tiles per level the rows hold
+  u32                 levels;                    // split passes
+};
+cudaError_t launch_triangle_split_levels(const StageCtx& c, const SplitLevels& lv, u32 blockSize, u32 grid,
+                                         cudaStream_t s);
 // triangle_tess_template_instantiate scratch, per part triangle
 struct InstantiateBuffers
 {
-  u32* vertexOffset;  // first generated vertex of each accepted part, ~0 otherwise
+  u32*                vertexOffset;  // first generated vertex of each accepted part, ~0 otherwise
+  unsigned long long* chunkSums;     // per 32 parts: packed (CLAS bytes << 20 | vertices)
 };
 
 // four launches (tile sums, tile scan, args, vertices); the slot needs 3 state rows of
@@ -84,6 +97,10 @@ cudaError_t launch_instantiate_alloc(const StageCtx& c, const InstantiateBuffers
 cudaError_t launch_instantiate_vertices(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
                                         u32 vertexBlocksPerSM, u32 vertexGridPerSM, cudaStream_t s);
 u32         instantiate_alloc_tiles(u32 maxParts);
+// the stage entry point's form: tile sums, tile scan, then arguments and
+// vertices in one kernel (PN / ripple: launch_triangle_instantiate)
+cudaError_t launch_instantiate_fused(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
+                                     u32 scanBlocksPerSM, u32 vertexBlocksPerSM, u32 vertexGridPerSM, cudaStream_t s);
 cudaError_t launch_blas_setup_insertion(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 cudaError_t launch_blas_clusters_insert(const StageCtx& c, u32* segStart, u32* segEnd, u32 stride, u32 grid,
                                         cudaStream_t s);

@@ -139,6 +139,87 @@ __device__ __forceinline__ void write_part_affine(PartAffine& r, const u32 corne
   r.q[5]      = make_float4(T1.x - T0.x, T1.y - T0.y, T2.x - T0.x, T2.y - T0.y);
 }
 
+// Encoded unit barycentrics: (1,0,0) -> 0, (0,1,0) -> 1, (0,0,1) -> 2, anything else -> 3.
+__device__ __forceinline__ u32 unit_corner(u32 e)
+{
+  return e == 0u ? 0u : (e == TC_TESSTABLE_COORD_MAX ? 1u : (e == (TC_TESSTABLE_COORD_MAX << 16) ? 2u : 3u));
+}
+
+// Every part classify writes is a whole base triangle: its three corners are
+// the base triangle's own corners, in the order get_config rotated them. Then
+// each corner's composed attribute (the barycentric composition of
+// write_part_affine) is exactly one base vertex's attribute, so the affine
+// form is the base attributes themselves, taken in corner order. Returns true
+// for such a part, with order[k] = the base vertex of corner k (a flipped
+// config swaps corners 0 and 1); otherwise order = {0, 1, 2}.
+__device__ __forceinline__ bool whole_triangle_order(const u32 corner[3], bool flipped, u32 order[3])
+{
+  u32        m0 = unit_corner(corner[0]), m1 = unit_corner(corner[1]), m2 = unit_corner(corner[2]);
+  const bool whole = max(m0, max(m1, m2)) < 3u && m0 != m1 && m1 != m2 && m0 != m2;
+  if(!whole)
+    m0 = 0, m1 = 1, m2 = 2;
+  else if(flipped)
+  {
+    const u32 t = m0;
+    m0          = m1;
+    m1          = t;
+  }
+  order[0] = m0, order[1] = m1, order[2] = m2;
+  return whole;
+}
+
+// write_part_affine for a whole-triangle part whose base attributes p / n /
+// uv are given in corner order: no compositions (the same values up to the
+// sign of exact zeros).
+__device__ __forceinline__ void write_part_affine_whole(PartAffine& r, const f3 p[3], const f3 n[3], const f2 uv[3],
+                                                        u32 firstVertex, const tc_DisplacementTexture& tx, float scale,
+                                                        float offset)
+{
+  const u32     w = tx.width;
+  const MapDesc m = make_map_desc(tx);
+  r.q[6]          = make_float4(scale, offset, __uint_as_float(firstVertex), __uint_as_float(m.kind));
+  r.q[7]          = m.q7;
+  r.q[8]          = m.q8;
+  const f3 E1     = sub3(p[1], p[0]), E2 = sub3(p[2], p[0]);
+  r.q[0]          = make_float4(p[0].x, p[0].y, p[0].z, E1.x);
+  r.q[1]          = make_float4(E1.y, E1.z, E2.x, E2.y);
+  r.q[2].x        = E2.z;
+  if(w == 0)
+    return;
+  const f3 N0 = normalize_fast(n[0]), N1 = normalize_fast(n[1]), N2 = normalize_fast(n[2]);
+  const f3 F1 = sub3(N1, N0), F2 = sub3(N2, N0);
+  r.q[2]      = make_float4(E2.z, N0.x, N0.y, N0.z);
+  r.q[3]      = make_float4(F1.x, F1.y, F1.z, F2.x);
+  r.q[4]      = make_float4(F2.y, F2.z, uv[0].x, uv[0].y);
+  r.q[5]      = make_float4(uv[1].x - uv[0].x, uv[1].y - uv[0].y, uv[2].x - uv[0].x, uv[2].y - uv[0].y);
+}
+
+// The affine form of part triangle `pt` (cluster / instance resolved by the
+// caller): base attributes loaded in corner order for a whole-triangle part,
+// else in base order and composed with the corners.
+__device__ __forceinline__ void part_affine(PartAffine& r, const u32 corner[3], bool flipped, const float* pos,
+                                            const float* nrm, const float* uvs, u32 firstLocalVertex,
+                                            const uint8_t* triIndices, u32 firstVertex, const tc_DisplacementTexture& tx,
+                                            float scale, float offset)
+{
+  u32        order[3];
+  const bool whole = whole_triangle_order(corner, flipped, order);
+  f3         bp[3], bn[3];
+  f2         bt[3];
+#pragma unroll
+  for(int v = 0; v < 3; v++)
+  {
+    const u32 vi = firstLocalVertex + triIndices[order[v]];
+    bp[v]        = ldg3(pos, vi);
+    bn[v]        = ldg3(nrm, vi);  // normalised in write_part_affine* (triangle_tess_template_instantiate.comp.glsl:329)
+    bt[v]        = ldg2(uvs, vi);
+  }
+  if(whole)
+    write_part_affine_whole(r, bp, bn, bt, firstVertex, tx, scale, offset);
+  else
+    write_part_affine(r, corner, flipped, bp, bn, bt, firstVertex, tx, scale, offset);
+}
+
 template <u32 Format>
 __device__ __forceinline__ float texel_at(u64 texels, u64 i)
 {

@@ -215,11 +215,12 @@ class Schedule(ctypes.Structure):
     _fields_ = [("classifyBlocksPerSM", ctypes.c_uint32), ("splitBlockSize", ctypes.c_uint32),
                 ("vertexBlocksPerSM", ctypes.c_uint32), ("scanBlocksPerSM", ctypes.c_uint32),
                 ("blocksPerSM", ctypes.c_uint32), ("fullVertexBlocksPerSM", ctypes.c_uint32),
-                ("vertexGridPerSM", ctypes.c_uint32), ("lookbackSpinLimit", ctypes.c_uint32)]
+                ("vertexGridPerSM", ctypes.c_uint32), ("lookbackSpinLimit", ctypes.c_uint32),
+                ("frameShape", ctypes.c_uint32), ("_pad", ctypes.c_uint32)]
 
 
 SCHEDULE_FIELDS = ("classifyBlocksPerSM", "splitBlockSize", "vertexBlocksPerSM", "scanBlocksPerSM", "blocksPerSM",
-                   "fullVertexBlocksPerSM", "vertexGridPerSM", "lookbackSpinLimit")
+                   "fullVertexBlocksPerSM", "vertexGridPerSM", "lookbackSpinLimit", "frameShape")
 
 
 RASTER_BATCH_VERTICES, RASTER_BATCH_TRIANGLES = 96, 121
@@ -248,7 +249,7 @@ class TableInfoC(ctypes.Structure):
 
 assert ctypes.sizeof(Caps) == 32
 assert ctypes.sizeof(FrameArgs) == 96
-assert ctypes.sizeof(Schedule) == 32
+assert ctypes.sizeof(Schedule) == 40
 
 
 def caps_from(cfg: dict) -> Caps:
