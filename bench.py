@@ -329,9 +329,12 @@ def split_timings(pipe, torch, frames, set_frame, flush):
             e1.record()
             torch.cuda.synchronize()
             res[form].append(e0.elapsed_time(e1))
+    res["per_pass_launches_samples"] = list(res["per_pass_launches_ms"])
+    res["one_launch_samples"] = list(res["one_launch_ms"])
     res["per_pass_launches_ms"] = statistics.median(res["per_pass_launches_ms"])
     res["one_launch_ms"] = statistics.median(res["one_launch_ms"])
-    res["split_items"] = int(pipe.outputs()["readback"]["numSplitTriangles"])
+    b = pipe.state.build.read(L.SceneBuilding, 1)[0]
+    res["split_items"] = int(b["splitWriteCounter"])
     return res
 
 
