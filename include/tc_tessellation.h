@@ -475,7 +475,9 @@ typedef struct tc_schedule {
                                  * side stream while the split passes run, the later runs after them; 1 allocates
                                  * every run once after the split passes (fewer launches when splits are rare).
                                  * Outputs are identical. */
-  uint32_t _pad[1];
+  uint32_t splitPerPass;        /* the batched frame's split passes: 0 in one launch (k_triangle_split_levels, cheap
+                                 * when they have little to do), 1 one launch per pass with the set-ups between
+                                 * (pays off when the passes are long). Outputs are identical. */
 } tc_schedule;
 
 typedef struct tc_context_desc {

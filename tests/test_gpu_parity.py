@@ -221,7 +221,7 @@ def test_schedules_change_timing_only(oracle):
         dict(classifyBlocksPerSM=4, scanBlocksPerSM=2, splitBlockSize=128, blocksPerSM=2, vertexBlocksPerSM=2,
              vertexGridPerSM=1),
         dict(classifyBlocksPerSM=16, scanBlocksPerSM=16, splitBlockSize=512, blocksPerSM=4, vertexBlocksPerSM=5,
-             fullVertexBlocksPerSM=8, frameShape=1),
+             fullVertexBlocksPerSM=8, frameShape=1, splitPerPass=1),
         dict(classifyBlocksPerSM=6, scanBlocksPerSM=1, splitBlockSize=256, blocksPerSM=1, vertexBlocksPerSM=1,
              fullVertexBlocksPerSM=1),
         dict(classifyBlocksPerSM=1, scanBlocksPerSM=4, splitBlockSize=256, blocksPerSM=1, vertexBlocksPerSM=6,
@@ -235,7 +235,7 @@ def test_schedules_change_timing_only(oracle):
             assert_same(pipe.outputs(), ref, f"schedule {sched} {mode}", vertex_tol=vertex_tolerance(sc))
     assert pipe.device_errors() == 0
     for bad in (dict(splitBlockSize=64), dict(vertexBlocksPerSM=0), dict(scanBlocksPerSM=65),
-                dict(fullVertexBlocksPerSM=65), dict(vertexGridPerSM=65), dict(frameShape=2)):
+                dict(fullVertexBlocksPerSM=65), dict(vertexGridPerSM=65), dict(frameShape=2), dict(splitPerPass=2)):
         with pytest.raises(native.TcError):
             pipe.set_schedule(bad)
     pipe.close()
@@ -244,8 +244,9 @@ def test_schedules_change_timing_only(oracle):
 @pytest.mark.parametrize("case", ["splits", "transient"])
 def test_frame_shapes_identical(oracle, case):
     """Both frame-graph shapes (the first part run allocated beside the split
-    passes, or every run after them) give the oracle's output, on a
-    split-heavy frame and on one with 1X + 2X transient builds."""
+    passes, or every run after them) and both split forms (one launch for all
+    passes, or one per pass) give the oracle's output, on a split-heavy frame
+    and on one with 1X + 2X transient builds."""
     from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
     sc = S.scene_icosphere(subdivisions=3, map_size=256)
     cam = S.Camera(eye=(0.0, 0.0, 1.08), center=(0.0, 0.0, 0.0), tess_rate_pixels=1.0, near=0.01, far=10.0)
@@ -259,8 +260,8 @@ def test_frame_shapes_identical(oracle, case):
         assert int(ref["readback"]["numSplitTriangles"]) > 0
     pipe = TessellationPipeline(sc, caps, flags)
     pipe.set_cameras(cam)
-    for shape in (1, 0):
-        pipe.set_schedule({"frameShape": shape})
+    for shape, per_pass in ((1, 0), (0, 1), (1, 1), (0, 0)):
+        pipe.set_schedule({"frameShape": shape, "splitPerPass": per_pass})
         for mode in ("batched", "graph"):
             pipe.build(mode)
             assert_same(pipe.outputs(), ref, f"{case} shape {shape} {mode}", vertex_tol=vertex_tolerance(sc))

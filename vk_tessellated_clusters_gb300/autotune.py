@@ -7,7 +7,8 @@ full-cluster vertex kernel (which runs beside the rest of the frame), the
 split tile size
 (128 threads x 16 items, 256 or 512 threads x 32 items), the split grid, and
 the frame graph's shape (the first part run allocated beside the split passes,
-or every run after them).
+or every run after them) and the split passes' form (one launch, or one per
+pass).
 Outputs do not depend on it (every allocation is a prefix sum in a fixed
 order), so tuning is a pure timing search.
 
@@ -32,6 +33,7 @@ SPACE = {
     "fullVertexBlocksPerSM": (1, 2, 3, 4),
     "vertexGridPerSM": (0, 8, 16),
     "frameShape": (0, 1),
+    "splitPerPass": (0, 1),
 }
 
 

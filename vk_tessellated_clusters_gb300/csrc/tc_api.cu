@@ -297,7 +297,8 @@ u32 frame_begin_grid(const tc_context* ctx, const tc_frame_args* a)
 // kBlasSetupFusedMax instances)
 uint64_t frame_launches(const tc_context* ctx, const tc_frame_args* a)
 {
-  return kFrameFixedLaunches + 1 - (a->numInstances <= kBlasSetupFusedMax ? 1 : 0)
+  return kFrameFixedLaunches + (ctx->schedule.splitPerPass ? split_passes(a->caps.splitFactor) : 1)
+         - (a->numInstances <= kBlasSetupFusedMax ? 1 : 0)
          - (ctx->schedule.frameShape == 1 ? 4 : 0)  // one allocation + vertex launch instead of two
          + ((a->flags & TC_FLAG_TRANSIENT_2X) ? 1 : 0);  // the 2X batches' vertices
 }
@@ -399,15 +400,26 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
                                               sched.vertexBlocksPerSM, sched.vertexGridPerSM, ctx->side));
   }
 
-  // every split pass in one persistent launch (level by level inside)
+  const u32 sb     = split_block(sched);
+  const u32 passes = split_passes(a->caps.splitFactor);
+  const u32 sgrid  = persistent_grid(ctx, ceil_div(a->caps.maxSplitTriangles, split_items_per_tile(sb)), bpsm * (512 / sb));
+  if(sched.splitPerPass)
   {
-    const u32   sb = split_block(sched);
-    SplitLevels lv = split_levels(ctx, split_passes(a->caps.splitFactor));
+    // one launch per pass, the pass set-up fused into its last block
+    for(u32 q = 0; q < passes; q++)
+    {
+      bind_slot(ctx, c, p.slotSplit0 + q, false);
+      c.fuseSetup = (q + 1 < passes) ? TC_BUILD_SETUP_SPLIT_PASS : TC_BUILD_SETUP_INSTANTIATE_TESS;
+      TC_CHECK_CUDA(launch_triangle_split(c, sb, sgrid, s));
+    }
+  }
+  else
+  {
+    // every split pass in one persistent launch (level by level inside)
+    SplitLevels lv = split_levels(ctx, passes);
     bind_slot(ctx, c, p.slotSplit0, false);
     c.fuseSetup = TC_BUILD_SETUP_INSTANTIATE_TESS;
-    TC_CHECK_CUDA(launch_triangle_split_levels(
-        c, lv, sb, persistent_grid(ctx, ceil_div(a->caps.maxSplitTriangles, split_items_per_tile(sb)), bpsm * (512 / sb)),
-        s));
+    TC_CHECK_CUDA(launch_triangle_split_levels(c, lv, sb, sgrid, s));
   }
   if(earlyRun0)
     TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evJoin, 0));
@@ -518,7 +530,7 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
     delete ctx;
     return TC_ERR_CUDA;
   }
-  ctx->schedule = {4, 256, 4, 4, 1, kDefaultFullVertexBlocksPerSM, 0, 0, 0, {0}};  // the batched scene's tuned shape
+  ctx->schedule = {4, 256, 4, 4, 1, kDefaultFullVertexBlocksPerSM, 0, 0, 0, 0};  // the batched scene's tuned shape
   ctx->plan     = make_plan(*desc);
   if(cudaMalloc(&ctx->dScratch, ctx->plan.totalBytes) != cudaSuccess
      || cudaMemset(ctx->dScratch, 0, ctx->plan.totalBytes) != cudaSuccess)
@@ -673,7 +685,7 @@ tc_status tc_set_schedule(tc_context* ctx, const tc_schedule* schedule)
       return TC_ERR_INVALID_ARG;
   if(q.splitBlockSize != 128 && q.splitBlockSize != 256 && q.splitBlockSize != 512)
     return TC_ERR_INVALID_ARG;
-  if(q.fullVertexBlocksPerSM > 64 || q.vertexGridPerSM > 64 || q.frameShape > 1)
+  if(q.fullVertexBlocksPerSM > 64 || q.vertexGridPerSM > 64 || q.frameShape > 1 || q.splitPerPass > 1)
     return TC_ERR_INVALID_ARG;
   ctx->schedule   = *schedule;
   if(ctx->schedule.fullVertexBlocksPerSM == 0)

@@ -216,11 +216,12 @@ class Schedule(ctypes.Structure):
                 ("vertexBlocksPerSM", ctypes.c_uint32), ("scanBlocksPerSM", ctypes.c_uint32),
                 ("blocksPerSM", ctypes.c_uint32), ("fullVertexBlocksPerSM", ctypes.c_uint32),
                 ("vertexGridPerSM", ctypes.c_uint32), ("lookbackSpinLimit", ctypes.c_uint32),
-                ("frameShape", ctypes.c_uint32), ("_pad", ctypes.c_uint32)]
+                ("frameShape", ctypes.c_uint32), ("splitPerPass", ctypes.c_uint32)]
 
 
 SCHEDULE_FIELDS = ("classifyBlocksPerSM", "splitBlockSize", "vertexBlocksPerSM", "scanBlocksPerSM", "blocksPerSM",
-                   "fullVertexBlocksPerSM", "vertexGridPerSM", "lookbackSpinLimit", "frameShape")
+                   "fullVertexBlocksPerSM", "vertexGridPerSM", "lookbackSpinLimit", "frameShape",
+                   "splitPerPass")
 
 
 RASTER_BATCH_VERTICES, RASTER_BATCH_TRIANGLES = 96, 121
