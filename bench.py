@@ -53,7 +53,7 @@ def parse_args():
     p.add_argument("--no-extras", action="store_true", help="skip the plain-path and terrain measurements")
     p.add_argument("--no-tune", action="store_true", help="keep the default launch schedule (no autotuning)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
-    p.add_argument("--profile-case", choices=["batched", "terrain", "transient", "raster"], default=None,
+    p.add_argument("--profile-case", choices=["batched", "terrain", "terrain_stages", "transient", "raster"], default=None,
                    help="run only `warmup` + `steps` graph frames of one case (for ncu captures) and exit")
     return p.parse_args()
 
@@ -237,13 +237,14 @@ def recorded_traffic(key: str):
 
 
 # What ncu shows limits each measured stage (profiles/: classify_batched.md,
-# instantiate_vertices_terrain.md); the roofline stays HBM bandwidth.
+# instantiate_parts_terrain.md); the roofline stays HBM bandwidth.
 LIMITERS = {
     "batched/cluster_classify": "instruction issue and latency, not DRAM: the 256 instances share 4 meshes, so "
                                 "the working set is L2-resident (DRAM 0.3-1.1 %); k_classify_count issue-bound "
                                 "(67 % issue active), k_classify_full_vertices long-scoreboard-bound",
-    "terrain/triangle_instantiate": "instruction issue and L1 wavefronts in k_instantiate_vertices (58-65 % issue "
-                                    "active, L1 70-80 %), DRAM traffic below the algorithmic bytes",
+    "terrain/triangle_instantiate": "L1 data pipe and instruction issue in k_instantiate_parts (61 % issue "
+                                    "active, LSU data pipe 73 %, DRAM 30 %), DRAM traffic below the "
+                                    "algorithmic bytes",
 }
 
 
@@ -937,7 +938,11 @@ def run_profile_case(args):
     pipe = TessellationPipeline(scene, caps, flags)
     for i, cam in enumerate(cams):
         pipe.set_cameras(cam, cams[i - 1] if i else cam)
-        pipe.build("graph")
+        if args.profile_case == "terrain_stages":  # the per-stage entry points, as the bench's stage timings run them
+            for name, extra in stage_sequence(pipe, pipe.args.numInstances):
+                pipe.stage(name, *extra)
+        else:
+            pipe.build("graph")
         if args.profile_case == "raster":
             pipe.raster_batches()
     torch.cuda.synchronize()
