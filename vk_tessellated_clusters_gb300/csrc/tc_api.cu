@@ -305,8 +305,10 @@ uint64_t frame_launches(const tc_context* ctx, const tc_frame_args* a)
 
 u32 insert_grid(const tc_context* ctx, const tc_frame_args* a)
 {
-  // tiles of 1024 instantiations per block (at least four blocks per SM)
-  return std::max(ctx->numSMs * 4, std::min(ceil_div(a->caps.maxGeneratedClusters, 1024), 1u << 16));
+  // tiles of 1024 instantiations, at most one resident wave of blocks that
+  // stride over them (blocks past the frame's instantiations only read the run
+  // table, but each costs a dispatch)
+  return std::max(1u, std::min(ceil_div(a->caps.maxGeneratedClusters, 1024), ctx->numSMs * 4));
 }
 
 SplitLevels split_levels(const tc_context* ctx, u32 passes)

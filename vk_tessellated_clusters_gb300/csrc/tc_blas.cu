@@ -246,16 +246,16 @@ __global__ void __launch_bounds__(kInsertBlock) k_blas_scatter(StageCtx c, const
 
 cudaError_t launch_blas_setup_insertion(const StageCtx& c, u32 grid, u32 block, cudaStream_t s)
 {
-  return launch_pdl(k_blas_setup_insertion, grid, block, s, c);
+  return launch_pdl_critical(k_blas_setup_insertion, grid, block, s, c);
 }
 
 cudaError_t launch_blas_clusters_insert(const StageCtx& c, u32* segStart, u32* segEnd, u32 stride, u32 grid,
                                         cudaStream_t s)
 {
-  cudaError_t e = launch_pdl(k_blas_segments, grid, kInsertBlock, s, c, segStart, segEnd, stride);
+  cudaError_t e = launch_pdl_critical(k_blas_segments, grid, kInsertBlock, s, c, segStart, segEnd, stride);
   if(e != cudaSuccess)
     return e;
-  return launch_pdl(k_blas_scatter, grid, kInsertBlock, s, c, segStart, segEnd, stride);
+  return launch_pdl_critical(k_blas_scatter, grid, kInsertBlock, s, c, segStart, segEnd, stride);
 }
 
 }  // namespace tc

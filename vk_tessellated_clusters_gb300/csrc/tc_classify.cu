@@ -663,6 +663,45 @@ __device__ __forceinline__ void full_steps(const FullRecord* rec, bool owner, u3
   }
 }
 
+// full_steps for a batch whose records share the attribute arrays, map,
+// displacement scale and offset (and, with the ripple, the instance): those
+// stay in registers (`u`, read once per batch), and each step takes only its
+// record's vertex-index offset and range end from the record's lane (two
+// shuffles) instead of the record from shared memory. Same operations, so the
+// same bits.
+template <u32 Kind>
+__device__ __forceinline__ void full_steps_uniform(const FullRecord& u, bool owner, u32 rStart, u32 rOff, u32 rStop,
+                                                   u32 rEnd, float* dst, const RippleParams& rp)
+{
+  const u32 lane  = threadIdx.x & 31;
+  const u32 below = (2u << lane) - 2u;
+#pragma unroll 2  // two steps in flight: their loads overlap
+  for(u32 base = 0; base < rEnd; base += 32)
+  {
+    const u32 before = __popc(__ballot_sync(0xFFFFFFFFu, owner && rStart <= base));
+    const u32 inside = __reduce_or_sync(0xFFFFFFFFu,
+                                        (owner && rStart > base && rStart < base + 32) ? 1u << (rStart - base) : 0u);
+    const u32 ri     = (before - 1 + __popc(inside & below)) & 31;
+    const u32 off    = __shfl_sync(0xFFFFFFFFu, rOff, ri);
+    const u32 stop   = __shfl_sync(0xFFFFFFFFu, rStop, ri);
+    const u32 jj     = base + lane;
+    // (transient builds leave index bytes and 2X batches between the ranges)
+    if(jj < stop)
+    {
+      const u32 vi = off + jj;
+      f3        p  = ldg3(u.pos, vi);
+      if(Kind != kAffineFlat)
+        p = full_vertex_k<Kind>(p, ldg3(u.nrm, vi), ldg2(u.uvs, vi), u.map, u.scale, u.offset);
+      if(rp.enabled)  // cluster_classify.comp.glsl:483-485
+        p = ripple(p, u.inst, u.size, rp);
+      float* d = dst + (u64)jj * 3;
+      d[0]     = p.x;
+      d[1]     = p.y;
+      d[2]     = p.z;
+    }
+  }
+}
+
 template <int MinBlocks>
 __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_write(StageCtx c, ClassifyScratch cs)
 {
@@ -1506,17 +1545,47 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_full_vertices(St
     const u32 kind0 = rec[0].map.kind;
     const u32 kw    = __all_sync(0xFFFFFFFFu, !own || kind == kind0) ? kind0 : ~0u;
     float*    dst   = gv + (u64)vBase * 3;
-    switch(kw)
+    // the usual batch: consecutive clusters of instances of one mesh and map
+    const FullRecord u    = rec[0];
+    const bool       same = !own
+                      || (rec[lane].pos == u.pos && rec[lane].nrm == u.nrm && rec[lane].uvs == u.uvs
+                          && rec[lane].map.kind == u.map.kind
+                          && __float_as_uint(rec[lane].map.q7.x) == __float_as_uint(u.map.q7.x)
+                          && __float_as_uint(rec[lane].map.q7.y) == __float_as_uint(u.map.q7.y)
+                          && __float_as_uint(rec[lane].map.q7.z) == __float_as_uint(u.map.q7.z)
+                          && __float_as_uint(rec[lane].map.q7.w) == __float_as_uint(u.map.q7.w)
+                          && __float_as_uint(rec[lane].scale) == __float_as_uint(u.scale)
+                          && __float_as_uint(rec[lane].offset) == __float_as_uint(u.offset)
+                          && (!rp.enabled || (rec[lane].inst == u.inst && __float_as_uint(rec[lane].size) == __float_as_uint(u.size))));
+    if(__all_sync(0xFFFFFFFFu, same))
     {
-      case affine_kind(TC_TEXEL_F32, true):
-        full_steps<affine_kind(TC_TEXEL_F32, true)>(rec, own, rStart, rEnd, dst, rp);
-        break;
-      case affine_kind(TC_TEXEL_F16, true):
-        full_steps<affine_kind(TC_TEXEL_F16, true)>(rec, own, rStart, rEnd, dst, rp);
-        break;
-      case kAffineFlat: full_steps<kAffineFlat>(rec, own, rStart, rEnd, dst, rp); break;
-      default: full_steps<~0u>(rec, own, rStart, rEnd, dst, rp); break;
+      // per record (lane r): vertex index of batch vertex jj is rOff + jj, for jj < rStop
+      const u32 rOff  = own ? rec[lane].first - rStart : 0u;
+      const u32 rStop = own ? rStart + rCount : 0u;
+      switch(u.map.kind)
+      {
+        case affine_kind(TC_TEXEL_F32, true):
+          full_steps_uniform<affine_kind(TC_TEXEL_F32, true)>(u, own, rStart, rOff, rStop, rEnd, dst, rp);
+          break;
+        case affine_kind(TC_TEXEL_F16, true):
+          full_steps_uniform<affine_kind(TC_TEXEL_F16, true)>(u, own, rStart, rOff, rStop, rEnd, dst, rp);
+          break;
+        case kAffineFlat: full_steps_uniform<kAffineFlat>(u, own, rStart, rOff, rStop, rEnd, dst, rp); break;
+        default: full_steps_uniform<~0u>(u, own, rStart, rOff, rStop, rEnd, dst, rp); break;
+      }
     }
+    else
+      switch(kw)
+      {
+        case affine_kind(TC_TEXEL_F32, true):
+          full_steps<affine_kind(TC_TEXEL_F32, true)>(rec, own, rStart, rEnd, dst, rp);
+          break;
+        case affine_kind(TC_TEXEL_F16, true):
+          full_steps<affine_kind(TC_TEXEL_F16, true)>(rec, own, rStart, rEnd, dst, rp);
+          break;
+        case kAffineFlat: full_steps<kAffineFlat>(rec, own, rStart, rEnd, dst, rp); break;
+        default: full_steps<~0u>(rec, own, rStart, rEnd, dst, rp); break;
+      }
     __syncwarp();  // records are rewritten by the next batch
   }
 }
@@ -1538,20 +1607,20 @@ cudaError_t launch_cluster_classify(const StageCtx& c, const ClassifyBuffers& bu
     const u32 tgrid = std::max(1u, std::min(classify_max_blocks(maxClusters), numSMs * std::max(6u, warpBlocksPerSM)));
     ClassifyScratch ts = cs;
     ts.writeBlocks     = tgrid;
-    cudaError_t e      = launch_pdl(k_classify_count<4, true>, tgrid, kBlock, s, c, ts);
+    cudaError_t e      = launch_pdl_critical(k_classify_count<4, true>, tgrid, kBlock, s, c, ts);
     if(e != cudaSuccess)
       return e;
-    return launch_pdl(k_classify_write_transient, tgrid, kBlock, s, c, ts);
+    return launch_pdl_critical(k_classify_write_transient, tgrid, kBlock, s, c, ts);
   }
   const int   occ = warpBlocksPerSM >= 8 ? 8 : (warpBlocksPerSM >= 5 ? 6 : 4);
-  cudaError_t e   = occ == 8   ? launch_pdl(k_classify_count<8>, grid, kBlock, s, c, cs)
-                    : occ == 6 ? launch_pdl(k_classify_count<6>, grid, kBlock, s, c, cs)
-                               : launch_pdl(k_classify_count<4>, grid, kBlock, s, c, cs);
+  cudaError_t e   = occ == 8   ? launch_pdl_critical(k_classify_count<8>, grid, kBlock, s, c, cs)
+                    : occ == 6 ? launch_pdl_critical(k_classify_count<6>, grid, kBlock, s, c, cs)
+                               : launch_pdl_critical(k_classify_count<4>, grid, kBlock, s, c, cs);
   if(e != cudaSuccess)
     return e;
-  return occ == 8   ? launch_pdl(k_classify_write<8>, grid, kBlock, s, c, cs)
-         : occ == 6 ? launch_pdl(k_classify_write<6>, grid, kBlock, s, c, cs)
-                    : launch_pdl(k_classify_write<4>, grid, kBlock, s, c, cs);
+  return occ == 8   ? launch_pdl_critical(k_classify_write<8>, grid, kBlock, s, c, cs)
+         : occ == 6 ? launch_pdl_critical(k_classify_write<6>, grid, kBlock, s, c, cs)
+                    : launch_pdl_critical(k_classify_write<4>, grid, kBlock, s, c, cs);
 }
 
 cudaError_t launch_classify_full_vertices(const StageCtx& c, const ClassifyBuffers& buf, u32 maxClusters, u32 numSMs,

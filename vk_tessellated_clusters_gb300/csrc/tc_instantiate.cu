@@ -948,12 +948,12 @@ cudaError_t launch_instantiate_alloc(const StageCtx& c, const InstantiateBuffers
 {
   const u32   tiles    = std::max(1u, instantiate_alloc_tiles(maxParts));
   const u32   tileGrid = std::max(1u, std::min(tiles, numSMs * std::max(1u, scanBlocksPerSM)));
-  cudaError_t e        = launch_pdl(k_instantiate_tile_sums, tileGrid, kBlock, s, c, buf);
+  cudaError_t e        = launch_pdl_critical(k_instantiate_tile_sums, tileGrid, kBlock, s, c, buf);
   if(e != cudaSuccess)
     return e;
-  if((e = launch_pdl(k_instantiate_tile_scan, 1u, kScanBlock, s, c)) != cudaSuccess)
+  if((e = launch_pdl_critical(k_instantiate_tile_scan, 1u, kScanBlock, s, c)) != cudaSuccess)
     return e;
-  return launch_pdl(k_instantiate_args, tileGrid, kBlock, s, c, buf);
+  return launch_pdl_critical(k_instantiate_args, tileGrid, kBlock, s, c, buf);
 }
 
 cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,

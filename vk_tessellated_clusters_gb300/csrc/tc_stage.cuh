@@ -44,6 +44,15 @@ inline int high_launch_priority()
   return greatest;
 }
 
+// A kernel on the frame's critical path (classify, the allocations, the BLAS
+// lists): highest launch priority, so that its blocks are dispatched before
+// pending blocks of the vertex kernels that run beside it on other streams.
+template <typename... Params, typename... Args>
+inline cudaError_t launch_pdl_critical(void (*kernel)(Params...), u32 grid, u32 block, cudaStream_t s, Args... args)
+{
+  return launch_pdl_prio(kernel, grid, block, high_launch_priority(), s, args...);
+}
+
 // Per-launch scratch: look-back tile states, the tile ticket, the "blocks done"
 // counter and the totals the last tile publishes. Zeroed before every launch.
 struct LaunchScratch
