@@ -364,7 +364,7 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
       cs = ctx->side2;
     }
     TC_CHECK_CUDA(
-        launch_clusters_cull(cc, persistent_grid(ctx, ceil_div(a->totalClusters, kCullTile), 4), kCullTile, cs));
+        launch_clusters_cull(cc, persistent_grid(ctx, ceil_div(a->totalClusters, kCullTile), 4), kCullTile, cs, flat));
   }
   c.flatVisible = flat ? 1u : 0u;
 

@@ -366,9 +366,9 @@ cudaError_t launch_frame_begin_instances(const StageCtx& c, u32 grid, cudaStream
   return launch_pdl(k_frame_begin_instances, grid, kInstanceTile, s, c);
 }
 
-cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStream_t s)
+cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStream_t s, bool side)
 {
-  return launch_pdl(k_clusters_cull, grid, block, s, c);
+  return side ? launch_side(k_clusters_cull, grid, block, s, c) : launch_pdl(k_clusters_cull, grid, block, s, c);
 }
 
 cudaError_t launch_build_setup(const StageCtx& c, u32 mode, cudaStream_t s)

@@ -53,7 +53,9 @@ cudaError_t launch_decode_hits(const StageCtx& c, const tc_hit* hits, u32 count,
 cudaError_t launch_instances_classify(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
 // frame_begin and instances_classify in one launch (block = kInstanceTile)
 cudaError_t launch_frame_begin_instances(const StageCtx& c, u32 grid, cudaStream_t s);
-cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStream_t s);
+// side: launched on a side stream beside classify (an ordinary launch, see
+// launch_side); otherwise programmatically after the kernel before it
+cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStream_t s, bool side = false);
 cudaError_t launch_build_setup(const StageCtx& c, u32 mode, cudaStream_t s);
 // the bounded look-back wait on its own (state: 3 words, zeroed here)
 cudaError_t launch_lookback_probe(unsigned long long* state, u32 published, u32* errorWord, u32 spinLimit,
