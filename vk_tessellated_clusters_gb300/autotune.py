@@ -31,7 +31,7 @@ SPACE = {
     "blocksPerSM": (1, 2, 4),
     "vertexBlocksPerSM": (3, 4, 5, 6),
     "fullVertexBlocksPerSM": (1, 2, 3, 4),
-    "vertexGridPerSM": (0, 8, 16),
+    "vertexGridPerSM": (0, 1, 2, 3, 8, 16),
     "frameShape": (0, 1),
     "splitPerPass": (0, 1),
 }
