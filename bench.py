@@ -430,19 +430,31 @@ def run_ours(args):
     errs = pipe.device_errors()
 
     # ---- e2e through the C ABI with host buffers ------------------------------
-    fc_host = torch.from_numpy(fc_bytes).pin_memory()
-    inst_host = torch.from_numpy(pipe.state.res.instance_records.view(np.uint8).copy()).pin_memory()
-    inst_dev = pipe.state.res.instances.handle
-    h2d = 2 * FC + inst_host.numel()
+    # A frame's inputs (its FrameConstants, the previous frame's, the instance
+    # records) sit side by side in one pinned host block and in one device
+    # block that the frame arguments point into: one upload per frame.
+    inst_rec = pipe.state.res.instance_records.view(np.uint8).reshape(-1)
+    blk = 2 * FC + inst_rec.size
+    host_np = np.empty((NUM_ORBIT_FRAMES, blk), np.uint8)
+    for f in range(NUM_ORBIT_FRAMES):
+        host_np[f, :FC] = fc_bytes[f]
+        host_np[f, FC:2 * FC] = fc_bytes[(f - 1) % NUM_ORBIT_FRAMES]
+        host_np[f, 2 * FC:] = inst_rec
+    host_blocks = torch.from_numpy(host_np).pin_memory()
+    dev_block = torch.empty(blk + 256, dtype=torch.uint8, device=dev)
+    base = (dev_block.data_ptr() + 255) // 256 * 256  # RenderInstance records 16-byte aligned (FC is a multiple of 16)
+    off = base - dev_block.data_ptr()
+    fa = pipe.state.args
+    saved_ptrs = (fa.view, fa.viewLast, fa.instances)
+    fa.view, fa.viewLast, fa.instances = base, base + FC, base + 2 * FC
+    h2d = blk
     e2e_times, e2e_tris = [], []
     for s in range(args.warmup + args.steps):
         f = s % NUM_ORBIT_FRAMES
         flush()  # before the step, as in the device-resident loop
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        view_t[:FC].copy_(fc_host[f], non_blocking=True)
-        last_t[:FC].copy_(fc_host[(f - 1) % NUM_ORBIT_FRAMES], non_blocking=True)
-        inst_dev[:inst_host.numel()].copy_(inst_host, non_blocking=True)
+        dev_block[off:off + blk].copy_(host_blocks[f], non_blocking=True)
         pipe.build("graph")
         rb_host.copy_(pipe.state.readback.handle[:L.Readback.itemsize], non_blocking=True)
         e1.record()
@@ -450,6 +462,7 @@ def run_ours(args):
         if s >= args.warmup:
             e2e_times.append(e0.elapsed_time(e1))
             e2e_tris.append(int(rb_host.numpy().view(L.Readback)[0]["numTotalTriangles"]))
+    fa.view, fa.viewLast, fa.instances = saved_ptrs
     e2e_value = sum(e2e_tris) / (sum(e2e_times) / 1e3)
 
     # ---- per-stage profile and roofline of the dominant kernel ---------------------
