@@ -75,6 +75,28 @@ def test_header_static_asserts_and_python_layouts(tmp_path):
     assert int(got["tc_TessTriangleInfo"]) == L.TessTriangleInfo.itemsize == 24
 
 
+def test_header_is_c_and_links_from_c(tmp_path, lib):
+    """The ABI as a C consumer (a cgo or N-API shim) sees it: the header
+    compiles as C11 and a C program links against the library and calls it."""
+    prog = tmp_path / "consumer.c"
+    prog.write_text('#include <stdio.h>\n#include "tc_tessellation.h"\n'
+                    "int main(void) {\n"
+                    "  tc_context* ctx = 0;\n"
+                    '  printf("%s|%s|%u|%d\\n", tc_version(), tc_status_string(TC_ERR_CAPACITY),\n'
+                    "         tc_split_pass_count(8), (int)tc_context_create(0, &ctx));\n"
+                    "  return sizeof(tc_SceneBuilding) == 368 && sizeof(tc_schedule) == 40 ? 0 : 1;\n"
+                    "}\n")
+    exe = tmp_path / "consumer"
+    libdir = os.path.dirname(native.LIB_PATH)
+    subprocess.check_call(["gcc", "-std=c11", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(prog),
+                           "-L", libdir, "-ltc_gb300", "-Wl,-rpath," + libdir, "-o", str(exe)])
+    out = subprocess.check_output([str(exe)], text=True).strip().split("|")
+    assert "sm_103a" in out[0]
+    assert out[1] == "request exceeds the context's capacity"
+    assert out[2] == "4"
+    assert int(out[3]) == L.TC_ERR_INVALID_ARG  # no descriptor
+
+
 def test_calls_without_gpu(lib):
     assert b"sm_103a" in lib.tc_version()
     assert lib.tc_status_string(L.TC_ERR_CAPACITY) == b"request exceeds the context's capacity"
