@@ -97,6 +97,7 @@ struct tc_context
   cudaEvent_t  evArgs1 = nullptr;  // later part runs allocated
   cudaEvent_t  evVerts = nullptr;  // all part vertices written
   cudaEvent_t  evInst  = nullptr;  // instances classified
+  cudaEvent_t  evScan0 = nullptr;  // first part run's offsets (and the counters after it)
 
   // graph cache
   cudaGraphExec_t graphExec = nullptr;
@@ -395,8 +396,11 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
     bind_slot(ctx, c0, p.slotInstantiate0, false);
     c0.fuseSetup = kNoSetup;
     c0.run       = 0;
-    TC_CHECK_CUDA(launch_instantiate_alloc(c0, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
-                                           sched.scanBlocksPerSM, ctx->side));
+    TC_CHECK_CUDA(launch_instantiate_prefix(c0, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
+                                            sched.scanBlocksPerSM, ctx->side));
+    TC_CHECK_CUDA(cudaEventRecord(ctx->evScan0, ctx->side));
+    TC_CHECK_CUDA(launch_instantiate_args(c0, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
+                                          sched.scanBlocksPerSM, ctx->side));
     TC_CHECK_CUDA(cudaEventRecord(ctx->evJoin, ctx->side));
     TC_CHECK_CUDA(launch_instantiate_vertices(c0, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
                                               sched.vertexBlocksPerSM, sched.vertexGridPerSM, ctx->side));
@@ -423,8 +427,11 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
     c.fuseSetup = TC_BUILD_SETUP_INSTANTIATE_TESS;
     TC_CHECK_CUDA(launch_triangle_split_levels(c, lv, sb, sgrid, s));
   }
+  // the later runs' offsets continue from the counters the first run's scan
+  // left; their arguments wait for the first run's (whose CLAS counts the
+  // BLAS set-up in their last block sums)
   if(earlyRun0)
-    TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evJoin, 0));
+    TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evScan0, 0));
   bind_slot(ctx, c, p.slotInstantiate, false);
   c.fuseSetup = TC_BUILD_SETUP_BUILD_BLAS;
   c.run       = earlyRun0 ? kRunsAfterFirst : kAllRuns;
@@ -432,8 +439,12 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   // the argument kernel's last block instead of a launch of their own
   const bool fuseBlas = a->numInstances <= kBlasSetupFusedMax;
   c.fuseBlasSetup     = fuseBlas ? 1u : 0u;
-  TC_CHECK_CUDA(launch_instantiate_alloc(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
-                                         sched.scanBlocksPerSM, s));
+  TC_CHECK_CUDA(launch_instantiate_prefix(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
+                                          sched.scanBlocksPerSM, s));
+  if(earlyRun0)
+    TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evJoin, 0));
+  TC_CHECK_CUDA(launch_instantiate_args(c, instantiate_buffers(ctx), a->caps.maxPartTriangles, ctx->numSMs,
+                                        sched.scanBlocksPerSM, s));
   c.fuseBlasSetup = 0;
   TC_CHECK_CUDA(cudaEventRecord(ctx->evArgs1, s));
   TC_CHECK_CUDA(cudaStreamWaitEvent(ctx->side, ctx->evArgs1, 0));
@@ -489,7 +500,8 @@ namespace {
 
 void destroy_streams(tc_context* ctx)
 {
-  for(cudaEvent_t* e : {&ctx->evFork, &ctx->evJoin, &ctx->evJoin2, &ctx->evArgs1, &ctx->evVerts, &ctx->evInst})
+  for(cudaEvent_t* e : {&ctx->evFork, &ctx->evJoin, &ctx->evJoin2, &ctx->evArgs1, &ctx->evVerts, &ctx->evInst,
+                        &ctx->evScan0})
     if(*e)
       cudaEventDestroy(*e), *e = nullptr;
   for(cudaStream_t* st : {&ctx->side, &ctx->side2})
@@ -526,7 +538,8 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
      || cudaEventCreateWithFlags(&ctx->evJoin2, cudaEventDisableTiming) != cudaSuccess
      || cudaEventCreateWithFlags(&ctx->evArgs1, cudaEventDisableTiming) != cudaSuccess
      || cudaEventCreateWithFlags(&ctx->evVerts, cudaEventDisableTiming) != cudaSuccess
-     || cudaEventCreateWithFlags(&ctx->evInst, cudaEventDisableTiming) != cudaSuccess)
+     || cudaEventCreateWithFlags(&ctx->evInst, cudaEventDisableTiming) != cudaSuccess
+     || cudaEventCreateWithFlags(&ctx->evScan0, cudaEventDisableTiming) != cudaSuccess)
   {
     destroy_streams(ctx);
     delete ctx;

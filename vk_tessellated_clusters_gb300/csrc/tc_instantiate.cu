@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kScanBlock) k_instantiate_tile_scan(StageCtx c
 {
   stage_prologue();
   __shared__ u64 s_warpData[32], s_warpVerts[32];
-  __shared__ u32 s_range[2];
+  __shared__ u32 s_range[2], s_first, s_tile;
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   tc_SceneBuilding* b = c.build;
   if(threadIdx.x == 0)
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kScanBlock) k_instantiate_tile_scan(StageCtx c
   const u32 n        = s_range[1] - s_range[0];
   const u32 numTiles = clamp_tiles(c, (n + kTile - 1) / kTile);
   const u32 stride   = c.scratch.lbStride;
-  u64 carryData = b->genClusterDataCounter, carryVerts = b->genVertexCounter;
+  u64       carryData = b->genClusterDataCounter, carryVerts = b->genVertexCounter;
   const u32 genBase = b->genClusterCounter;
   for(u32 t0 = 0; t0 < numTiles; t0 += kScanBlock)
   {
@@ -221,17 +221,75 @@ __global__ void __launch_bounds__(kScanBlock) k_instantiate_tile_scan(StageCtx c
     carryVerts = s_warpVerts[0];
     __syncthreads();
   }
+  // Accepted instantiations: the run's parts before the first one that fails
+  // the capacity test (triangle_tess_template_instantiate.comp.glsl:160-167).
+  // The offsets count every attempt, so every later part fails too: the
+  // accepted parts are a prefix, counted here rather than by the argument
+  // launch, so that the next run's allocation need not wait for it.
+  const tc_caps& k        = c.caps;
+  const u64      maxData  = (u64)k.maxGeneratedClusterMegs * 1024ull * 1024ull;
+  const u32      attempts = min(n, numTiles * kTile);
+  u32            accepted = attempts;
+  if(carryVerts > k.maxGeneratedVertices || carryData > maxData || (u64)genBase + attempts > k.maxGeneratedClusters)
+  {
+    // the first tile whose inclusive end exceeds a cap, then its first part that does
+    if(threadIdx.x == 0)
+    {
+      s_first = (u64)genBase < k.maxGeneratedClusters ? k.maxGeneratedClusters - genBase : 0u;
+      s_tile  = 0xFFFFFFFFu;
+    }
+    __syncthreads();
+    for(u32 t = threadIdx.x; t < numTiles; t += kScanBlock)
+    {
+      const u64 v = c.scratch.lbState[t];
+      if(c.scratch.lbState[stride + t] + (v >> kPackShift) > maxData
+         || c.scratch.lbState[2 * stride + t] + (v & kPackMask) > k.maxGeneratedVertices)
+        atomicMin(&s_tile, t);
+    }
+    __syncthreads();
+    const u32 tf = s_tile;
+    if(tf < numTiles)
+    {
+      const tc_TessTriangleInfo* parts = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
+      const u32                  q     = tf * kTile + threadIdx.x;
+      const u64                  own   = q < n ? part_packed(c, part_cfg(parts, s_range[0] + q)) : 0ull;
+      const u64                  d = own >> kPackShift, vx = own & kPackMask;
+      const u64                  id = warp_inclusive<u64>(d, lane), iv = warp_inclusive<u64>(vx, lane);
+      if(lane == 31)
+      {
+        s_warpData[warp]  = id;
+        s_warpVerts[warp] = iv;
+      }
+      __syncthreads();
+      if(warp == 0)
+      {
+        const u64 wd = s_warpData[lane], wv = s_warpVerts[lane];
+        const u64 sd = warp_inclusive<u64>(wd, lane), sv = warp_inclusive<u64>(wv, lane);
+        s_warpData[lane]  = sd - wd;
+        s_warpVerts[lane] = sv - wv;
+      }
+      __syncthreads();
+      const u64 inData  = c.scratch.lbState[stride + tf] + s_warpData[warp] + id;
+      const u64 inVerts = c.scratch.lbState[2 * stride + tf] + s_warpVerts[warp] + iv;
+      if(q < n && (inData > maxData || inVerts > k.maxGeneratedVertices))
+        atomicMin(&s_first, q);
+    }
+    __syncthreads();
+    accepted = min(attempts, s_first);
+  }
   if(threadIdx.x == 0)
   {
     *c.scratch.ticket   = 0;  // the chunk ticket of the vertex launch that follows
     c.scratch.totals[0] = genBase;
     // instantiation slots continue after the accepted ones (transient builds
     // take generated-cluster slots but no instantiation slot)
-    c.scratch.totals[1] = b->tempInstantiateCounter;
+    const u32 temp         = b->tempInstantiateCounter;
+    c.scratch.totals[1]    = temp;
+    b->tempInstantiateCounter = temp + accepted;
     if(numTiles)
     {
       // the reference's counters count every attempt, accepted or not
-      b->genClusterCounter     = genBase + min(n, numTiles * kTile);
+      b->genClusterCounter     = genBase + attempts;
       b->genClusterDataCounter = carryData;
       b->genVertexCounter      = (u32)carryVerts;
     }
@@ -279,7 +337,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_instantiate_args(StageCtx c, Inst
   stage_prologue();
   __shared__ u64        s_rowWarp[kItems][kWarps];  // per row and warp: packed warp totals
   __shared__ u32        s_flag, s_range[2];
-  __shared__ u32        s_blasKey[kWarps][2], s_blasCnt[kWarps][2], s_stat[kWarps][2];
+  __shared__ u32        s_blasKey[kWarps][2], s_blasCnt[kWarps][2], s_stat[kWarps];
   const u32         lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   tc_SceneBuilding* b    = c.build;
   if(threadIdx.x == 0)
@@ -295,7 +353,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_instantiate_args(StageCtx c, Inst
   const tc_TessTriangleInfo* parts        = reinterpret_cast<const tc_TessTriangleInfo*>(b->partTriangles);
   const u64                  maxData      = (u64)k.maxGeneratedClusterMegs * 1024ull * 1024ull;
   tc_BlasBuildInfo*          blas         = reinterpret_cast<tc_BlasBuildInfo*>(b->blasBuildInfos);
-  u32                        statTris = 0, statTemp = 0;
+  u32                        statTris = 0;
 
   for(u32 tile = blockIdx.x; tile < numTiles; tile += gridDim.x)
   {
@@ -372,7 +430,6 @@ __global__ void __launch_bounds__(kBlock, 4) k_instantiate_args(StageCtx c, Inst
       reinterpret_cast<u32*>(b->tempInstanceIDs)[tempOffset]      = inst[i];
       reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset] = b->genClusterData + dataOffset;
       statTris += table_entry(c.table, cfg[i]).numTriangles;
-      statTemp += 1;
       if(inst[i] != runInst)
       {
         if(runCount)
@@ -449,23 +506,19 @@ __global__ void __launch_bounds__(kBlock, 4) k_instantiate_args(StageCtx c, Inst
   for(int o = 16; o > 0; o >>= 1)
   {
     statTris += __shfl_xor_sync(0xFFFFFFFFu, statTris, o);
-    statTemp += __shfl_xor_sync(0xFFFFFFFFu, statTemp, o);
   }
   if(lane == 0)
   {
-    s_stat[warp][0] = statTris;
-    s_stat[warp][1] = statTemp;
+    s_stat[warp] = statTris;
   }
   __syncthreads();
   if(threadIdx.x == 0)
   {
-    u32 t = 0, q = 0;
+    u32 t = 0;
     for(u32 w = 0; w < kWarps; w++)
-      t += s_stat[w][0], q += s_stat[w][1];
+      t += s_stat[w];
     if(t)
       atomicAdd(&c.readback->numTotalTriangles, t);
-    if(q)
-      atomicAdd(&b->tempInstantiateCounter, q);
   }
 
   if(last_block_done(c, &s_flag))
@@ -679,7 +732,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_parts(StageCt
   stage_prologue();
   __shared__ PartAffine s_part[kWarps][kPartsPerWarp];
   __shared__ ChunkStage s_stage[kWarps];
-  __shared__ u32        s_range[2], s_flag, s_stat[kWarps][2];
+  __shared__ u32        s_range[2], s_flag, s_stat[kWarps];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if(threadIdx.x == 0)
     part_range(c, s_range[0], s_range[1]);
@@ -700,7 +753,7 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_parts(StageCt
   const u64                  tempBase  = c.scratch.totals[1];
   PartAffine*                sp        = s_part[warp];
   ChunkStage&                stage     = s_stage[warp];
-  u32                        statTris = 0, statTemp = 0;
+  u32                        statTris = 0;
   u32                        carryKey = 0xFFFFFFFFu, carryCnt = 0;  // warp-uniform
 
   // stage chunk `ck`'s records; vo marks the lanes with a part (0) or none (~0)
@@ -775,7 +828,6 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_parts(StageCt
       reinterpret_cast<u32*>(b->tempInstanceIDs)[tempOffset]      = r0.x;
       reinterpret_cast<u64*>(b->tempClusterAddresses)[tempOffset] = b->genClusterData + dataOffset;
       statTris += table_entry(c.table, cfg).numTriangles;
-      statTemp += 1;
     }
     // CLAS reference counts per instance (the chunk's parts are instance-sorted):
     // groups of equal instance, the first continuing the warp's carried count
@@ -834,23 +886,19 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_instantiate_parts(StageCt
   for(int o = 16; o > 0; o >>= 1)
   {
     statTris += __shfl_xor_sync(0xFFFFFFFFu, statTris, o);
-    statTemp += __shfl_xor_sync(0xFFFFFFFFu, statTemp, o);
   }
   if(lane == 0)
   {
-    s_stat[warp][0] = statTris;
-    s_stat[warp][1] = statTemp;
+    s_stat[warp] = statTris;
   }
   __syncthreads();
   if(threadIdx.x == 0)
   {
-    u32 t = 0, qn = 0;
+    u32 t = 0;
     for(u32 wi = 0; wi < kWarps; wi++)
-      t += s_stat[wi][0], qn += s_stat[wi][1];
+      t += s_stat[wi];
     if(t)
       atomicAdd(&c.readback->numTotalTriangles, t);
-    if(qn)
-      atomicAdd(&b->tempInstantiateCounter, qn);
   }
 
   if(last_block_done(c, &s_flag))
@@ -943,17 +991,32 @@ __global__ void __launch_bounds__(kBlock) k_instantiate_vertices_deform(StageCtx
 
 u32 instantiate_alloc_tiles(u32 maxParts) { return (maxParts + kTile - 1) / kTile; }
 
+cudaError_t launch_instantiate_prefix(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
+                                      u32 scanBlocksPerSM, cudaStream_t s)
+{
+  const u32         tiles    = std::max(1u, instantiate_alloc_tiles(maxParts));
+  const u32         tileGrid = std::max(1u, std::min(tiles, numSMs * std::max(1u, scanBlocksPerSM)));
+  const cudaError_t e        = launch_pdl_critical(k_instantiate_tile_sums, tileGrid, kBlock, s, c, buf);
+  if(e != cudaSuccess)
+    return e;
+  return launch_pdl_critical(k_instantiate_tile_scan, 1u, kScanBlock, s, c);
+}
+
+cudaError_t launch_instantiate_args(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
+                                    u32 scanBlocksPerSM, cudaStream_t s)
+{
+  const u32 tiles    = std::max(1u, instantiate_alloc_tiles(maxParts));
+  const u32 tileGrid = std::max(1u, std::min(tiles, numSMs * std::max(1u, scanBlocksPerSM)));
+  return launch_pdl_critical(k_instantiate_args, tileGrid, kBlock, s, c, buf);
+}
+
 cudaError_t launch_instantiate_alloc(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
                                      u32 scanBlocksPerSM, cudaStream_t s)
 {
-  const u32   tiles    = std::max(1u, instantiate_alloc_tiles(maxParts));
-  const u32   tileGrid = std::max(1u, std::min(tiles, numSMs * std::max(1u, scanBlocksPerSM)));
-  cudaError_t e        = launch_pdl_critical(k_instantiate_tile_sums, tileGrid, kBlock, s, c, buf);
+  const cudaError_t e = launch_instantiate_prefix(c, buf, maxParts, numSMs, scanBlocksPerSM, s);
   if(e != cudaSuccess)
     return e;
-  if((e = launch_pdl_critical(k_instantiate_tile_scan, 1u, kScanBlock, s, c)) != cudaSuccess)
-    return e;
-  return launch_pdl_critical(k_instantiate_args, tileGrid, kBlock, s, c, buf);
+  return launch_instantiate_args(c, buf, maxParts, numSMs, scanBlocksPerSM, s);
 }
 
 cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,

@@ -96,6 +96,12 @@ cudaError_t launch_triangle_instantiate(const StageCtx& c, const InstantiateBuff
 // the allocation alone
 cudaError_t launch_instantiate_alloc(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
                                      u32 scanBlocksPerSM, cudaStream_t s);
+// its two parts: the offsets (tile sums and scan; they advance the counters,
+// the instantiation counter by the run's accepted parts), then the arguments
+cudaError_t launch_instantiate_prefix(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
+                                      u32 scanBlocksPerSM, cudaStream_t s);
+cudaError_t launch_instantiate_args(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
+                                    u32 scanBlocksPerSM, cudaStream_t s);
 cudaError_t launch_instantiate_vertices(const StageCtx& c, const InstantiateBuffers& buf, u32 maxParts, u32 numSMs,
                                         u32 vertexBlocksPerSM, u32 vertexGridPerSM, cudaStream_t s);
 u32         instantiate_alloc_tiles(u32 maxParts);
