@@ -13,8 +13,8 @@ Outputs do not depend on it (every allocation is a prefix sum in a fixed
 order), so tuning is a pure timing search.
 
 Search: coordinate descent from the current schedule; each candidate is timed
-as the median CUDA-event duration of whole graph frames over the caller's
-frames, with L2 flushed before each frame. Two sweeps over the parameters
+as the mean CUDA-event duration of whole graph frames over the caller's
+frames (three passes), with L2 flushed before each frame. Two sweeps over the parameters
 usually settle; each trial re-captures the frame graph once.
 
     best, report = autotune(pipe, frames, set_frame, flush)
@@ -26,7 +26,7 @@ import statistics
 
 SPACE = {
     "classifyBlocksPerSM": (4, 6, 8, 16),
-    "scanBlocksPerSM": (2, 4, 8, 16),
+    "scanBlocksPerSM": (1, 2, 4, 8, 16),
     "splitBlockSize": (128, 256, 512),
     "blocksPerSM": (1, 2, 4),
     "vertexBlocksPerSM": (3, 4, 5, 6),
@@ -38,7 +38,9 @@ SPACE = {
 
 
 def time_schedule(pipe, sched: dict, frames, set_frame, flush, reps: int = 1) -> float:
-    """Median graph-frame time (ms) of `sched` over `frames`."""
+    """Mean graph-frame time (ms) of `sched` over `frames` x `reps` (the mean,
+    not the median: frame throughput is total triangles over total time, so
+    a schedule's slow frames count as much as its typical one)."""
     torch = pipe.torch
     pipe.set_schedule(sched)
     set_frame(frames[0])
@@ -54,10 +56,10 @@ def time_schedule(pipe, sched: dict, frames, set_frame, flush, reps: int = 1) ->
             e1.record()
             torch.cuda.synchronize()
             ts.append(e0.elapsed_time(e1))
-    return statistics.median(ts)
+    return statistics.mean(ts)
 
 
-def autotune(pipe, frames, set_frame, flush, space: dict | None = None, sweeps: int = 2, reps: int = 1):
+def autotune(pipe, frames, set_frame, flush, space: dict | None = None, sweeps: int = 2, reps: int = 3):
     """Coordinate descent over `space`; returns (best schedule, report)."""
     space = dict(space or SPACE)
     start = pipe.schedule()
