@@ -515,7 +515,7 @@ def run_ours(args):
         result["terrain"] = terrain_bandwidth(torch, dev, local, peak, tune=not args.no_tune)
         t = result["terrain"]
         # the instantiate stage of the bandwidth configuration, beside the headline's dominant kernel
-        inst = {"kernel": "triangle_instantiate", "workload": "config 2 terrain (" + t["workload"] + ")",
+        inst = {"kernel": "triangle_instantiate", "workload": t["workload"],
                 "bound": "hbm", "achieved": t["instantiate_gbs"], "peak": peak, "unit": "GB/s",
                 "frac": t["instantiate_frac_of_peak"], "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": t["instantiate_algorithmic_bytes"],
