@@ -20,13 +20,13 @@ def caps():
 
 
 # reduced: subdivision 4, 256² map, a far camera mixing 59 full clusters and
-# 1344 part triangles; config3: the plain small config at full size (icosphere
-# of 20,480 triangles, 1024² fp32 map of 4 octaves, camera at distance 3,
-# 8 px per segment), the frame the backward is specified on
+# 1344 part triangles; icosphere_20480: the small plain frame at full size
+# (icosphere of 20,480 triangles, 1024² fp32 map of 4 octaves, camera at
+# distance 3, 8 px per segment), the frame the backward is specified on
 CASES = {
     "reduced": dict(subdivisions=4, map_size=256,
                     cam=S.Camera(eye=(0.0, 0.0, 8.0), center=(0.0, 0.0, 0.0), tess_rate_pixels=8.0)),
-    "config3": dict(subdivisions=5, map_size=1024, cam=S.camera_icosphere()),
+    "icosphere_20480": dict(subdivisions=5, map_size=1024, cam=S.camera_icosphere()),
 }
 
 
@@ -37,7 +37,7 @@ def setup(oracle, request):
     from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
     case = CASES[request.param]
     sc = S.scene_icosphere(subdivisions=case["subdivisions"], map_size=case["map_size"])
-    if request.param == "config3":
+    if request.param == "icosphere_20480":
         assert sc.total_triangles == 20480 and sc.textures[0].texels.shape == (1024, 1024)
     cam = case["cam"]
     pipe = TessellationPipeline(sc, caps(), FLAGS)
