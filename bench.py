@@ -13,9 +13,12 @@ CUDA graph of one persistent launch per stage.
   value : tessellated triangles per second (Readback.numTotalTriangles / frame
           time), frame inputs resident in HBM, CUDA events on the launching
           stream, L2 flushed (256 MiB write) between timed frames
-  e2e   : same metric through the C ABI with host buffers: per frame the
-          FrameConstants pair and the RenderInstance array are copied from
-          pinned host memory and the Readback copied back, inside the events
+  e2e   : same metric through the C ABI with host buffers
+          (tc_frame_build_graph_host): per frame the FrameConstants pair and
+          the RenderInstance array are read from pinned host memory and the
+          Readback written back to it by kernels of the frame graph, inside
+          the events (memcpy_variant: the same traffic by cudaMemcpyAsync
+          around tc_frame_build_graph)
   roofline : the frame's dominant kernel, algorithmic bytes (metrics.py) over
           its CUDA-event duration, against the measured HBM copy bandwidth
   cpu_baseline : the CPU oracle (C++ restatement of the reference shaders,
@@ -431,8 +434,9 @@ def run_ours(args):
 
     # ---- e2e through the C ABI with host buffers ------------------------------
     # A frame's inputs (its FrameConstants, the previous frame's, the instance
-    # records) sit side by side in one pinned host block and in one device
-    # block that the frame arguments point into: one upload per frame.
+    # records) sit side by side in one block: the application's per-frame data
+    # (pageable) is written into one pinned staging block, which the frame
+    # moves into one device block that the frame arguments point into.
     inst_rec = pipe.state.res.instance_records.view(np.uint8).reshape(-1)
     blk = 2 * FC + inst_rec.size
     host_np = np.empty((NUM_ORBIT_FRAMES, blk), np.uint8)
@@ -440,7 +444,8 @@ def run_ours(args):
         host_np[f, :FC] = fc_bytes[f]
         host_np[f, FC:2 * FC] = fc_bytes[(f - 1) % NUM_ORBIT_FRAMES]
         host_np[f, 2 * FC:] = inst_rec
-    host_blocks = torch.from_numpy(host_np).pin_memory()
+    stage = torch.empty(blk, dtype=torch.uint8, pin_memory=True)
+    stage_np = stage.numpy()
     dev_block = torch.empty(blk + 256, dtype=torch.uint8, device=dev)
     base = (dev_block.data_ptr() + 255) // 256 * 256  # RenderInstance records 16-byte aligned (FC is a multiple of 16)
     off = base - dev_block.data_ptr()
@@ -448,22 +453,36 @@ def run_ours(args):
     saved_ptrs = (fa.view, fa.viewLast, fa.instances)
     fa.view, fa.viewLast, fa.instances = base, base + FC, base + 2 * FC
     h2d = blk
-    e2e_times, e2e_tris = [], []
-    for s in range(args.warmup + args.steps):
-        f = s % NUM_ORBIT_FRAMES
-        flush()  # before the step, as in the device-resident loop
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        dev_block[off:off + blk].copy_(host_blocks[f], non_blocking=True)
+
+    def e2e_run(step):
+        times_, tris_ = [], []
+        for s in range(args.warmup + args.steps):
+            f = s % NUM_ORBIT_FRAMES
+            flush()  # before the step, as in the device-resident loop
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            stage_np[:] = host_np[f]
+            step()
+            e1.record()
+            e1.synchronize()
+            if s >= args.warmup:
+                times_.append(e0.elapsed_time(e1))
+                tris_.append(int(rb_host.numpy().view(L.Readback)[0]["numTotalTriangles"]))
+        return times_, tris_
+
+    # the public call: the frame graph reads the input block from pinned host
+    # memory and writes the Readback to pinned host memory itself
+    e2e_times, e2e_tris = e2e_run(lambda: pipe.build_host(stage.data_ptr(), base, blk, rb_host.data_ptr()))
+    e2e_value = sum(e2e_tris) / (sum(e2e_times) / 1e3)
+
+    # the same traffic through the copy engines (cudaMemcpyAsync each way) around tc_frame_build_graph
+    def memcpy_step():
+        dev_block[off:off + blk].copy_(stage, non_blocking=True)
         pipe.build("graph")
         rb_host.copy_(pipe.state.readback.handle[:L.Readback.itemsize], non_blocking=True)
-        e1.record()
-        e1.synchronize()
-        if s >= args.warmup:
-            e2e_times.append(e0.elapsed_time(e1))
-            e2e_tris.append(int(rb_host.numpy().view(L.Readback)[0]["numTotalTriangles"]))
+
+    mc_times, mc_tris = e2e_run(memcpy_step)
     fa.view, fa.viewLast, fa.instances = saved_ptrs
-    e2e_value = sum(e2e_tris) / (sum(e2e_times) / 1e3)
 
     # ---- per-stage profile and roofline of the dominant kernel ---------------------
     prof_frames = list(range(0, NUM_ORBIT_FRAMES, max(1, NUM_ORBIT_FRAMES // 6)))[:6]
@@ -496,7 +515,10 @@ def run_ours(args):
                    "l2": "flushed between timed frames (256 MiB write)", "mode": "CUDA graph, batched persistent stages",
                    "schedule": pipe.schedule(), "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": "tris/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": L.Readback.itemsize, "ms_per_step": statistics.mean(e2e_times)},
+                "d2h_bytes_per_step": L.Readback.itemsize, "ms_per_step": statistics.mean(e2e_times),
+                "call": "tc_frame_build_graph_host",
+                "memcpy_variant": {"value": sum(mc_tris) / (sum(mc_times) / 1e3),
+                                   "ms_per_step": statistics.mean(mc_times)}},
         "gpu_launches": gpu_launches,
         "clocks": clk.summary(),
         "roofline": roof,

@@ -540,6 +540,23 @@ tc_status tc_frame_build(tc_context* ctx, const tc_frame_args* args, void* strea
  * the args; a change of args re-records. */
 tc_status tc_frame_build_graph(tc_context* ctx, const tc_frame_args* args, void* stream);
 
+/* The graph frame of tc_frame_build_graph with the frame's host traffic inside
+ * the graph: its first kernel copies inputBytes from the pinned host block
+ * hostInputs to the device block deviceInputs (which args->view, viewLast and
+ * instances may point into), its last kernel copies the frame's tc_Readback to
+ * the pinned host buffer hostReadback, which holds it once the stream has
+ * passed the call. Replaces the reference's per-frame upload of the frame
+ * constants (src/renderer_raytrace_clusters_tess.cpp:415, vkCmdUpdateBuffer)
+ * and its Readback copy to a host-visible buffer (src/resources.cpp:83-90,
+ * read in src/resources.cpp:497-501) without copy-engine round trips.
+ * Host buffers: pinned and mapped (cudaHostAlloc, or cudaHostRegister with
+ * cudaHostRegisterMapped); hostInputs and deviceInputs 16-byte aligned,
+ * hostReadback 8-byte aligned (else TC_ERR_INVALID_ARG). inputBytes 0 skips
+ * the upload, hostReadback NULL the Readback copy. The graph is keyed by the
+ * args and the three buffers' addresses; a change re-records. */
+tc_status tc_frame_build_graph_host(tc_context* ctx, const tc_frame_args* args, const void* hostInputs,
+                                    uint64_t deviceInputs, uint64_t inputBytes, void* hostReadback, void* stream);
+
 /* Same frame, with every stage launched once per instance (and per split pass)
  * from the host: the reference's per-instance dispatch pattern of clusters_cull
  * (src/renderer_raytrace_clusters_tess.cpp:454-460) applied to all stages.

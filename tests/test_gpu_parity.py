@@ -485,3 +485,70 @@ def test_raster_batches_match_oracle(oracle, case):
     cm = float(np.abs(want["clipPositions"]).max())
     assert np.abs(got["clipPositions"].astype(np.float64) - want["clipPositions"]).max() <= 1e-5 * cm + 1e-4
     pipe.close()
+
+
+def test_host_io_frames_match_oracle(oracle):
+    """tc_frame_build_graph_host: each frame's inputs (its frame constants,
+    the previous frame's, the instance records) read from a pinned host block
+    and its Readback written to pinned host memory by kernels of the frame
+    graph; per orbit frame the outputs match the oracle and the host Readback
+    equals the device one. Unpinned or misaligned host buffers are argument
+    errors that launch nothing and leave the context usable."""
+    import torch
+    from vk_tessellated_clusters_gb300 import native
+    from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
+    from vk_tessellated_clusters_gb300.scene import frame_constants
+    sc = S.scene_batched(num_instances=32, map_size=64)
+    caps = small_caps()
+    pipe = TessellationPipeline(sc, caps, FLAGS)
+    FC = L.FrameConstants.itemsize
+    RB = L.Readback.itemsize
+    rec = pipe.state.res.instance_records.view(np.uint8).reshape(-1)
+    frames = (3, 4, 9)
+    blk = 2 * FC + rec.size
+    assert blk % 16 == 0
+    host = torch.empty((len(frames), blk), dtype=torch.uint8, pin_memory=True)
+    for k, f in enumerate(frames):
+        host[k, :FC] = torch.from_numpy(np.frombuffer(frame_constants(S.camera_orbit(f)).tobytes(), np.uint8).copy())
+        host[k, FC:2 * FC] = torch.from_numpy(
+            np.frombuffer(frame_constants(S.camera_orbit(f - 1)).tobytes(), np.uint8).copy())
+        host[k, 2 * FC:] = torch.from_numpy(rec.copy())
+    rb_host = torch.zeros(RB, dtype=torch.uint8, pin_memory=True)
+    dev_block = torch.empty(blk + 256, dtype=torch.uint8, device="cuda")
+    base = (dev_block.data_ptr() + 255) // 256 * 256
+    fa = pipe.args
+    saved = (fa.view, fa.viewLast, fa.instances)
+    fa.view, fa.viewLast, fa.instances = base, base + FC, base + 2 * FC
+    for k, f in enumerate(frames):
+        rb_host.zero_()
+        pipe.build_host(host[k].data_ptr(), base, blk, rb_host.data_ptr())
+        torch.cuda.synchronize()
+        out = pipe.outputs()
+        ref_state, _ = oracle.frame(sc, S.camera_orbit(f), caps, FLAGS, camera_last=S.camera_orbit(f - 1))
+        assert_same(out, ref_state.outputs(oracle.entries), f"host-io frame {f}", vertex_tol=vertex_tolerance(sc))
+        assert np.array_equal(rb_host.numpy(), pipe.state.readback.handle[:RB].cpu().numpy()), f"frame {f}"
+        assert int(rb_host.numpy().view(L.Readback)[0]["numTotalTriangles"]) > 0
+
+    # argument errors: a pageable host block, a misaligned one, a misaligned Readback buffer
+    pageable = np.zeros(blk + 64, np.uint8)
+    p_addr = (pageable.ctypes.data + 15) // 16 * 16
+    for hin, hrb in ((p_addr, rb_host.data_ptr()), (host[0].data_ptr() + 4, rb_host.data_ptr()),
+                     (host[0].data_ptr(), rb_host.data_ptr() + 4)):
+        with pytest.raises(native.TcError) as e:
+            pipe.build_host(hin, base, blk, hrb)
+        assert e.value.status == L.TC_ERR_INVALID_ARG
+
+    # the context still replays: the last frame again, then the Readback alone
+    # with the frame reading the resident buffers
+    pipe.build_host(host[2].data_ptr(), base, blk, rb_host.data_ptr())
+    torch.cuda.synchronize()
+    last = pipe.outputs()
+    fa.view, fa.viewLast, fa.instances = saved
+    pipe.set_cameras(S.camera_orbit(frames[2]), S.camera_orbit(frames[2] - 1))
+    rb_host.zero_()
+    pipe.build_host(0, 0, 0, rb_host.data_ptr())
+    torch.cuda.synchronize()
+    assert_same(pipe.outputs(), last, "readback-only frame")
+    assert np.array_equal(rb_host.numpy(), pipe.state.readback.handle[:RB].cpu().numpy())
+    assert pipe.device_errors() == 0
+    pipe.close()

@@ -59,6 +59,27 @@ struct Plan
   size_t totalBytes;
 };
 
+// A frame's host traffic inside its graph (tc_frame_build_graph_host): the
+// device aliases of the pinned host buffers, the device input block.
+struct HostIo
+{
+  const void* hostIn   = nullptr;  // device alias of the caller's input block
+  void*       devIn    = nullptr;
+  uint64_t    bytes    = 0;
+  void*       hostRb   = nullptr;  // device alias of the caller's Readback buffer
+  const void* callerIn = nullptr;  // the caller's addresses
+  const void* callerRb = nullptr;
+  bool same_buffers(const HostIo& o) const
+  {
+    return callerIn == o.callerIn && devIn == o.devIn && bytes == o.bytes && callerRb == o.callerRb;
+  }
+  bool operator==(const HostIo& o) const
+  {
+    return same_buffers(o) && hostIn == o.hostIn && hostRb == o.hostRb;
+  }
+  uint64_t launches() const { return (bytes ? 1 : 0) + (hostRb ? 1 : 0); }
+};
+
 u32 ceil_div(u64 a, u64 b) { return (u32)((a + b - 1) / b); }
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -104,6 +125,7 @@ struct tc_context
   cudaGraph_t     graph     = nullptr;
   tc_frame_args   graphArgs = {};
   tc_schedule     graphSchedule = {};
+  HostIo          graphIo       = {};
   bool            graphValid = false;
 
   std::mutex mutex;
@@ -336,12 +358,14 @@ u32 split_items_per_tile(u32 block) { return block == 128 ? 16 : 32; }
 
 // The batched frame: one persistent launch per stage, build_setup fused into the
 // producers' last block. Graph-capturable (no host synchronisation, no allocation).
-tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStream_t s)
+tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStream_t s, const HostIo& io = HostIo())
 {
   const Plan&        p     = ctx->plan;
   const tc_schedule& sched = ctx->schedule;
   const u32          bpsm  = std::max(1u, sched.blocksPerSM);
   TC_CHECK_CUDA(cudaMemsetAsync(ctx->dScratch, 0, p.frameBytes, s));
+  if(io.bytes)
+    TC_CHECK_CUDA(launch_host_upload(io.hostIn, io.devIn, io.bytes, ctx->numSMs, s));
 
   StageCtx c = base_ctx(ctx, a);
   bind_slot(ctx, c, p.slotInstances, false);
@@ -463,9 +487,94 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   TC_CHECK_CUDA(launch_blas_clusters_insert(c, seg, seg + (size_t)p.segStride * p.segRows, p.segStride, insert_grid(ctx, a), s));
   TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evVerts, 0));
   TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evJoin2, 0));
+  if(io.hostRb)
+    TC_CHECK_CUDA(launch_host_readback(c.readback, io.hostRb, s));
 
-  ctx->launches += frame_launches(ctx, a);
+  ctx->launches += frame_launches(ctx, a) + io.launches();
   return TC_OK;
+}
+
+// Replays the batched frame's graph (recorded again when the args, the
+// schedule or the host buffers changed).
+tc_status graph_frame(tc_context* ctx, const tc_frame_args* args, const HostIo& io, cudaStream_t s)
+{
+  if(!ctx->graphValid || std::memcmp(&ctx->graphArgs, args, sizeof(tc_frame_args)) != 0
+     || std::memcmp(&ctx->graphSchedule, &ctx->schedule, sizeof(tc_schedule)) != 0 || !(ctx->graphIo == io))
+  {
+    if(ctx->graphExec)
+      cudaGraphExecDestroy(ctx->graphExec);
+    if(ctx->graph)
+      cudaGraphDestroy(ctx->graph);
+    ctx->graphExec  = nullptr;
+    ctx->graph      = nullptr;
+    ctx->graphValid = false;
+    // capture on a private stream so the caller's stream may be the legacy default stream
+    cudaStream_t cap;
+    TC_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    uint64_t launchesBefore = ctx->launches;
+    if(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    {
+      cudaStreamDestroy(cap);
+      return TC_ERR_CUDA;
+    }
+    tc_status rst = record_batched_frame(ctx, args, cap, io);
+    cudaGraph_t g  = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    ctx->launches = launchesBefore;
+    if(rst != TC_OK)
+    {
+      if(g)
+        cudaGraphDestroy(g);
+      return rst;
+    }
+    if(ce != cudaSuccess)
+      return TC_ERR_CUDA;
+    ctx->graph = g;
+    TC_CHECK_CUDA(cudaGraphInstantiate(&ctx->graphExec, g, 0));
+    ctx->graphArgs     = *args;
+    ctx->graphSchedule = ctx->schedule;
+    ctx->graphIo       = io;
+    ctx->graphValid    = true;
+  }
+  TC_CHECK_CUDA(cudaGraphLaunch(ctx->graphExec, s));
+  ctx->launches += frame_launches(ctx, args) + io.launches();
+  return TC_OK;
+}
+
+// The device alias of [p, p + bytes) in pinned, mapped host memory, or null
+// when either end is not pinned host memory or the two ends are not one
+// contiguous mapping.
+void* host_alias(const void* p, uint64_t bytes)
+{
+  cudaPointerAttributes a0, a1;
+  const char* last = static_cast<const char*>(p) + bytes - 1;
+  if(cudaPointerGetAttributes(&a0, p) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess)
+  {
+    cudaGetLastError();  // not sticky: clear it for the caller
+    return nullptr;
+  }
+  if(a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+    return nullptr;
+  if(static_cast<char*>(a1.devicePointer) - static_cast<char*>(a0.devicePointer) != (ptrdiff_t)(bytes - 1))
+    return nullptr;
+  return a0.devicePointer;
+}
+
+// Whether both ends of [p, p + bytes) are device (or managed) memory.
+bool device_range(const void* p, uint64_t bytes)
+{
+  cudaPointerAttributes a0, a1;
+  const char* last = static_cast<const char*>(p) + bytes - 1;
+  if(cudaPointerGetAttributes(&a0, p) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess)
+  {
+    cudaGetLastError();
+    return false;
+  }
+  auto dev = [](const cudaPointerAttributes& a) {
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  };
+  return dev(a0) && dev(a1);
 }
 
 }  // namespace
@@ -730,48 +839,46 @@ tc_status tc_frame_build_graph(tc_context* ctx, const tc_frame_args* args, void*
   tc_status st = validate(ctx, args);
   if(st != TC_OK)
     return st;
-  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  if(!ctx->graphValid || std::memcmp(&ctx->graphArgs, args, sizeof(tc_frame_args)) != 0
-     || std::memcmp(&ctx->graphSchedule, &ctx->schedule, sizeof(tc_schedule)) != 0)
+  return graph_frame(ctx, args, HostIo(), reinterpret_cast<cudaStream_t>(stream));
+}
+
+tc_status tc_frame_build_graph_host(tc_context* ctx, const tc_frame_args* args, const void* hostInputs,
+                                    uint64_t deviceInputs, uint64_t inputBytes, void* hostReadback, void* stream)
+{
+  tc_status st = validate(ctx, args);
+  if(st != TC_OK)
+    return st;
+  if(inputBytes && (!hostInputs || !deviceInputs || (reinterpret_cast<uintptr_t>(hostInputs) & 15) || (deviceInputs & 15)))
+    return TC_ERR_INVALID_ARG;
+  if(hostReadback && (reinterpret_cast<uintptr_t>(hostReadback) & 7))
+    return TC_ERR_INVALID_ARG;
+  HostIo io;
+  io.bytes    = inputBytes;
+  io.devIn    = inputBytes ? reinterpret_cast<void*>(deviceInputs) : nullptr;
+  io.callerIn = inputBytes ? hostInputs : nullptr;
+  io.callerRb = hostReadback;
+  if(ctx->graphValid && io.same_buffers(ctx->graphIo))
   {
-    if(ctx->graphExec)
-      cudaGraphExecDestroy(ctx->graphExec);
-    if(ctx->graph)
-      cudaGraphDestroy(ctx->graph);
-    ctx->graphExec  = nullptr;
-    ctx->graph      = nullptr;
-    ctx->graphValid = false;
-    // capture on a private stream so the caller's stream may be the legacy default stream
-    cudaStream_t cap;
-    TC_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-    uint64_t launchesBefore = ctx->launches;
-    if(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
-    {
-      cudaStreamDestroy(cap);
-      return TC_ERR_CUDA;
-    }
-    tc_status rst = record_batched_frame(ctx, args, cap);
-    cudaGraph_t g  = nullptr;
-    cudaError_t ce = cudaStreamEndCapture(cap, &g);
-    cudaStreamDestroy(cap);
-    ctx->launches = launchesBefore;
-    if(rst != TC_OK)
-    {
-      if(g)
-        cudaGraphDestroy(g);
-      return rst;
-    }
-    if(ce != cudaSuccess)
-      return TC_ERR_CUDA;
-    ctx->graph = g;
-    TC_CHECK_CUDA(cudaGraphInstantiate(&ctx->graphExec, g, 0));
-    ctx->graphArgs     = *args;
-    ctx->graphSchedule = ctx->schedule;
-    ctx->graphValid    = true;
+    // checked when the graph was recorded
+    io.hostIn = ctx->graphIo.hostIn;
+    io.hostRb = ctx->graphIo.hostRb;
   }
-  TC_CHECK_CUDA(cudaGraphLaunch(ctx->graphExec, s));
-  ctx->launches += frame_launches(ctx, args);
-  return TC_OK;
+  else
+  {
+    if(inputBytes)
+    {
+      io.hostIn = host_alias(hostInputs, inputBytes);
+      if(!io.hostIn || !device_range(io.devIn, inputBytes))
+        return TC_ERR_INVALID_ARG;
+    }
+    if(hostReadback)
+    {
+      io.hostRb = host_alias(hostReadback, sizeof(tc_Readback));
+      if(!io.hostRb)
+        return TC_ERR_INVALID_ARG;
+    }
+  }
+  return graph_frame(ctx, args, io, reinterpret_cast<cudaStream_t>(stream));
 }
 
 tc_status tc_frame_begin(tc_context* ctx, const tc_frame_args* a, void* stream)

@@ -1,5 +1,7 @@
 // tc_frame.cu — per-frame reset, instance classification, cluster culling and
 // the standalone build_setup kernel.
+#include <algorithm>
+
 #include "tc_kernels.h"
 #include "tc_stage.cuh"
 
@@ -338,8 +340,68 @@ __global__ void k_lookback_probe(u64* state, u32 published, u32* errorWord, u32 
 }
 
 // ---------------------------------------------------------------------------
+// A frame's host traffic inside its graph (tc_frame_build_graph_host): the
+// input block (frame constants, instance records) read from mapped pinned host
+// memory before the frame, the Readback written back to it after the frame.
+// Plain loads and stores through the mapping replace the copy-engine round
+// trips of cudaMemcpyAsync (the reference: vkCmdUpdateBuffer of the frame
+// constants, src/renderer_raytrace_clusters_tess.cpp:415, and the Readback copy
+// to a host-visible buffer, src/resources.cpp:83-90). The kernel boundary
+// makes the stores visible to the host once the stream has passed the frame.
+// ---------------------------------------------------------------------------
+
+constexpr u32 kUploadPerThread = 4;  // 16-byte loads in flight per thread before its stores
+
+__global__ void k_host_upload(const uint4* __restrict__ src, uint4* __restrict__ dst, u64 n16,
+                              const unsigned char* __restrict__ srcTail, unsigned char* __restrict__ dstTail, u32 tail)
+{
+  stage_prologue();
+  const u64 stride = (u64)gridDim.x * blockDim.x;
+  for(u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride * kUploadPerThread)
+  {
+    uint4 v[kUploadPerThread];
+#pragma unroll
+    for(u32 k = 0; k < kUploadPerThread; k++)
+      if(i + k * stride < n16)
+        v[k] = src[i + k * stride];
+#pragma unroll
+    for(u32 k = 0; k < kUploadPerThread; k++)
+      if(i + k * stride < n16)
+        dst[i + k * stride] = v[k];
+  }
+  if(blockIdx.x == 0 && threadIdx.x < tail)
+    dstTail[threadIdx.x] = srcTail[threadIdx.x];
+}
+
+__global__ void k_host_readback(const u32* __restrict__ src, u32* __restrict__ dst, u32 words)
+{
+  stage_prologue();
+  for(u32 i = threadIdx.x; i < words; i += blockDim.x)
+    dst[i] = src[i];
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+
+cudaError_t launch_host_upload(const void* src, void* dst, u64 bytes, u32 maxGrid, cudaStream_t s)
+{
+  const u64 n16   = bytes / 16;
+  const u32 tail  = (u32)(bytes % 16);
+  const u64 per   = 256ull * kUploadPerThread;
+  const u32 grid  = (u32)std::max<u64>(1, std::min<u64>((n16 + per - 1) / per, maxGrid));
+  const auto* s8  = static_cast<const unsigned char*>(src) + n16 * 16;
+  auto*       d8  = static_cast<unsigned char*>(dst) + n16 * 16;
+  return launch_side(k_host_upload, grid, 256, s, static_cast<const uint4*>(src), static_cast<uint4*>(dst), n16, s8,
+                     d8, tail);
+}
+
+cudaError_t launch_host_readback(const tc_Readback* src, void* dst, cudaStream_t s)
+{
+  static_assert(sizeof(tc_Readback) % 4 == 0, "the Readback is copied in 32-bit words");
+  return launch_side(k_host_readback, 1, 256, s, reinterpret_cast<const u32*>(src), static_cast<u32*>(dst),
+                     (u32)(sizeof(tc_Readback) / 4));
+}
 
 cudaError_t launch_lookback_probe(u64* state, u32 published, u32* errorWord, u32 spinLimit, cudaStream_t s)
 {

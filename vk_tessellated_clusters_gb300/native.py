@@ -38,6 +38,7 @@ def _bind(lib):
         "tc_get_schedule": (st, [vp, ctypes.POINTER(L.Schedule)]),
         "tc_frame_build": (st, [vp, ctypes.POINTER(L.FrameArgs), vp]),
         "tc_frame_build_graph": (st, [vp, ctypes.POINTER(L.FrameArgs), vp]),
+        "tc_frame_build_graph_host": (st, [vp, ctypes.POINTER(L.FrameArgs), vp, u64, u64, vp, vp]),
         "tc_frame_build_plain": (st, [vp, ctypes.POINTER(L.FrameArgs), vp]),
         "tc_frame_begin": (st, [vp, ctypes.POINTER(L.FrameArgs), vp]),
         "tc_instances_classify": (st, [vp, ctypes.POINTER(L.FrameArgs), vp]),
@@ -72,7 +73,7 @@ def exported_symbols() -> list[str]:
     return [
         "tc_version", "tc_status_string", "tc_context_create", "tc_context_destroy", "tc_table_init",
         "tc_table_set_templates", "tc_set_schedule", "tc_get_schedule", "tc_frame_build", "tc_frame_build_graph",
-        "tc_frame_build_plain", "tc_frame_begin", "tc_instances_classify", "tc_clusters_cull", "tc_build_setup",
+        "tc_frame_build_graph_host", "tc_frame_build_plain", "tc_frame_begin", "tc_instances_classify", "tc_clusters_cull", "tc_build_setup",
         "tc_cluster_classify", "tc_triangle_split", "tc_triangle_split_all", "tc_triangle_instantiate", "tc_triangle_instantiate_run",
         "tc_blas_setup_insertion", "tc_blas_clusters_insert", "tc_blas_setup_insertion_noalloc",
         "tc_split_pass_count", "tc_instantiate_backward",

@@ -92,6 +92,16 @@ class TessellationPipeline:
               "plain": self.lib.tc_frame_build_plain}[mode]
         native.check(fn(self.ctx, ctypes.byref(self.args), self.stream()), f"tc_frame_build ({mode})")
 
+    def build_host(self, host_inputs: int, device_inputs: int, nbytes: int, host_readback: int) -> None:
+        """The graph frame with its host traffic inside the graph
+        (tc_frame_build_graph_host): `nbytes` from the pinned host block at
+        `host_inputs` to the device block at `device_inputs` before the frame
+        (the frame args may point into it), the Readback to the pinned host
+        buffer at `host_readback` after it."""
+        native.check(self.lib.tc_frame_build_graph_host(self.ctx, ctypes.byref(self.args), host_inputs, device_inputs,
+                                                        nbytes, host_readback, self.stream()),
+                     "tc_frame_build_graph_host")
+
     def stage(self, name: str, *extra) -> None:
         f = getattr(self.lib, "tc_" + name)
         native.check(f(self.ctx, ctypes.byref(self.args), *extra, self.stream()), name)
