@@ -56,7 +56,8 @@ def parse_args():
     p.add_argument("--no-extras", action="store_true", help="skip the plain-path and terrain measurements")
     p.add_argument("--no-tune", action="store_true", help="keep the default launch schedule (no autotuning)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
-    p.add_argument("--profile-case", choices=["batched", "terrain", "terrain_stages", "transient", "raster"], default=None,
+    p.add_argument("--profile-case", choices=["batched", "batched_host", "terrain", "terrain_stages", "transient", "raster"],
+                   default=None,
                    help="run only `warmup` + `steps` graph frames of one case (for ncu captures) and exit")
     return p.parse_args()
 
@@ -994,12 +995,13 @@ def terrain_caps():
 
 def run_profile_case(args):
     """A short, fixed sequence of frames of one case: the command ncu captures."""
+    import numpy as np
     import torch
     from vk_tessellated_clusters_gb300 import layouts as L
     from vk_tessellated_clusters_gb300 import scene as S
     from vk_tessellated_clusters_gb300.pipeline import TessellationPipeline
     flags = L.FLAG_CULLING
-    if args.profile_case in ("batched", "transient", "raster"):
+    if args.profile_case in ("batched", "batched_host", "transient", "raster"):
         scene, caps = S.scene_batched(256), L.default_caps()
         cams = [S.camera_orbit(f) for f in range(args.warmup + args.steps)]
         if args.profile_case == "transient":
@@ -1008,7 +1010,28 @@ def run_profile_case(args):
         scene, caps = S.scene_terrain(), terrain_caps()
         cams = [S.camera_terrain()] * (args.warmup + args.steps)
     pipe = TessellationPipeline(scene, caps, flags)
+    host_io = args.profile_case == "batched_host"
+    if host_io:
+        # the e2e form: frame constants and instance records from one pinned
+        # staging block, the Readback to pinned host memory (tc_frame_build_graph_host)
+        FC = L.FrameConstants.itemsize
+        rec = pipe.state.res.instance_records.view(np.uint8).reshape(-1)
+        blk = 2 * FC + rec.size
+        stage = torch.empty(blk, dtype=torch.uint8, pin_memory=True)
+        stage_np = stage.numpy()
+        stage_np[2 * FC:] = rec
+        dev_block = torch.empty(blk + 256, dtype=torch.uint8, device="cuda")
+        base = (dev_block.data_ptr() + 255) // 256 * 256
+        rb_host = torch.empty(L.Readback.itemsize, dtype=torch.uint8, pin_memory=True)
+        fa = pipe.args
+        fa.view, fa.viewLast, fa.instances = base, base + FC, base + 2 * FC
     for i, cam in enumerate(cams):
+        if host_io:
+            torch.cuda.synchronize()  # the previous frame has read the staging block
+            stage_np[:FC] = np.frombuffer(S.frame_constants(cam).tobytes(), np.uint8)
+            stage_np[FC:2 * FC] = np.frombuffer(S.frame_constants(cams[i - 1] if i else cam).tobytes(), np.uint8)
+            pipe.build_host(stage.data_ptr(), base, blk, rb_host.data_ptr())
+            continue
         pipe.set_cameras(cam, cams[i - 1] if i else cam)
         if args.profile_case == "terrain_stages":  # the per-stage entry points, as the bench's stage timings run them
             for name, extra in stage_sequence(pipe, pipe.args.numInstances):
@@ -1019,7 +1042,9 @@ def run_profile_case(args):
             pipe.raster_batches()
     torch.cuda.synchronize()
     print(json.dumps({"profile_case": args.profile_case, "frames": len(cams), "device_errors": pipe.device_errors(),
-                      "readback_tris": int(pipe.state.readback.read(L.Readback, 1)[0]["numTotalTriangles"])}))
+                      "readback_tris": int(pipe.state.readback.read(L.Readback, 1)[0]["numTotalTriangles"]),
+                      "host_readback_tris": int(rb_host.numpy().view(L.Readback)[0]["numTotalTriangles"]) if host_io
+                      else None}))
     pipe.close()
     return 0
 
