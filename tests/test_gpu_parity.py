@@ -507,22 +507,29 @@ def test_host_io_frames_match_oracle(oracle):
     frames = (3, 4, 9)
     blk = 2 * FC + rec.size
     assert blk % 16 == 0
-    host = torch.empty((len(frames), blk), dtype=torch.uint8, pin_memory=True)
+    # rows of blk + 16 bytes: the second frame also uploads a 4-byte tail
+    # (inputBytes not a multiple of 16) into slack past the frame's inputs
+    host = torch.zeros((len(frames), blk + 16), dtype=torch.uint8, pin_memory=True)
     for k, f in enumerate(frames):
         host[k, :FC] = torch.from_numpy(np.frombuffer(frame_constants(S.camera_orbit(f)).tobytes(), np.uint8).copy())
         host[k, FC:2 * FC] = torch.from_numpy(
             np.frombuffer(frame_constants(S.camera_orbit(f - 1)).tobytes(), np.uint8).copy())
-        host[k, 2 * FC:] = torch.from_numpy(rec.copy())
+        host[k, 2 * FC:blk] = torch.from_numpy(rec.copy())
+    tail = torch.tensor([0xA5, 0x5A, 0x3C, 0x77], dtype=torch.uint8)
+    host[1, blk:blk + 4] = tail
     rb_host = torch.zeros(RB, dtype=torch.uint8, pin_memory=True)
-    dev_block = torch.empty(blk + 256, dtype=torch.uint8, device="cuda")
+    dev_block = torch.zeros(blk + 512, dtype=torch.uint8, device="cuda")
     base = (dev_block.data_ptr() + 255) // 256 * 256
+    off = base - dev_block.data_ptr()
     fa = pipe.args
     saved = (fa.view, fa.viewLast, fa.instances)
     fa.view, fa.viewLast, fa.instances = base, base + FC, base + 2 * FC
     for k, f in enumerate(frames):
         rb_host.zero_()
-        pipe.build_host(host[k].data_ptr(), base, blk, rb_host.data_ptr())
+        pipe.build_host(host[k].data_ptr(), base, blk + (4 if k == 1 else 0), rb_host.data_ptr())
         torch.cuda.synchronize()
+        if k == 1:
+            assert torch.equal(dev_block[off + blk:off + blk + 4].cpu(), tail)
         out = pipe.outputs()
         ref_state, _ = oracle.frame(sc, S.camera_orbit(f), caps, FLAGS, camera_last=S.camera_orbit(f - 1))
         assert_same(out, ref_state.outputs(oracle.entries), f"host-io frame {f}", vertex_tol=vertex_tolerance(sc))
@@ -550,5 +557,18 @@ def test_host_io_frames_match_oracle(oracle):
     torch.cuda.synchronize()
     assert_same(pipe.outputs(), last, "readback-only frame")
     assert np.array_equal(rb_host.numpy(), pipe.state.readback.handle[:RB].cpu().numpy())
+
+    # the frame constants from the uploaded block, the instance records from the
+    # resident buffer: the upload runs as its own kernel before the frame
+    # (the frame's first kernel reads its inputs from the host block only when
+    # all of them lie in it)
+    fa.view, fa.viewLast = base, base + FC
+    rb_host.zero_()
+    pipe.build_host(host[0].data_ptr(), base, blk, rb_host.data_ptr())
+    torch.cuda.synchronize()
+    ref_state, _ = oracle.frame(sc, S.camera_orbit(frames[0]), caps, FLAGS, camera_last=S.camera_orbit(frames[0] - 1))
+    assert_same(pipe.outputs(), ref_state.outputs(oracle.entries), "separate upload", vertex_tol=vertex_tolerance(sc))
+    assert np.array_equal(rb_host.numpy(), pipe.state.readback.handle[:RB].cpu().numpy())
+    fa.view, fa.viewLast = saved[0], saved[1]
     assert pipe.device_errors() == 0
     pipe.close()

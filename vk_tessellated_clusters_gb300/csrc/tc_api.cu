@@ -69,15 +69,16 @@ struct HostIo
   void*       hostRb   = nullptr;  // device alias of the caller's Readback buffer
   const void* callerIn = nullptr;  // the caller's addresses
   const void* callerRb = nullptr;
+  bool        fused    = false;    // the upload runs inside the frame's first kernel (inputs_in_block)
   bool same_buffers(const HostIo& o) const
   {
     return callerIn == o.callerIn && devIn == o.devIn && bytes == o.bytes && callerRb == o.callerRb;
   }
   bool operator==(const HostIo& o) const
   {
-    return same_buffers(o) && hostIn == o.hostIn && hostRb == o.hostRb;
+    return same_buffers(o) && hostIn == o.hostIn && hostRb == o.hostRb && fused == o.fused;
   }
-  uint64_t launches() const { return (bytes ? 1 : 0) + (hostRb ? 1 : 0); }
+  uint64_t launches() const { return (bytes && !fused ? 1 : 0) + (hostRb ? 1 : 0); }
 };
 
 u32 ceil_div(u64 a, u64 b) { return (u32)((a + b - 1) / b); }
@@ -119,6 +120,7 @@ struct tc_context
   cudaEvent_t  evVerts = nullptr;  // all part vertices written
   cudaEvent_t  evInst  = nullptr;  // instances classified
   cudaEvent_t  evScan0 = nullptr;  // first part run's offsets (and the counters after it)
+  cudaEvent_t  evCull  = nullptr;  // clusters_cull done (on the second side stream)
 
   // graph cache
   cudaGraphExec_t graphExec = nullptr;
@@ -364,13 +366,32 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   const tc_schedule& sched = ctx->schedule;
   const u32          bpsm  = std::max(1u, sched.blocksPerSM);
   TC_CHECK_CUDA(cudaMemsetAsync(ctx->dScratch, 0, p.frameBytes, s));
-  if(io.bytes)
-    TC_CHECK_CUDA(launch_host_upload(io.hostIn, io.devIn, io.bytes, ctx->numSMs, s));
 
   StageCtx c = base_ctx(ctx, a);
   bind_slot(ctx, c, p.slotInstances, false);
-  TC_CHECK_CUDA(launch_frame_begin_instances(
-      c, std::max(frame_begin_grid(ctx, a), ceil_div(a->numInstances, kInstanceTile)), s));
+  const u32 beginGrid = std::max(frame_begin_grid(ctx, a), ceil_div(a->numInstances, kInstanceTile));
+  if(io.bytes)
+  {
+    const HostUpload up = {io.hostIn, io.devIn, io.bytes};
+    if(io.fused)
+    {
+      // the first kernel copies the block and reads its own inputs from the host block
+      StageCtx  ch   = c;
+      const u64 d0   = reinterpret_cast<u64>(io.devIn);
+      auto      host = [&](uint64_t ptr) { return static_cast<const char*>(io.hostIn) + (ptr - d0); };
+      ch.view        = reinterpret_cast<const tc_FrameConstants*>(host(a->view));
+      ch.viewLast    = reinterpret_cast<const tc_FrameConstants*>(host(a->viewLast));
+      ch.instances   = reinterpret_cast<const tc_RenderInstance*>(host(a->instances));
+      TC_CHECK_CUDA(launch_frame_begin_instances_upload(ch, up, beginGrid, s));
+    }
+    else
+    {
+      TC_CHECK_CUDA(launch_host_upload(up, ctx->numSMs, s));
+      TC_CHECK_CUDA(launch_frame_begin_instances(c, beginGrid, s));
+    }
+  }
+  else
+    TC_CHECK_CUDA(launch_frame_begin_instances(c, beginGrid, s));
 
   // With RT semantics every cluster of every instance is visible, in instance
   // order: classify reads that list from the instances' cluster prefix and
@@ -390,6 +411,8 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
     }
     TC_CHECK_CUDA(
         launch_clusters_cull(cc, persistent_grid(ctx, ceil_div(a->totalClusters, kCullTile), 4), kCullTile, cs, flat));
+    if(flat && io.hostRb)
+      TC_CHECK_CUDA(cudaEventRecord(ctx->evCull, cs));
   }
   c.flatVisible = flat ? 1u : 0u;
 
@@ -485,10 +508,19 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
 
   u32* seg = reinterpret_cast<u32*>(ctx->dScratch + p.segOffset);
   TC_CHECK_CUDA(launch_blas_clusters_insert(c, seg, seg + (size_t)p.segStride * p.segRows, p.segStride, insert_grid(ctx, a), s));
+  if(io.hostRb)
+  {
+    // Every Readback writer is behind this point on this stream (the first
+    // part run's argument kernel joined at evJoin) except clusters_cull on the
+    // second side stream, whose fused set-up writes numVisibleClusters; the
+    // vertex kernels still running beside write none. So the copy to the host
+    // waits for the cull alone and overlaps the vertex kernels' tails.
+    if(flat)
+      TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evCull, 0));
+    TC_CHECK_CUDA(launch_host_readback(c.readback, io.hostRb, s));
+  }
   TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evVerts, 0));
   TC_CHECK_CUDA(cudaStreamWaitEvent(s, ctx->evJoin2, 0));
-  if(io.hostRb)
-    TC_CHECK_CUDA(launch_host_readback(c.readback, io.hostRb, s));
 
   ctx->launches += frame_launches(ctx, a) + io.launches();
   return TC_OK;
@@ -561,6 +593,16 @@ void* host_alias(const void* p, uint64_t bytes)
   return a0.devicePointer;
 }
 
+// Whether the frame constants (this frame's and last frame's) and the
+// instance records all lie in the uploaded block [d0, d0 + bytes): then the
+// frame's first kernel can read them from the host block while it uploads it.
+bool inputs_in_block(const tc_frame_args* a, uint64_t d0, uint64_t bytes)
+{
+  auto inside = [&](uint64_t p, uint64_t size) { return p >= d0 && p - d0 <= bytes && size <= bytes - (p - d0); };
+  return inside(a->view, sizeof(tc_FrameConstants)) && inside(a->viewLast, sizeof(tc_FrameConstants))
+         && inside(a->instances, (uint64_t)a->numInstances * sizeof(tc_RenderInstance));
+}
+
 // Whether both ends of [p, p + bytes) are device (or managed) memory.
 bool device_range(const void* p, uint64_t bytes)
 {
@@ -610,7 +652,7 @@ namespace {
 void destroy_streams(tc_context* ctx)
 {
   for(cudaEvent_t* e : {&ctx->evFork, &ctx->evJoin, &ctx->evJoin2, &ctx->evArgs1, &ctx->evVerts, &ctx->evInst,
-                        &ctx->evScan0})
+                        &ctx->evScan0, &ctx->evCull})
     if(*e)
       cudaEventDestroy(*e), *e = nullptr;
   for(cudaStream_t* st : {&ctx->side, &ctx->side2})
@@ -648,7 +690,8 @@ tc_status tc_context_create(const tc_context_desc* desc, tc_context** outCtx)
      || cudaEventCreateWithFlags(&ctx->evArgs1, cudaEventDisableTiming) != cudaSuccess
      || cudaEventCreateWithFlags(&ctx->evVerts, cudaEventDisableTiming) != cudaSuccess
      || cudaEventCreateWithFlags(&ctx->evInst, cudaEventDisableTiming) != cudaSuccess
-     || cudaEventCreateWithFlags(&ctx->evScan0, cudaEventDisableTiming) != cudaSuccess)
+     || cudaEventCreateWithFlags(&ctx->evScan0, cudaEventDisableTiming) != cudaSuccess
+     || cudaEventCreateWithFlags(&ctx->evCull, cudaEventDisableTiming) != cudaSuccess)
   {
     destroy_streams(ctx);
     delete ctx;
@@ -857,6 +900,7 @@ tc_status tc_frame_build_graph_host(tc_context* ctx, const tc_frame_args* args, 
   io.devIn    = inputBytes ? reinterpret_cast<void*>(deviceInputs) : nullptr;
   io.callerIn = inputBytes ? hostInputs : nullptr;
   io.callerRb = hostReadback;
+  io.fused    = inputBytes && inputs_in_block(args, deviceInputs, inputBytes);
   if(ctx->graphValid && io.same_buffers(ctx->graphIo))
   {
     // checked when the graph was recorded

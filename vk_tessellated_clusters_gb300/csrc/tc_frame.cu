@@ -352,10 +352,12 @@ __global__ void k_lookback_probe(u64* state, u32 published, u32* errorWord, u32 
 
 constexpr u32 kUploadPerThread = 4;  // 16-byte loads in flight per thread before its stores
 
-__global__ void k_host_upload(const uint4* __restrict__ src, uint4* __restrict__ dst, u64 n16,
-                              const unsigned char* __restrict__ srcTail, unsigned char* __restrict__ dstTail, u32 tail)
+// the grid's share of a host upload (16-byte words, then the tail bytes)
+__device__ __forceinline__ void host_upload_body(const HostUpload& u)
 {
-  stage_prologue();
+  const uint4* __restrict__ src = static_cast<const uint4*>(u.src);
+  uint4* __restrict__ dst       = static_cast<uint4*>(u.dst);
+  const u64 n16    = u.bytes / 16;
   const u64 stride = (u64)gridDim.x * blockDim.x;
   for(u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride * kUploadPerThread)
   {
@@ -369,8 +371,27 @@ __global__ void k_host_upload(const uint4* __restrict__ src, uint4* __restrict__
       if(i + k * stride < n16)
         dst[i + k * stride] = v[k];
   }
+  const u32 tail = (u32)(u.bytes % 16);
   if(blockIdx.x == 0 && threadIdx.x < tail)
-    dstTail[threadIdx.x] = srcTail[threadIdx.x];
+    static_cast<unsigned char*>(u.dst)[n16 * 16 + threadIdx.x] = static_cast<const unsigned char*>(u.src)[n16 * 16 + threadIdx.x];
+}
+
+__global__ void k_host_upload(HostUpload u)
+{
+  stage_prologue();
+  host_upload_body(u);
+}
+
+// The batched frame's first kernel with the upload in it: every block copies
+// its share of the input block, and the frame's own reads of the frame
+// constants and instance records (c points them into the host block) go to
+// the host memory directly. Kernels after it read the device copy.
+__global__ void k_frame_begin_instances_upload(StageCtx c, HostUpload u)
+{
+  stage_prologue();
+  host_upload_body(u);
+  frame_begin_body(c);
+  instances_classify_body(c);
 }
 
 __global__ void k_host_readback(const u32* __restrict__ src, u32* __restrict__ dst, u32 words)
@@ -384,16 +405,16 @@ __global__ void k_host_readback(const u32* __restrict__ src, u32* __restrict__ d
 // launchers
 // ---------------------------------------------------------------------------
 
-cudaError_t launch_host_upload(const void* src, void* dst, u64 bytes, u32 maxGrid, cudaStream_t s)
+cudaError_t launch_host_upload(const HostUpload& u, u32 maxGrid, cudaStream_t s)
 {
-  const u64 n16   = bytes / 16;
-  const u32 tail  = (u32)(bytes % 16);
-  const u64 per   = 256ull * kUploadPerThread;
-  const u32 grid  = (u32)std::max<u64>(1, std::min<u64>((n16 + per - 1) / per, maxGrid));
-  const auto* s8  = static_cast<const unsigned char*>(src) + n16 * 16;
-  auto*       d8  = static_cast<unsigned char*>(dst) + n16 * 16;
-  return launch_side(k_host_upload, grid, 256, s, static_cast<const uint4*>(src), static_cast<uint4*>(dst), n16, s8,
-                     d8, tail);
+  const u64 per  = 256ull * kUploadPerThread;
+  const u32 grid = (u32)std::max<u64>(1, std::min<u64>((u.bytes / 16 + per - 1) / per, maxGrid));
+  return launch_side(k_host_upload, grid, 256, s, u);
+}
+
+cudaError_t launch_frame_begin_instances_upload(const StageCtx& c, const HostUpload& u, u32 grid, cudaStream_t s)
+{
+  return launch_pdl(k_frame_begin_instances_upload, grid, kInstanceTile, s, c, u);
 }
 
 cudaError_t launch_host_readback(const tc_Readback* src, void* dst, cudaStream_t s)

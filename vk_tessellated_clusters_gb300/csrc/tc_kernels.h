@@ -58,10 +58,19 @@ cudaError_t launch_frame_begin_instances(const StageCtx& c, u32 grid, cudaStream
 cudaError_t launch_clusters_cull(const StageCtx& c, u32 grid, u32 block, cudaStream_t s, bool side = false);
 cudaError_t launch_build_setup(const StageCtx& c, u32 mode, cudaStream_t s);
 // a frame's host traffic: `bytes` from mapped pinned host memory (src, its
-// device alias) to device memory, at most maxGrid blocks; the Readback to
-// mapped pinned host memory (dst, its device alias). Both 16-byte aligned
-// (the upload) or 4-byte aligned (the Readback).
-cudaError_t launch_host_upload(const void* src, void* dst, unsigned long long bytes, u32 maxGrid, cudaStream_t s);
+// device alias) to device memory, both 16-byte aligned; the Readback to
+// mapped pinned host memory (dst, its device alias, 4-byte aligned)
+struct HostUpload
+{
+  const void*        src;
+  void*              dst;
+  unsigned long long bytes;
+};
+// on its own (at most maxGrid blocks), or inside the batched frame's first
+// kernel (launch_frame_begin_instances with the upload; c's frame constants
+// and instance records point into the host block)
+cudaError_t launch_host_upload(const HostUpload& u, u32 maxGrid, cudaStream_t s);
+cudaError_t launch_frame_begin_instances_upload(const StageCtx& c, const HostUpload& u, u32 grid, cudaStream_t s);
 cudaError_t launch_host_readback(const tc_Readback* src, void* dst, cudaStream_t s);
 // the bounded look-back wait on its own (state: 3 words, zeroed here)
 cudaError_t launch_lookback_probe(unsigned long long* state, u32 published, u32* errorWord, u32 spinLimit,
