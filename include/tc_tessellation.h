@@ -543,9 +543,9 @@ tc_status tc_frame_build_graph(tc_context* ctx, const tc_frame_args* args, void*
 /* The graph frame of tc_frame_build_graph with the frame's host traffic inside
  * the graph: its first kernel copies inputBytes from the pinned host block
  * hostInputs to the device block deviceInputs (which args->view, viewLast and
- * instances may point into), its last kernel copies the frame's tc_Readback to
- * the pinned host buffer hostReadback, which holds it once the stream has
- * passed the call. Replaces the reference's per-frame upload of the frame
+ * instances may point into), and once the frame's counters are final a kernel
+ * of the graph copies its tc_Readback to the pinned host buffer hostReadback,
+ * which holds it once the stream has passed the call. Replaces the reference's per-frame upload of the frame
  * constants (src/renderer_raytrace_clusters_tess.cpp:415, vkCmdUpdateBuffer)
  * and its Readback copy to a host-visible buffer (src/resources.cpp:83-90,
  * read in src/resources.cpp:497-501) without copy-engine round trips.
