@@ -342,7 +342,8 @@ __global__ void k_lookback_probe(u64* state, u32 published, u32* errorWord, u32 
 // ---------------------------------------------------------------------------
 // A frame's host traffic inside its graph (tc_frame_build_graph_host): the
 // input block (frame constants, instance records) read from mapped pinned host
-// memory before the frame, the Readback written back to it after the frame.
+// memory at the frame's start, the Readback written back to it once the
+// frame's counters are final.
 // Plain loads and stores through the mapping replace the copy-engine round
 // trips of cudaMemcpyAsync (the reference: vkCmdUpdateBuffer of the frame
 // constants, src/renderer_raytrace_clusters_tess.cpp:415, and the Readback copy
