@@ -2,7 +2,8 @@
 
 - the batched scene (256 instances of four meshes, 512² fp32 maps, orbit
   camera, culling on) on the frames the bench's timed steps start with, through
-  the CUDA graph like the bench;
+  the CUDA graph like the bench, and one frame from host buffers like the
+  bench's end-to-end figure;
 - the terrain (1024² quads, 4096² fp16 fBm map of 8 octaves, grazing camera at
   3840x2160, the bench's terrain capacities): the split passes fire and the
   fp16 texel path samples every vertex;
@@ -67,6 +68,40 @@ def test_batched_scene_full_size_bit_exact(oracle, batched, frame):
     states = want["instanceStates"]
     assert (states & L.INSTANCE_VISIBLE_BIT).any() and not (states & L.INSTANCE_VISIBLE_BIT).all()
     assert_same(got, want, f"batched frame {frame}", vertex_tol=vertex_tolerance(sc))
+
+
+def test_batched_scene_from_host_buffers_bit_exact(oracle, batched):
+    """The bench's end-to-end form at full size: frame 5 through
+    tc_frame_build_graph_host (frame constants and instance records from a
+    pinned staging block, the Readback to pinned host memory) matches the
+    oracle, and the host Readback equals the device one."""
+    import torch
+    sc, pipe = batched
+    FC = L.FrameConstants.itemsize
+    rec = pipe.state.res.instance_records.view(np.uint8).reshape(-1)
+    blk = 2 * FC + rec.size
+    stage = torch.empty(blk, dtype=torch.uint8, pin_memory=True)
+    sn = stage.numpy()
+    cam, last = S.camera_orbit(5), S.camera_orbit(4)
+    sn[:FC] = np.frombuffer(S.frame_constants(cam).tobytes(), np.uint8)
+    sn[FC:2 * FC] = np.frombuffer(S.frame_constants(last).tobytes(), np.uint8)
+    sn[2 * FC:] = rec
+    dev_block = torch.empty(blk + 256, dtype=torch.uint8, device="cuda")
+    base = (dev_block.data_ptr() + 255) // 256 * 256
+    rb_host = torch.zeros(L.Readback.itemsize, dtype=torch.uint8, pin_memory=True)
+    fa = pipe.args
+    saved = (fa.view, fa.viewLast, fa.instances)
+    fa.view, fa.viewLast, fa.instances = base, base + FC, base + 2 * FC
+    try:
+        pipe.build_host(stage.data_ptr(), base, blk, rb_host.data_ptr())
+        torch.cuda.synchronize()
+        got = pipe.outputs()
+    finally:
+        fa.view, fa.viewLast, fa.instances = saved
+    assert pipe.device_errors() == 0
+    assert np.array_equal(rb_host.numpy(), pipe.state.readback.handle[:L.Readback.itemsize].cpu().numpy())
+    st, _ = oracle.frame(sc, cam, L.default_caps(), L.FLAG_CULLING, camera_last=last)
+    assert_same(got, st.outputs(oracle.entries), "batched frame 5 from host buffers", vertex_tol=vertex_tolerance(sc))
 
 
 def test_batched_scene_full_size_fp64_error(oracle, batched):
