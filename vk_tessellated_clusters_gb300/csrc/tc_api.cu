@@ -365,10 +365,15 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   const Plan&        p     = ctx->plan;
   const tc_schedule& sched = ctx->schedule;
   const u32          bpsm  = std::max(1u, sched.blocksPerSM);
-  TC_CHECK_CUDA(cudaMemsetAsync(ctx->dScratch, 0, p.frameBytes, s));
 
+  // No memset before the frame: the instance classification's slot (the
+  // first) puts itself back to zero after each use, and the frame's first
+  // kernel zeroes the rest of the frame's scratch, which only later kernels use.
   StageCtx c = base_ctx(ctx, a);
-  bind_slot(ctx, c, p.slotInstances, false);
+  bind_slot(ctx, c, p.slotInstances, true);
+  const size_t zeroOff = align_up(p.slots[p.slotInstances].ctrlOffset + kCtrlBytes, 256);
+  c.zeroBase           = reinterpret_cast<uint4*>(ctx->dScratch + zeroOff);
+  c.zeroN16            = (p.frameBytes - zeroOff) / 16;
   const u32 beginGrid = std::max(frame_begin_grid(ctx, a), ceil_div(a->numInstances, kInstanceTile));
   if(io.bytes)
   {
@@ -392,6 +397,8 @@ tc_status record_batched_frame(tc_context* ctx, const tc_frame_args* a, cudaStre
   }
   else
     TC_CHECK_CUDA(launch_frame_begin_instances(c, beginGrid, s));
+  c.zeroBase = nullptr;
+  c.zeroN16  = 0;
 
   // With RT semantics every cluster of every instance is visible, in instance
   // order: classify reads that list from the instances' cluster prefix and

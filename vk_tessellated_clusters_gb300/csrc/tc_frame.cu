@@ -132,6 +132,10 @@ __device__ inline void frame_begin_body(const StageCtx& c)
     for(u32 i = threadIdx.x; i < kRunStartsSize; i += blockDim.x)
       c.runStarts[i] = 0;
   }
+  // the batched frame's scratch for the stages after this one (their
+  // look-back states and counters), in place of a memset before the frame
+  for(u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < c.zeroN16; i += (u64)gridDim.x * blockDim.x)
+    c.zeroBase[i] = make_uint4(0u, 0u, 0u, 0u);
   // the split queue is filled with ~0 every frame
   u32* split = reinterpret_cast<u32*>(b->splitTriangles);
   if(split)

@@ -124,6 +124,8 @@ struct StageCtx
   u32                           flatVisible;    // classify: the visible list is every cluster in instance order
                                                 // (RT semantics, whole window), read from instClusterStart
                                                 // instead of waiting for clusters_cull
+  uint4*                        zeroBase;  // frame_begin: scratch it zeroes (the batched frame's later slots), or null
+  u64                           zeroN16;   // its size in 16-byte words
 };
 
 constexpr u32 kNoSetup        = 0xFFFFFFFFu;
