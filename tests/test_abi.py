@@ -105,6 +105,8 @@ def test_calls_without_gpu(lib):
     # argument validation happens before any CUDA call
     assert lib.tc_context_create(None, None) == L.TC_ERR_INVALID_ARG
     assert lib.tc_frame_build(None, None, None) == L.TC_ERR_INVALID_ARG
+    assert lib.tc_frame_build_graph(None, None, None) == L.TC_ERR_INVALID_ARG
+    assert lib.tc_frame_build_graph_host(None, None, None, 0, 0, None, None) == L.TC_ERR_INVALID_ARG
     assert lib.tc_context_destroy(None) == L.TC_ERR_INVALID_ARG
 
 
