@@ -475,3 +475,31 @@ def test_raster_batches_restatement(oracle):
                         np.float64).reshape(4, 4).T
         c = r["clipPositions"][cv[p]:cv[p + 1]].astype(np.float64)
         np.testing.assert_allclose(c, np.c_[w, np.ones(len(w))] @ vp.T, rtol=1e-5, atol=1e-4)
+
+
+def test_factor_one_shortcut_never_changes_a_factor():
+    """The classify kernel skips an edge's square root when
+    (|d|^2 * spl^2) * (viewportH * tessRate)^2 < 2.25 * (1 - 1e-5) in single
+    precision and takes the factor as 1 (tc_device.cuh, edge_factor). Restated
+    here in float32 (each operation rounded like the GPU's) on seeded edges
+    spread over [0, 3] and packed around the 1.5 threshold: wherever the
+    shortcut answers, the full evaluation rint(((sqrt(s) * spl) * vh) * rate)
+    clamped to [1, 32768] is 1 as well."""
+    f32 = np.float32
+    rng = np.random.default_rng(7)
+    bound = f32(2.2499775)
+    n, claims = 500_000, 0
+    for it, (vh, rate) in enumerate([(1080.0, 0.25), (2160.0, 0.25), (1080.0, 0.125), (720.0, 1.0)]):
+        vh, rate = f32(vh), f32(rate)
+        x_target = 1.5 + rng.uniform(-3e-5, 3e-5, n) if it % 2 else rng.uniform(0.0, 3.0, n)
+        spl = rng.uniform(1e-4, 1.0, n).astype(f32)
+        e = (x_target / (spl.astype(np.float64) * float(vh) * float(rate))).astype(f32)
+        s = (e.astype(np.float64) ** 2 * rng.uniform(0.999, 1.001, n)).astype(f32)
+        k = f32(vh * rate)
+        t = (s * (spl * spl)) * f32(k * k)
+        claim = t < bound
+        x = ((np.sqrt(s) * spl) * vh) * rate
+        f = np.minimum(np.maximum(np.rint(x), f32(1)), f32(32768))
+        assert not np.any(claim & (f != 1))
+        claims += int(claim.sum())
+    assert claims > n  # the shortcut answers for a good share of the edges

@@ -151,16 +151,37 @@ __device__ __forceinline__ float rcp_of_clamped_min(float da, float db, float ra
   return nearPlane > m ? rNear : rm;
 }
 
+// The factor of edge a-b, round_clamp_factor(|a - b|, spl, fp), without the
+// square root where the answer is certainly 1. That factor is 1 exactly when
+// x = ((|a - b| * spl) * viewportH) * tessRate is below 1.5 (rint then gives
+// at most 1). t = (|a - b|^2 * spl^2) * (viewportH * tessRate)^2 in single
+// precision carries five roundings (relative error below 3.0e-7) and x four
+// (below 2.4e-7), so t < 2.25 * (1 - 1e-5) puts x below 1.5 * (1 - 4.6e-6):
+// the factor is 1, the same result as the full evaluation. Every other edge
+// (and NaN or infinite t) takes the full evaluation, on the same |a - b|^2.
+constexpr float kFactorOneBound = 2.2499775f;  // 2.25 * (1 - 1e-5)
+
+__device__ __forceinline__ u32 edge_factor(f3 a, f3 b, float spl, float k2, const FactorParams& fp)
+{
+  const f3    d  = sub3(a, b);
+  const float s2 = dot3(d, d);
+  if((s2 * (spl * spl)) * k2 < kFactorOneBound)
+    return 1u;
+  return round_clamp_factor(__fsqrt_rn(s2), spl, fp);
+}
+
 __device__ __forceinline__ uint3 tess_factors_hoisted(f3 a, f3 b, f3 c, float da, float db, float dc, float ra, float rb,
                                                       float rc, float rNear, const FactorParams& fp)
 {
   const float sx = rcp_of_clamped_min(da, db, ra, rb, fp.nearPlane, rNear);
   const float sy = rcp_of_clamped_min(db, dc, rb, rc, fp.nearPlane, rNear);
   const float sz = rcp_of_clamped_min(dc, da, rc, ra, fp.nearPlane, rNear);
+  const float k  = fp.viewportH * fp.tessRate;
+  const float k2 = k * k;
   uint3       f;
-  f.x = round_clamp_factor(dist3(a, b), sx, fp);
-  f.y = round_clamp_factor(dist3(b, c), sy, fp);
-  f.z = round_clamp_factor(dist3(c, a), sz, fp);
+  f.x = edge_factor(a, b, sx, k2, fp);
+  f.y = edge_factor(b, c, sy, k2, fp);
+  f.z = edge_factor(c, a, sz, k2, fp);
   return f;
 }
 
