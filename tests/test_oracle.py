@@ -503,3 +503,37 @@ def test_factor_one_shortcut_never_changes_a_factor():
         assert not np.any(claim & (f != 1))
         claims += int(claim.sum())
     assert claims > n  # the shortcut answers for a good share of the edges
+
+
+def test_cluster_factor_one_shortcut_never_changes_a_factor():
+    """The classify kernel skips a cluster's distances, their reciprocals and
+    every edge's square root when each edge passes
+    |d|^2 * (viewportH * tessRate)^2 < 2.25 * (1 - 1e-5) * max(near^2, min(da^2, db^2))
+    in single precision (tc_device.cuh, edge_factor_one_sq) and takes all its
+    factors as 1. Restated in float32 on seeded edges packed around the
+    threshold: wherever the test passes, the full evaluation (the distances'
+    roots, the reciprocal of the clamped nearer one, the edge's root, rint of the
+    product, clamp) gives 1 as well."""
+    f32 = np.float32
+    rng = np.random.default_rng(11)
+    bound = f32(2.2499775)
+    n, claims = 500_000, 0
+    for it, (vh, rate, near) in enumerate([(1080.0, 0.25, 0.01), (2160.0, 0.25, 0.1), (1080.0, 0.125, 0.01),
+                                           (720.0, 1.0, 2.0)]):
+        vh, rate, near = f32(vh), f32(rate), f32(near)
+        da2 = (rng.uniform(0.0, 4.0, n) ** 4).astype(f32)  # squared distances of the two ends
+        db2 = (da2.astype(np.float64) * rng.uniform(0.9, 1.1, n)).astype(f32)
+        da, db = np.sqrt(da2), np.sqrt(db2)
+        m = np.minimum(da, db)
+        q = np.where(near > m, near, np.where(da <= db, da, db))
+        spl = f32(1) / q
+        x_target = 1.5 + rng.uniform(-3e-5, 3e-5, n) if it % 2 else rng.uniform(0.0, 3.0, n)
+        e = (x_target / (spl.astype(np.float64) * float(vh) * float(rate))).astype(f32)
+        s2 = (e.astype(np.float64) ** 2 * rng.uniform(0.999, 1.001, n)).astype(f32)
+        k = f32(vh * rate)
+        claim = s2 * f32(k * k) < bound * np.maximum(f32(near * near), np.minimum(da2, db2))
+        x = ((np.sqrt(s2) * spl) * vh) * rate
+        f = np.minimum(np.maximum(np.rint(x), f32(1)), f32(32768))
+        assert not np.any(claim & (f != 1))
+        claims += int(claim.sum())
+    assert claims > n

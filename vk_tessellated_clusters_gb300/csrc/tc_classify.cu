@@ -438,8 +438,12 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c
   const tc_ClusterInfo*   vis     = reinterpret_cast<const tc_ClusterInfo*>(b->visibleClusters);
   const FactorParams      fp      = factor_params(c);
   const float             rNear   = __fdiv_rn(1.0f, fp.nearPlane);
+  const float             kRate   = fp.viewportH * fp.tessRate;
+  const float             k2      = kRate * kRate;
+  const float             near2   = fp.nearPlane * fp.nearPlane;
   const bool              culling = (c.flags & TC_FLAG_CULLING) != 0;
   const u32               sf      = clamp_split_factor(c.caps.splitFactor);
+  const u32               wordOnes = classify_triangle(make_uint3(1u, 1u, 1u), sf);  // a triangle of factors 1
   if(blockIdx.x == 0 && threadIdx.x == 0)  // the offsets continue from the counters' current values
   {
     if constexpr(Trans)
@@ -521,29 +525,57 @@ __global__ void __launch_bounds__(kBlock, MinBlocks) k_classify_count(StageCtx c
           m[q] = __ldg(in->worldMatrix.m + q);
         for(u32 i = lane; i < nv; i += 32)
         {
-          const f3    w = xform_point(m, ldg3(pos, firstV + i));
-          const float d = dist3(w, fp.viewPos);
-          s_vert[warp][i] = w;
-          s_dist[warp][i] = {d, __fdiv_rn(1.0f, d)};
+          const f3 w  = xform_point(m, ldg3(pos, firstV + i));
+          const f3 dv = sub3(w, fp.viewPos);
+          s_vert[warp][i]   = w;
+          s_dist[warp][i].x = dot3(dv, dv);  // squared: the distance and its reciprocal only when needed
         }
         __syncwarp();
-        auto classify = [&](u32 idx, u32& mOut, u32& wOut) {
+        // A cluster whose every edge provably has factor 1 (edge_factor_one_sq:
+        // squared lengths and distances, no roots or divisions) is classified
+        // without the distances; the word is that of factors (1, 1, 1).
+        auto allOne = [&](u32 idx) {
           const u32   i0 = idx & 0xFF, i1 = (idx >> 8) & 0xFF, i2 = idx >> 16;
-          const f2    d0 = s_dist[warp][i0], d1 = s_dist[warp][i1], d2 = s_dist[warp][i2];
-          const uint3 f  = tess_factors_hoisted(s_vert[warp][i0], s_vert[warp][i1], s_vert[warp][i2], d0.x, d1.x,
-                                                d2.x, d0.y, d1.y, d2.y, rNear, fp);
-          mOut           = max(max(f.x, f.y), f.z);
-          wOut           = classify_triangle(f, sf);
-          if constexpr(Trans)  // factors of a 2X candidate, for its triangle map (cluster_classify.comp.glsl:817)
-            if(mOut <= 2)
-              wOut |= ((f.x - 1) | ((f.y - 1) << 1) | ((f.z - 1) << 2)) << kWordFactorShift;
+          const f3    v0 = s_vert[warp][i0], v1 = s_vert[warp][i1], v2 = s_vert[warp][i2];
+          const float q0 = s_dist[warp][i0].x, q1 = s_dist[warp][i1].x, q2 = s_dist[warp][i2].x;
+          return edge_factor_one_sq(v0, v1, q0, q1, k2, near2) && edge_factor_one_sq(v1, v2, q1, q2, k2, near2)
+                 && edge_factor_one_sq(v2, v0, q2, q0, k2, near2);
         };
-        if(lane < nt)
-          classify(ia, m0, w0);
-        if(lane + 32 < nt)
-          classify(ib, m1, w1);
-        simple = __popc(__ballot_sync(0xFFFFFFFFu, lane < nt && m0 == 1))
-                 + __popc(__ballot_sync(0xFFFFFFFFu, lane + 32 < nt && m1 == 1));
+        if(__all_sync(0xFFFFFFFFu, (lane >= nt || allOne(ia)) && (lane + 32 >= nt || allOne(ib))))
+        {
+          if(lane < nt)
+            m0 = 1, w0 = wordOnes;
+          if(lane + 32 < nt)
+            m1 = 1, w1 = wordOnes;
+          simple = nt;
+        }
+        else
+        {
+          for(u32 i = lane; i < nv; i += 32)
+          {
+            const float d     = __fsqrt_rn(s_dist[warp][i].x);  // dist3(w, viewPos)
+            s_dist[warp][i].y = __fdiv_rn(1.0f, d);
+            s_dist[warp][i].x = d;
+          }
+          __syncwarp();
+          auto classify = [&](u32 idx, u32& mOut, u32& wOut) {
+            const u32   i0 = idx & 0xFF, i1 = (idx >> 8) & 0xFF, i2 = idx >> 16;
+            const f2    d0 = s_dist[warp][i0], d1 = s_dist[warp][i1], d2 = s_dist[warp][i2];
+            const uint3 f  = tess_factors_hoisted(s_vert[warp][i0], s_vert[warp][i1], s_vert[warp][i2], d0.x, d1.x,
+                                                  d2.x, d0.y, d1.y, d2.y, rNear, fp);
+            mOut           = max(max(f.x, f.y), f.z);
+            wOut           = classify_triangle(f, sf);
+            if constexpr(Trans)  // factors of a 2X candidate, for its triangle map (cluster_classify.comp.glsl:817)
+              if(mOut <= 2)
+                wOut |= ((f.x - 1) | ((f.y - 1) << 1) | ((f.z - 1) << 2)) << kWordFactorShift;
+          };
+          if(lane < nt)
+            classify(ia, m0, w0);
+          if(lane + 32 < nt)
+            classify(ib, m1, w1);
+          simple = __popc(__ballot_sync(0xFFFFFFFFu, lane < nt && m0 == 1))
+                   + __popc(__ballot_sync(0xFFFFFFFFu, lane + 32 < nt && m1 == 1));
+        }
         __syncwarp();  // s_vert is reused by the next cluster
       }
       const bool full  = simple == nt;

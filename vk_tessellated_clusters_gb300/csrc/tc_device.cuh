@@ -170,6 +170,23 @@ __device__ __forceinline__ u32 edge_factor(f3 a, f3 b, float spl, float k2, cons
   return round_clamp_factor(__fsqrt_rn(s2), spl, fp);
 }
 
+// edge_factor's test from squared quantities alone: da2, db2 are the squared
+// distances of a and b to the view position (tess_factors_hoisted takes their
+// square roots as da, db), near2 = nearPlane^2, k2 = (viewportH * tessRate)^2.
+// With u = 2^-24 and Q = max(nearPlane, min(sqrt(da2), sqrt(db2))): the left
+// side is at least |a - b|^2 * (viewportH * tessRate)^2 * (1 - u)^4, the
+// right side at most 2.25 * (1 - 1e-5) * Q^2 * (1 + u)^2, and the factor's
+// product x at most |a - b| / Q * viewportH * tessRate * (1 + u)^6 (the
+// roots, the reciprocal and three products), so a true test puts x below
+// 1.5 * (1 - 5e-6 + 9u) < 1.5: the factor is 1. NaN and infinite values fail
+// the test (or give x = 0 and the factor 1 as well).
+__device__ __forceinline__ bool edge_factor_one_sq(f3 a, f3 b, float da2, float db2, float k2, float near2)
+{
+  const f3    d  = sub3(a, b);
+  const float s2 = dot3(d, d);
+  return s2 * k2 < kFactorOneBound * fmaxf(near2, fminf(da2, db2));
+}
+
 __device__ __forceinline__ uint3 tess_factors_hoisted(f3 a, f3 b, f3 c, float da, float db, float dc, float ra, float rb,
                                                       float rc, float rNear, const FactorParams& fp)
 {
